@@ -1,0 +1,371 @@
+"""Benchmark of the sparse-register-tiling SpMM on GB300.
+
+Workload (default): the FFN-shaped plain-FP32 SpMM -- A 2048 x 512 at 90 % sparsity with
+log-normal row skew (sigma 0.5), values N(0, 0.02), packed with M_r = 4 and the identity
+nanokernel set (mapping 61fee); B 512 x 512 FP32 N(0, 1).  One step runs the SpMM on R
+independent replicas (distinct seeds) whose working set (R x ~6 MB) is several times the L2,
+so every step streams A, B and C from HBM.
+
+  python bench.py [--steps K] [--warmup W] [--gpus N] [--impl spreg|reference]
+
+Prints one JSON line.  value = algorithmic GB/s of the whole job (packed values + column
+indices + nkern_counts + panel descriptors + B + C per SpMM, divided by the device time of
+the timed steps); e2e = the same metric through the host-buffer C ABI call
+(spreg_matmul_run: B copied in, C copied out, inside the timed region).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "sparse-register-tiling_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = ("SpMM %HBM peak (plain FP32 sparse-register-tiling SpMM, A 2048x512 @90% row-skew, "
+          "N=512, M_r=4 identity): algorithmic GB/s")
+UNIT = "GB/s"
+L2_BYTES = 129 * 2 ** 20
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["spreg", "reference"], default="spreg")
+    ap.add_argument("--replicas", type=int, default=96)
+    ap.add_argument("--m", type=int, default=2048)
+    ap.add_argument("--k", type=int, default=512)
+    ap.add_argument("--n", type=int, default=512)
+    ap.add_argument("--sparsity", type=float, default=0.9)
+    ap.add_argument("--nr", type=int, default=0)
+    ap.add_argument("--no-graph", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def make_inputs(args, rank: int):
+    from spreg import synth
+    As, Bs = [], []
+    for r in range(args.replicas):
+        seed = 1000 * (rank + 1) + r
+        As.append(synth.row_skew(args.m, args.k, args.sparsity, seed=seed, sigma=0.5, std=0.02))
+        Bs.append(synth.dense(args.k, args.n, seed=seed + 500000))
+    return As, Bs
+
+
+def algorithmic_bytes_oracle(pk, n: int) -> int:
+    """Same count as PackedMatrix.algorithmic_bytes for an oracle packing (FP32)."""
+    s = pk.sizes
+    return int(s["num_values"] * 4 + s["num_col_indices"] * 4 + s["num_units"] * pk.t.num_nkern * 4
+               + s["num_units"] * 32 + pk.K * n * 4 + pk.M * n * 4)
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms while running."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+        self.t = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            if self.t:
+                self.t.join(timeout=2)
+
+    def summary(self) -> dict:
+        mhz, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                mhz.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not mhz:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(mhz), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(mhz)}
+
+
+def load_traffic():
+    path = os.path.join(ROOT, "profiles", "exec_fp32_2048x512_n512.json")
+    if os.path.exists(path):
+        try:
+            with open(path) as f:
+                return json.load(f).get("dram_bytes_per_launch")
+        except (OSError, ValueError):
+            return None
+    return None
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def cpu_baseline(As, Bs, args, seconds: float, threads: int = 0):
+    """Restated reference executor (oracle, OpenMP) on a bounded sample of the same workload."""
+    from oracle import oracle as O
+    from spreg.mapping import Mapping
+    t = O.Tables.of(Mapping.identity(4))
+    done_bytes, done_flops, runs, i = 0, 0, 0, 0
+    packs = {}
+    t0 = time.perf_counter()
+    elapsed = 0.0
+    while elapsed < seconds and runs < 10000:
+        r = i % len(As)
+        if r not in packs:
+            packs[r] = O.Packed(t, As[r])
+        pk = packs[r]
+        s = time.perf_counter()
+        pk.execute(Bs[r], threads=threads)
+        elapsed_run = time.perf_counter() - s
+        done_bytes += algorithmic_bytes_oracle(pk, args.n)
+        done_flops += 2 * pk.sizes["nnz"] * args.n
+        runs += 1
+        i += 1
+        elapsed += elapsed_run
+        if time.perf_counter() - t0 > 3 * seconds:
+            break
+    return {"value": done_bytes / elapsed / 1e9, "unit": UNIT, "gflops": done_flops / elapsed / 1e9,
+            "cores": threads if threads > 0 else O.max_threads(), "kind": "port",
+            "sample": f"{runs} SpMMs of the workload ({len(packs)} distinct replicas), {elapsed:.1f} s of "
+                      "executor time, restated reference executor (oracle/spreg_oracle.c) with OpenMP over panels"}
+
+
+def run_reference(args):
+    """--impl reference: the reference's CPU algorithm (restated; its own executor source is absent)."""
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    O.build(with_reference=False) if not os.path.exists(O.LIB_PATH) else None
+    As, Bs = make_inputs(args, 0)
+    from spreg.mapping import Mapping
+    t = O.Tables.of(Mapping.identity(4))
+    packs = [O.Packed(t, A) for A in As]
+    per_step = sum(algorithmic_bytes_oracle(p, args.n) for p in packs)
+    for _ in range(args.warmup):
+        for p, B in zip(packs, Bs):
+            p.execute(B)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for p, B in zip(packs, Bs):
+            p.execute(B)
+    dt = time.perf_counter() - t0
+    v = per_step * args.steps / dt / 1e9
+    cores = O.max_threads()
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded row-skew sparse A, N(0,1) B)",
+            "config": {"workload": f"spmm_fp32_{args.m}x{args.k}_s{args.sparsity}_n{args.n}_x{args.replicas}",
+                       "replicas": args.replicas, "m": args.m, "k": args.k, "n": args.n, "sparsity": args.sparsity,
+                       "mr": 4, "mapping": "61fee"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"the full workload ({args.replicas} replicas) per step, restated reference "
+                                       "executor (oracle/spreg_oracle.c), OpenMP over all host threads"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import torch
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local if ws > 1 else 0)
+    torch.cuda.set_device(dev)
+
+    from oracle import oracle as O
+    from spreg import Mapping, MatMulSpecialized, PackedMatrix, TileConfig, synth
+
+    m = Mapping.identity(4)
+    As, Bs = make_inputs(args, rank)
+    packs, Bd, Cd = [], [], []
+    for A, B in zip(As, Bs):
+        packs.append(PackedMatrix.from_dense(torch.from_numpy(A).to(dev), m))
+        Bd.append(torch.from_numpy(B).to(dev))
+        Cd.append(torch.empty((args.m, args.n), device=dev))
+    torch.cuda.synchronize()
+    bytes_per = [p.algorithmic_bytes(args.n) for p in packs]
+    flops_per = [p.flops(args.n) for p in packs]
+    step_bytes, step_flops = sum(bytes_per), sum(flops_per)
+    working_set = step_bytes
+
+    # parity spot check of replica 0 against the oracle before timing anything
+    ref0 = O.Packed(O.Tables.of(m), As[0])
+    got0 = packs[0].execute(Bd[0], Cd[0], nr=args.nr).cpu().numpy()
+    parity_ok = bool(np.array_equal(got0.view(np.uint32), ref0.execute(Bs[0]).view(np.uint32)))
+
+    stream = torch.cuda.current_stream()
+
+    def step():
+        for p, B, C in zip(packs, Bd, Cd):
+            p.execute(B, C, nr=args.nr)
+
+    launches_per_step = len(packs)
+    graph = None
+    if not args.no_graph:
+        try:
+            s = torch.cuda.Stream()
+            s.wait_stream(torch.cuda.current_stream())
+            with torch.cuda.stream(s):
+                step()
+            torch.cuda.current_stream().wait_stream(s)
+            torch.cuda.synchronize()
+            graph = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(graph):
+                step()
+            torch.cuda.synchronize()
+        except Exception as e:  # capture unsupported: launch directly
+            print(f"graph capture failed ({e}); timing direct launches", file=sys.stderr)
+            graph = None
+
+    run = graph.replay if graph is not None else step
+    for _ in range(max(args.warmup, 3)):
+        run()
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev.index) as clk:
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            run()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    if ws > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+        torch.distributed.barrier()
+    sec = ms / 1e3
+    value = step_bytes * args.steps * ws / sec / 1e9
+    gflops = step_flops * args.steps * ws / sec / 1e9
+    ms_per_step = ms / args.steps
+
+    # roofline of the executor kernel (one launch per replica per step)
+    peak, peak_kind = measured_peaks()
+    launch_s = sec / (args.steps * launches_per_step)
+    achieved = (step_bytes / launches_per_step) / launch_s / 1e9
+    traffic = load_traffic()
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "peak_source": f"{peak_kind} hbm_gbs", "traffic": traffic,
+                "kernel": "spreg::exec_kernel<4,4,float,float,float>",
+                "algorithmic_bytes_per_launch": step_bytes / launches_per_step,
+                "flops_per_launch": step_flops / launches_per_step, "gflops": gflops,
+                "launch_us": launch_s * 1e6}
+
+    # e2e through the host-buffer C ABI (MatMulSpecialized operator()(C, B))
+    e2e_n = min(len(As), 16)
+    mms, Bh, Ch = [], [], []
+    for A, B in zip(As[:e2e_n], Bs[:e2e_n]):
+        rp, ci, v = synth.to_csr(A)
+        mms.append(MatMulSpecialized(args.m, args.k, args.n, v, rp, ci, TileConfig(nr=args.nr), 1, "", m))
+        Bh.append(torch.from_numpy(B).pin_memory())
+        Ch.append(torch.empty((args.m, args.n), dtype=torch.float32).pin_memory())
+    for mm, B, C in zip(mms, Bh, Ch):
+        mm(C, B)
+    e2e_ok = bool(np.array_equal(Ch[0].numpy(), ref0.execute(Bs[0]))) if parity_ok else False
+    e2e_steps = max(2, args.steps // 4)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        for mm, B, C in zip(mms, Bh, Ch):
+            mm(C, B)
+    e2e_sec = time.perf_counter() - t0
+    e2e_bytes = sum(bytes_per[:e2e_n]) * e2e_steps
+    e2e = {"value": e2e_bytes / e2e_sec / 1e9, "unit": UNIT,
+           "h2d_bytes_per_step": e2e_n * args.k * args.n * 4, "d2h_bytes_per_step": e2e_n * args.m * args.n * 4,
+           "path": "spreg_matmul_run (host B in, host C out, synchronous per SpMM)", "replicas_per_step": e2e_n,
+           "bit_exact_vs_oracle": e2e_ok}
+    del mms
+
+    cpu = None
+    if rank == 0:
+        cpu = cpu_baseline(As, Bs, args, args.cpu_seconds)
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded row-skew sparse A, N(0,1) B)",
+                "config": {"workload": f"spmm_fp32_{args.m}x{args.k}_s{args.sparsity}_n{args.n}_x{args.replicas}",
+                           "replicas": args.replicas, "m": args.m, "k": args.k, "n": args.n,
+                           "sparsity": args.sparsity, "mr": 4, "mapping": "61fee", "nr": args.nr or "auto",
+                           "cuda_graph": graph is not None,
+                           "l2": f"inputs larger than L2: working set {working_set / 2**20:.0f} MiB per step "
+                                 f"vs {L2_BYTES / 2**20:.0f} MiB L2",
+                           "parallelism": f"replicas x{ws}"},
+                "gflops": gflops, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+                "clocks": clk.summary(), "gpu_launches": launches_per_step * args.steps,
+                "parity_bit_exact_vs_oracle": parity_ok}
+        print(json.dumps(line))
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,237 @@
+/*
+ * spreg.h -- C ABI of the GB300 sparse-register-tiling SpMM library (libspreg.so).
+ *
+ * The library packs a pruned sparse weight A once ("inspector") and multiplies the packed
+ * form against dense B on an sm_103a GPU ("executor").  Every entry point takes plain
+ * pointers and sizes, returns an int status (SPREG_OK == 0) and never exits the process;
+ * the message of the last failure on the calling thread is spreg_last_error().
+ *
+ * Pointer convention: arrays named *_host are host memory; every other array pointer is
+ * device memory of the current CUDA device.  Every device entry point takes an explicit
+ * stream (a cudaStream_t; NULL is the legacy default stream).
+ *
+ * Reference interfaces this ABI replaces (paths inside the reference project):
+ *   - sbench/SOP/_C/pytorch_wrapper_intrin.cpp.template:84-98, 101-262, 351-392, 396-409
+ *     (sort_and_encode_patterns, SOPTile.pack_panel / pack_tile / padding, execute_tile)
+ *   - sbench/SOP/sop_driver.py:38-129 (make_sop_module, SOPModule.make_sop_tile)
+ *   - cpp_testbed/src/spmm/nano/SpMM_SOP.h:107-178 (sop::MatMulSpecialized constructor,
+ *     get_config, allocate_executor, operator()(C, B), require_storage)
+ *   - cpp_testbed/demo/count_nkerns.cpp:52-128 (tiled packer: M_c x K_c tiles, load_c)
+ */
+#ifndef SPREG_H
+#define SPREG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Same object as cudaStream_t; declared here so callers need no CUDA header. */
+typedef struct CUstream_st *spreg_stream_t;
+
+/* ---------------------------------------------------------------- status codes */
+enum {
+    SPREG_OK = 0,
+    SPREG_ERR_INVALID_ARG = 1, /* bad argument (reference: TORCH_CHECK failure) */
+    SPREG_ERR_CUDA = 2,        /* a CUDA runtime call failed */
+    SPREG_ERR_UNSUPPORTED = 3, /* valid request outside what this build supports */
+    SPREG_ERR_STATE = 4,       /* call out of order (e.g. execute before pack_tile) */
+    SPREG_ERR_CHECK = 5,       /* a device-side check failed (packer invariant, bad code) */
+    SPREG_ERR_NOMEM = 6        /* device allocation failed */
+};
+
+typedef enum {
+    SPREG_F32 = 0,  /* float */
+    SPREG_BF16 = 1, /* bfloat16, FP32 accumulation */
+    SPREG_F16 = 2   /* IEEE half with a power-of-two scale per row panel, FP32 accumulation */
+} spreg_dtype;
+
+/* Encoded id of the all-zero pattern; sorts after every nanokernel id (template:77). */
+#define SPREG_ZERO_PATTERN_ID 0xFFFF
+/* Largest supported panel height M_r (patterns are M_r-bit masks). */
+#define SPREG_MAX_MR 8
+
+/* Message of the last failed call on this thread ("" if none). */
+const char *spreg_last_error(void);
+/* Library version, major*10000 + minor*100 + patch. */
+int spreg_version(void);
+
+/* ------------------------------------------------- nanokernel set + pattern mapping
+ * A mapping sends every M_r-bit column pattern p in [0, 2^M_r) to a list of nanokernel
+ * patterns; the column is emitted once per listed pattern (sop_driver.py:50-65).  Lists
+ * live in map_codes[map_offsets[p] .. map_offsets[p+1]).  A listed 0 drops the column.
+ * The nanokernel set is `nanokernels` (the module's `patterns`, sop_driver.py:88-106) or,
+ * if NULL, every distinct nonzero pattern that the mapping lists.  Nanokernel ids are the
+ * set sorted by (popcount, value); that order is this library's definition of
+ * MicroKernel::encode_nkern_pattern, whose source is absent from the reference.
+ */
+typedef struct spreg_mapping spreg_mapping;
+
+int spreg_mapping_create(int32_t mr, const int32_t *map_offsets_host, const int32_t *map_codes_host,
+                         const int32_t *nanokernels_host, int32_t num_nanokernels, spreg_mapping **out);
+void spreg_mapping_destroy(spreg_mapping *m);
+int32_t spreg_mapping_mr(const spreg_mapping *m);
+/* MicroKernel::num_nkern_patterns() (template:44). */
+int32_t spreg_mapping_num_nkern(const spreg_mapping *m);
+/* out_host[id] = nanokernel pattern of id (MicroKernel::decode_nkern_pattern). */
+int spreg_mapping_nkern_patterns(const spreg_mapping *m, int32_t *out_host);
+/* MicroKernel::encode_nkern_pattern: id, SPREG_ZERO_PATTERN_ID for 0, -1 if not in the set. */
+int32_t spreg_mapping_encode(const spreg_mapping *m, int32_t pattern);
+
+/* sort_and_encode_patterns (template:84-98): encoded[i] = encode(pat_codes[order[i]]) with
+ * `order` the stable sort of the encoded ids, zero pattern last.  Device arrays of n. */
+int spreg_sort_and_encode_patterns(const spreg_mapping *m, const int32_t *pat_codes, int64_t n,
+                                   int32_t *encoded, int32_t *order, spreg_stream_t stream);
+
+/* ------------------------------------------------------------------ packed matrix
+ * A packed matrix is the reference's SOPTile arena (template:219-261): for every packed
+ * unit (one M_r-row panel, or one panel of one M_c x K_c tile) in order
+ *   [values | pad to 64 B | col_indices (int32) | pad to 64 B | nkern_counts (int32) | pad to 64 B]
+ * with values in ascending-row order per entry and entries stably sorted by nanokernel id.
+ * Units are ordered row tile, then K tile, then panel (count_nkerns.cpp:78-125).
+ */
+typedef struct spreg_packed spreg_packed;
+
+typedef struct {
+    int64_t values_off; /* byte offset of the unit's values in the arena */
+    int64_t cols_off;   /* byte offset of the unit's col_indices */
+    int64_t counts_off; /* byte offset of the unit's nkern_counts */
+    int32_t num_values; /* MicroKernelPackedData::num_nnz (includes padding zeros) */
+    int32_t num_cols;   /* MicroKernelPackedData::num_col_indices */
+} spreg_panel_desc;
+
+typedef struct {
+    int64_t rows, cols;        /* M, K of A */
+    int64_t num_panels;        /* ceil(M / M_r) row panels */
+    int64_t num_units;         /* packed units = descriptors */
+    int32_t mr, num_nkern;
+    int32_t m_tile, k_tile;    /* M_c, K_c (rows / columns per tile) */
+    int32_t num_k_tiles;       /* K tiles per row tile */
+    int32_t value_dtype;       /* spreg_dtype of the stored values */
+    int64_t col_offset;        /* added to every stored column index */
+    int64_t nnz;               /* nonzeros of A */
+    int64_t num_values;        /* sum of num_values (nnz + padding) */
+    int64_t num_col_indices;   /* sum of num_cols */
+    int64_t padding;           /* emitted zero values (SOPTile::padding) */
+    int64_t arena_bytes;       /* bytes of the arena */
+    int64_t required_storage;  /* reference bound sum(values + cols + counts + 3*64) (template:222-229) */
+    int64_t algorithmic_bytes; /* values + col indices + counts + descriptors + scales */
+    int64_t empty_units;       /* units of tiles with no nonzero (EMPTY_TILE, count_nkerns.cpp:114-117) */
+} spreg_packed_info;
+
+typedef struct {
+    int64_t rows, cols, nnz;
+    const int32_t *row_ptrs; /* rows + 1 */
+    const int32_t *col_inds; /* nnz, any order within a row, no duplicates */
+    const float *values;     /* nnz; explicit zeros are treated as zeros */
+} spreg_csr;
+
+typedef struct {
+    int32_t m_tile;      /* M_c, multiple of M_r; 0 = one row tile */
+    int32_t k_tile;      /* K_c; 0 = one K tile */
+    int64_t col_offset;  /* added to stored column indices (SOPTile.pack_panel col_offset) */
+    int32_t value_dtype; /* spreg_dtype of stored values */
+} spreg_pack_opts;
+
+/* Pack a CSR matrix (device arrays) -- the MicroKernelPacker / MatMulSpecialized inspector. */
+int spreg_pack_csr(const spreg_mapping *m, const spreg_csr *a, const spreg_pack_opts *opts,
+                   spreg_packed **out, spreg_stream_t stream);
+/* Pack a dense row-major M x K matrix (device, leading dimension lda); nonzeros define patterns. */
+int spreg_pack_dense(const spreg_mapping *m, const float *a, int64_t rows, int64_t cols, int64_t lda,
+                     const spreg_pack_opts *opts, spreg_packed **out, spreg_stream_t stream);
+void spreg_packed_destroy(spreg_packed *p);
+int spreg_packed_get_info(const spreg_packed *p, spreg_packed_info *info);
+/* Device pointers of the arena, the descriptors and (F16 only, else NULL) per-panel scales. */
+int spreg_packed_device_ptrs(const spreg_packed *p, const void **arena, const spreg_panel_desc **descs,
+                             const float **scales);
+/* Copy arena, descriptors and scales to host buffers (any may be NULL); synchronises `stream`. */
+int spreg_packed_to_host(const spreg_packed *p, void *arena_host, int64_t arena_bytes,
+                         spreg_panel_desc *descs_host, int64_t num_descs, float *scales_host,
+                         int64_t num_scales, spreg_stream_t stream);
+
+/* ---------------------------------------------------------- SOPTile (Python path)
+ * Mirrors SOPTile(rows, cols, num_panels).pack_panel(...) / pack_tile() / padding()
+ * (template:101-262).  pack_panel takes host arrays: n (code, column) entries in caller
+ * order and the panel's dense values, dense_panel_host[c * M_r + r] for c < panel_cols.
+ * pack_panel validates and stages; pack_tile runs the GPU packer over all panels.
+ */
+typedef struct spreg_tile spreg_tile;
+
+int spreg_tile_create(const spreg_mapping *m, int64_t rows, int64_t cols, int64_t num_panels,
+                      spreg_tile **out);
+int spreg_tile_pack_panel(spreg_tile *t, int64_t panel_id, int64_t col_offset, const int32_t *pat_codes_host,
+                          const int32_t *col_indices_host, int64_t n, const float *dense_panel_host,
+                          int64_t panel_cols);
+int spreg_tile_pack(spreg_tile *t, int32_t value_dtype, spreg_stream_t stream);
+/* Padding zeros of the packed tile (valid after spreg_tile_pack; -1 before). */
+int64_t spreg_tile_padding(const spreg_tile *t);
+/* The packed matrix of a packed tile (owned by the tile), NULL before spreg_tile_pack. */
+const spreg_packed *spreg_tile_packed(const spreg_tile *t);
+void spreg_tile_destroy(spreg_tile *t);
+
+/* ------------------------------------------------------------------------ executor */
+enum { SPREG_EPILOGUE_NONE = 0, SPREG_EPILOGUE_RELU = 1 };
+
+typedef struct {
+    const void *b;       /* K x ldb row-major, element type b_dtype (same family as the values) */
+    int64_t ldb;
+    void *c;             /* M x ldc row-major, element type c_dtype (F32 or BF16) */
+    int64_t ldc;
+    int64_t n;           /* columns of B and C to compute (N_c) */
+    int32_t b_dtype, c_dtype;
+    int32_t load_c;      /* 1: C += A.B (template:290-297 load_c) ; 0: C = A.B */
+    int32_t epilogue;    /* SPREG_EPILOGUE_* applied to the stored result */
+    int32_t nr;          /* columns per warp strip: 32, 64, 128 or 256; 0 = automatic */
+    int32_t warps_per_cta; /* 1..8; 0 = automatic */
+} spreg_exec_args;
+
+/* One SpMM: C (+)= A . B over the first n columns -- sop_multiple_panel_executor (template:265-305). */
+int spreg_execute(const spreg_packed *a, const spreg_exec_args *args, spreg_stream_t stream);
+
+/* Many SpMMs of uneven shape in ONE launch, from a (matrix, panel, column-strip) work list. */
+typedef struct {
+    const spreg_packed *a;
+    spreg_exec_args args;
+} spreg_work_item;
+
+int spreg_execute_batched(const spreg_work_item *items_host, int32_t num_items, spreg_stream_t stream);
+
+/* execute_tile (template:351-392): C = A.B over n_c columns, timed: warm-up num_runs runs,
+ * then 150 x num_runs timed runs; *median_ns = median per-run time in nanoseconds. */
+int spreg_execute_timed(const spreg_packed *a, const spreg_exec_args *args, int64_t num_runs,
+                        double *median_ns, spreg_stream_t stream);
+
+/* ------------------------------------------- MatMulSpecialized (C++ path, host buffers) */
+typedef struct {
+    int32_t m_tile, k_tile, n_tile; /* M_c, K_c, N_c (SOPConfig m_tile/k_tile/n_tile) */
+    int32_t nr;                     /* columns per warp strip, 0 = automatic */
+    int32_t outer_schedule;         /* KNM=0, NKM=1, ... accepted; the GPU grid order is fixed */
+    int32_t value_dtype;            /* spreg_dtype of stored values */
+    int32_t sparse_a, tiling_strategy, beta_10x; /* accepted and reported; no GPU effect */
+} spreg_tile_config;
+
+typedef struct spreg_matmul spreg_matmul;
+
+/* sop::MatMulSpecialized(m, k, n, values, row_ptrs, col_inds, TileConfig, ...) with HOST CSR. */
+int spreg_matmul_create(int32_t m, int32_t k, int32_t n, const float *values_host, const int32_t *row_ptrs_host,
+                        const int32_t *col_inds_host, const spreg_tile_config *cfg, const spreg_mapping *map,
+                        spreg_matmul **out);
+/* allocate_executor(n): device staging for B (k x n) and C (m x n). */
+int spreg_matmul_allocate_executor(spreg_matmul *mm, int32_t n);
+/* operator()(C, B) with HOST buffers: copy B in, C = A.B, copy C out (synchronous). */
+int spreg_matmul_run(spreg_matmul *mm, float *c_host, const float *b_host);
+/* Same on device buffers (ldb = ldc = n), asynchronous on `stream`. */
+int spreg_matmul_run_device(spreg_matmul *mm, float *c, const float *b, spreg_stream_t stream);
+int spreg_matmul_get_config(const spreg_matmul *mm, spreg_tile_config *cfg);
+/* require_storage: the packed bound (template:222-229 summed over tiles). */
+int64_t spreg_matmul_required_storage(const spreg_matmul *mm);
+const spreg_packed *spreg_matmul_packed(const spreg_matmul *mm);
+void spreg_matmul_destroy(spreg_matmul *mm);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPREG_H */
