@@ -50,8 +50,14 @@ def parse():
     ap.add_argument("--n", type=int, default=512)
     ap.add_argument("--sparsity", type=float, default=0.9)
     ap.add_argument("--nr", type=int, default=0)
+    ap.add_argument("--staging", type=int, default=0, help="0 auto, 1 shared-memory B strips, 2 L1/L2")
+    ap.add_argument("--meta", type=int, default=0, help="0 auto, 1 execution-layout kernel, 2 register streams")
+    ap.add_argument("--dtype", choices=["f32", "bf16"], default="f32",
+                    help="storage of A values and B (FP32 accumulation and FP32 C either way)")
     ap.add_argument("--no-graph", action="store_true")
-    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--batched", type=int, default=1, help="1: one batched launch per step; 0: one launch per SpMM")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline budget; 0 skips it")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end leg")
     return ap.parse_args()
 
 
@@ -242,29 +248,38 @@ def main():
 
     m = Mapping.identity(4)
     As, Bs = make_inputs(args, rank)
+    vd = spreg_dtype = (0 if args.dtype == "f32" else 1)
+    tdt = torch.float32 if args.dtype == "f32" else torch.bfloat16
     packs, Bd, Cd = [], [], []
     for A, B in zip(As, Bs):
-        packs.append(PackedMatrix.from_dense(torch.from_numpy(A).to(dev), m))
-        Bd.append(torch.from_numpy(B).to(dev))
+        packs.append(PackedMatrix.from_dense(torch.from_numpy(A).to(dev), m, value_dtype=vd))
+        Bd.append(torch.from_numpy(B).to(dev).to(tdt))
         Cd.append(torch.empty((args.m, args.n), device=dev))
     torch.cuda.synchronize()
-    bytes_per = [p.algorithmic_bytes(args.n) for p in packs]
+    bsz = 4 if args.dtype == "f32" else 2
+    bytes_per = [p.algorithmic_bytes(args.n, b_bytes=bsz) for p in packs]
     flops_per = [p.flops(args.n) for p in packs]
     step_bytes, step_flops = sum(bytes_per), sum(flops_per)
     working_set = step_bytes
 
     # parity spot check of replica 0 against the oracle before timing anything
-    ref0 = O.Packed(O.Tables.of(m), As[0])
-    got0 = packs[0].execute(Bd[0], Cd[0], nr=args.nr).cpu().numpy()
-    parity_ok = bool(np.array_equal(got0.view(np.uint32), ref0.execute(Bs[0]).view(np.uint32)))
+    ref0 = O.Packed(O.Tables.of(m), As[0], value_dtype=spreg_dtype)
+    got0 = packs[0].execute(Bd[0], Cd[0], nr=args.nr, staging=args.staging, meta=args.meta).cpu().numpy()
+    B0ref = Bs[0] if args.dtype == "f32" else Bd[0].cpu().view(torch.int16).numpy().view(np.uint16)
+    parity_ok = bool(np.array_equal(got0.view(np.uint32), ref0.execute(B0ref).view(np.uint32)))
 
     stream = torch.cuda.current_stream()
+    from spreg.packed import execute_batched
+    work = [(p, B, C, dict(nr=args.nr, meta=args.meta)) for p, B, C in zip(packs, Bd, Cd)]
 
     def step():
-        for p, B, C in zip(packs, Bd, Cd):
-            p.execute(B, C, nr=args.nr)
+        if args.batched:
+            execute_batched(work)  # all replicas in one launch of the persistent kernel
+        else:
+            for p, B, C in zip(packs, Bd, Cd):
+                p.execute(B, C, nr=args.nr, staging=args.staging, meta=args.meta)
 
-    launches_per_step = len(packs)
+    launches_per_step = 1 if args.batched else len(packs)
     graph = None
     if not args.no_graph:
         try:
@@ -311,16 +326,19 @@ def main():
     peak, peak_kind = measured_peaks()
     launch_s = sec / (args.steps * launches_per_step)
     achieved = (step_bytes / launches_per_step) / launch_s / 1e9
+    spmm_us = sec / (args.steps * len(packs)) * 1e6
     traffic = load_traffic()
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "peak_source": f"{peak_kind} hbm_gbs", "traffic": traffic,
-                "kernel": "spreg::exec_kernel<4,4,float,float,float>",
+                "kernel": "spreg::exec_batch_kernel<4,NV,%s>" % ("float,float,float" if args.dtype == "f32" else
+                                                                  "bf16,bf16,float"),
+                "spmm_us": spmm_us, "launches_per_step": launches_per_step,
                 "algorithmic_bytes_per_launch": step_bytes / launches_per_step,
                 "flops_per_launch": step_flops / launches_per_step, "gflops": gflops,
                 "launch_us": launch_s * 1e6}
 
     # e2e through the host-buffer C ABI (MatMulSpecialized operator()(C, B))
-    e2e_n = min(len(As), 16)
+    e2e_n = 0 if (args.no_e2e or args.dtype != "f32") else min(len(As), 16)
     mms, Bh, Ch = [], [], []
     for A, B in zip(As[:e2e_n], Bs[:e2e_n]):
         rp, ci, v = synth.to_csr(A)
@@ -329,7 +347,7 @@ def main():
         Ch.append(torch.empty((args.m, args.n), dtype=torch.float32).pin_memory())
     for mm, B, C in zip(mms, Bh, Ch):
         mm(C, B)
-    e2e_ok = bool(np.array_equal(Ch[0].numpy(), ref0.execute(Bs[0]))) if parity_ok else False
+    e2e_ok = bool(np.array_equal(Ch[0].numpy(), ref0.execute(Bs[0]))) if (parity_ok and e2e_n) else False
     e2e_steps = max(2, args.steps // 4)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -338,24 +356,25 @@ def main():
             mm(C, B)
     e2e_sec = time.perf_counter() - t0
     e2e_bytes = sum(bytes_per[:e2e_n]) * e2e_steps
-    e2e = {"value": e2e_bytes / e2e_sec / 1e9, "unit": UNIT,
+    e2e = {"value": e2e_bytes / e2e_sec / 1e9 if e2e_n else None, "unit": UNIT,
            "h2d_bytes_per_step": e2e_n * args.k * args.n * 4, "d2h_bytes_per_step": e2e_n * args.m * args.n * 4,
            "path": "spreg_matmul_run (host B in, host C out, synchronous per SpMM)", "replicas_per_step": e2e_n,
            "bit_exact_vs_oracle": e2e_ok}
     del mms
 
     cpu = None
-    if rank == 0:
+    if rank == 0 and args.cpu_seconds > 0:
         cpu = cpu_baseline(As, Bs, args, args.cpu_seconds)
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded row-skew sparse A, N(0,1) B)",
-                "config": {"workload": f"spmm_fp32_{args.m}x{args.k}_s{args.sparsity}_n{args.n}_x{args.replicas}",
+                "vs_baseline": None, "dtype": args.dtype, "data": "synthetic (seeded row-skew sparse A, N(0,1) B)",
+                "config": {"workload": f"spmm_{args.dtype}_{args.m}x{args.k}_s{args.sparsity}_n{args.n}_x{args.replicas}",
                            "replicas": args.replicas, "m": args.m, "k": args.k, "n": args.n,
                            "sparsity": args.sparsity, "mr": 4, "mapping": "61fee", "nr": args.nr or "auto",
-                           "cuda_graph": graph is not None,
+                           "b_staging": {0: "auto", 1: "shared-memory strips", 2: "L1/L2"}[args.staging],
+                           "cuda_graph": graph is not None, "batched_launch": bool(args.batched),
                            "l2": f"inputs larger than L2: working set {working_set / 2**20:.0f} MiB per step "
                                  f"vs {L2_BYTES / 2**20:.0f} MiB L2",
                            "parallelism": f"replicas x{ws}"},

@@ -184,7 +184,10 @@ typedef struct {
     int32_t load_c;      /* 1: C += A.B (template:290-297 load_c) ; 0: C = A.B */
     int32_t epilogue;    /* SPREG_EPILOGUE_* applied to the stored result */
     int32_t nr;          /* columns per warp strip: 32, 64, 128 or 256; 0 = automatic */
-    int32_t warps_per_cta; /* 1..8; 0 = automatic */
+    int32_t warps_per_cta; /* 1..8 for the L1/L2 kernel; 0 = automatic */
+    int32_t b_staging;   /* 0 automatic, 1 stage B strips in shared memory (bulk copies), 2 read B via L1/L2 */
+    int32_t meta_staging; /* 0 automatic, 1 stage each panel's execution block in shared memory, 2 stream
+                             the packed arena through registers */
 } spreg_exec_args;
 
 /* One SpMM: C (+)= A . B over the first n columns -- sop_multiple_panel_executor (template:265-305). */
@@ -197,6 +200,10 @@ typedef struct {
 } spreg_work_item;
 
 int spreg_execute_batched(const spreg_work_item *items_host, int32_t num_items, spreg_stream_t stream);
+
+/* Status word of the current device: nonzero once a kernel gave up a bounded wait (its results
+ * are then incomplete).  Synchronous; reset != 0 clears it. */
+int spreg_device_status(int32_t *status_host, int32_t reset);
 
 /* execute_tile (template:351-392): C = A.B over n_c columns, timed: warm-up num_runs runs,
  * then 150 x num_runs timed runs; *median_ns = median per-run time in nanoseconds. */

@@ -27,6 +27,7 @@ void packed_release(spreg_packed *);
 int execute_impl(const spreg_packed *, const spreg_exec_args *, cudaStream_t);
 int execute_timed_impl(const spreg_packed *, const spreg_exec_args *, int64_t, double *, cudaStream_t);
 int execute_batched_impl(const spreg_work_item *, int32_t, cudaStream_t);
+int device_status_impl(int32_t *, int);
 
 static std::mutex g_map_mu;
 
@@ -349,6 +350,11 @@ int spreg_execute(const spreg_packed *a, const spreg_exec_args *args, spreg_stre
 int spreg_execute_batched(const spreg_work_item *items, int32_t num_items, spreg_stream_t stream) {
     clear_error();
     return execute_batched_impl(items, num_items, (cudaStream_t)stream);
+}
+
+int spreg_device_status(int32_t *status, int32_t reset) {
+    clear_error();
+    return device_status_impl(status, reset);
 }
 
 int spreg_execute_timed(const spreg_packed *a, const spreg_exec_args *args, int64_t num_runs, double *median_ns,

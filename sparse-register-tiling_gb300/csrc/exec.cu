@@ -1,7 +1,18 @@
-// exec.cu -- host side of the executor: argument checks, strip-width choice, launches.
+// exec.cu -- host side of the executor: argument checks, strip widths, work lists, launches.
+//
+// Every SpMM call becomes one or two "problems" of the batched persistent kernel
+// (exec_batch_kernel): whole column strips of 32 * NV columns, plus an NV = 1 problem for the
+// columns past the last whole strip.  spreg_execute_batched groups the problems of many SpMMs by
+// kernel configuration (M_r, NV, data types) and runs each group in one launch.  Packs whose
+// execution blocks do not fit the per-warp buffers, or calls that ask for it (meta_staging = 2),
+// run the register-stream kernel (exec_kernel) instead.
 #include "exec_kernel.cuh"
 
 #include <algorithm>
+#include <atomic>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <vector>
 
 namespace spreg {
@@ -39,26 +50,102 @@ cudaError_t launch_mr(int mr, const ExecParams &p, int nv, int combo, dim3 grid,
     }
 }
 
+template <int MR>
+cudaError_t launch_combo_batch(const BatchParams &p, int nv, int combo, unsigned grid, int threads, size_t smem,
+                               cudaStream_t s) {
+    switch (combo) {
+    case COMBO_F32: return launch_exec_batch<MR, COMBO_F32>(p, nv, grid, threads, smem, s);
+    case COMBO_BF16_F32OUT: return launch_exec_batch<MR, COMBO_BF16_F32OUT>(p, nv, grid, threads, smem, s);
+    case COMBO_BF16_BF16OUT: return launch_exec_batch<MR, COMBO_BF16_BF16OUT>(p, nv, grid, threads, smem, s);
+    case COMBO_F16_F32OUT: return launch_exec_batch<MR, COMBO_F16_F32OUT>(p, nv, grid, threads, smem, s);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_mr_batch(int mr, const BatchParams &p, int nv, int combo, unsigned grid, int threads, size_t smem,
+                            cudaStream_t s) {
+    switch (mr) {
+    case 2: return launch_combo_batch<2>(p, nv, combo, grid, threads, smem, s);
+    case 4: return launch_combo_batch<4>(p, nv, combo, grid, threads, smem, s);
+    case 6: return launch_combo_batch<6>(p, nv, combo, grid, threads, smem, s);
+    case 8: return launch_combo_batch<8>(p, nv, combo, grid, threads, smem, s);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
 }  // namespace
 
-// Floats per lane chosen automatically: wide strips amortise the per-entry index and value
-// loads over more columns, narrow strips give more warps when N is small.
-int auto_nv(int64_t n, int64_t panels) {
+// ------------------------------------------------------------------ per-device facts
+struct DevFacts {
+    int sms = 0;
+    int smem_optin = 0;
+    int smem_per_sm = 0;
+    int *status = nullptr;     // status word of bounded waits
+    int *counters = nullptr;   // work counters handed out round robin, one per launch
+};
+constexpr int kCounters = 4096;
+
+int dev_facts(DevFacts **out) {
+    static DevFacts facts[64];
+    static std::mutex mu;
+    int dev = 0;
+    SPREG_CUDA(cudaGetDevice(&dev));
+    SPREG_CHECK_ARG(dev >= 0 && dev < 64, "device ordinal %d out of range", dev);
+    std::lock_guard<std::mutex> lk(mu);
+    DevFacts &f = facts[dev];
+    if (!f.status) {
+        SPREG_CUDA(cudaDeviceGetAttribute(&f.sms, cudaDevAttrMultiProcessorCount, dev));
+        SPREG_CUDA(cudaDeviceGetAttribute(&f.smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+        SPREG_CUDA(cudaDeviceGetAttribute(&f.smem_per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
+        if (f.smem_optin > kMaxSmem) f.smem_optin = kMaxSmem;
+        int *buf = nullptr;
+        SPREG_CUDA(cudaMalloc(&buf, sizeof(int) * (1 + kCounters)));
+        SPREG_CUDA(cudaMemset(buf, 0, sizeof(int) * (1 + kCounters)));
+        f.status = buf;
+        f.counters = buf + 1;
+    }
+    *out = &f;
+    return SPREG_OK;
+}
+
+int *next_counter(DevFacts *f) {
+    static std::atomic<unsigned> next{0};
+    return f->counters + (next.fetch_add(1) % kCounters);
+}
+
+int device_status_impl(int32_t *status, int reset) {
+    DevFacts *f;
+    int st = dev_facts(&f);
+    if (st) return st;
+    int v = 0;
+    SPREG_CUDA(cudaMemcpy(&v, f->status, sizeof(int), cudaMemcpyDeviceToHost));
+    if (reset) SPREG_CUDA(cudaMemset(f->status, 0, sizeof(int)));
+    if (status) *status = v;
+    return SPREG_OK;
+}
+
+// Columns per lane (strip width / 32) chosen automatically: wide strips amortise the per-entry
+// index and value loads over more columns, narrow strips give more items when the problem is small.
+int auto_nv(int64_t n, int64_t panels, int sms) {
     int nv = 1;
     if (n >= 64) nv = 2;
     if (n >= 128) nv = 4;
-    // keep at least ~4 warps per SM of work
-    while (nv > 1 && panels * ((n + 32 * nv - 1) / (32 * nv)) < 152 * 4) nv >>= 1;
+    while (nv > 1 && panels * (n / (32 * nv)) < (int64_t)sms * 8) nv >>= 1;
     return nv;
 }
 
-struct LaunchPlan {
-    ExecParams p;
-    int mr, combo, nv, warps;
-    int64_t n_main;  // columns covered by the NV launch (whole strips)
+// ------------------------------------------------------------------ one call -> problems
+struct CallPlan {
+    int mr, combo, nv;
+    bool stream_kernel;      // run exec_kernel (register streams) instead of the batch kernel
+    XProblem main, tail;     // whole strips (NV) and the NV = 1 remainder
+    bool has_main, has_tail;
+    int64_t xbuf;            // per-warp buffer for this pack
+    ExecParams sp;           // parameters of the register-stream kernel
+    int warps;
 };
 
-int plan_exec(const spreg_packed *a, const spreg_exec_args *args, LaunchPlan *lp) {
+int plan_call(const spreg_packed *a, const spreg_exec_args *args, CallPlan *cp) {
     SPREG_CHECK_ARG(a && args, "null packed matrix or args");
     const spreg_packed_info &in = a->info;
     const int combo = combo_of(in.value_dtype, args->b_dtype, args->c_dtype);
@@ -66,26 +153,71 @@ int plan_exec(const spreg_packed *a, const spreg_exec_args *args, LaunchPlan *lp
                     "C is F32, or BF16 for BF16 values)", in.value_dtype, args->b_dtype, args->c_dtype);
     SPREG_CHECK_ARG(args->n >= 0, "n must be >= 0");
     SPREG_CHECK_ARG(args->n == 0 || in.rows == 0 || (args->c && (args->b || in.cols == 0)), "null B or C");
-    SPREG_CHECK_ARG(args->ldb >= args->n || in.cols == 0, "ldb (%lld) < n (%lld)", (long long)args->ldb, (long long)args->n);
+    SPREG_CHECK_ARG(args->ldb >= args->n || in.cols == 0, "ldb (%lld) < n (%lld)", (long long)args->ldb,
+                    (long long)args->n);
     SPREG_CHECK_ARG(args->ldc >= args->n, "ldc (%lld) < n (%lld)", (long long)args->ldc, (long long)args->n);
     SPREG_CHECK_ARG(args->epilogue == SPREG_EPILOGUE_NONE || args->epilogue == SPREG_EPILOGUE_RELU, "bad epilogue");
+    SPREG_CHECK_ARG(args->meta_staging >= 0 && args->meta_staging <= 2, "meta_staging must be 0, 1 or 2");
+    SPREG_CHECK_ARG(args->b_staging >= 0 && args->b_staging <= 2, "b_staging must be 0, 1 or 2");
+    SPREG_CHECK_ARG(args->b_staging != 1, "B strip staging in shared memory is not offered: it measured slower "
+                    "than L1/L2 reads of B at every size tried");
+    int dev = -1;
+    SPREG_CUDA(cudaGetDevice(&dev));
+    SPREG_CHECK_ARG(dev == a->device, "packed matrix lives on device %d, current device is %d", a->device, dev);
+    DevFacts *f;
+    int st = dev_facts(&f);
+    if (st) return st;
     int nv;
     switch (args->nr) {
-    case 0: nv = auto_nv(args->n, in.num_panels); break;
+    case 0: nv = auto_nv(args->n, in.num_panels, f->sms); break;
     case 32: nv = 1; break;
     case 64: nv = 2; break;
     case 128: nv = 4; break;
-    case 256: nv = 8; break;
-    default: SPREG_FAIL(SPREG_ERR_INVALID_ARG, "nr must be 0, 32, 64, 128 or 256 (got %d)", args->nr);
+    default: SPREG_FAIL(SPREG_ERR_INVALID_ARG, "nr must be 0, 32, 64 or 128 (got %d)", args->nr);
     }
     const size_t bsz = dtype_bytes(args->b_dtype), csz = dtype_bytes(args->c_dtype);
     while (nv > 1 && !(aligned(args->b, bsz * nv) && args->ldb % nv == 0 && aligned(args->c, csz * nv) &&
                        args->ldc % nv == 0))
         nv >>= 1;
-    int warps = args->warps_per_cta > 0 ? args->warps_per_cta : 4;
-    SPREG_CHECK_ARG(warps >= 1 && warps <= 8, "warps_per_cta must be in [1, 8]");
+    cp->mr = in.mr;
+    cp->combo = combo;
+    cp->nv = nv;
+    cp->warps = args->warps_per_cta > 0 ? args->warps_per_cta : 4;
+    SPREG_CHECK_ARG(cp->warps >= 1 && cp->warps <= 8, "warps_per_cta must be in [1, 8]");
+    const int64_t n_main = (args->n / (32 * nv)) * (32 * nv);
+    cp->xbuf = (a->max_exec_bytes + 127) / 128 * 128;
+    const bool x_fits = a->exec && 1024 + 2 * cp->xbuf <= f->smem_optin;
+    SPREG_CHECK_ARG(args->meta_staging != 1 || x_fits, "the execution-layout kernel cannot run this pack "
+                    "(largest block %lld bytes)", (long long)a->max_exec_bytes);
+    cp->stream_kernel = args->meta_staging == 2 || !x_fits;
 
-    ExecParams &p = lp->p;
+    XProblem base = {};
+    base.exec = a->exec;
+    base.exec_offs = a->exec_offs;
+    base.scales = a->scales;
+    base.B = args->b;
+    base.C = args->c;
+    base.ldb = args->ldb;
+    base.ldc = args->ldc;
+    base.M = in.rows;
+    base.P = (int32_t)a->geom.P;
+    base.T = (int32_t)a->geom.T;
+    base.ppt = (int32_t)a->geom.ppt;
+    base.load_c = args->load_c ? 1 : 0;
+    base.epilogue = args->epilogue;
+    cp->has_main = n_main > 0 && base.P > 0;
+    cp->has_tail = args->n > n_main && base.P > 0;
+    cp->main = base;
+    cp->main.col_begin = 0;
+    cp->main.col_end = n_main;
+    cp->main.S = (int32_t)(n_main / (32 * nv));
+    cp->tail = base;
+    cp->tail.col_begin = n_main;
+    cp->tail.col_end = args->n;
+    cp->tail.S = (int32_t)((args->n - n_main + 31) / 32);
+
+    ExecParams &p = cp->sp;
+    p = ExecParams{};
     p.arena = a->arena;
     p.descs = a->descs;
     p.scales = a->scales;
@@ -95,76 +227,133 @@ int plan_exec(const spreg_packed *a, const spreg_exec_args *args, LaunchPlan *lp
     p.ldc = args->ldc;
     p.M = in.rows;
     p.N = args->n;
-    p.col_begin = 0;
     p.P = a->geom.P;
     p.ppt = a->geom.ppt;
     p.T = a->geom.T;
     p.nk = in.num_nkern;
     p.load_c = args->load_c ? 1 : 0;
     p.epilogue = args->epilogue;
-    p.pad_ = 0;
+    p.status = f->status;
     for (int i = 0; i < 256; ++i) p.id_pattern[i] = a->id_to_pattern[i];
-    lp->mr = in.mr;
-    lp->combo = combo;
-    lp->nv = nv;
-    lp->warps = warps;
-    lp->n_main = nv > 1 ? (args->n / (32 * nv)) * (32 * nv) : 0;
     return SPREG_OK;
 }
 
-int launch_plan(const LaunchPlan &lp, cudaStream_t stream) {
-    if (lp.p.N == 0 || lp.p.P == 0) return SPREG_OK;
-    const unsigned gx = (unsigned)((lp.p.P + lp.warps - 1) / lp.warps);
-    const int threads = 32 * lp.warps;
-    SPREG_CHECK_ARG(gx <= 0x7FFFFFFFu, "too many panels");
-    if (lp.n_main > 0) {
-        const int64_t gy = lp.n_main / (32 * lp.nv);
-        SPREG_CHECK_ARG(gy <= 65535, "n too large for one launch");
-        ExecParams p = lp.p;
+// Register-stream kernel for one call: NV launch over whole strips, NV = 1 launch for the rest.
+int launch_stream(const CallPlan &cp, cudaStream_t stream) {
+    const unsigned gx = (unsigned)((cp.sp.P + cp.warps - 1) / cp.warps);
+    const int threads = 32 * cp.warps;
+    if (cp.has_main) {
+        ExecParams p = cp.sp;
         p.col_begin = 0;
-        cudaError_t e = launch_mr(lp.mr, p, lp.nv, lp.combo, dim3(gx, (unsigned)gy), threads, stream);
-        if (e != cudaSuccess) SPREG_FAIL(SPREG_ERR_CUDA, "executor launch: %s", cudaGetErrorString(e));
-    }
-    const int64_t tail = lp.p.N - lp.n_main;
-    if (tail > 0) {
-        const int64_t gy = (tail + 31) / 32;
+        const int64_t gy = cp.main.S;
         SPREG_CHECK_ARG(gy <= 65535, "n too large for one launch");
-        ExecParams p = lp.p;
-        p.col_begin = lp.n_main;
-        cudaError_t e = launch_mr(lp.mr, p, 1, lp.combo, dim3(gx, (unsigned)gy), threads, stream);
+        cudaError_t e = launch_mr(cp.mr, p, cp.nv, cp.combo, dim3(gx, (unsigned)gy), threads, stream);
         if (e != cudaSuccess) SPREG_FAIL(SPREG_ERR_CUDA, "executor launch: %s", cudaGetErrorString(e));
     }
+    if (cp.has_tail) {
+        ExecParams p = cp.sp;
+        p.col_begin = cp.tail.col_begin;
+        const int64_t gy = cp.tail.S;
+        SPREG_CHECK_ARG(gy <= 65535, "n too large for one launch");
+        cudaError_t e = launch_mr(cp.mr, p, 1, cp.combo, dim3(gx, (unsigned)gy), threads, stream);
+        if (e != cudaSuccess) SPREG_FAIL(SPREG_ERR_CUDA, "executor launch: %s", cudaGetErrorString(e));
+    }
+    return SPREG_OK;
+}
+
+// One batch-kernel launch per group of at most kMaxBatchProblems problems of one configuration.
+struct Group {
+    int mr, combo, nv;
+    std::vector<XProblem> probs;
+    int64_t xbuf = 0;
+};
+
+int launch_groups(std::map<std::tuple<int, int, int>, Group> &groups, cudaStream_t stream) {
+    DevFacts *f;
+    int st = dev_facts(&f);
+    if (st) return st;
+    for (auto &kv : groups) {
+        Group &g = kv.second;
+        for (size_t first = 0; first < g.probs.size(); first += kMaxBatchProblems) {
+            const size_t cnt = std::min<size_t>(kMaxBatchProblems, g.probs.size() - first);
+            BatchParams bp;
+            bp.nprob = (int32_t)cnt;
+            int64_t items = 0;
+            for (size_t i = 0; i < cnt; ++i) {
+                bp.prob[i] = g.probs[first + i];
+                bp.prob[i].item_begin = items;
+                items += (int64_t)bp.prob[i].P * bp.prob[i].S;
+            }
+            if (items == 0) continue;
+            SPREG_CHECK_ARG(items <= INT32_MAX, "too many work items in one launch");
+            bp.items = items;
+            bp.xbuf = (int32_t)g.xbuf;
+            bp.status = f->status;
+            bp.counter = next_counter(f);
+            // warps per CTA: 8, fewer if the buffers do not fit
+            int nw = 8;
+            while (nw > 1 && 1024 + 2 * g.xbuf * nw > f->smem_optin) nw >>= 1;
+            const size_t smem = (size_t)(1024 + 2 * g.xbuf * nw);
+            const int threads = 32 * nw;
+            const int per_sm = std::max(1, std::min((int)(f->smem_per_sm / (int64_t)smem), 2048 / threads));
+            const int64_t ctas = std::min<int64_t>((int64_t)f->sms * per_sm, (items + nw - 1) / nw);
+            SPREG_CUDA(cudaMemsetAsync(bp.counter, 0, sizeof(int), stream));
+            cudaError_t e = launch_mr_batch(g.mr, bp, g.nv, g.combo, (unsigned)ctas, threads, smem, stream);
+            if (e != cudaSuccess) SPREG_FAIL(SPREG_ERR_CUDA, "batched executor launch: %s", cudaGetErrorString(e));
+        }
+    }
+    return SPREG_OK;
+}
+
+void add_call(std::map<std::tuple<int, int, int>, Group> &groups, const CallPlan &cp) {
+    auto add = [&](const XProblem &pr, int nv) {
+        Group &g = groups[std::make_tuple(cp.mr, cp.combo, nv)];
+        g.mr = cp.mr;
+        g.combo = cp.combo;
+        g.nv = nv;
+        g.probs.push_back(pr);
+        g.xbuf = std::max(g.xbuf, cp.xbuf);
+    };
+    if (cp.has_main) add(cp.main, cp.nv);
+    if (cp.has_tail) add(cp.tail, 1);
+}
+
+int run_calls(const spreg_packed *const *as, const spreg_exec_args *const *args, int32_t n, cudaStream_t stream) {
+    std::map<std::tuple<int, int, int>, Group> groups;
+    std::vector<CallPlan> streams;
+    for (int32_t i = 0; i < n; ++i) {
+        CallPlan cp;
+        int st = plan_call(as[i], args[i], &cp);
+        if (st != SPREG_OK) return st;
+        if (cp.stream_kernel) streams.push_back(cp);
+        else add_call(groups, cp);
+    }
+    int st = launch_groups(groups, stream);
+    if (st != SPREG_OK) return st;
+    for (const CallPlan &cp : streams)
+        if ((st = launch_stream(cp, stream))) return st;
     return SPREG_OK;
 }
 
 int execute_impl(const spreg_packed *a, const spreg_exec_args *args, cudaStream_t stream) {
-    LaunchPlan lp;
-    int st = plan_exec(a, args, &lp);
-    if (st != SPREG_OK) return st;
-    int dev = -1;
-    SPREG_CUDA(cudaGetDevice(&dev));
-    SPREG_CHECK_ARG(dev == a->device, "packed matrix lives on device %d, current device is %d", a->device, dev);
-    return launch_plan(lp, stream);
+    return run_calls(&a, &args, 1, stream);
 }
 
 int execute_timed_impl(const spreg_packed *a, const spreg_exec_args *args, int64_t num_runs, double *median_ns,
                        cudaStream_t stream) {
     SPREG_CHECK_ARG(median_ns, "null median_ns");
     SPREG_CHECK_ARG(num_runs >= 1, "num_runs must be >= 1");
-    LaunchPlan lp;
-    int st = plan_exec(a, args, &lp);
-    if (st != SPREG_OK) return st;
+    int st;
     const int kIters = 150;  // MEASURED_ITERATIONS of template:317
     for (int64_t r = 0; r < num_runs; ++r)
-        if ((st = launch_plan(lp, stream))) return st;
+        if ((st = execute_impl(a, args, stream))) return st;
     std::vector<cudaEvent_t> ev(2 * kIters);
     for (auto &e : ev) SPREG_CUDA(cudaEventCreate(&e));
-    for (int it = 0; it < kIters; ++it) {
+    st = SPREG_OK;
+    for (int it = 0; it < kIters && !st; ++it) {
         cudaEventRecord(ev[2 * it], stream);
-        for (int64_t r = 0; r < num_runs; ++r)
-            if ((st = launch_plan(lp, stream))) break;
+        for (int64_t r = 0; r < num_runs && !st; ++r) st = execute_impl(a, args, stream);
         cudaEventRecord(ev[2 * it + 1], stream);
-        if (st) break;
     }
     cudaError_t e = cudaStreamSynchronize(stream);
     std::vector<double> t(kIters);
@@ -183,16 +372,13 @@ int execute_timed_impl(const spreg_packed *a, const spreg_exec_args *args, int64
 
 int execute_batched_impl(const spreg_work_item *items, int32_t n, cudaStream_t stream) {
     SPREG_CHECK_ARG(n >= 0 && (n == 0 || items), "bad work list");
-    std::vector<LaunchPlan> plans((size_t)n);
+    std::vector<const spreg_packed *> as((size_t)n);
+    std::vector<const spreg_exec_args *> args((size_t)n);
     for (int32_t i = 0; i < n; ++i) {
-        int st = plan_exec(items[i].a, &items[i].args, &plans[i]);
-        if (st != SPREG_OK) return st;
+        as[i] = items[i].a;
+        args[i] = &items[i].args;
     }
-    for (int32_t i = 0; i < n; ++i) {
-        int st = launch_plan(plans[i], stream);
-        if (st != SPREG_OK) return st;
-    }
-    return SPREG_OK;
+    return run_calls(as.data(), args.data(), n, stream);
 }
 
 }  // namespace spreg

@@ -28,6 +28,12 @@ struct ExecParams {
     int64_t ldb, ldc, M, N;
     int64_t col_begin;  // first column handled by this launch
     int64_t P, ppt, T;
+    int64_t b_row0, b_rows;  // rows of B the packed column indices reach (staged kernel)
+    int *status;             // device status word: set when a bounded wait gives up
+    const uint8_t *exec;     // execution layout blocks (one per unit)
+    const int64_t *exec_offs;
+    int32_t xbuf;            // bytes of one per-warp metadata buffer (>= largest block)
+    int32_t pad2_;
     int32_t nk, load_c, epilogue, pad_;
     uint8_t id_pattern[256];
 };
@@ -136,15 +142,83 @@ template <int NV, class H> struct VecIO16 {
 template <int NV> struct VecIO<NV, __nv_bfloat16> : VecIO16<NV, __nv_bfloat16> {};
 template <int NV> struct VecIO<NV, __half> : VecIO16<NV, __half> {};
 
+// ------------------------------------------------------------------ B row sources
+// GlobalB reads the B rows of one lane's columns through L1/L2.
+template <int NV, class TB> struct GlobalB {
+    const TB *p;  // B + this lane's first column
+    int64_t ld;
+    bool valid;   // NV == 1 lanes past the last column read zeros and never store
+    __device__ __forceinline__ void load(int k, float (&b)[NV]) const {
+        if constexpr (NV == 1) {
+            b[0] = valid ? DT<TB>::to_f32(__ldg(p + (int64_t)k * ld)) : 0.0f;
+        } else {
+            VecIO<NV, TB>::load(p + (int64_t)k * ld, b);
+        }
+    }
+};
+
+// ------------------------------------------------------------------ metadata streams
+// A unit's column indices, values and nkern_counts are each read front to back.  A Stream keeps a
+// 64-element window of one of them in two registers per lane (element i of the window is lane
+// i % 32 of cur / nxt) and refills 32 elements as soon as 32 have been consumed, so every refill
+// load has 32 elements of work to hide behind.  All lanes hold the same position (warp-uniform).
+template <class T> struct RawOf { using R = T; };
+template <> struct RawOf<__nv_bfloat16> { using R = unsigned short; };
+template <> struct RawOf<__half> { using R = unsigned short; };
+
+template <class T> struct Stream {
+    using R = typename RawOf<T>::R;
+    const R *p;      // next element to load into the window
+    int64_t left;    // elements from p on that belong to the array
+    R cur, nxt;      // window elements [0, 32) and [32, 64)
+    int pos;         // window position of the next element to take
+
+    __device__ __forceinline__ static R load1(const R *q, int64_t left, int lane) {
+        return lane < left ? __ldg(q + lane) : R(0);
+    }
+    __device__ __forceinline__ void init(const T *base, int64_t n) {
+        const int lane = threadIdx.x & 31;
+        p = reinterpret_cast<const R *>(base);
+        left = n;
+        cur = load1(p, left, lane);
+        nxt = load1(p + 32, left - 32, lane);
+        p += 64;
+        left -= 64;
+        pos = 0;
+    }
+    // Make sure the next `need` (<= 32) elements are inside the window.
+    __device__ __forceinline__ void ensure() {
+        if (pos >= 32) {
+            cur = nxt;
+            nxt = load1(p, left, threadIdx.x & 31);
+            p += 32;
+            left -= 32;
+            pos -= 32;
+        }
+    }
+    __device__ __forceinline__ R at(int i) const {  // window element pos + i (pos + i < 64)
+        const int w = pos + i;
+        return __shfl_sync(0xffffffffu, w < 32 ? cur : nxt, w & 31);
+    }
+};
+
+__device__ __forceinline__ float raw_to_f32(float v) { return v; }
+template <class TV> __device__ __forceinline__ float val_f32(typename RawOf<TV>::R r) {
+    if constexpr (std::is_same<TV, float>::value) return r;
+    else return DT<TV>::to_f32(*reinterpret_cast<const TV *>(&r));
+}
+
 // ------------------------------------------------------------------ nanokernel loops
-// acc[r] += value * b for every set row r of PAT, values consumed in ascending row order.
+// acc[r] += value * b for every set row r of PAT (values in ascending row order, starting at
+// window offset vbase of the value stream).
 template <int PAT, int MR, int NV, class TV>
-__device__ __forceinline__ void fma_pattern(const TV *__restrict__ v, const float (&b)[NV], float (&acc)[MR][NV]) {
+__device__ __forceinline__ void fma_entry(const Stream<TV> &vs, const int vbase, const float (&b)[NV],
+                                          float (&acc)[MR][NV]) {
     int q = 0;
 #pragma unroll
     for (int r = 0; r < MR; ++r) {
         if ((PAT >> r) & 1) {
-            const float a = DT<TV>::to_f32(__ldg(v + q));
+            const float a = val_f32<TV>(vs.at(vbase + q));
             ++q;
 #pragma unroll
             for (int j = 0; j < NV; ++j) acc[r][j] = fmaf(a, b[j], acc[r][j]);
@@ -152,33 +226,44 @@ __device__ __forceinline__ void fma_pattern(const TV *__restrict__ v, const floa
     }
 }
 
-// n entries of one nanokernel id.  NV == 1 lanes may lie past the last column (valid == false):
-// they read zeros and never store.  NV > 1 launches only cover whole strips.
-template <int PAT, int MR, int NV, class TV, class TB>
-__device__ __forceinline__ void run_group(const int n, const int32_t *__restrict__ cols, const TV *__restrict__ vals,
-                                          const TB *__restrict__ Bc, const int64_t ldb, const bool valid,
+// n entries of one nanokernel id, U at a time: U B-row loads are issued before their FMAs.
+template <int PAT, int MR, int NV, class TV, class BL>
+__device__ __forceinline__ void run_group(int n, Stream<int32_t> &cs, Stream<TV> &vs, const BL &bl,
                                           float (&acc)[MR][NV]) {
     constexpr int PC = cpopc(PAT);
-#pragma unroll 2
-    for (int e = 0; e < n; ++e) {
-        const int64_t k = __ldg(cols + e);
+    constexpr int U0 = NV >= 4 ? 2 : 4;
+    constexpr int U = (U0 * PC <= 32) ? U0 : (32 / PC);
+    for (; n >= U; n -= U) {
+        cs.ensure();
+        vs.ensure();
+        float b[U][NV];
+#pragma unroll
+        for (int u = 0; u < U; ++u) bl.load(cs.at(u), b[u]);
+#pragma unroll
+        for (int u = 0; u < U; ++u) fma_entry<PAT, MR, NV, TV>(vs, u * PC, b[u], acc);
+        cs.pos += U;
+        vs.pos += U * PC;
+    }
+    for (; n > 0; --n) {
+        cs.ensure();
+        vs.ensure();
         float b[NV];
-        if constexpr (NV == 1) {
-            b[0] = valid ? DT<TB>::to_f32(__ldg(Bc + k * ldb)) : 0.0f;
-        } else {
-            VecIO<NV, TB>::load(Bc + k * ldb, b);
-        }
-        fma_pattern<PAT, MR, NV, TV>(vals + e * PC, b, acc);
+        bl.load(cs.at(0), b);
+        fma_entry<PAT, MR, NV, TV>(vs, 0, b, acc);
+        cs.pos += 1;
+        vs.pos += PC;
     }
 }
 
-// M_r = 8 has 255 patterns; compiling a loop per pattern takes minutes, so M_r = 8 specialises the
-// single rows and the nanokernels of the reference's M_r = 8 "orig" (400fa) and "alt" (747f9) sets
-// (tools/paper/configs.py:84-87) and runs any other pattern through run_group_nibbles.
+// M_r = 6 and 8 have 63 and 255 patterns; compiling a loop per pattern takes minutes, so M_r = 8
+// specialises the single rows and the nanokernels of the reference's M_r = 8 "orig" (400fa) and
+// "alt" (747f9) sets (tools/paper/configs.py:84-87), M_r = 6 the single rows, and any other
+// pattern runs through the nibble path (rows 0-3, then rows 4-7, one 16-way switch each).
 template <int MR>
 __host__ __device__ constexpr bool fast_pattern(int P) {
     if (P <= 0 || P >= (1 << MR)) return false;
-    if (MR < 8) return true;
+    if (MR <= 4) return true;
+    if (MR == 6) return (P & (P - 1)) == 0;  // single rows; other M_r = 6 patterns take the nibble path
     switch (P) {
     case 1: case 2: case 4: case 8: case 16: case 32: case 64: case 128:
     case 15: case 60: case 85: case 170: case 195: case 240:
@@ -189,14 +274,15 @@ __host__ __device__ constexpr bool fast_pattern(int P) {
     }
 }
 
-// Rows BASE .. BASE+3 of a 4-bit sub-pattern Q, values in ascending row order.
+// Rows BASE .. BASE+3 of a 4-bit sub-pattern Q (values from window offset vbase).
 template <int Q, int BASE, int MR, int NV, class TV>
-__device__ __forceinline__ void fma_nibble(const TV *__restrict__ v, const float (&b)[NV], float (&acc)[MR][NV]) {
+__device__ __forceinline__ void fma_nibble(const Stream<TV> &vs, const int vbase, const float (&b)[NV],
+                                           float (&acc)[MR][NV]) {
     int q = 0;
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
-        if ((Q >> r) & 1) {
-            const float a = DT<TV>::to_f32(__ldg(v + q));
+        if (((Q >> r) & 1) && BASE + r < MR) {
+            const float a = val_f32<TV>(vs.at(vbase + q));
             ++q;
 #pragma unroll
             for (int j = 0; j < NV; ++j) acc[BASE + r][j] = fmaf(a, b[j], acc[BASE + r][j]);
@@ -205,24 +291,19 @@ __device__ __forceinline__ void fma_nibble(const TV *__restrict__ v, const float
 }
 
 // Any M_r = 8 pattern: rows 0-3 then rows 4-7, each through a 16-way switch per entry.
-template <int MR, int NV, class TV, class TB>
-__device__ __forceinline__ void run_group_nibbles(const int pat, const int n, const int32_t *__restrict__ cols,
-                                               const TV *__restrict__ vals, const TB *__restrict__ Bc,
-                                               const int64_t ldb, const bool valid, float (&acc)[MR][NV]) {
-    if constexpr (MR == 8) {
+template <int MR, int NV, class TV, class BL>
+__device__ __forceinline__ void run_group_nibbles(const int pat, int n, Stream<int32_t> &cs, Stream<TV> &vs,
+                                                  const BL &bl, float (&acc)[MR][NV]) {
+    if constexpr (MR > 4) {
         const int lo = pat & 15, hi = (pat >> 4) & 15;
         const int plo = __popc(lo), pc = __popc(pat);
-        for (int e = 0; e < n; ++e) {
-            const int64_t k = __ldg(cols + e);
+        for (; n > 0; --n) {
+            cs.ensure();
+            vs.ensure();
             float b[NV];
-            if constexpr (NV == 1) {
-                b[0] = valid ? DT<TB>::to_f32(__ldg(Bc + k * ldb)) : 0.0f;
-            } else {
-                VecIO<NV, TB>::load(Bc + k * ldb, b);
-            }
-            const TV *v = vals + (int64_t)e * pc;
-#define SPREG_NIB_LO(Q) case Q: fma_nibble<Q, 0, MR, NV, TV>(v, b, acc); break;
-#define SPREG_NIB_HI(Q) case Q: fma_nibble<Q, 4, MR, NV, TV>(v + plo, b, acc); break;
+            bl.load(cs.at(0), b);
+#define SPREG_NIB_LO(Q) case Q: fma_nibble<Q, 0, MR, NV, TV>(vs, 0, b, acc); break;
+#define SPREG_NIB_HI(Q) case Q: fma_nibble<Q, 4, MR, NV, TV>(vs, plo, b, acc); break;
             switch (lo) {
                 SPREG_NIB_LO(1) SPREG_NIB_LO(2) SPREG_NIB_LO(3) SPREG_NIB_LO(4) SPREG_NIB_LO(5)
                 SPREG_NIB_LO(6) SPREG_NIB_LO(7) SPREG_NIB_LO(8) SPREG_NIB_LO(9) SPREG_NIB_LO(10)
@@ -237,6 +318,8 @@ __device__ __forceinline__ void run_group_nibbles(const int pat, const int n, co
             }
 #undef SPREG_NIB_LO
 #undef SPREG_NIB_HI
+            cs.pos += 1;
+            vs.pos += pc;
         }
     }
 }
@@ -245,16 +328,15 @@ __device__ __forceinline__ void run_group_nibbles(const int pat, const int n, co
 #define SPREG_C16(F, b) SPREG_C4(F, b) SPREG_C4(F, (b) + 4) SPREG_C4(F, (b) + 8) SPREG_C4(F, (b) + 12)
 #define SPREG_C64(F, b) SPREG_C16(F, b) SPREG_C16(F, (b) + 16) SPREG_C16(F, (b) + 32) SPREG_C16(F, (b) + 48)
 
-template <int MR, int NV, class TV, class TB>
-__device__ __forceinline__ void dispatch_group(const int pat, const int n, const int32_t *__restrict__ cols,
-                                               const TV *__restrict__ vals, const TB *__restrict__ Bc,
-                                               const int64_t ldb, const bool valid, float (&acc)[MR][NV]) {
-#define SPREG_CASE(P)                                                                                 \
-    case (P):                                                                                         \
-        if constexpr (fast_pattern<MR>(P)) {                                                          \
-            run_group<fast_pattern<MR>(P) ? (P) : 1, MR, NV, TV, TB>(n, cols, vals, Bc, ldb, valid, acc); \
-            return;                                                                                   \
-        }                                                                                             \
+template <int MR, int NV, class TV, class BL>
+__device__ __forceinline__ void dispatch_group(const int pat, const int n, Stream<int32_t> &cs, Stream<TV> &vs,
+                                               const BL &bl, float (&acc)[MR][NV]) {
+#define SPREG_CASE(P)                                                                  \
+    case (P):                                                                          \
+        if constexpr (fast_pattern<MR>(P)) {                                           \
+            run_group<fast_pattern<MR>(P) ? (P) : 1, MR, NV, TV, BL>(n, cs, vs, bl, acc); \
+            return;                                                                    \
+        }                                                                              \
         break;
     switch (pat) {
         SPREG_C64(SPREG_CASE, 0)
@@ -265,21 +347,16 @@ __device__ __forceinline__ void dispatch_group(const int pat, const int n, const
         break;
     }
 #undef SPREG_CASE
-    if constexpr (MR == 8) run_group_nibbles<MR, NV, TV, TB>(pat, n, cols, vals, Bc, ldb, valid, acc);
+    if constexpr (MR > 4) run_group_nibbles<MR, NV, TV, BL>(pat, n, cs, vs, bl, acc);
 }
 
-// ------------------------------------------------------------------ the kernel
-template <int MR, int NV, class TV, class TB, class TC>
-__global__ void __launch_bounds__(256) exec_kernel(const __grid_constant__ ExecParams p) {
-    const int lane = threadIdx.x & 31;
-    const int64_t gp = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    if (gp >= p.P) return;
-    const int64_t col0 = p.col_begin + (int64_t)blockIdx.y * (32 * NV) + (int64_t)lane * NV;
-    const bool valid = col0 < p.N;  // NV > 1 launches cover whole strips only
+// ------------------------------------------------------------------ one row panel x one strip
+template <int MR, int NV, class TV, class TC, class BL>
+__device__ __forceinline__ void process_panel(const ExecParams &p, const int64_t gp, const int64_t col0,
+                                              const bool valid, const BL &bl) {
     constexpr bool SCALED = std::is_same<TV, __half>::value;
     const int64_t row0 = gp * MR;
     TC *C = reinterpret_cast<TC *>(p.C);
-
     float acc[MR][NV];
 #pragma unroll
     for (int r = 0; r < MR; ++r)
@@ -290,24 +367,22 @@ __global__ void __launch_bounds__(256) exec_kernel(const __grid_constant__ ExecP
         for (int r = 0; r < MR; ++r)
             if (row0 + r < p.M) VecIO<NV, TC>::load_plain(C + (row0 + r) * p.ldc + col0, acc[r]);
     }
-
-    const TB *Bc = reinterpret_cast<const TB *>(p.B) + col0;
     for (int64_t tj = 0; tj < p.T; ++tj) {
         const spreg_panel_desc d = p.descs[unit_index(gp, tj, p.ppt, p.T, p.P)];
         if (d.num_cols == 0) continue;
-        const int32_t *__restrict__ cnt = reinterpret_cast<const int32_t *>(p.arena + d.counts_off);
-        const int32_t *__restrict__ cols = reinterpret_cast<const int32_t *>(p.arena + d.cols_off);
-        const TV *__restrict__ vals = reinterpret_cast<const TV *>(p.arena + d.values_off);
+        Stream<int32_t> ks, cs;
+        Stream<TV> vs;
+        ks.init(reinterpret_cast<const int32_t *>(p.arena + d.counts_off), p.nk);
+        cs.init(reinterpret_cast<const int32_t *>(p.arena + d.cols_off), d.num_cols);
+        vs.init(reinterpret_cast<const TV *>(p.arena + d.values_off), d.num_values);
         for (int id = 0; id < p.nk; ++id) {
-            const int n = __ldg(cnt + id);
+            ks.ensure();
+            const int n = ks.at(0);
+            ks.pos += 1;
             if (n == 0) continue;
-            const int pat = p.id_pattern[id];
-            dispatch_group<MR, NV, TV, TB>(pat, n, cols, vals, Bc, p.ldb, valid, acc);
-            cols += n;
-            vals += n * __popc(pat);
+            dispatch_group<MR, NV, TV, BL>(p.id_pattern[id], n, cs, vs, bl, acc);
         }
     }
-
     if (!valid) return;
     const float s = SCALED ? p.scales[gp] : 1.0f;
 #pragma unroll
@@ -336,6 +411,450 @@ __global__ void __launch_bounds__(256) exec_kernel(const __grid_constant__ ExecP
     }
 }
 
+// ------------------------------------------------------------------ kernels
+// B through L1/L2: one warp per (row panel, strip); grid (panel groups, strips).
+template <int MR, int NV, class TV, class TB, class TC>
+__global__ void __launch_bounds__(256, 1) exec_kernel(const __grid_constant__ ExecParams p) {
+    const int lane = threadIdx.x & 31;
+    const int64_t gp = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (gp >= p.P) return;
+    const int64_t col0 = p.col_begin + (int64_t)blockIdx.y * (32 * NV) + (int64_t)lane * NV;
+    const bool valid = col0 < p.N;  // NV > 1 launches cover whole strips only
+    GlobalB<NV, TB> bl{reinterpret_cast<const TB *>(p.B) + col0, p.ldb, valid};
+    process_panel<MR, NV, TV, TC>(p, gp, col0, valid, bl);
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_copy_g2s(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(dst), "l"(src), "r"(bytes), "r"(bar) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t phase) {
+    uint32_t ok;
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(ok) : "r"(bar), "r"(phase) : "memory");
+    return ok != 0;
+}
+
+// Bounded wait on an mbarrier phase; false after the limit (then *status records `code`).
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t phase, int *status, int code) {
+    for (uint32_t it = 0; it < (1u << 22); ++it)
+        if (mbar_try_wait(bar, phase)) return true;
+    if (status) atomicCAS(status, 0, code);
+    return false;
+}
+
+// ================================================================== execution-layout executor
+__device__ __forceinline__ uint32_t lds_u32(uint32_t a) {
+    uint32_t v;
+    asm volatile("ld.shared.b32 %0, [%1];" : "=r"(v) : "r"(a));
+    return v;
+}
+__device__ __forceinline__ uint4 lds_u128(uint32_t a) {
+    uint4 v;
+    asm volatile("ld.shared.v4.b32 {%0, %1, %2, %3}, [%4];" : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "r"(a));
+    return v;
+}
+__device__ __forceinline__ unsigned short lds_u16(uint32_t a) {
+    unsigned short v;
+    asm volatile("ld.shared.b16 %0, [%1];" : "=h"(v) : "r"(a));
+    return v;
+}
+template <class TV> __device__ __forceinline__ float word_val(uint32_t w, int half) {
+    if constexpr (sizeof(TV) == 4) {
+        return __uint_as_float(w);
+    } else {
+        const unsigned short h = (unsigned short)(half ? (w >> 16) : (w & 0xFFFFu));
+        return DT<TV>::to_f32(*reinterpret_cast<const TV *>(&h));
+    }
+}
+// Value i (compile-time after unrolling) of a block of quads.
+template <class TV, int NQ> __device__ __forceinline__ float quad_val(const uint4 (&q)[NQ], int i) {
+    constexpr int PER_WORD = 4 / sizeof(TV);
+    const int w = i / PER_WORD;
+    const uint4 &qq = q[w / 4];
+    const uint32_t word = (w % 4 == 0) ? qq.x : (w % 4 == 1) ? qq.y : (w % 4 == 2) ? qq.z : qq.w;
+    return word_val<TV>(word, i % PER_WORD);
+}
+template <class TV> __device__ __forceinline__ float lds_val(uint32_t a) {
+    if constexpr (sizeof(TV) == 4) return __uint_as_float(lds_u32(a));
+    else return word_val<TV>(lds_u16(a), 0);
+}
+
+__device__ __forceinline__ uint2 lds_u64(uint32_t a) {
+    uint2 v;
+    asm volatile("ld.shared.v2.b32 {%0, %1}, [%2];" : "=r"(v.x), "=r"(v.y) : "r"(a));
+    return v;
+}
+
+// The FMAs of one step (4 entries) of a group of pattern PAT: the step's 4 * PC values are PC
+// broadcast loads of 16 (FP32) or 8 (16-bit) bytes; entry u's values follow in ascending row
+// order.  FULL steps have 4 entries; the last step of a group has m < 4 (entries u >= m skipped).
+template <int PAT, int MR, int NV, class TV, bool FULL>
+__device__ __forceinline__ void step_fma(const uint32_t vs, const int m, const float (&b)[4][NV], float (&acc)[MR][NV]) {
+    constexpr int PC = cpopc(PAT);
+    constexpr int VB = (int)sizeof(TV);
+    uint32_t vw[PC * VB];
+#pragma unroll
+    for (int i = 0; i < PC; ++i) {
+        if constexpr (VB == 4) {
+            const uint4 t = lds_u128(vs + 16u * i);
+            vw[4 * i] = t.x; vw[4 * i + 1] = t.y; vw[4 * i + 2] = t.z; vw[4 * i + 3] = t.w;
+        } else {
+            const uint2 t = lds_u64(vs + 8u * i);
+            vw[2 * i] = t.x; vw[2 * i + 1] = t.y;
+        }
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        if (FULL || u < m) {
+            int q = 0;
+#pragma unroll
+            for (int r = 0; r < MR; ++r) {
+                if ((PAT >> r) & 1) {
+                    const int vi = u * PC + q;
+                    const float a = word_val<TV>(vw[vi * VB / 4], (vi * VB / 2) & 1);
+                    ++q;
+#pragma unroll
+                    for (int j = 0; j < NV; ++j) acc[r][j] = fmaf(a, b[u][j], acc[r][j]);
+                }
+            }
+        }
+    }
+}
+
+// Rows BASE .. BASE+3 of the 4-bit sub-pattern Q of one entry (values from shared address va).
+template <int Q, int BASE, int MR, int NV, class TV>
+__device__ __forceinline__ void fma_nibble_x(uint32_t va, const float (&b)[NV], float (&acc)[MR][NV]) {
+    int q = 0;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        if (((Q >> r) & 1) && BASE + r < MR) {
+            const float a = lds_val<TV>(va + (uint32_t)(q * sizeof(TV)));
+            ++q;
+#pragma unroll
+            for (int j = 0; j < NV; ++j) acc[BASE + r][j] = fmaf(a, b[j], acc[BASE + r][j]);
+        }
+    }
+}
+
+// One step of a pattern without its own FMA block (M_r 6 and 8): entry by entry, rows 0-3 then
+// rows 4-7 through 16-way switches.
+template <int MR, int NV, class TV>
+__device__ __forceinline__ void step_fma_nibbles(const int pat, const uint32_t vs, const int m, const float (&b)[4][NV],
+                                                 float (&acc)[MR][NV]) {
+    if constexpr (MR > 4) {
+        const int lo = pat & 15, hi = (pat >> 4) & 15;
+        const uint32_t plo = (uint32_t)(__popc(lo) * sizeof(TV)), ent = (uint32_t)(__popc(pat) * sizeof(TV));
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            if (u < m) {
+                const uint32_t va = vs + ent * u;
+#define SPREG_XLO(Q) case Q: fma_nibble_x<Q, 0, MR, NV, TV>(va, b[u], acc); break;
+#define SPREG_XHI(Q) case Q: fma_nibble_x<Q, 4, MR, NV, TV>(va + plo, b[u], acc); break;
+                switch (lo) {
+                    SPREG_XLO(1) SPREG_XLO(2) SPREG_XLO(3) SPREG_XLO(4) SPREG_XLO(5) SPREG_XLO(6) SPREG_XLO(7)
+                    SPREG_XLO(8) SPREG_XLO(9) SPREG_XLO(10) SPREG_XLO(11) SPREG_XLO(12) SPREG_XLO(13) SPREG_XLO(14)
+                    SPREG_XLO(15)
+                    default: break;
+                }
+                switch (hi) {
+                    SPREG_XHI(1) SPREG_XHI(2) SPREG_XHI(3) SPREG_XHI(4) SPREG_XHI(5) SPREG_XHI(6) SPREG_XHI(7)
+                    SPREG_XHI(8) SPREG_XHI(9) SPREG_XHI(10) SPREG_XHI(11) SPREG_XHI(12) SPREG_XHI(13) SPREG_XHI(14)
+                    SPREG_XHI(15)
+                    default: break;
+                }
+#undef SPREG_XLO
+#undef SPREG_XHI
+            }
+        }
+    }
+}
+
+// The FMA block of one step, selected by one uniform switch on the pattern.
+template <int MR, int NV, class TV, bool FULL>
+__device__ __forceinline__ void step_dispatch(const int pat, const uint32_t vs, const int m, const float (&b)[4][NV],
+                                              float (&acc)[MR][NV]) {
+    bool done = false;
+#define SPREG_CASE(P)                                                                \
+    case (P):                                                                        \
+        if constexpr (fast_pattern<MR>(P)) {                                         \
+            step_fma<fast_pattern<MR>(P) ? (P) : 1, MR, NV, TV, FULL>(vs, m, b, acc); \
+            done = true;                                                             \
+        }                                                                            \
+        break;
+    switch (pat) {
+        SPREG_C64(SPREG_CASE, 0)
+        SPREG_C64(SPREG_CASE, 64)
+        SPREG_C64(SPREG_CASE, 128)
+        SPREG_C64(SPREG_CASE, 192)
+    default:
+        break;
+    }
+#undef SPREG_CASE
+    if (!done) step_fma_nibbles<MR, NV, TV>(pat, vs, FULL ? 4 : m, b, acc);
+}
+
+// n entries of one group: full steps of 4 entries (one 16-byte broadcast load of column indices,
+// 4 B rows, the pattern's FMA block), then one predicated step for the last n % 4 entries.
+template <int MR, int NV, class TV, class BL>
+__device__ __forceinline__ void run_group_x(const int pat, const int n, uint32_t cs, uint32_t vs, const BL &bl,
+                                            float (&acc)[MR][NV]) {
+    const uint32_t vstep = 4u * (uint32_t)sizeof(TV) * (uint32_t)__popc(pat);
+    const int full = n >> 2;
+#pragma unroll 1
+    for (int s = 0; s < full; ++s) {
+        const uint4 k4 = lds_u128(cs);
+        float b[4][NV];
+        bl.load((int)k4.x, b[0]);
+        bl.load((int)k4.y, b[1]);
+        bl.load((int)k4.z, b[2]);
+        bl.load((int)k4.w, b[3]);
+        step_dispatch<MR, NV, TV, true>(pat, vs, 4, b, acc);
+        cs += 16u;
+        vs += vstep;
+    }
+    const int m = n & 3;
+    if (m) {
+        const uint4 k4 = lds_u128(cs);
+        const int ks[4] = {(int)k4.x, (int)k4.y, (int)k4.z, (int)k4.w};
+        float b[4][NV];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (u < m) bl.load(ks[u], b[u]);
+        step_dispatch<MR, NV, TV, false>(pat, vs, m, b, acc);
+    }
+}
+
+// C tile of one row panel: load (load_c) / store with scale and epilogue.
+template <int MR, int NV, class TV, class TC>
+__device__ __forceinline__ void panel_acc_init(const ExecParams &p, int64_t row0, int64_t col0, float (&acc)[MR][NV]) {
+    constexpr bool SCALED = std::is_same<TV, __half>::value;
+#pragma unroll
+    for (int r = 0; r < MR; ++r)
+#pragma unroll
+        for (int j = 0; j < NV; ++j) acc[r][j] = 0.0f;
+    if (!SCALED && p.load_c) {
+        const TC *C = reinterpret_cast<const TC *>(p.C);
+#pragma unroll
+        for (int r = 0; r < MR; ++r)
+            if (row0 + r < p.M) VecIO<NV, TC>::load_plain(C + (row0 + r) * p.ldc + col0, acc[r]);
+    }
+}
+template <int MR, int NV, class TV, class TC>
+__device__ __forceinline__ void panel_store(const ExecParams &p, int64_t gp, int64_t row0, int64_t col0,
+                                            const float (&acc)[MR][NV]) {
+    constexpr bool SCALED = std::is_same<TV, __half>::value;
+    TC *C = reinterpret_cast<TC *>(p.C);
+    const float s = SCALED ? p.scales[gp] : 1.0f;
+#pragma unroll
+    for (int r = 0; r < MR; ++r) {
+        if (row0 + r >= p.M) continue;
+        TC *cp = C + (row0 + r) * p.ldc + col0;
+        float o[NV];
+#pragma unroll
+        for (int j = 0; j < NV; ++j) o[j] = acc[r][j];
+        if (SCALED) {
+            if (p.load_c) {
+                float cin[NV];
+                VecIO<NV, TC>::load_plain(cp, cin);
+#pragma unroll
+                for (int j = 0; j < NV; ++j) o[j] = fmaf(o[j], s, cin[j]);
+            } else {
+#pragma unroll
+                for (int j = 0; j < NV; ++j) o[j] = o[j] * s;
+            }
+        }
+        if (p.epilogue == SPREG_EPILOGUE_RELU) {
+#pragma unroll
+            for (int j = 0; j < NV; ++j) o[j] = fmaxf(o[j], 0.0f);
+        }
+        VecIO<NV, TC>::store(cp, o);
+    }
+}
+
+// ================================================================== batched persistent executor
+// One launch runs many SpMMs (problems) of uneven shape.  The work is a list of items
+// (problem, row panel, column strip); warps take items from a global counter (zeroed by the host
+// before the launch) until the list is exhausted, so every SM stays busy to the end whatever the
+// row skew.  For each item the warp bulk-copies the execution blocks of the panel's K-tile units
+// into a shared-memory buffer; two buffers per warp keep the next block in flight while the
+// current one computes.  Problems of one launch share M_r, the strip width and the data types;
+// the problem table travels in the kernel parameters, so a launch needs no host-to-device copy
+// and can be captured in a CUDA graph.
+constexpr int kMaxBatchProblems = 224;
+
+struct XProblem {
+    const uint8_t *exec;        // execution layout of the packed matrix
+    const int64_t *exec_offs;   // units + 1 block offsets
+    const float *scales;        // per-row-panel F16 scales (else null)
+    const void *B;
+    void *C;
+    int64_t ldb, ldc, M;
+    int64_t col_begin;          // first column of the problem's strips
+    int64_t col_end;            // columns >= col_end are not computed (NV = 1 tails)
+    int64_t item_begin;         // first global item
+    int32_t P, S, T, ppt;       // row panels, strips, K tiles, panels per row tile
+    int32_t load_c, epilogue, pad0, pad1;
+};
+
+struct BatchParams {
+    int *counter;               // work counter, zero at launch
+    int *status;                // device status word of bounded waits
+    int64_t items;              // total items
+    int32_t nprob, xbuf;        // problems; bytes of one per-warp buffer
+    XProblem prob[kMaxBatchProblems];
+};
+
+struct XJob {
+    int64_t gp;   // row panel
+    int32_t pi;   // problem index (-1: no job)
+    int32_t strip, t;
+};
+
+__device__ __forceinline__ int find_problem(const BatchParams &bp, int64_t item) {
+    int lo = 0, hi = bp.nprob - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (bp.prob[mid].item_begin <= item) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Next job after `j` in this warp's sequence: the next K tile of the same item, or a new item.
+__device__ __forceinline__ XJob next_job(const BatchParams &bp, const XJob &j, int *counter, int lane) {
+    if (j.pi >= 0 && j.t + 1 < bp.prob[j.pi].T) return XJob{j.gp, j.pi, j.strip, j.t + 1};
+    int it = 0;
+    if (lane == 0) it = atomicAdd(counter, 1);
+    const int64_t item = __shfl_sync(0xffffffffu, it, 0);
+    if (item >= bp.items) return XJob{0, -1, 0, 0};
+    const int pi = find_problem(bp, item);
+    const XProblem &pr = bp.prob[pi];
+    const int64_t local = item - pr.item_begin;
+    return XJob{local / pr.S, pi, (int32_t)(local % pr.S), 0};
+}
+
+__device__ __forceinline__ void issue_job(const BatchParams &bp, const XJob &j, uint32_t buf, uint32_t bar, int lane) {
+    if (lane == 0 && j.pi >= 0) {
+        const XProblem &pr = bp.prob[j.pi];
+        const int64_t u = unit_index(j.gp, j.t, pr.ppt, pr.T, pr.P);
+        const int64_t off = pr.exec_offs[u];
+        const uint32_t bytes = (uint32_t)(pr.exec_offs[u + 1] - off);
+        fence_proxy_async_smem();
+        mbar_arrive_expect_tx(bar, bytes);
+        bulk_copy_g2s(buf, pr.exec + off, bytes, bar);
+    }
+}
+
+// C tile init / store for one (problem, panel, strip).
+template <int MR, int NV, class TV, class TC>
+__device__ __forceinline__ void x_acc_init(const XProblem &pr, int64_t row0, int64_t col0, bool valid,
+                                           float (&acc)[MR][NV]) {
+    constexpr bool SCALED = std::is_same<TV, __half>::value;
+#pragma unroll
+    for (int r = 0; r < MR; ++r)
+#pragma unroll
+        for (int j = 0; j < NV; ++j) acc[r][j] = 0.0f;
+    if (!SCALED && pr.load_c && valid) {
+        const TC *C = reinterpret_cast<const TC *>(pr.C);
+#pragma unroll
+        for (int r = 0; r < MR; ++r)
+            if (row0 + r < pr.M) VecIO<NV, TC>::load_plain(C + (row0 + r) * pr.ldc + col0, acc[r]);
+    }
+}
+template <int MR, int NV, class TV, class TC>
+__device__ __forceinline__ void x_store(const XProblem &pr, int64_t gp, int64_t row0, int64_t col0, bool valid,
+                                        const float (&acc)[MR][NV]) {
+    if (!valid) return;
+    constexpr bool SCALED = std::is_same<TV, __half>::value;
+    TC *C = reinterpret_cast<TC *>(pr.C);
+    const float s = SCALED ? pr.scales[gp] : 1.0f;
+#pragma unroll
+    for (int r = 0; r < MR; ++r) {
+        if (row0 + r >= pr.M) continue;
+        TC *cp = C + (row0 + r) * pr.ldc + col0;
+        float o[NV];
+#pragma unroll
+        for (int j = 0; j < NV; ++j) o[j] = acc[r][j];
+        if (SCALED) {
+            if (pr.load_c) {
+                float cin[NV];
+                VecIO<NV, TC>::load_plain(cp, cin);
+#pragma unroll
+                for (int j = 0; j < NV; ++j) o[j] = fmaf(o[j], s, cin[j]);
+            } else {
+#pragma unroll
+                for (int j = 0; j < NV; ++j) o[j] = o[j] * s;
+            }
+        }
+        if (pr.epilogue == SPREG_EPILOGUE_RELU) {
+#pragma unroll
+            for (int j = 0; j < NV; ++j) o[j] = fmaxf(o[j], 0.0f);
+        }
+        VecIO<NV, TC>::store(cp, o);
+    }
+}
+
+template <int MR, int NV, class TV, class TB, class TC>
+__global__ void __launch_bounds__(256, 1) exec_batch_kernel(const __grid_constant__ BatchParams bp) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(smem);
+    const uint32_t bar0 = sbase + 16u * warp, bar1 = bar0 + 8u;
+    const uint32_t xb = (uint32_t)bp.xbuf;
+    const uint32_t buf0 = sbase + 1024u + 2u * xb * warp, buf1 = buf0 + xb;
+    if (lane == 0) {
+        mbar_init(bar0, 1);
+        mbar_init(bar1, 1);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    fence_proxy_async_smem();
+    __syncwarp();
+
+    XJob j0 = next_job(bp, XJob{0, -1, 0, 0}, bp.counter, lane);
+    issue_job(bp, j0, buf0, bar0, lane);
+    XJob j1 = next_job(bp, j0, bp.counter, lane);
+    issue_job(bp, j1, buf1, bar1, lane);
+    XJob last = j1;
+    uint32_t ph0 = 0u, ph1 = 0u;
+    float acc[MR][NV];
+
+#pragma unroll 1
+    for (int b = 0;; b ^= 1) {
+        const XJob j = b ? j1 : j0;
+        if (j.pi < 0) break;
+        const uint32_t buf = b ? buf1 : buf0, bar = b ? bar1 : bar0;
+        if (!mbar_wait_bounded(bar, b ? ph1 : ph0, bp.status, 2)) break;
+        if (b) ph1 ^= 1u; else ph0 ^= 1u;
+        const XProblem &pr = bp.prob[j.pi];
+        const int64_t row0 = j.gp * MR;
+        const int64_t col0 = pr.col_begin + (int64_t)j.strip * (32 * NV) + (int64_t)lane * NV;
+        const bool valid = col0 < pr.col_end;
+        if (j.t == 0) x_acc_init<MR, NV, TV, TC>(pr, row0, col0, valid, acc);
+        const GlobalB<NV, TB> bl{reinterpret_cast<const TB *>(pr.B) + col0, pr.ldb, valid};
+        const uint32_t G = lds_u32(buf);
+#pragma unroll 1
+        for (uint32_t g = 0; g < G; ++g) {
+            const uint4 rec = lds_u128(buf + 16u + 16u * g);
+            run_group_x<MR, NV, TV>((int)rec.x, (int)rec.y, buf + rec.z, buf + rec.w, bl, acc);
+        }
+        __syncwarp();
+        // refill this buffer with the job after the last one issued
+        const XJob jn = next_job(bp, last, bp.counter, lane);
+        issue_job(bp, jn, buf, bar, lane);
+        last = jn;
+        if (b) j1 = jn; else j0 = jn;
+        if (j.t == pr.T - 1) x_store<MR, NV, TV, TC>(pr, j.gp, row0, col0, valid, acc);
+    }
+}
+
 // Launch one executor kernel.  One translation unit per (M_r, dtype combination) instantiates
 // launch_exec (generated by build.py) so that the kernels compile in parallel.
 enum ExecCombo { COMBO_F32 = 0, COMBO_BF16_F32OUT = 1, COMBO_BF16_BF16OUT = 2, COMBO_F16_F32OUT = 3, NUM_COMBOS = 4 };
@@ -346,8 +865,13 @@ template <> struct ComboTypes<COMBO_BF16_F32OUT> { using V = __nv_bfloat16; usin
 template <> struct ComboTypes<COMBO_BF16_BF16OUT> { using V = __nv_bfloat16; using B = __nv_bfloat16; using C = __nv_bfloat16; };
 template <> struct ComboTypes<COMBO_F16_F32OUT> { using V = __half; using B = __half; using C = float; };
 
+// Largest dynamic shared memory a staged-strip CTA may use (opt-in limit of sm_100-class parts).
+constexpr int kMaxSmem = 227 * 1024;
+
 template <int MR, int COMBO>
 cudaError_t launch_exec(const ExecParams &p, int nv, dim3 grid, int threads, cudaStream_t s);
+template <int MR, int COMBO>
+cudaError_t launch_exec_batch(const BatchParams &p, int nv, unsigned grid, int threads, size_t smem, cudaStream_t s);
 
 #define SPREG_INSTANTIATE_EXEC(MR, COMBO)                                                             \
     template <>                                                                                       \
@@ -359,10 +883,35 @@ cudaError_t launch_exec(const ExecParams &p, int nv, dim3 grid, int threads, cud
         case 1: exec_kernel<MR, 1, V, B, C><<<grid, threads, 0, s>>>(p); break;                       \
         case 2: exec_kernel<MR, 2, V, B, C><<<grid, threads, 0, s>>>(p); break;                       \
         case 4: exec_kernel<MR, 4, V, B, C><<<grid, threads, 0, s>>>(p); break;                       \
-        case 8: exec_kernel<MR, 8, V, B, C><<<grid, threads, 0, s>>>(p); break;                       \
         default: return cudaErrorInvalidValue;                                                        \
         }                                                                                             \
         return cudaGetLastError();                                                                    \
+    }                                                                                                 \
+    template <>                                                                                       \
+    cudaError_t launch_exec_batch<MR, COMBO>(const BatchParams &p, int nv, unsigned grid, int threads, size_t smem, \
+                                             cudaStream_t s) {                                        \
+        using V = ComboTypes<COMBO>::V;                                                               \
+        using B = ComboTypes<COMBO>::B;                                                               \
+        using C = ComboTypes<COMBO>::C;                                                               \
+        static bool configured[64][5] = {};                                                           \
+        int dev = 0;                                                                                  \
+        cudaGetDevice(&dev);                                                                          \
+        auto run = [&](auto kern) -> cudaError_t {                                                    \
+            if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;                                  \
+            if (!configured[dev][nv]) {                                                               \
+                cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem); \
+                if (e != cudaSuccess) return e;                                                       \
+                configured[dev][nv] = true;                                                           \
+            }                                                                                         \
+            kern<<<grid, threads, smem, s>>>(p);                                                      \
+            return cudaGetLastError();                                                                \
+        };                                                                                            \
+        switch (nv) {                                                                                 \
+        case 1: return run(exec_batch_kernel<MR, 1, V, B, C>);                                        \
+        case 2: return run(exec_batch_kernel<MR, 2, V, B, C>);                                        \
+        case 4: return run(exec_batch_kernel<MR, 4, V, B, C>);                                        \
+        default: return cudaErrorInvalidValue;                                                        \
+        }                                                                                             \
     }
 
 }  // namespace spreg

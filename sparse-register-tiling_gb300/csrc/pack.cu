@@ -110,12 +110,27 @@ __device__ inline float block_max(float v, float *s_tmp) {
     return m;
 }
 
+// Execution block size of a unit from its per-id counts (thread 0 of the CTA).
+__device__ inline void exec_size(const MapTable &mt, const int *counts, int vb, int32_t *bytes, int32_t *groups) {
+    int64_t sz = sizeof(ExecHeader);
+    int g = 0;
+    for (int id = 0; id < mt.num_nkern; ++id) {
+        const int64_t n = counts[id];
+        if (!n) continue;
+        ++g;
+        sz += sizeof(ExecGroup) + exec_cols_bytes(n) + exec_vals_bytes(n, __popc(mt.id_to_pattern[id]), vb);
+    }
+    *bytes = (int32_t)sz;
+    *groups = g;
+}
+
 // ------------------------------------------------------------------ count pass (columns)
 template <class Loader>
 __global__ void __launch_bounds__(CH) count_cols_kernel(const Geom g, const Loader ld, const MapTable *__restrict__ mt,
                                                         int32_t *__restrict__ unit_counts, UnitStats *__restrict__ stats,
                                                         unsigned *__restrict__ panel_maxabs,
-                                                        unsigned long long *__restrict__ tile_nnz, DevError *err) {
+                                                        unsigned long long *__restrict__ tile_nnz, DevError *err,
+                                                        const int vb) {
     __shared__ MapTable s_mt;
     __shared__ float s_val[SPREG_MAX_MR][CH];
     __shared__ uint32_t s_seen[SPREG_MAX_MR][CHW];
@@ -169,7 +184,9 @@ __global__ void __launch_bounds__(CH) count_cols_kernel(const Geom g, const Load
     if (threadIdx.x == 0) {
         long long nu = 0;
         for (int id = 0; id < nk; ++id) nu += s_count[id];
-        stats[u] = UnitStats{(int32_t)nu, (int32_t)tot_v, (int32_t)tot_pad, (int32_t)tot_nnz};
+        int32_t xb, xg;
+        exec_size(s_mt, s_count, vb, &xb, &xg);
+        stats[u] = UnitStats{(int32_t)nu, (int32_t)tot_v, (int32_t)tot_pad, (int32_t)tot_nnz, xb, xg};
         if (tot_v != tot_pad + tot_nnz) raise_err(err, 2, u, (int)tot_v);
         atomicMax(&panel_maxabs[gp], __float_as_uint(tot_mx));
         const int64_t ti = gp / g.ppt;
@@ -193,7 +210,8 @@ struct ListSrc {
 __global__ void __launch_bounds__(CH) count_list_kernel(const ListSrc src, const MapTable *__restrict__ mt,
                                                         int32_t *__restrict__ unit_counts,
                                                         UnitStats *__restrict__ stats, unsigned *__restrict__ panel_maxabs,
-                                                        unsigned long long *__restrict__ tile_nnz, DevError *err) {
+                                                        unsigned long long *__restrict__ tile_nnz, DevError *err,
+                                                        const int vb) {
     __shared__ MapTable s_mt;
     __shared__ int s_count[256];
     __shared__ long long s_tmp[CH / 32];
@@ -234,7 +252,9 @@ __global__ void __launch_bounds__(CH) count_list_kernel(const ListSrc src, const
     if (threadIdx.x == 0) {
         long long nu = 0;
         for (int id = 0; id < nk; ++id) nu += s_count[id];
-        stats[p] = UnitStats{(int32_t)nu, (int32_t)tot_v, (int32_t)tot_pad, (int32_t)tot_nnz};
+        int32_t xb, xg;
+        exec_size(s_mt, s_count, vb, &xb, &xg);
+        stats[p] = UnitStats{(int32_t)nu, (int32_t)tot_v, (int32_t)tot_pad, (int32_t)tot_nnz, xb, xg};
         if (tot_v != tot_pad + tot_nnz) raise_err(err, 2, p, (int)tot_v);
         panel_maxabs[p] = __float_as_uint(tot_mx);
         atomicAdd(&tile_nnz[0], (unsigned long long)tot_nnz);
@@ -246,21 +266,25 @@ __global__ void __launch_bounds__(1024) layout_kernel(const int64_t units, const
                                                       const int64_t ppt, const int64_t T, const int64_t P,
                                                       const UnitStats *__restrict__ stats,
                                                       const unsigned long long *__restrict__ tile_nnz,
-                                                      spreg_panel_desc *__restrict__ descs, PackTotals *tot) {
+                                                      spreg_panel_desc *__restrict__ descs, PackTotals *tot,
+                                                      int64_t *__restrict__ exec_offs) {
     __shared__ long long s_scan[1024];
-    __shared__ long long s_carry;
-    __shared__ unsigned long long s_acc[7];
+    __shared__ long long s_xscan[1024];
+    __shared__ long long s_carry, s_xcarry;
+    __shared__ unsigned long long s_acc[8];
     const int t = threadIdx.x;
-    if (t == 0) s_carry = 0;
-    if (t < 7) s_acc[t] = 0;
+    if (t == 0) { s_carry = 0; s_xcarry = 0; }
+    if (t < 8) s_acc[t] = 0;
     __syncthreads();
     long long my_v = 0, my_u = 0, my_pad = 0, my_nnz = 0, my_req = 0, my_empty = 0;
     for (int64_t base = 0; base < units; base += 1024) {
         const int64_t u = base + t;
-        long long size = 0;
-        UnitStats st = {0, 0, 0, 0};
+        long long size = 0, xsize = 0;
+        UnitStats st = {0, 0, 0, 0, 0, 0};
         if (u < units) {
             st = stats[u];
+            xsize = st.exec_bytes;
+            atomicMax(&s_acc[7], (unsigned long long)xsize);
             size = align64((int64_t)st.num_values * vb) + align64((int64_t)st.num_cols * 4) + align64((int64_t)nk * 4);
             my_v += st.num_values;
             my_u += st.num_cols;
@@ -272,13 +296,17 @@ __global__ void __launch_bounds__(1024) layout_kernel(const int64_t units, const
             if (tile_nnz[(gp / ppt) * T + tj] == 0) my_empty++;
         }
         s_scan[t] = size;
+        s_xscan[t] = xsize;
         __syncthreads();
         for (int o = 1; o < 1024; o <<= 1) {
             const long long add = t >= o ? s_scan[t - o] : 0;
+            const long long xadd = t >= o ? s_xscan[t - o] : 0;
             __syncthreads();
             s_scan[t] += add;
+            s_xscan[t] += xadd;
             __syncthreads();
         }
+        if (u < units) exec_offs[u] = s_xcarry + s_xscan[t] - xsize;
         if (u < units) {
             const long long off = s_carry + s_scan[t] - size;
             spreg_panel_desc d;
@@ -290,7 +318,7 @@ __global__ void __launch_bounds__(1024) layout_kernel(const int64_t units, const
             descs[u] = d;
         }
         __syncthreads();
-        if (t == 0) s_carry += s_scan[1023];
+        if (t == 0) { s_carry += s_scan[1023]; s_xcarry += s_xscan[1023]; }
         __syncthreads();
     }
     atomicAdd(&s_acc[0], (unsigned long long)my_v);
@@ -308,6 +336,9 @@ __global__ void __launch_bounds__(1024) layout_kernel(const int64_t units, const
         tot->nnz = (long long)s_acc[3];
         tot->required_storage = (long long)s_acc[4];
         tot->empty_units = (long long)s_acc[5];
+        tot->exec_bytes = s_xcarry;
+        tot->max_exec_bytes = (long long)s_acc[7];
+        exec_offs[units] = s_xcarry;
     }
 }
 
@@ -330,22 +361,39 @@ struct EmitShared {
     int start[256];
     int vstart[256];
     int run[256];
+    int xcol[256];   // byte offset of an id's cols in the unit's execution block
+    int xval[256];   // byte offset of an id's values
     uint32_t bits[256][CHW];
     uint16_t pref[256][CHW];
 };
 
-// Per-id exclusive scans of entry and value counts; writes the unit's nkern_counts.
-__device__ inline void emit_prologue(EmitShared &s, const MapTable &mt, const int32_t *counts, int32_t *out_counts) {
+// Per-id exclusive scans of entry and value counts; writes the unit's nkern_counts and the
+// header and group records of its execution block.
+__device__ inline void emit_prologue(EmitShared &s, const MapTable &mt, const int32_t *counts, int32_t *out_counts,
+                                     uint8_t *xblock, int vb) {
     const int nk = mt.num_nkern;
     for (int id = threadIdx.x; id < nk; id += blockDim.x) out_counts[id] = counts[id];
     if (threadIdx.x == 0) {
-        int e = 0, v = 0;
+        int e = 0, v = 0, g = 0;
+        for (int id = 0; id < nk; ++id) g += counts[id] != 0;
+        int64_t off = sizeof(ExecHeader) + (int64_t)g * sizeof(ExecGroup);
+        ExecGroup *grp = reinterpret_cast<ExecGroup *>(xblock + sizeof(ExecHeader));
+        g = 0;
         for (int id = 0; id < nk; ++id) {
+            const int n = counts[id];
+            const int pc = __popc(mt.id_to_pattern[id]);
             s.start[id] = e;
             s.vstart[id] = v;
-            e += counts[id];
-            v += counts[id] * __popc(mt.id_to_pattern[id]);
+            e += n;
+            v += n * pc;
+            s.xcol[id] = (int)off;
+            s.xval[id] = (int)(off + exec_cols_bytes(n));
+            if (n) {
+                grp[g++] = ExecGroup{mt.id_to_pattern[id], (uint32_t)n, (uint32_t)s.xcol[id], (uint32_t)s.xval[id]};
+                off += exec_cols_bytes(n) + exec_vals_bytes(n, pc, vb);
+            }
         }
+        *reinterpret_cast<ExecHeader *>(xblock) = ExecHeader{(uint32_t)g, (uint32_t)off, 0u, 0u};
     }
     for (int id = threadIdx.x; id < 256; id += blockDim.x) s.run[id] = 0;
 }
@@ -381,7 +429,8 @@ __global__ void __launch_bounds__(CH) emit_cols_kernel(const Geom g, const Loade
                                                        const int32_t *__restrict__ unit_counts,
                                                        const spreg_panel_desc *__restrict__ descs,
                                                        uint8_t *__restrict__ arena, const float *__restrict__ scales,
-                                                       const int64_t col_offset) {
+                                                       const int64_t col_offset, uint8_t *__restrict__ exec,
+                                                       const int64_t *__restrict__ exec_offs) {
     __shared__ MapTable s_mt;
     __shared__ float s_val[SPREG_MAX_MR][CH];
     __shared__ uint32_t s_seen[SPREG_MAX_MR][CHW];
@@ -398,7 +447,9 @@ __global__ void __launch_bounds__(CH) emit_cols_kernel(const Geom g, const Loade
     __syncthreads();
     const int nk = s_mt.num_nkern;
     const int mr = s_mt.mr;
-    emit_prologue(s, s_mt, unit_counts + u * nk, reinterpret_cast<int32_t *>(arena + d.counts_off));
+    uint8_t *xb = exec + exec_offs[u];
+    emit_prologue(s, s_mt, unit_counts + u * nk, reinterpret_cast<int32_t *>(arena + d.counts_off), xb,
+                  (int)sizeof(TV));
     int32_t *out_cols = reinterpret_cast<int32_t *>(arena + d.cols_off);
     TV *out_vals = reinterpret_cast<TV *>(arena + d.values_off);
     const float inv = scales ? 1.0f / scales[gp] : 1.0f;  // exact: scales are powers of two
@@ -426,13 +477,18 @@ __global__ void __launch_bounds__(CH) emit_cols_kernel(const Geom g, const Loade
                 const int code = s_mt.map_codes[pat][q];
                 const int id = s_mt.code_to_id[code];
                 const int rank = slot_rank(s, id, t);
-                out_cols[s.start[id] + rank] = (int32_t)(c0 + t + col_offset);
+                const int32_t colv = (int32_t)(c0 + t + col_offset);
+                out_cols[s.start[id] + rank] = colv;
+                reinterpret_cast<int32_t *>(xb + s.xcol[id])[rank] = colv;
+                TV *xv = reinterpret_cast<TV *>(xb + s.xval[id]) + rank * __popc(code);
                 int vo = s.vstart[id] + rank * __popc(code);
                 for (int r = 0; r < mr; ++r)
                     if ((code >> r) & 1) {
                         float v = s_val[r][t];
                         if (DT<TV>::id == SPREG_F16) v *= inv;
-                        out_vals[vo++] = DT<TV>::from_f32(v);
+                        const TV q = DT<TV>::from_f32(v);
+                        out_vals[vo++] = q;
+                        *xv++ = q;
                     }
             }
         }
@@ -447,7 +503,8 @@ template <class TV>
 __global__ void __launch_bounds__(CH) emit_list_kernel(const ListSrc src, const MapTable *__restrict__ mt,
                                                        const int32_t *__restrict__ unit_counts,
                                                        const spreg_panel_desc *__restrict__ descs,
-                                                       uint8_t *__restrict__ arena, const float *__restrict__ scales) {
+                                                       uint8_t *__restrict__ arena, const float *__restrict__ scales,
+                                                       uint8_t *__restrict__ exec, const int64_t *__restrict__ exec_offs) {
     __shared__ MapTable s_mt;
     __shared__ EmitShared s;
     const int64_t p = blockIdx.x;
@@ -456,7 +513,9 @@ __global__ void __launch_bounds__(CH) emit_list_kernel(const ListSrc src, const 
     __syncthreads();
     const int nk = s_mt.num_nkern;
     const int mr = s_mt.mr;
-    emit_prologue(s, s_mt, unit_counts + p * nk, reinterpret_cast<int32_t *>(arena + d.counts_off));
+    uint8_t *xb = exec + exec_offs[p];
+    emit_prologue(s, s_mt, unit_counts + p * nk, reinterpret_cast<int32_t *>(arena + d.counts_off), xb,
+                  (int)sizeof(TV));
     int32_t *out_cols = reinterpret_cast<int32_t *>(arena + d.cols_off);
     TV *out_vals = reinterpret_cast<TV *>(arena + d.values_off);
     const float inv = scales ? 1.0f / scales[p] : 1.0f;
@@ -483,13 +542,18 @@ __global__ void __launch_bounds__(CH) emit_list_kernel(const ListSrc src, const 
         __syncthreads();
         if (t < w && id < nk) {
             const int rank = slot_rank(s, id, t);
-            out_cols[s.start[id] + rank] = (int32_t)(col + coff);
+            const int32_t colv = (int32_t)(col + coff);
+            out_cols[s.start[id] + rank] = colv;
+            reinterpret_cast<int32_t *>(xb + s.xcol[id])[rank] = colv;
+            TV *xv = reinterpret_cast<TV *>(xb + s.xval[id]) + rank * __popc(code);
             int vo = s.vstart[id] + rank * __popc(code);
             for (int r = 0; r < mr; ++r)
                 if ((code >> r) & 1) {
                     float v = dense[col * mr + r];
                     if (DT<TV>::id == SPREG_F16) v *= inv;
-                    out_vals[vo++] = DT<TV>::from_f32(v);
+                    const TV q = DT<TV>::from_f32(v);
+                    out_vals[vo++] = q;
+                    *xv++ = q;
                 }
         }
         __syncthreads();
@@ -602,6 +666,8 @@ void release(spreg_packed *p) {
     if (p->arena) cudaFree(p->arena);
     if (p->descs) cudaFree(p->descs);
     if (p->scales) cudaFree(p->scales);
+    if (p->exec) cudaFree(p->exec);
+    if (p->exec_offs) cudaFree(p->exec_offs);
     delete p;
 }
 
@@ -618,8 +684,10 @@ int finish_pack(const spreg_mapping *m, const Geom &g, int value_dtype, int64_t 
     for (int i = 0; i < 256; ++i) p->id_to_pattern[i] = (uint8_t)(i < nk ? m->id_to_pattern[i] : 0);
     const int64_t units = g.units;
     cudaError_t e = cudaMalloc(&p->descs, (size_t)(units > 0 ? units : 1) * sizeof(spreg_panel_desc));
+    if (e == cudaSuccess) e = cudaMalloc(&p->exec_offs, (size_t)(units + 1) * sizeof(int64_t));
     if (e != cudaSuccess) { release(p); SPREG_FAIL(SPREG_ERR_NOMEM, "cudaMalloc(descs): %s", cudaGetErrorString(e)); }
-    layout_kernel<<<1, 1024, 0, stream>>>(units, nk, vb, g.ppt, g.T, g.P, sc.stats, sc.tile_nnz, p->descs, sc.totals);
+    layout_kernel<<<1, 1024, 0, stream>>>(units, nk, vb, g.ppt, g.T, g.P, sc.stats, sc.tile_nnz, p->descs, sc.totals,
+                                          p->exec_offs);
     PackTotals tot;
     DevError derr;
     cudaMemcpyAsync(&tot, sc.totals, sizeof tot, cudaMemcpyDeviceToHost, stream);
@@ -635,6 +703,11 @@ int finish_pack(const spreg_mapping *m, const Geom &g, int value_dtype, int64_t 
     e = cudaMalloc(&p->arena, (size_t)(arena_bytes > 0 ? arena_bytes : 64));
     if (e != cudaSuccess) { release(p); SPREG_FAIL(SPREG_ERR_NOMEM, "cudaMalloc(arena %lld B): %s", (long long)arena_bytes, cudaGetErrorString(e)); }
     cudaMemsetAsync(p->arena, 0, (size_t)(arena_bytes > 0 ? arena_bytes : 64), stream);
+    p->exec_bytes = tot.exec_bytes;
+    p->max_exec_bytes = tot.max_exec_bytes;
+    e = cudaMalloc(&p->exec, (size_t)(tot.exec_bytes > 0 ? tot.exec_bytes : 64));
+    if (e != cudaSuccess) { release(p); SPREG_FAIL(SPREG_ERR_NOMEM, "cudaMalloc(exec %lld B): %s", (long long)tot.exec_bytes, cudaGetErrorString(e)); }
+    cudaMemsetAsync(p->exec, 0, (size_t)(tot.exec_bytes > 0 ? tot.exec_bytes : 64), stream);
     if (value_dtype == SPREG_F16) {
         e = cudaMalloc(&p->scales, (size_t)(g.P > 0 ? g.P : 1) * sizeof(float));
         if (e != cudaSuccess) { release(p); SPREG_FAIL(SPREG_ERR_NOMEM, "cudaMalloc(scales): %s", cudaGetErrorString(e)); }
@@ -719,19 +792,20 @@ int pack_columns(const spreg_mapping *m, const Geom &g, const Loader &ld, const 
     if (g.units > 0) {
         if (g.units > INT32_MAX) SPREG_FAIL(SPREG_ERR_UNSUPPORTED, "too many packed units");
         count_cols_kernel<Loader><<<(unsigned)g.units, CH, 0, stream>>>(g, ld, mt, sc.unit_counts, sc.stats,
-                                                                          sc.panel_maxabs, sc.tile_nnz, sc.err);
+                                                                          sc.panel_maxabs, sc.tile_nnz, sc.err,
+                                                                          dtype_bytes(value_dtype));
         SPREG_CUDA(cudaGetLastError());
     }
     auto emit = [&](spreg_packed *p) {
         if (value_dtype == SPREG_F32)
             emit_cols_kernel<Loader, float><<<(unsigned)g.units, CH, 0, stream>>>(
-                g, ld, mt, sc.unit_counts, p->descs, p->arena, nullptr, col_offset);
+                g, ld, mt, sc.unit_counts, p->descs, p->arena, nullptr, col_offset, p->exec, p->exec_offs);
         else if (value_dtype == SPREG_BF16)
             emit_cols_kernel<Loader, __nv_bfloat16><<<(unsigned)g.units, CH, 0, stream>>>(
-                g, ld, mt, sc.unit_counts, p->descs, p->arena, nullptr, col_offset);
+                g, ld, mt, sc.unit_counts, p->descs, p->arena, nullptr, col_offset, p->exec, p->exec_offs);
         else
             emit_cols_kernel<Loader, __half><<<(unsigned)g.units, CH, 0, stream>>>(
-                g, ld, mt, sc.unit_counts, p->descs, p->arena, p->scales, col_offset);
+                g, ld, mt, sc.unit_counts, p->descs, p->arena, p->scales, col_offset, p->exec, p->exec_offs);
     };
     return finish_pack(m, g, value_dtype, col_offset, o ? o->m_tile : 0, o ? o->k_tile : 0, sc, mt, emit, out, stream);
 }
@@ -742,7 +816,7 @@ int pack_dense_impl(const spreg_mapping *m, const float *a, int64_t rows, int64_
                     const spreg_pack_opts *o, spreg_packed **out, cudaStream_t stream) {
     SPREG_CHECK_ARG(m && out, "null mapping or output");
     SPREG_CHECK_ARG(rows == 0 || cols == 0 || a, "null matrix");
-    SPREG_CHECK_ARG(lda >= cols, "lda (%lld) < cols (%lld)", (long long)lda, (long long)cols);
+    SPREG_CHECK_ARG(rows == 0 || lda >= cols, "lda (%lld) < cols (%lld)", (long long)lda, (long long)cols);
     Geom g;
     int st = make_geom(m, rows, cols, o, &g);
     if (st != SPREG_OK) return st;
@@ -810,19 +884,20 @@ int pack_lists_impl(const spreg_mapping *m, int64_t rows, int64_t cols, int64_t 
                 (const int64_t *)b_coff.p};
     if (num_panels > 0) {
         count_list_kernel<<<(unsigned)num_panels, CH, 0, stream>>>(src, mt, sc.unit_counts, sc.stats,
-                                                                    sc.panel_maxabs, sc.tile_nnz, sc.err);
+                                                                    sc.panel_maxabs, sc.tile_nnz, sc.err,
+                                                                    dtype_bytes(value_dtype));
         SPREG_CUDA(cudaGetLastError());
     }
     auto emit = [&](spreg_packed *p) {
         if (value_dtype == SPREG_F32)
             emit_list_kernel<float><<<(unsigned)num_panels, CH, 0, stream>>>(src, mt, sc.unit_counts, p->descs,
-                                                                              p->arena, nullptr);
+                                                                              p->arena, nullptr, p->exec, p->exec_offs);
         else if (value_dtype == SPREG_BF16)
-            emit_list_kernel<__nv_bfloat16><<<(unsigned)num_panels, CH, 0, stream>>>(src, mt, sc.unit_counts,
-                                                                                      p->descs, p->arena, nullptr);
+            emit_list_kernel<__nv_bfloat16><<<(unsigned)num_panels, CH, 0, stream>>>(
+                src, mt, sc.unit_counts, p->descs, p->arena, nullptr, p->exec, p->exec_offs);
         else
             emit_list_kernel<__half><<<(unsigned)num_panels, CH, 0, stream>>>(src, mt, sc.unit_counts, p->descs,
-                                                                               p->arena, p->scales);
+                                                                               p->arena, p->scales, p->exec, p->exec_offs);
     };
     return finish_pack(m, g, value_dtype, 0, 0, 0, sc, mt, emit, out, stream);
 }

@@ -115,7 +115,27 @@ struct UnitStats {
     int32_t num_values;  // values V (nnz + padding)
     int32_t padding;     // emitted zeros
     int32_t nnz;         // nonzeros of the unit's dense panel slice
+    int32_t exec_bytes;  // bytes of the unit's execution block
+    int32_t num_groups;  // ids with a nonzero count
 };
+
+// Execution layout: per unit a 16-byte-aligned block read by the executor in one bulk copy:
+//   [ExecHeader][ExecGroup x num_groups][per group: cols (pad to 4 entries) | values (pad to 4 entries, 16 B)]
+// Groups are the ids with a nonzero count, in id order; every group's cols and values start on a
+// 16-byte boundary, so the executor fetches the indices and values of 4 entries with vector loads.
+struct ExecHeader {
+    uint32_t num_groups, block_bytes, pad0, pad1;
+};
+struct ExecGroup {
+    uint32_t pattern, count, cols_off, vals_off;  // offsets in bytes from the block start
+};
+constexpr int kExecPad = 4;  // entries per group are padded to a multiple of this
+__host__ __device__ inline int64_t pad_entries(int64_t n) { return (n + kExecPad - 1) / kExecPad * kExecPad; }
+// Bytes of a group's cols and values sections in the execution block.
+__host__ __device__ inline int64_t exec_cols_bytes(int64_t n) { return pad_entries(n) * 4; }
+__host__ __device__ inline int64_t exec_vals_bytes(int64_t n, int pc, int vb) {
+    return (pad_entries(n) * pc * vb + 15) / 16 * 16;
+}
 
 // Totals written by the layout pass (one struct, copied to the host once).
 struct PackTotals {
@@ -126,6 +146,8 @@ struct PackTotals {
     long long nnz;
     long long required_storage;
     long long empty_units;
+    long long exec_bytes;      // execution layout bytes
+    long long max_exec_bytes;  // largest execution block of one unit
 };
 
 // Device-side check words: first failing unit / code.
@@ -156,4 +178,8 @@ struct spreg_packed {
     spreg_panel_desc *descs = nullptr;
     float *scales = nullptr;
     uint8_t id_to_pattern[256] = {};
+    uint8_t *exec = nullptr;        // execution layout (derived from the arena by the packer)
+    int64_t *exec_offs = nullptr;   // units + 1 block offsets
+    int64_t exec_bytes = 0;
+    int64_t max_exec_bytes = 0;
 };

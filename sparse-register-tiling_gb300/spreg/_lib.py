@@ -66,7 +66,8 @@ class PackOpts(C.Structure):
 class ExecArgs(C.Structure):
     _fields_ = [("b", C.c_void_p), ("ldb", C.c_int64), ("c", C.c_void_p), ("ldc", C.c_int64), ("n", C.c_int64),
                 ("b_dtype", C.c_int32), ("c_dtype", C.c_int32), ("load_c", C.c_int32), ("epilogue", C.c_int32),
-                ("nr", C.c_int32), ("warps_per_cta", C.c_int32)]
+                ("nr", C.c_int32), ("warps_per_cta", C.c_int32), ("b_staging", C.c_int32),
+                ("meta_staging", C.c_int32)]
 
 
 class WorkItem(C.Structure):
@@ -106,6 +107,7 @@ PROTOTYPES = {
     "spreg_tile_destroy": (None, [P]),
     "spreg_execute": (C.c_int, [P, C.POINTER(ExecArgs), P]),
     "spreg_execute_batched": (C.c_int, [P, C.c_int32, P]),
+    "spreg_device_status": (C.c_int, [C.POINTER(C.c_int32), C.c_int32]),
     "spreg_execute_timed": (C.c_int, [P, C.POINTER(ExecArgs), C.c_int64, C.POINTER(C.c_double), P]),
     "spreg_matmul_create": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, P, P, P, C.POINTER(TileConfig), P,
                                       C.POINTER(P)]),

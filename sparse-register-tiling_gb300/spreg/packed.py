@@ -115,24 +115,26 @@ class PackedMatrix:
         return arena[:n_arena], descs[: self.info["num_units"]], sc
 
     # ---------------------------------------------------------------- executor
-    def exec_args(self, B, C_out, n=None, load_c=False, epilogue=_lib.EPILOGUE_NONE, nr=0, warps=0) -> _lib.ExecArgs:
+    def exec_args(self, B, C_out, n=None, load_c=False, epilogue=_lib.EPILOGUE_NONE, nr=0, warps=0,
+                  staging=0, meta=0) -> _lib.ExecArgs:
         n = B.shape[1] if n is None else int(n)
         return _lib.ExecArgs(B.data_ptr(), B.stride(0), C_out.data_ptr(), C_out.stride(0), n,
                              torch_dtype_code(B.dtype), torch_dtype_code(C_out.dtype), int(bool(load_c)),
-                             int(epilogue), int(nr), int(warps))
+                             int(epilogue), int(nr), int(warps), int(staging), int(meta))
 
     def _check_operands(self, B, C_out):
         _require_cuda(B, "B")
         _require_cuda(C_out, "C")
         if B.dim() != 2 or C_out.dim() != 2 or B.stride(1) != 1 or C_out.stride(1) != 1:
             raise ValueError("B and C must be 2-D with unit column stride")
-        if B.shape[0] != self.info["cols"] + self.info["col_offset"] and B.shape[0] < self.info["cols"]:
-            raise ValueError(f"B has {B.shape[0]} rows, A has {self.info['cols']} columns")
+        need = self.info["cols"] + self.info["col_offset"]
+        if B.shape[0] < need:
+            raise ValueError(f"B has {B.shape[0]} rows; the packed column indices reach {need}")
         if C_out.shape[0] != self.info["rows"]:
             raise ValueError(f"C has {C_out.shape[0]} rows, A has {self.info['rows']}")
 
     def execute(self, B, C_out=None, n=None, load_c=False, epilogue=_lib.EPILOGUE_NONE, nr=0, warps=0,
-                out_dtype=None, stream=None):
+                out_dtype=None, stream=None, staging=0, meta=0):
         """C (+)= A . B over the first n columns of B; returns C."""
         import torch
         if C_out is None:
@@ -141,14 +143,15 @@ class PackedMatrix:
             C_out = torch.empty((self.info["rows"], B.shape[1]), device=B.device,
                                 dtype=out_dtype if out_dtype is not None else torch.float32)
         self._check_operands(B, C_out)
-        args = self.exec_args(B, C_out, n, load_c, epilogue, nr, warps)
+        args = self.exec_args(B, C_out, n, load_c, epilogue, nr, warps, staging, meta)
         _lib.check(_lib.lib().spreg_execute(self._h, C.byref(args), _lib.stream_handle(stream)))
         return C_out
 
-    def execute_timed(self, B, C_out, num_runs: int = 1, n=None, nr=0, warps=0, stream=None) -> float:
+    def execute_timed(self, B, C_out, num_runs: int = 1, n=None, nr=0, warps=0, stream=None, staging=0,
+                      meta=0) -> float:
         """Median per-run time (ns) over 150 x num_runs runs of C = A . B (template:308-349)."""
         self._check_operands(B, C_out)
-        args = self.exec_args(B, C_out, n, False, 0, nr, warps)
+        args = self.exec_args(B, C_out, n, False, 0, nr, warps, staging, meta)
         t = C.c_double()
         _lib.check(_lib.lib().spreg_execute_timed(self._h, C.byref(args), int(num_runs), C.byref(t),
                                                   _lib.stream_handle(stream)))
@@ -171,6 +174,13 @@ class PackedMatrix:
                 self._h = None
         except Exception:
             pass
+
+
+def device_status(reset: bool = False) -> int:
+    """Status word of the current device (nonzero: a kernel gave up a bounded wait)."""
+    v = C.c_int32()
+    _lib.check(_lib.lib().spreg_device_status(C.byref(v), int(bool(reset))))
+    return int(v.value)
 
 
 def execute_batched(items, stream=None) -> None:

@@ -89,7 +89,7 @@ def test_pack_rejects_uncovering_mapping(cuda):
         gpu_pack(A, bad)
 
 
-def _exec_both(pm, ref, B, n=None, nr=0, load_c=False, C0=None, epilogue=0, c_dtype=_lib.F32):
+def _exec_both(pm, ref, B, n=None, nr=0, load_c=False, C0=None, epilogue=0, c_dtype=_lib.F32, meta=0):
     torch_b = {_lib.F32: torch.float32, _lib.BF16: torch.bfloat16, _lib.F16: torch.float16}[pm.value_dtype]
     tb = torch.from_numpy(B).to(torch_b).cuda()
     Bref = B if pm.value_dtype == _lib.F32 else tb.cpu().view(torch.int16).numpy().view(np.uint16)
@@ -99,7 +99,7 @@ def _exec_both(pm, ref, B, n=None, nr=0, load_c=False, C0=None, epilogue=0, c_dt
     if C0 is not None:
         Cg.copy_(torch.from_numpy(C0).to(out_t))
         Cr[...] = C0 if c_dtype == _lib.F32 else Cg.cpu().view(torch.int16).numpy().view(np.uint16)
-    pm.execute(tb, Cg, n=n, nr=nr, load_c=load_c, epilogue=epilogue)
+    pm.execute(tb, Cg, n=n, nr=nr, load_c=load_c, epilogue=epilogue, meta=meta)
     ref.execute(Bref, Cr, n=n, load_c=load_c, epilogue=epilogue, c_dtype=c_dtype)
     got = Cg.cpu()
     got = got.numpy() if c_dtype == _lib.F32 else got.view(torch.int16).numpy().view(np.uint16)
@@ -107,27 +107,31 @@ def _exec_both(pm, ref, B, n=None, nr=0, load_c=False, C0=None, epilogue=0, c_dt
 
 
 @pytest.mark.parametrize("mkey", ["id2", "id4", "id6", "id8", "400fa", "747f9", "33960", "75f82"])
-@pytest.mark.parametrize("n,nr", [(1, 0), (31, 32), (64, 64), (100, 0), (256, 128), (257, 256), (512, 0), (96, 64)])
-def test_execute_fp32_bit_exact(cuda, mkey, n, nr):
+@pytest.mark.parametrize("n,nr", [(1, 0), (31, 32), (64, 64), (100, 0), (256, 128), (257, 128), (512, 0), (96, 64)])
+@pytest.mark.parametrize("meta", [1, 2])
+def test_execute_fp32_bit_exact(cuda, mkey, n, nr, meta):
+    """Both executor kernels (execution-layout blocks staged per warp / arena streamed through
+    registers) against the oracle."""
     m = MAPPINGS[mkey]()
     A = synth.row_skew(70, 300, 0.85, seed=n, std=1.0)
     B = synth.dense(300, n, seed=n + 1)
     pm, ref = gpu_pack(A, m), O.Packed(O.Tables.of(m), A)
-    got, want = _exec_both(pm, ref, B, nr=nr)
+    got, want = _exec_both(pm, ref, B, nr=nr, meta=meta)
     assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
     assert O.rel_err(got, O.dense_fp64(A, B)) <= 1e-5
 
 
 @pytest.mark.parametrize("vd", [_lib.F32, _lib.BF16, _lib.F16])
 @pytest.mark.parametrize("load_c,epi", [(False, 0), (True, 0), (True, 1), (False, 1)])
-def test_execute_dtypes_load_c_epilogue(cuda, vd, load_c, epi):
-    m = Mapping.identity(4)
+@pytest.mark.parametrize("meta", [1, 2])
+def test_execute_dtypes_load_c_epilogue(cuda, vd, load_c, epi, meta):
+    m = Mapping.identity(4) if meta == 1 else Mapping.load("400fa")
     A = synth.row_skew(66, 200, 0.8, seed=2, std=0.02)
     B = synth.dense(200, 130, seed=3)
     C0 = synth.dense(66, 130, seed=4)
     pm = gpu_pack(A, m, value_dtype=vd)
     ref = O.Packed(O.Tables.of(m), A, value_dtype=vd)
-    got, want = _exec_both(pm, ref, B, load_c=load_c, C0=C0 if load_c else None, epilogue=epi)
+    got, want = _exec_both(pm, ref, B, load_c=load_c, C0=C0 if load_c else None, epilogue=epi, meta=meta)
     assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
     exact = O.dense_fp64(A, B) + (C0 if load_c else 0)
     if epi:
@@ -146,7 +150,7 @@ def test_execute_bf16_output(cuda):
 
 
 @pytest.mark.parametrize("tiles", [(8, 64), (16, 256), (4, 7)])
-def test_execute_tiled_bit_exact(cuda, tiles):
+def test_execute_tiled_bit_exact_auto(cuda, tiles):
     m = Mapping.identity(4)
     A = synth.row_skew(90, 333, 0.9, seed=7, std=1.0)
     A[:, 64:128] = 0
@@ -268,18 +272,28 @@ def test_matmul_specialized_host_and_device(cuda):
 
 
 def test_execute_batched_equals_individual(cuda):
-    m = Mapping.identity(4)
-    items, want = [], []
-    for i, (M, K, N) in enumerate([(64, 128, 32), (100, 77, 257), (8, 512, 1), (256, 64, 128)]):
+    """Uneven SpMMs (mappings, M_r, dtypes, N with tails, K tiles) in one call: each result is the
+    same as its own call and as the oracle."""
+    cases = [(64, 128, 32, "id4", _lib.F32, 0), (100, 77, 257, "400fa", _lib.F32, 0), (8, 512, 1, "id4", _lib.F32, 0),
+             (256, 64, 128, "id4", _lib.BF16, 0), (300, 200, 96, "747f9", _lib.BF16, 0),
+             (90, 333, 200, "id4", _lib.F32, 64), (512, 512, 512, "id4", _lib.F32, 0)]
+    items, want, refs = [], [], []
+    for i, (M, K, N, mk, vd, kt) in enumerate(cases):
+        m = MAPPINGS[mk]()
         A = synth.row_skew(M, K, 0.8, seed=i, std=1.0)
-        B = torch.from_numpy(synth.dense(K, N, seed=100 + i)).cuda()
-        pm = gpu_pack(A, m)
+        Bn = synth.dense(K, N, seed=100 + i)
+        tdt = torch.float32 if vd == _lib.F32 else torch.bfloat16
+        B = torch.from_numpy(Bn).to(tdt).cuda()
+        pm = gpu_pack(A, m, value_dtype=vd, k_tile=kt)
         Cb = torch.zeros((M, N), device="cuda")
         items.append((pm, B, Cb, {}))
         want.append(pm.execute(B))
+        ref = O.Packed(O.Tables.of(m), A, value_dtype=vd, k_tile=kt)
+        refs.append(ref.execute(Bn if vd == _lib.F32 else B.cpu().view(torch.int16).numpy().view(np.uint16)))
     execute_batched(items)
-    for (pm, B, Cb, _), w in zip(items, want):
+    for (pm, B, Cb, _), w, r in zip(items, want, refs):
         assert torch.equal(Cb, w)
+        assert np.array_equal(Cb.cpu().numpy().view(np.uint32), r.view(np.uint32))
 
 
 def test_empty_and_degenerate(cuda):
@@ -289,3 +303,61 @@ def test_empty_and_degenerate(cuda):
         pm = gpu_pack(A, m)
         C = pm.execute(torch.ones((shape[1], 9), device="cuda"))
         assert torch.all(C == 0) and C.shape == (shape[0], 9)
+
+
+@pytest.mark.parametrize("mkey", ["id4", "id6", "id8", "400fa", "747f9"])
+@pytest.mark.parametrize("meta", [1, 2])
+@pytest.mark.parametrize("vd", [_lib.F32, _lib.BF16])
+@pytest.mark.parametrize("n,nr", [(128, 64), (256, 128), (512, 0), (300, 64), (64, 32)])
+def test_execute_kernels_bit_exact(cuda, mkey, meta, vd, n, nr):
+    """Batched execution-layout kernel (meta 1) and register-stream kernel (meta 2): identical bits."""
+    m = MAPPINGS[mkey]()
+    A = synth.row_skew(520, 384, 0.9, seed=n + nr, std=0.5)
+    B = synth.dense(384, n, seed=n)
+    pm, ref = gpu_pack(A, m, value_dtype=vd), O.Packed(O.Tables.of(m), A, value_dtype=vd)
+    torch_b = torch.float32 if vd == _lib.F32 else torch.bfloat16
+    tb = torch.from_numpy(B).to(torch_b).cuda()
+    Cg = pm.execute(tb, nr=nr, meta=meta).cpu().numpy()
+    Bref = B if vd == _lib.F32 else tb.cpu().view(torch.int16).numpy().view(np.uint16)
+    want = ref.execute(Bref)
+    assert np.array_equal(Cg.view(np.uint32), want.view(np.uint32))
+
+
+def test_b_staging_request_is_rejected(cuda):
+    m = Mapping.identity(4)
+    pm = gpu_pack(synth.bernoulli(64, 64, 0.5, seed=1), m)
+    with pytest.raises(_lib.SpregError, match="not offered"):
+        pm.execute(torch.ones((64, 64), device="cuda"), staging=1)
+
+
+@pytest.mark.parametrize("meta", [1, 2])
+def test_execute_with_col_offset(cuda, meta):
+    """A tile packed with a column offset reads B rows [offset, offset + K)."""
+    m = Mapping.identity(4)
+    A = synth.row_skew(256, 200, 0.85, seed=3, std=1.0)
+    off = 37
+    B = synth.dense(200 + off + 11, 256, seed=4)
+    pm = gpu_pack(A, m, col_offset=off)
+    ref = O.Packed(O.Tables.of(m), A, col_offset=off)
+    C = pm.execute(torch.from_numpy(B).cuda(), nr=64, meta=meta).cpu().numpy()
+    assert np.array_equal(C.view(np.uint32), ref.execute(B).view(np.uint32))
+    assert O.rel_err(C, O.dense_fp64(A, B[off:off + 200])) <= 1e-5
+
+
+@pytest.mark.parametrize("tiles", [(8, 64), (16, 256), (4, 7)])
+@pytest.mark.parametrize("meta", [1, 2])
+def test_execute_tiled_kernels(cuda, tiles, meta):
+    """K-tiled packs on both kernels: units of one row panel run in K-tile order."""
+    m = Mapping.load("400fa") if tiles[0] % 8 == 0 else Mapping.identity(4)
+    A = synth.row_skew(90, 333, 0.9, seed=7, std=1.0)
+    A[:, 64:128] = 0
+    B = synth.dense(333, 200, seed=8)
+    pm = gpu_pack(A, m, m_tile=tiles[0], k_tile=tiles[1])
+    ref = O.Packed(O.Tables.of(m), A, m_tile=tiles[0], k_tile=tiles[1])
+    got, want = _exec_both(pm, ref, B, meta=meta)
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
+def test_device_status_clear(cuda):
+    from spreg.packed import device_status
+    assert device_status(reset=True) == 0
