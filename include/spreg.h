@@ -201,6 +201,20 @@ typedef struct {
 
 int spreg_execute_batched(const spreg_work_item *items_host, int32_t num_items, spreg_stream_t stream);
 
+/* Executor for callers that cannot allocate device memory while they run it (a serving loop whose
+ * memory belongs to another allocator, or a path that must not add the synchronisation a first
+ * cudaMalloc can cause).  Same work list and results as spreg_execute_batched, but it calls no
+ * cudaMalloc / cudaFree: its scratch (a status word and one work counter per launch) is a static
+ * device array of SPREG_NOALLOC_MAX_LAUNCHES + 1 ints that every GPU loading the library keeps
+ * until exit.  A list that needs more than SPREG_NOALLOC_MAX_LAUNCHES launches (one launch per
+ * group of up to 224 SpMMs of one M_r / strip width / dtype combination) is rejected.  The first
+ * call on each device looks up the array's device address; make it before any stream capture.
+ * Calls share the array and clear it at their start, so calls that overlap on the GPU race.
+ * Runs only the batched execution-layout kernel (no meta_staging = 2, no oversized blocks).
+ * It has no counterpart in the reference. */
+#define SPREG_NOALLOC_MAX_LAUNCHES 64
+int spreg_execute_batched_noalloc(const spreg_work_item *items_host, int32_t num_items, spreg_stream_t stream);
+
 /* Status word of the current device: nonzero once a kernel gave up a bounded wait (its results
  * are then incomplete).  Synchronous; reset != 0 clears it. */
 int spreg_device_status(int32_t *status_host, int32_t reset);

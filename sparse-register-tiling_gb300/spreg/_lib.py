@@ -108,6 +108,7 @@ PROTOTYPES = {
     "spreg_execute": (C.c_int, [P, C.POINTER(ExecArgs), P]),
     "spreg_execute_batched": (C.c_int, [P, C.c_int32, P]),
     "spreg_device_status": (C.c_int, [C.POINTER(C.c_int32), C.c_int32]),
+    "spreg_execute_batched_noalloc": (C.c_int, [P, C.c_int32, P]),
     "spreg_execute_timed": (C.c_int, [P, C.POINTER(ExecArgs), C.c_int64, C.POINTER(C.c_double), P]),
     "spreg_matmul_create": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, P, P, P, C.POINTER(TileConfig), P,
                                       C.POINTER(P)]),
