@@ -41,7 +41,7 @@ L2_BYTES = 129 * 2 ** 20
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["spreg", "reference"], default="spreg")
     ap.add_argument("--replicas", type=int, default=96)
@@ -58,6 +58,10 @@ def parse():
     ap.add_argument("--batched", type=int, default=1, help="1: one batched launch per step; 0: one launch per SpMM")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline budget; 0 skips it")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end leg")
+    ap.add_argument("--serving", type=int, default=1, help="1: add the serving-loop measurement to the line")
+    ap.add_argument("--serve-requests", type=int, default=768)
+    ap.add_argument("--serve-slots", type=int, default=128)
+    ap.add_argument("--serve-budget-mb", type=int, default=1024)
     return ap.parse_args()
 
 
@@ -161,6 +165,76 @@ def measured_peaks():
             d = json.load(f)
         return float(d["hbm_gbs"]), "measured"
     return 6800.0, "fallback"
+
+
+def serving_bench(args, dev) -> dict:
+    """12-block sparse MLP (d_model 1024, d_ff 4096, 90 % row-skew, BF16-representable weights
+    N(0, 0.02)) served to requests of log-normal token counts (median 64, sigma 1, 1..2048):
+    the continuous-batching BF16 server against the plain per-request FP32 path."""
+    import torch
+    from spreg import synth
+    from spreg.serving import (Request, Server, SparseMLP, mlp_reference_fp64, mlp_weights, output_fp32,
+                               prepare_requests, serve_per_request)
+    d_model, d_ff, blocks = 1024, 4096, 12
+    w = mlp_weights(d_model, d_ff, blocks, 0.9, seed=77, std=0.02, sigma=0.5)
+    bf = SparseMLP(w, "bf16", device=dev)
+    fp = SparseMLP(w, "f32", device=dev)
+    R = args.serve_requests
+    ns = synth.token_counts(R, median=64, sigma=1.0, lo=1, hi=2048, seed=5)
+    g = synth.rng(6)
+    xs = [synth.round_bf16(g.standard_normal((d_model, int(n))).astype(np.float32)) for n in ns]
+
+    def reqs_for(model, count, rate, seed):
+        arr = synth.poisson_arrivals(count, rate, seed=seed)
+        rs = [Request(i, int(ns[i]), x=xs[i], arrival=float(arr[i])) for i in range(count)]
+        prepare_requests(model, rs)
+        return rs
+
+    server = Server(bf, budget_bytes=args.serve_budget_mb << 20, max_slots=args.serve_slots)
+    server.run(reqs_for(bf, 16, float("inf"), 1))        # warm-up (first-call set-up, caches)
+    serve_per_request(fp, reqs_for(fp, 8, float("inf"), 1))
+    torch.cuda.synchronize()
+
+    # capacity: every request queued at t = 0
+    rb = reqs_for(bf, R, float("inf"), 2)
+    cap_b = server.run(rb)
+    n_plain = max(32, R // 3)
+    rp = reqs_for(fp, n_plain, float("inf"), 2)
+    cap_p = serve_per_request(fp, rp)
+
+    # accuracy of served outputs against the FP64 stack (three small requests)
+    pick = [i for i in np.argsort(ns[:n_plain])[:3]]
+    err_b = max(float(np.linalg.norm(output_fp32(rb[i]) - (ref := mlp_reference_fp64(w, xs[i])))
+                      / np.linalg.norm(ref)) for i in pick)
+    err_p = max(float(np.linalg.norm(output_fp32(rp[i]) - (ref := mlp_reference_fp64(w, xs[i])))
+                      / np.linalg.norm(ref)) for i in pick)
+
+    # latency under Poisson arrivals at rates relative to the per-request path's capacity
+    sweep = []
+    for mult in (0.5, 0.9, 2.0, 4.0):
+        rate = mult * cap_p.req_per_s
+        cnt_b = min(R, max(64, int(rate * 0.5)))
+        sb = server.run(reqs_for(bf, cnt_b, rate, 10 + int(mult * 10)))
+        row = {"rate_req_s": rate, "batched_bf16": _stat(sb)}
+        if mult <= 2.0:
+            cnt_p = min(n_plain, max(32, int(rate * 0.3)))
+            row["per_request_fp32"] = _stat(serve_per_request(fp, reqs_for(fp, cnt_p, rate, 10 + int(mult * 10))))
+        sweep.append(row)
+    return {"workload": "12-block sparse MLP d_model 1024 / d_ff 4096 @90% row-skew, BF16-representable weights "
+                        "N(0,0.02), tokens log-normal(median 64, sigma 1) in 1..2048, residual stream",
+            "batched_bf16": _stat(cap_b) | {"max_batch": cap_b.max_batch, "iterations": cap_b.iterations,
+                                           "peak_activation_mib": cap_b.peak_activation_bytes / 2 ** 20,
+                                           "slots": args.serve_slots, "budget_mib": args.serve_budget_mb},
+            "per_request_fp32": _stat(cap_p),
+            "req_s_ratio": cap_b.req_per_s / cap_p.req_per_s,
+            "rel_err_vs_fp64": {"batched_bf16": err_b, "per_request_fp32": err_p, "bf16_tolerance": 1e-2},
+            "sweep": sweep,
+            "capacity_note": "capacity = all requests queued at t=0; latency = arrival to output in host memory"}
+
+
+def _stat(st) -> dict:
+    return {"req_s": st.req_per_s, "tokens_s": st.tokens_per_s, "p50_ms": st.p50_ms, "p99_ms": st.p99_ms,
+            "mean_ms": st.mean_ms, "requests": st.requests}
 
 
 def cpu_baseline(As, Bs, args, seconds: float, threads: int = 0):
@@ -362,6 +436,10 @@ def main():
            "bit_exact_vs_oracle": e2e_ok}
     del mms
 
+    serving = None
+    if args.serving:
+        serving = serving_bench(args, dev)
+
     cpu = None
     if rank == 0 and args.cpu_seconds > 0:
         cpu = cpu_baseline(As, Bs, args, args.cpu_seconds)
@@ -378,7 +456,7 @@ def main():
                            "l2": f"inputs larger than L2: working set {working_set / 2**20:.0f} MiB per step "
                                  f"vs {L2_BYTES / 2**20:.0f} MiB L2",
                            "parallelism": f"replicas x{ws}"},
-                "gflops": gflops, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+                "gflops": gflops, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "serving": serving,
                 "clocks": clk.summary(), "gpu_launches": launches_per_step * args.steps,
                 "parity_bit_exact_vs_oracle": parity_ok}
         print(json.dumps(line))

@@ -69,3 +69,26 @@ def to_csr(a: np.ndarray):
 
 def sparsity_of(a: np.ndarray) -> float:
     return 1.0 - np.count_nonzero(a) / max(a.size, 1)
+
+
+def round_bf16(a: np.ndarray) -> np.ndarray:
+    """FP32 values rounded to the nearest BF16 value (ties to even), returned as FP32 (finite input)."""
+    u = np.ascontiguousarray(a, dtype=np.float32).view(np.uint32).astype(np.uint64)
+    u = (u + 0x7FFF + ((u >> 16) & 1)) & 0xFFFF0000
+    return u.astype(np.uint32).view(np.float32)
+
+
+def token_counts(count: int, median: float = 64.0, sigma: float = 1.0, lo: int = 1, hi: int = 2048,
+                 seed: int = 0) -> np.ndarray:
+    """Per-request token counts ~ log-normal(median, sigma), rounded and clipped to [lo, hi]."""
+    g = rng(seed)
+    n = np.rint(median * np.exp(sigma * g.standard_normal(count)))
+    return np.clip(n, lo, hi).astype(np.int64)
+
+
+def poisson_arrivals(count: int, rate: float, seed: int = 0) -> np.ndarray:
+    """Arrival times (s) of a Poisson process of the given rate (req/s); rate = inf puts all at 0."""
+    if not np.isfinite(rate):
+        return np.zeros(count)
+    g = rng(seed)
+    return np.cumsum(g.exponential(1.0 / rate, count))
