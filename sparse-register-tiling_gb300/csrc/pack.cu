@@ -276,7 +276,7 @@ __global__ void __launch_bounds__(1024) layout_kernel(const int64_t units, const
     if (t == 0) { s_carry = 0; s_xcarry = 0; }
     if (t < 8) s_acc[t] = 0;
     __syncthreads();
-    long long my_v = 0, my_u = 0, my_pad = 0, my_nnz = 0, my_req = 0, my_empty = 0;
+    long long my_v = 0, my_u = 0, my_pad = 0, my_nnz = 0, my_req = 0, my_empty = 0, my_xmax = 0;
     for (int64_t base = 0; base < units; base += 1024) {
         const int64_t u = base + t;
         long long size = 0, xsize = 0;
@@ -284,7 +284,7 @@ __global__ void __launch_bounds__(1024) layout_kernel(const int64_t units, const
         if (u < units) {
             st = stats[u];
             xsize = st.exec_bytes;
-            atomicMax(&s_acc[7], (unsigned long long)xsize);
+            my_xmax = xsize > my_xmax ? xsize : my_xmax;
             size = align64((int64_t)st.num_values * vb) + align64((int64_t)st.num_cols * 4) + align64((int64_t)nk * 4);
             my_v += st.num_values;
             my_u += st.num_cols;
@@ -321,12 +321,26 @@ __global__ void __launch_bounds__(1024) layout_kernel(const int64_t units, const
         if (t == 0) { s_carry += s_scan[1023]; s_xcarry += s_xscan[1023]; }
         __syncthreads();
     }
-    atomicAdd(&s_acc[0], (unsigned long long)my_v);
-    atomicAdd(&s_acc[1], (unsigned long long)my_u);
-    atomicAdd(&s_acc[2], (unsigned long long)my_pad);
-    atomicAdd(&s_acc[3], (unsigned long long)my_nnz);
-    atomicAdd(&s_acc[4], (unsigned long long)my_req);
-    atomicAdd(&s_acc[5], (unsigned long long)my_empty);
+    // warp sums first: one shared atomic per warp instead of 1024 contending ones
+    for (int o = 16; o > 0; o >>= 1) {
+        my_v += __shfl_down_sync(0xffffffffu, my_v, o);
+        my_u += __shfl_down_sync(0xffffffffu, my_u, o);
+        my_pad += __shfl_down_sync(0xffffffffu, my_pad, o);
+        my_nnz += __shfl_down_sync(0xffffffffu, my_nnz, o);
+        my_req += __shfl_down_sync(0xffffffffu, my_req, o);
+        my_empty += __shfl_down_sync(0xffffffffu, my_empty, o);
+        const long long xm = __shfl_down_sync(0xffffffffu, my_xmax, o);
+        my_xmax = xm > my_xmax ? xm : my_xmax;
+    }
+    if ((t & 31) == 0) {
+        atomicAdd(&s_acc[0], (unsigned long long)my_v);
+        atomicAdd(&s_acc[1], (unsigned long long)my_u);
+        atomicAdd(&s_acc[2], (unsigned long long)my_pad);
+        atomicAdd(&s_acc[3], (unsigned long long)my_nnz);
+        atomicAdd(&s_acc[4], (unsigned long long)my_req);
+        atomicAdd(&s_acc[5], (unsigned long long)my_empty);
+        atomicMax(&s_acc[7], (unsigned long long)my_xmax);
+    }
     __syncthreads();
     if (t == 0) {
         tot->arena_bytes = s_carry;
