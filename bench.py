@@ -174,11 +174,14 @@ def serving_bench(args, dev) -> dict:
     import torch
     from spreg import synth
     from spreg.serving import (Request, Server, SparseMLP, mlp_reference_fp64, mlp_weights, output_fp32,
-                               prepare_requests, serve_per_request)
+                               prepare_requests, serve_per_request, tune_mlp)
     d_model, d_ff, blocks = 1024, 4096, 12
     w = mlp_weights(d_model, d_ff, blocks, 0.9, seed=77, std=0.02, sigma=0.5)
-    bf = SparseMLP(w, "bf16", device=dev)
-    fp = SparseMLP(w, "f32", device=dev)
+    t_tune = time.perf_counter()
+    configs, tuned = tune_mlp(w, "bf16", n=96, batch=32, device=dev)
+    t_tune = time.perf_counter() - t_tune
+    bf = SparseMLP(w, "bf16", device=dev, configs=configs)
+    fp = SparseMLP(w, "f32", device=dev)  # the plain path: M_r = 4 identity, untiled, auto N_r
     R = args.serve_requests
     ns = synth.token_counts(R, median=64, sigma=1.0, lo=1, hi=2048, seed=5)
     g = synth.rng(6)
@@ -225,7 +228,10 @@ def serving_bench(args, dev) -> dict:
             "batched_bf16": _stat(cap_b) | {"max_batch": cap_b.max_batch, "iterations": cap_b.iterations,
                                            "peak_activation_mib": cap_b.peak_activation_bytes / 2 ** 20,
                                            "slots": args.serve_slots, "budget_mib": args.serve_budget_mb},
-            "per_request_fp32": _stat(cap_p),
+            "per_request_fp32": _stat(cap_p) | {"packing": "M_r=4 identity, untiled, N_r auto"},
+            "autotuned_packing": {"up": tuned[0].best.name(), "down": tuned[1].best.name(),
+                                  "tune_seconds": t_tune,
+                                  "measured_ns_per_spmm": {"up": tuned[0].measured_ns, "down": tuned[1].measured_ns}},
             "req_s_ratio": cap_b.req_per_s / cap_p.req_per_s,
             "rel_err_vs_fp64": {"batched_bf16": err_b, "per_request_fp32": err_p, "bf16_tolerance": 1e-2},
             "sweep": sweep,

@@ -221,9 +221,14 @@ def mlp_reference_fp64(weights, x: np.ndarray) -> np.ndarray:
 
 class SparseMLP:
     """Packed, device-resident weights of a sparse MLP stack, stored as ``dtype`` ("bf16"/"f32");
-    activations use the same type and accumulate in FP32."""
+    activations use the same type and accumulate in FP32.
 
-    def __init__(self, weights, dtype: str = "bf16", mapping: Optional[Mapping] = None, device=None):
+    ``configs`` (one dict per layer, keys ``mr``, ``mapping``, ``k_tile``; see `tune_mlp`) packs each
+    layer with its own panel height, nanokernel set and K tile; by default every layer uses
+    ``mapping`` (M_r = 4 identity) untiled."""
+
+    def __init__(self, weights, dtype: str = "bf16", mapping: Optional[Mapping] = None, device=None,
+                 configs: Optional[Sequence[dict]] = None):
         import torch
         from .packed import PackedMatrix
         if dtype not in ("bf16", "f32"):
@@ -235,13 +240,21 @@ class SparseMLP:
         self.act_torch = torch.bfloat16 if dtype == "bf16" else torch.float32
         self.elem = 2 if dtype == "bf16" else 4
         self.d_ff, self.d_model = weights[0][0].shape
+        if configs is not None and len(configs) != 2 * len(weights):
+            raise ValueError(f"configs needs one entry per layer ({2 * len(weights)}), got {len(configs)}")
+        self.configs = list(configs) if configs is not None else None
         self.layers = []
-        for wu, wd in weights:
+        for b, (wu, wd) in enumerate(weights):
             if wu.shape != (self.d_ff, self.d_model) or wd.shape != (self.d_model, self.d_ff):
                 raise ValueError("every block needs W_up d_ff x d_model and W_down d_model x d_ff")
-            for w in (wu, wd):
+            for j, w in enumerate((wu, wd)):
                 t = torch.from_numpy(np.ascontiguousarray(w, dtype=np.float32)).to(self.device)
-                self.layers.append(PackedMatrix.from_dense(t, self.mapping, value_dtype=self.act_code))
+                mp, kt = self.mapping, 0
+                if self.configs is not None:
+                    from .autotune import mapping_of
+                    cfg = self.configs[2 * b + j]
+                    mp, kt = mapping_of(int(cfg["mr"]), cfg["mapping"]), int(cfg.get("k_tile", 0))
+                self.layers.append(PackedMatrix.from_dense(t, mp, k_tile=kt, value_dtype=self.act_code))
                 del t
         self.blocks = len(weights)
 
@@ -283,6 +296,16 @@ class SparseMLP:
             up.execute(x_dev, h_dev, n=n, epilogue=_lib.EPILOGUE_RELU, stream=stream)
             down.execute(h_dev, x_dev, n=n, load_c=True, stream=stream)
         return x_dev
+
+
+def tune_mlp(weights, dtype: str = "bf16", n: int = 96, batch: int = 32, top: int = 6, device=None):
+    """Per-layer packings for `SparseMLP` from the autotuner: block 0's up and down projections are
+    tuned for ``batch`` concurrent requests of ``n`` tokens and every block reuses them (all blocks
+    share shapes and sparsity).  Returns (configs, tune results)."""
+    from .autotune import tune
+    res = [tune(w, n, dtype, top=top, batch=batch, device=device) for w in weights[0]]
+    cfg = [{"mr": r.best.mr, "mapping": r.best.mapping, "k_tile": r.best.k_tile, "nr": r.best.nr} for r in res]
+    return [dict(cfg[l % 2]) for l in range(2 * len(weights))], res
 
 
 # ---------------------------------------------------------------------------- serving

@@ -1,0 +1,103 @@
+"""Autotuner: statistics against the oracle packing, cost-model fitting, ranking; GPU tuning."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from spreg import synth
+from spreg.autotune import (Candidate, Costs, candidates, fit_costs, heuristic_bucket, mapping_of, model_row,
+                            panel_codes, panel_stats, rank)
+
+CASES = [(2, "identity"), (4, "identity"), (8, "identity"), (8, "400fa"), (8, "747f9")]
+
+
+@pytest.mark.parametrize("mr,mp", CASES)
+@pytest.mark.parametrize("shape,sp", [((61, 97), 0.8), ((128, 256), 0.95), ((37, 64), 0.5)])
+def test_panel_stats_match_oracle_packing(mr, mp, shape, sp):
+    A = synth.row_skew(*shape, sp, seed=shape[0] + mr, sigma=0.5)
+    m = mapping_of(mr, mp)
+    st = panel_stats(A != 0, mr, m)
+    pk = O.Packed(O.Tables.of(m), A)
+    assert st.P == pk.num_panels
+    assert st.U == pk.sizes["num_col_indices"]
+    assert st.V == pk.sizes["num_values"]
+    assert st.padding == pk.sizes["padding"]
+    assert st.nnz == pk.sizes["nnz"]
+    # G: nonzero nkern_counts of every panel, read out of the oracle arena
+    nk = pk.t.num_nkern
+    G = 0
+    maxU = 0
+    for d in pk.descs:
+        counts = pk.arena[d["counts_off"]: d["counts_off"] + 4 * nk].view(np.int32)
+        G += int(np.count_nonzero(counts))
+        maxU = max(maxU, int(d["num_cols"]))
+    assert st.G == G
+    assert st.max_panel_U == maxU
+
+
+def test_panel_codes_bits():
+    mask = np.zeros((5, 3), dtype=bool)
+    mask[0, 0] = mask[3, 0] = mask[4, 2] = True
+    c = panel_codes(mask, 4)
+    assert c.shape == (2, 3)
+    assert c[0, 0] == 0b1001 and c[1, 2] == 0b0001 and c[0, 1] == 0
+
+
+def test_heuristic_buckets():
+    assert heuristic_bucket(0.65, 32) == ("(0,0.7]", 32)
+    assert heuristic_bucket(0.75, 100) == ("(0.7,0.8]", 128)
+    assert heuristic_bucket(0.9, 300) == ("(0.8,0.9]", 256)
+    assert heuristic_bucket(0.98, 4096) == ("(0.9,1]", 512)
+
+
+def test_fit_costs_recovers_coefficients():
+    true = [3000.0, 15.0, 5.0, 2.0, 0.5, 30.0]
+    samples = []
+    for i, (shape, sp) in enumerate([((512, 512), 0.8), ((1024, 256), 0.9), ((256, 2048), 0.95),
+                                     ((2048, 512), 0.7), ((640, 640), 0.85), ((300, 900), 0.6)]):
+        st = panel_stats(synth.row_skew(*shape, sp, seed=i) != 0, 4, mapping_of(4, "identity"))
+        for n in (16, 64, 256, 1000):
+            samples.append(("f32", st, n, 2, float(np.dot(true, model_row(st, n, 2)))))
+    c = fit_costs(samples)
+    np.testing.assert_allclose(c.table[Costs.key(4, 2, "f32")], true, rtol=1e-6, atol=1e-6)
+
+
+def test_costs_save_load(tmp_path):
+    c = Costs.default()
+    c.table[Costs.key(8, 4, "bf16")] = [1.0, 2.0, 3.0, 4.0, 5.0, 6.0]
+    p = tmp_path / "c.json"
+    c.save(str(p), {"samples": 3})
+    d = Costs.load(str(p))
+    assert d.table[Costs.key(8, 4, "bf16")] == [1.0, 2.0, 3.0, 4.0, 5.0, 6.0]
+
+
+def test_rank_orders_all_candidates():
+    A = synth.row_skew(512, 512, 0.9, seed=1)
+    ranked, stats = rank(A != 0, 48, "f32", Costs.default())
+    ts = [t for t, _ in ranked]
+    assert ts == sorted(ts)
+    names = {c.name() for _, c in ranked}
+    assert names == {c.name() for c in candidates(48)}
+    assert "M4N64_identity" in names and "M8N32_400fa" in names and "M4N128_identity" not in names
+    assert set(stats) == {(2, "identity"), (4, "identity"), (8, "identity"), (8, "400fa"), (8, "747f9")}
+    assert Candidate(4, "identity", 64).name() == "M4N64_identity"
+    assert Candidate(2, "identity", 32, 1024).name() == "M2N32_identity_K1024"
+    wide = {c.name() for c in candidates(64, (2,), k=2048)}
+    assert {"M2N64_identity", "M2N64_identity_K512", "M2N64_identity_K1024"} <= wide
+    assert not any("_K" in c.name() for c in candidates(64, (4,), k=512))
+
+
+@pytest.mark.gpu
+def test_tune_picks_a_measured_candidate_and_it_is_exact(cuda):
+    import torch
+    from spreg import PackedMatrix
+    from spreg.autotune import tune
+    A = synth.row_skew(1024, 512, 0.9, seed=4)
+    res = tune(A, 128, "f32", top=3)
+    assert res.best.name() in res.measured_ns and len(res.measured_ns) == 3
+    assert res.measured_ns[res.best.name()] == min(res.measured_ns.values())
+    m = mapping_of(res.best.mr, res.best.mapping)
+    B = synth.dense(512, 128, seed=5)
+    pm = PackedMatrix.from_dense(torch.from_numpy(A).cuda(), m)
+    got = pm.execute(torch.from_numpy(B).cuda(), nr=res.best.nr).cpu().numpy()
+    want = O.Packed(O.Tables.of(m), A).execute(B)
+    np.testing.assert_array_equal(got.view(np.uint32), want.view(np.uint32))

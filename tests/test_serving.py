@@ -234,3 +234,26 @@ def test_serving_realtime_poisson(cuda):
     assert all(r.t_done >= r.t_admit >= r.arrival for r in reqs)
     st2 = serve_per_request(model, reqs)
     assert st2.requests == 40 and all(r.t_done >= r.arrival for r in reqs)
+
+
+@pytest.mark.gpu
+def test_serving_tiled_mixed_configs(cuda):
+    """Per-layer packings (M_r 2/8, K tiles, a non-identity mapping) keep alone == mix and the
+    FP64 tolerance."""
+    from spreg.serving import Server, SparseMLP, output_fp32, prepare_requests
+    w = mlp_weights(64, 1024, 2, 0.9, seed=11)
+    cfg = [{"mr": 2, "mapping": "identity", "k_tile": 0}, {"mr": 2, "mapping": "identity", "k_tile": 512},
+           {"mr": 8, "mapping": "400fa", "k_tile": 0}, {"mr": 4, "mapping": "identity", "k_tile": 256}]
+    model = SparseMLP(w, "bf16", configs=cfg)
+    g = np.random.default_rng(2)
+    ns = [5, 70, 129, 1]
+    reqs = [Request(i, n, x=synth.round_bf16(g.standard_normal((64, n)).astype(np.float32)), arrival=float(i))
+            for i, n in enumerate(ns)]
+    prepare_requests(model, reqs)
+    Server(model, budget_bytes=32 << 20, max_slots=8).run(reqs, realtime=False)
+    for r in reqs:
+        alone = Request(50 + r.rid, r.n, x=r.x)
+        prepare_requests(model, [alone])
+        Server(model, budget_bytes=8 << 20, max_slots=1).run([alone], realtime=False)
+        np.testing.assert_array_equal(output_fp32(alone), output_fp32(r))
+        assert rel_err(output_fp32(r), mlp_reference_fp64(w, r.x)) <= BF16_TOL
