@@ -151,6 +151,25 @@ int spreg_packed_to_host(const spreg_packed *p, void *arena_host, int64_t arena_
                          spreg_panel_desc *descs_host, int64_t num_descs, float *scales_host,
                          int64_t num_scales, spreg_stream_t stream);
 
+/* Geometry an arena was packed with (spreg_pack_opts plus A's shape). */
+typedef struct {
+    int64_t rows, cols;      /* A is rows x cols */
+    int32_t m_tile, k_tile;  /* M_c, K_c (0: one tile) */
+    int64_t col_offset;
+    int32_t value_dtype;
+    int32_t reserved;        /* 0 */
+} spreg_arena_geom;
+
+/* Rebuild a packed matrix from host copies of an earlier packing's arena, descriptors and F16
+ * scales (spreg_packed_to_host), e.g. read back from a file.  The arena keeps the byte layout of
+ * SOPTile::pack_tile (sbench/SOP/_C/pytorch_wrapper_intrin.cpp.template:219-261); the executor's
+ * layout is rebuilt from it on the device.  Every unit is checked (descriptors inside the arena
+ * and equal to the layout of their counts, counts adding up to the unit's columns and values,
+ * columns inside the unit's K tile); a failed check is SPREG_ERR_CHECK.  Synchronises `stream`. */
+int spreg_pack_from_arena(const spreg_mapping *m, const spreg_arena_geom *geom, const void *arena_host,
+                          int64_t arena_bytes, const spreg_panel_desc *descs_host, int64_t num_units,
+                          const float *scales_host, int64_t num_scales, spreg_packed **out, spreg_stream_t stream);
+
 /* ---------------------------------------------------------- SOPTile (Python path)
  * Mirrors SOPTile(rows, cols, num_panels).pack_panel(...) / pack_tile() / padding()
  * (template:101-262).  pack_panel takes host arrays: n (code, column) entries in caller

@@ -58,8 +58,8 @@ def _gen_exec_units() -> list[str]:
         for c in EXEC_COMBOS:
             path = os.path.join(BUILD, f"exec_mr{mr}_c{c}.cu")
             text = (f'// generated by build.py: executor kernels for M_r = {mr}, dtype combination {c}\n'
-                    f'#include "{os.path.join(CSRC, "exec_kernel.cuh")}"\n'
-                    f'namespace spreg {{ SPREG_INSTANTIATE_EXEC({mr}, {c}) }}\n')
+                    f'#include "{os.path.join(CSRC, "exec_tile.cuh")}"\n'
+                    f'namespace spreg {{ SPREG_INSTANTIATE_EXEC({mr}, {c}) SPREG_INSTANTIATE_TILE({mr}, {c}) }}\n')
             if not os.path.exists(path) or open(path).read() != text:
                 with open(path, "w") as f:
                     f.write(text)

@@ -15,6 +15,8 @@ void set_error(const std::string &msg) { g_last_error = msg; }
 void clear_error() { g_last_error.clear(); }
 
 // Implemented in pack.cu / exec.cu.
+int pack_from_arena_impl(const spreg_mapping *, const spreg_arena_geom *, const void *, int64_t,
+                         const spreg_panel_desc *, int64_t, const float *, int64_t, spreg_packed **, cudaStream_t);
 int pack_dense_impl(const spreg_mapping *, const float *, int64_t, int64_t, int64_t, const spreg_pack_opts *,
                     spreg_packed **, cudaStream_t);
 int pack_csr_impl(const spreg_mapping *, const spreg_csr *, const spreg_pack_opts *, spreg_packed **, cudaStream_t);
@@ -201,6 +203,15 @@ int spreg_pack_dense(const spreg_mapping *m, const float *a, int64_t rows, int64
     clear_error();
     if (out) *out = nullptr;
     return pack_dense_impl(m, a, rows, cols, lda, opts, out, (cudaStream_t)stream);
+}
+
+int spreg_pack_from_arena(const spreg_mapping *m, const spreg_arena_geom *geom, const void *arena_host,
+                          int64_t arena_bytes, const spreg_panel_desc *descs_host, int64_t num_units,
+                          const float *scales_host, int64_t num_scales, spreg_packed **out, spreg_stream_t stream) {
+    clear_error();
+    if (out) *out = nullptr;
+    return pack_from_arena_impl(m, geom, arena_host, arena_bytes, descs_host, num_units, scales_host, num_scales, out,
+                                (cudaStream_t)stream);
 }
 
 void spreg_packed_destroy(spreg_packed *p) { packed_release(p); }

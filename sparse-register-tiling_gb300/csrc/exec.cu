@@ -5,8 +5,9 @@
 // columns past the last whole strip.  spreg_execute_batched groups the problems of many SpMMs by
 // kernel configuration (M_r, NV, data types) and runs each group in one launch.  Packs whose
 // execution blocks do not fit the per-warp buffers, or calls that ask for it (meta_staging = 2),
-// run the register-stream kernel (exec_kernel) instead.
-#include "exec_kernel.cuh"
+// run the register-stream kernel (exec_kernel) instead.  Calls with b_staging = 1 run the
+// shared-memory B-tile kernel (exec_tile_kernel), grouped the same way.
+#include "exec_tile.cuh"
 
 #include <algorithm>
 #include <atomic>
@@ -73,6 +74,29 @@ cudaError_t launch_mr_batch(int mr, const BatchParams &p, int nv, int combo, uns
     }
 }
 
+template <int MR>
+cudaError_t launch_combo_tile(const TileParams &p, int nv, int combo, unsigned grid, int threads, size_t smem,
+                              cudaStream_t s) {
+    switch (combo) {
+    case COMBO_F32: return launch_exec_tile<MR, COMBO_F32>(p, nv, grid, threads, smem, s);
+    case COMBO_BF16_F32OUT: return launch_exec_tile<MR, COMBO_BF16_F32OUT>(p, nv, grid, threads, smem, s);
+    case COMBO_BF16_BF16OUT: return launch_exec_tile<MR, COMBO_BF16_BF16OUT>(p, nv, grid, threads, smem, s);
+    case COMBO_F16_F32OUT: return launch_exec_tile<MR, COMBO_F16_F32OUT>(p, nv, grid, threads, smem, s);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_mr_tile(int mr, const TileParams &p, int nv, int combo, unsigned grid, int threads, size_t smem,
+                           cudaStream_t s) {
+    switch (mr) {
+    case 2: return launch_combo_tile<2>(p, nv, combo, grid, threads, smem, s);
+    case 4: return launch_combo_tile<4>(p, nv, combo, grid, threads, smem, s);
+    case 6: return launch_combo_tile<6>(p, nv, combo, grid, threads, smem, s);
+    case 8: return launch_combo_tile<8>(p, nv, combo, grid, threads, smem, s);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
 }  // namespace
 
 // ------------------------------------------------------------------ per-device facts
@@ -135,10 +159,16 @@ int auto_nv(int64_t n, int64_t panels, int sms) {
 }
 
 // ------------------------------------------------------------------ one call -> problems
+// Largest B tile (K tile rows x strip bytes) the shared-memory B kernel stages per stage.
+constexpr int64_t kTileMaxStageB = 96 * 1024;
+
 struct CallPlan {
     int mr, combo, nv;
     bool stream_kernel;      // run exec_kernel (register streams) instead of the batch kernel
+    bool tile;               // run exec_tile_kernel (B tiles in shared memory)
     XProblem main, tail;     // whole strips (NV) and the NV = 1 remainder
+    TProblem tmain, ttail;   // the same problems for exec_tile_kernel
+    int64_t stage_b_main, stage_b_tail;
     bool has_main, has_tail;
     int64_t xbuf;            // per-warp buffer for this pack
     ExecParams sp;           // parameters of the register-stream kernel
@@ -159,8 +189,6 @@ int plan_call(const spreg_packed *a, const spreg_exec_args *args, CallPlan *cp) 
     SPREG_CHECK_ARG(args->epilogue == SPREG_EPILOGUE_NONE || args->epilogue == SPREG_EPILOGUE_RELU, "bad epilogue");
     SPREG_CHECK_ARG(args->meta_staging >= 0 && args->meta_staging <= 2, "meta_staging must be 0, 1 or 2");
     SPREG_CHECK_ARG(args->b_staging >= 0 && args->b_staging <= 2, "b_staging must be 0, 1 or 2");
-    SPREG_CHECK_ARG(args->b_staging != 1, "B strip staging in shared memory is not offered: it measured slower "
-                    "than L1/L2 reads of B at every size tried");
     int dev = -1;
     SPREG_CUDA(cudaGetDevice(&dev));
     SPREG_CHECK_ARG(dev == a->device, "packed matrix lives on device %d, current device is %d", a->device, dev);
@@ -191,6 +219,23 @@ int plan_call(const spreg_packed *a, const spreg_exec_args *args, CallPlan *cp) 
                     "(largest block %lld bytes)", (long long)a->max_exec_bytes);
     cp->stream_kernel = args->meta_staging == 2 || !x_fits;
 
+    // Shared-memory B tiles: one copy per K tile row of the strip's columns (16-byte aligned rows,
+    // reads rounded up to 16 bytes stay inside each row of B), a tile that fits a stage, and the
+    // column ranges of K tiles (not the per-panel offsets of panel-by-panel packs).
+    const int64_t kt_rows = a->geom.kt;
+    auto tile_rows_ok = [&](int nvv, int64_t col_end) {
+        const int64_t stage_b = kt_rows * 32 * nvv * (int64_t)bsz;
+        const int64_t need = (col_end * (int64_t)bsz + 15) / 16 * 16;
+        return stage_b <= kTileMaxStageB && need <= args->ldb * (int64_t)bsz;
+    };
+    const bool tile_base_ok = a->exec && !a->list_packed && aligned(args->b, 16) &&
+                              (args->ldb * (int64_t)bsz) % 16 == 0 && 1024 + 2 * cp->xbuf <= f->smem_optin;
+    if (args->b_staging == 1) {
+        SPREG_CHECK_ARG(tile_base_ok, "shared-memory B tiles need a dense/CSR pack, a 16-byte aligned B with "
+                        "16-byte aligned rows, and execution blocks that fit shared memory");
+        SPREG_CHECK_ARG(args->meta_staging != 2, "b_staging = 1 runs the execution-layout metadata path");
+    }
+
     XProblem base = {};
     base.exec = a->exec;
     base.exec_offs = a->exec_offs;
@@ -215,6 +260,44 @@ int plan_call(const spreg_packed *a, const spreg_exec_args *args, CallPlan *cp) 
     cp->tail.col_begin = n_main;
     cp->tail.col_end = args->n;
     cp->tail.S = (int32_t)((args->n - n_main + 31) / 32);
+
+    cp->tile = false;
+    if (args->b_staging == 1) {
+        const bool main_ok = !cp->has_main || tile_rows_ok(nv, n_main);
+        const bool tail_ok = !cp->has_tail || tile_rows_ok(1, args->n);
+        SPREG_CHECK_ARG(main_ok && tail_ok, "shared-memory B tiles: a K tile of %lld rows x %d columns exceeds a "
+                        "stage (%lld bytes), or the last columns round past ldb; pack with a smaller k_tile",
+                        (long long)kt_rows, 32 * nv, (long long)kTileMaxStageB);
+        cp->tile = true;
+        cp->stream_kernel = false;
+        TProblem tb = {};
+        tb.exec = a->exec;
+        tb.exec_offs = a->exec_offs;
+        tb.scales = a->scales;
+        tb.B = args->b;
+        tb.C = args->c;
+        tb.ldb = args->ldb;
+        tb.ldc = args->ldc;
+        tb.M = in.rows;
+        tb.P = (int32_t)a->geom.P;
+        tb.T = (int32_t)a->geom.T;
+        tb.ppt = (int32_t)a->geom.ppt;
+        tb.load_c = args->load_c ? 1 : 0;
+        tb.epilogue = args->epilogue;
+        tb.kt = (int32_t)kt_rows;
+        tb.krows = (int32_t)a->geom.K;
+        tb.col_offset = (int32_t)in.col_offset;
+        cp->tmain = tb;
+        cp->tmain.col_begin = 0;
+        cp->tmain.col_end = n_main;
+        cp->tmain.S = cp->main.S;
+        cp->ttail = tb;
+        cp->ttail.col_begin = n_main;
+        cp->ttail.col_end = args->n;
+        cp->ttail.S = cp->tail.S;
+        cp->stage_b_main = (kt_rows * 32 * nv * (int64_t)bsz + 127) / 128 * 128;
+        cp->stage_b_tail = (kt_rows * 32 * (int64_t)bsz + 127) / 128 * 128;
+    }
 
     ExecParams &p = cp->sp;
     p = ExecParams{};
@@ -305,6 +388,71 @@ int launch_groups(std::map<std::tuple<int, int, int>, Group> &groups, cudaStream
     return SPREG_OK;
 }
 
+// One tile-kernel launch per group of at most kMaxBatchProblems problems of one configuration.
+struct TileGroup {
+    int mr, combo, nv;
+    std::vector<TProblem> probs;
+    int64_t xbuf = 0, stage_b = 0;
+};
+
+int launch_tile_groups(std::map<std::tuple<int, int, int>, TileGroup> &groups, cudaStream_t stream) {
+    DevFacts *f;
+    int st = dev_facts(&f);
+    if (st) return st;
+    for (auto &kv : groups) {
+        TileGroup &g = kv.second;
+        // consumer warps: 16, fewer if the stages do not fit
+        int W = kTileMaxWarps;
+        auto smem_for = [&](int w) { return (int64_t)1024 + kTileStages * (g.stage_b + (int64_t)w * g.xbuf); };
+        while (W > 1 && smem_for(W) > f->smem_optin) W >>= 1;
+        SPREG_CHECK_ARG(smem_for(W) <= f->smem_optin, "shared-memory B tiles: a stage does not fit (%lld bytes)",
+                        (long long)smem_for(W));
+        const size_t smem = (size_t)smem_for(W);
+        const int threads = 32 * (W + 1);
+        for (size_t first = 0; first < g.probs.size(); first += kMaxBatchProblems) {
+            const size_t cnt = std::min<size_t>(kMaxBatchProblems, g.probs.size() - first);
+            TileParams tp;
+            tp.nprob = (int32_t)cnt;
+            int64_t jobs = 0;
+            for (size_t i = 0; i < cnt; ++i) {
+                TProblem &pr = tp.prob[i];
+                pr = g.probs[first + i];
+                pr.groups = (pr.P + W - 1) / W;
+                pr.job_begin = jobs;
+                jobs += (int64_t)pr.groups * pr.S;
+            }
+            if (jobs == 0) continue;
+            SPREG_CHECK_ARG(jobs <= INT32_MAX, "too many jobs in one launch");
+            tp.jobs = jobs;
+            tp.xbuf = (int32_t)g.xbuf;
+            tp.warps = W;
+            tp.stage_b = (int32_t)g.stage_b;
+            tp.status = f->status;
+            tp.counter = next_counter(f);
+            const int per_sm = std::max(1, std::min((int)(f->smem_per_sm / (int64_t)smem), 2048 / threads));
+            const int64_t ctas = std::min<int64_t>((int64_t)f->sms * per_sm, jobs);
+            SPREG_CUDA(cudaMemsetAsync(tp.counter, 0, sizeof(int), stream));
+            cudaError_t e = launch_mr_tile(g.mr, tp, g.nv, g.combo, (unsigned)ctas, threads, smem, stream);
+            if (e != cudaSuccess) SPREG_FAIL(SPREG_ERR_CUDA, "tile executor launch: %s", cudaGetErrorString(e));
+        }
+    }
+    return SPREG_OK;
+}
+
+void add_tile_call(std::map<std::tuple<int, int, int>, TileGroup> &groups, const CallPlan &cp) {
+    auto add = [&](const TProblem &pr, int nv, int64_t stage_b) {
+        TileGroup &g = groups[std::make_tuple(cp.mr, cp.combo, nv)];
+        g.mr = cp.mr;
+        g.combo = cp.combo;
+        g.nv = nv;
+        g.probs.push_back(pr);
+        g.xbuf = std::max(g.xbuf, cp.xbuf);
+        g.stage_b = std::max(g.stage_b, stage_b);
+    };
+    if (cp.has_main) add(cp.tmain, cp.nv, cp.stage_b_main);
+    if (cp.has_tail) add(cp.ttail, 1, cp.stage_b_tail);
+}
+
 void add_call(std::map<std::tuple<int, int, int>, Group> &groups, const CallPlan &cp) {
     auto add = [&](const XProblem &pr, int nv) {
         Group &g = groups[std::make_tuple(cp.mr, cp.combo, nv)];
@@ -320,16 +468,19 @@ void add_call(std::map<std::tuple<int, int, int>, Group> &groups, const CallPlan
 
 int run_calls(const spreg_packed *const *as, const spreg_exec_args *const *args, int32_t n, cudaStream_t stream) {
     std::map<std::tuple<int, int, int>, Group> groups;
+    std::map<std::tuple<int, int, int>, TileGroup> tgroups;
     std::vector<CallPlan> streams;
     for (int32_t i = 0; i < n; ++i) {
         CallPlan cp;
         int st = plan_call(as[i], args[i], &cp);
         if (st != SPREG_OK) return st;
-        if (cp.stream_kernel) streams.push_back(cp);
+        if (cp.tile) add_tile_call(tgroups, cp);
+        else if (cp.stream_kernel) streams.push_back(cp);
         else add_call(groups, cp);
     }
     int st = launch_groups(groups, stream);
     if (st != SPREG_OK) return st;
+    if ((st = launch_tile_groups(tgroups, stream))) return st;
     for (const CallPlan &cp : streams)
         if ((st = launch_stream(cp, stream))) return st;
     return SPREG_OK;

@@ -1,0 +1,331 @@
+// exec_tile.cuh -- executor variant that stages B in shared memory, one K tile at a time.
+//
+// A job is (problem, group of W row panels, strip of 32 * NV columns).  One CTA runs W consumer
+// warps (warp w owns panel group * W + w, its accumulators in registers as in exec_batch_kernel)
+// and one producer warp.  For every K tile t of the job the producer bulk-copies
+//   * the tile's B rows [col_offset + t * K_c, ... + K_c) x the strip's columns, and
+//   * the execution block of unit (panel, t) of every consumer warp
+// into one stage of a ring of kTileStages stages, and arrives on the stage's "full" barrier
+// (expect_tx of all bytes).  Consumers gather B rows out of shared memory (one broadcast-free
+// 4 * NV-byte load per lane per entry) and arrive on the stage's "empty" barrier when done; the
+// producer refills a stage after all W consumers released it.  Jobs follow each other through
+// the same ring, so the producer fetches the next job's first tile while consumers finish the
+// last tile of the current one.
+//
+// B rows are read from L2 once per job instead of once per packed entry: for the W panels of a
+// job a B row is copied once, while the gathers of exec_batch_kernel fetch it once per entry
+// that references it (about W * (1 - sparsity^M_r) times).  Per output element the FMA chain is
+// the same as the other executors (K tiles in order, entries in packed order), so the results
+// are bit-identical.
+//
+// Every wait is bounded; a wait that gives up records a code in the device status word and the
+// warp stops, the producer first waiting (bounded) for the copies it issued.
+#pragma once
+#include "exec_kernel.cuh"
+
+namespace spreg {
+
+constexpr int kTileStages = 2;
+constexpr int kTileMaxWarps = 16;  // consumer warps per CTA
+
+struct TProblem {
+    const uint8_t *exec;        // execution layout of the packed matrix
+    const int64_t *exec_offs;   // units + 1 block offsets
+    const float *scales;        // per-row-panel F16 scales (else null)
+    const void *B;
+    void *C;
+    int64_t ldb, ldc, M;
+    int64_t col_begin;          // first column of the problem's strips
+    int64_t col_end;            // columns >= col_end are not computed
+    int64_t job_begin;          // first global job
+    int32_t P, S, T, ppt;       // row panels, strips, K tiles, panels per row tile
+    int32_t load_c, epilogue;
+    int32_t kt, krows;          // B rows per K tile, B rows of all tiles (columns of A)
+    int32_t col_offset, groups; // first B row of tile 0; panel groups of W panels
+};
+static_assert(sizeof(TProblem) == 128, "TProblem is 128 bytes");
+
+struct TileParams {
+    int *counter;               // job counter, zero at launch
+    int *status;                // device status word of bounded waits
+    int64_t jobs;               // total jobs
+    int32_t nprob;
+    int32_t xbuf;               // bytes of one consumer's metadata slot
+    int32_t warps;              // consumer warps W
+    int32_t stage_b;            // bytes of one stage's B tile
+    TProblem prob[kMaxBatchProblems];
+};
+
+__device__ __forceinline__ int find_tproblem(const TileParams &tp, int64_t job) {
+    int lo = 0, hi = tp.nprob - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (tp.prob[mid].job_begin <= job) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void sts_v4(uint32_t a, int x, int y, int z, int w) {
+    asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(a), "r"(x), "r"(y), "r"(z), "r"(w) : "memory");
+}
+__device__ __forceinline__ int4 lds_v4(uint32_t a) {
+    int4 v;
+    asm volatile("ld.shared.v4.b32 {%0, %1, %2, %3}, [%4];" : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "r"(a)
+                 : "memory");
+    return v;
+}
+
+// B rows of one lane's columns out of a shared-memory tile: row c of B is tile row c - r0.
+template <int NV, class TB> struct SmemB {
+    uint32_t base;       // tile + this lane's first column
+    int32_t r0;          // B row of tile row 0
+    uint32_t row_bytes;  // 32 * NV * sizeof(TB)
+    __device__ __forceinline__ void load(int k, float (&b)[NV]) const {
+        const uint32_t a = base + (uint32_t)(k - r0) * row_bytes;
+        if constexpr (sizeof(TB) == 4) {
+            if constexpr (NV == 1) {
+                b[0] = __uint_as_float(lds_u32(a));
+            } else if constexpr (NV == 2) {
+                const uint2 v = lds_u64(a);
+                b[0] = __uint_as_float(v.x); b[1] = __uint_as_float(v.y);
+            } else {
+                const uint4 v = lds_u128(a);
+                b[0] = __uint_as_float(v.x); b[1] = __uint_as_float(v.y);
+                b[2] = __uint_as_float(v.z); b[3] = __uint_as_float(v.w);
+            }
+        } else {
+            if constexpr (NV == 1) {
+                b[0] = word_val<TB>(lds_u16(a), 0);
+            } else if constexpr (NV == 2) {
+                const uint32_t w = lds_u32(a);
+                b[0] = word_val<TB>(w, 0); b[1] = word_val<TB>(w, 1);
+            } else {
+                const uint2 v = lds_u64(a);
+                b[0] = word_val<TB>(v.x, 0); b[1] = word_val<TB>(v.x, 1);
+                b[2] = word_val<TB>(v.y, 0); b[3] = word_val<TB>(v.y, 1);
+            }
+        }
+    }
+};
+
+// C tile init / store of one (problem, panel, strip), as x_acc_init / x_store.
+template <int MR, int NV, class TV, class TC>
+__device__ __forceinline__ void t_acc_init(const TProblem &pr, int64_t row0, int64_t col0, bool valid,
+                                           float (&acc)[MR][NV]) {
+    constexpr bool SCALED = std::is_same<TV, __half>::value;
+#pragma unroll
+    for (int r = 0; r < MR; ++r)
+#pragma unroll
+        for (int j = 0; j < NV; ++j) acc[r][j] = 0.0f;
+    if (!SCALED && pr.load_c && valid) {
+        const TC *C = reinterpret_cast<const TC *>(pr.C);
+#pragma unroll
+        for (int r = 0; r < MR; ++r)
+            if (row0 + r < pr.M) VecIO<NV, TC>::load_plain(C + (row0 + r) * pr.ldc + col0, acc[r]);
+    }
+}
+template <int MR, int NV, class TV, class TC>
+__device__ __forceinline__ void t_store(const TProblem &pr, int64_t gp, int64_t row0, int64_t col0, bool valid,
+                                        const float (&acc)[MR][NV]) {
+    if (!valid) return;
+    constexpr bool SCALED = std::is_same<TV, __half>::value;
+    TC *C = reinterpret_cast<TC *>(pr.C);
+    const float s = SCALED ? pr.scales[gp] : 1.0f;
+#pragma unroll
+    for (int r = 0; r < MR; ++r) {
+        if (row0 + r >= pr.M) continue;
+        TC *cp = C + (row0 + r) * pr.ldc + col0;
+        float o[NV];
+#pragma unroll
+        for (int j = 0; j < NV; ++j) o[j] = acc[r][j];
+        if (SCALED) {
+            if (pr.load_c) {
+                float cin[NV];
+                VecIO<NV, TC>::load_plain(cp, cin);
+#pragma unroll
+                for (int j = 0; j < NV; ++j) o[j] = fmaf(o[j], s, cin[j]);
+            } else {
+#pragma unroll
+                for (int j = 0; j < NV; ++j) o[j] = o[j] * s;
+            }
+        }
+        if (pr.epilogue == SPREG_EPILOGUE_RELU) {
+#pragma unroll
+            for (int j = 0; j < NV; ++j) o[j] = fmaxf(o[j], 0.0f);
+        }
+        VecIO<NV, TC>::store(cp, o);
+    }
+}
+
+// Shared memory: [0, 64) full / empty barriers, [256, 256 + 16 * stages) job of each stage,
+// from 1024 the stages: B tile (stage_b bytes) then W metadata slots (xbuf bytes each).
+template <int MR, int NV, class TV, class TB, class TC>
+__global__ void __launch_bounds__(32 * (kTileMaxWarps + 1), 1) exec_tile_kernel(const __grid_constant__ TileParams tp) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    constexpr uint32_t ROWB = 32u * NV * (uint32_t)sizeof(TB);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int W = tp.warps;
+    const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(smem);
+    const uint32_t full0 = sbase, empty0 = sbase + 8u * kTileStages, jobs0 = sbase + 256u;
+    const uint32_t stage_bytes = (uint32_t)tp.stage_b + (uint32_t)W * (uint32_t)tp.xbuf;
+    const uint32_t stage0 = sbase + 1024u;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kTileStages; ++s) {
+            mbar_init(full0 + 8u * s, 1);
+            mbar_init(empty0 + 8u * s, (uint32_t)W);
+        }
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    __syncthreads();
+
+    if (warp == W) {
+        // ------------------------------------------------------------ producer
+        int pi = -1, group = 0, strip = 0, t = 0;
+        auto fetch = [&]() {
+            int it = 0;
+            if (lane == 0) it = atomicAdd(tp.counter, 1);
+            const int64_t job = __shfl_sync(0xffffffffu, it, 0);
+            if (job >= tp.jobs) {
+                pi = -1;
+                return;
+            }
+            pi = find_tproblem(tp, job);
+            const int64_t local = job - tp.prob[pi].job_begin;
+            group = (int)(local / tp.prob[pi].S);
+            strip = (int)(local % tp.prob[pi].S);
+            t = 0;
+        };
+        fetch();
+        int64_t last_seq[kTileStages];
+#pragma unroll
+        for (int s = 0; s < kTileStages; ++s) last_seq[s] = -1;
+        bool ok = true;
+#pragma unroll 1
+        for (int64_t seq = 0;; ++seq) {
+            const int s = (int)(seq % kTileStages);
+            const uint32_t full = full0 + 8u * s, empty = empty0 + 8u * s;
+            if (seq >= kTileStages &&
+                !mbar_wait_bounded(empty, (uint32_t)(((seq / kTileStages) - 1) & 1), tp.status, 5)) {
+                ok = false;
+                break;
+            }
+            if (pi < 0) {
+                if (lane == 0) {
+                    sts_v4(jobs0 + 16u * s, -1, 0, 0, 0);
+                    mbar_arrive(full);
+                }
+                break;
+            }
+            const TProblem &pr = tp.prob[pi];
+            const int64_t r0 = (int64_t)pr.col_offset + (int64_t)t * pr.kt;
+            const int64_t rl = (int64_t)pr.krows - (int64_t)t * pr.kt;
+            const int nrows = (int)(rl < pr.kt ? rl : pr.kt);
+            const int64_t c0 = pr.col_begin + (int64_t)strip * (32 * NV);
+            const int64_t ncols = (pr.col_end - c0) < 32 * NV ? (pr.col_end - c0) : 32 * NV;
+            const uint32_t wbytes = (uint32_t)((ncols * (int64_t)sizeof(TB) + 15) & ~(int64_t)15);
+            uint32_t mbytes = 0;
+            int64_t moff = 0;
+            const int64_t gp = (int64_t)group * W + lane;
+            if (lane < W && gp < pr.P) {
+                const int64_t u = unit_index(gp, t, pr.ppt, pr.T, pr.P);
+                moff = pr.exec_offs[u];
+                mbytes = (uint32_t)(pr.exec_offs[u + 1] - moff);
+            }
+            uint32_t total = mbytes;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) total += __shfl_xor_sync(0xffffffffu, total, o);
+            total += wbytes * (uint32_t)nrows;
+            if (lane == 0) {
+                sts_v4(jobs0 + 16u * s, pi, group, strip, t);
+                mbar_arrive_expect_tx(full, total);
+            }
+            __syncwarp();
+            const uint32_t sb = stage0 + (uint32_t)s * stage_bytes;
+            const char *bsrc = reinterpret_cast<const char *>(pr.B) + c0 * (int64_t)sizeof(TB);
+            const int64_t ldb_bytes = pr.ldb * (int64_t)sizeof(TB);
+            for (int r = lane; r < nrows; r += 32)
+                bulk_copy_g2s(sb + (uint32_t)r * ROWB, bsrc + (r0 + r) * ldb_bytes, wbytes, full);
+            if (mbytes) bulk_copy_g2s(sb + (uint32_t)tp.stage_b + (uint32_t)lane * (uint32_t)tp.xbuf, pr.exec + moff,
+                                      mbytes, full);
+            last_seq[s] = seq;
+            if (++t == pr.T) fetch();
+        }
+        if (!ok) {
+            // copies still in flight land in stages whose full barrier has not flipped yet
+#pragma unroll
+            for (int s = 0; s < kTileStages; ++s)
+                if (last_seq[s] >= 0)
+                    mbar_wait_bounded(full0 + 8u * s, (uint32_t)((last_seq[s] / kTileStages) & 1), tp.status, 7);
+        }
+        return;
+    }
+
+    // ---------------------------------------------------------------- consumers
+    float acc[MR][NV];
+#pragma unroll 1
+    for (int64_t seq = 0;; ++seq) {
+        const int s = (int)(seq % kTileStages);
+        if (!mbar_wait_bounded(full0 + 8u * s, (uint32_t)((seq / kTileStages) & 1), tp.status, 6)) break;
+        const int4 ji = lds_v4(jobs0 + 16u * s);
+        if (ji.x < 0) break;
+        const TProblem &pr = tp.prob[ji.x];
+        const int64_t gp = (int64_t)ji.y * W + warp;
+        const int t = ji.w;
+        if (gp < pr.P) {
+            const int64_t row0 = gp * MR;
+            const int64_t col0 = pr.col_begin + (int64_t)ji.z * (32 * NV) + (int64_t)lane * NV;
+            const bool valid = col0 < pr.col_end;
+            if (t == 0) t_acc_init<MR, NV, TV, TC>(pr, row0, col0, valid, acc);
+            const uint32_t sb = stage0 + (uint32_t)s * stage_bytes;
+            const uint32_t buf = sb + (uint32_t)tp.stage_b + (uint32_t)warp * (uint32_t)tp.xbuf;
+            const SmemB<NV, TB> bl{sb + (uint32_t)lane * (uint32_t)(NV * sizeof(TB)),
+                                   (int32_t)(pr.col_offset + (int64_t)t * pr.kt), ROWB};
+            const uint32_t G = lds_u32(buf);
+#pragma unroll 1
+            for (uint32_t g = 0; g < G; ++g) {
+                const uint4 rec = lds_u128(buf + 16u + 16u * g);
+                run_group_x<MR, NV, TV>((int)rec.x, (int)rec.y, buf + rec.z, buf + rec.w, bl, acc);
+            }
+            if (t == pr.T - 1) t_store<MR, NV, TV, TC>(pr, gp, row0, col0, valid, acc);
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(empty0 + 8u * s);
+    }
+}
+
+template <int MR, int COMBO>
+cudaError_t launch_exec_tile(const TileParams &p, int nv, unsigned grid, int threads, size_t smem, cudaStream_t s);
+
+#define SPREG_INSTANTIATE_TILE(MR, COMBO)                                                             \
+    template <>                                                                                       \
+    cudaError_t launch_exec_tile<MR, COMBO>(const TileParams &p, int nv, unsigned grid, int threads, size_t smem, \
+                                            cudaStream_t s) {                                         \
+        using V = ComboTypes<COMBO>::V;                                                               \
+        using B = ComboTypes<COMBO>::B;                                                               \
+        using C = ComboTypes<COMBO>::C;                                                               \
+        static bool configured[64][5] = {};                                                           \
+        int dev = 0;                                                                                  \
+        cudaGetDevice(&dev);                                                                          \
+        auto run = [&](auto kern) -> cudaError_t {                                                    \
+            if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;                                  \
+            if (!configured[dev][nv]) {                                                               \
+                cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem); \
+                if (e != cudaSuccess) return e;                                                       \
+                configured[dev][nv] = true;                                                           \
+            }                                                                                         \
+            kern<<<grid, threads, smem, s>>>(p);                                                      \
+            return cudaGetLastError();                                                                \
+        };                                                                                            \
+        switch (nv) {                                                                                 \
+        case 1: return run(exec_tile_kernel<MR, 1, V, B, C>);                                         \
+        case 2: return run(exec_tile_kernel<MR, 2, V, B, C>);                                         \
+        case 4: return run(exec_tile_kernel<MR, 4, V, B, C>);                                         \
+        default: return cudaErrorInvalidValue;                                                        \
+        }                                                                                             \
+    }
+
+}  // namespace spreg

@@ -647,6 +647,135 @@ const MapTable *mapping_device_table(const spreg_mapping *m, int *status);
 
 namespace {
 
+
+// ------------------------------------------------------------------ packed arena import
+// Count pass over an arena read back from a file: each unit's descriptor must address bytes inside
+// the arena (4-byte aligned), its nkern_counts must be non-negative and add up to num_cols and, with
+// the nanokernels' popcounts, to num_values, and its column indices must lie in its K tile.  Then
+// the statistics of the ordinary count pass (padding = zero values, execution block size).
+__global__ void __launch_bounds__(CH) arena_count_kernel(const Geom g, const MapTable *__restrict__ mt,
+                                                         const uint8_t *__restrict__ arena, const int64_t arena_bytes,
+                                                         const spreg_panel_desc *__restrict__ descs, const int vb,
+                                                         const int64_t col_offset, int32_t *__restrict__ unit_counts,
+                                                         UnitStats *__restrict__ stats,
+                                                         unsigned long long *__restrict__ tile_nnz, DevError *err) {
+    __shared__ MapTable s_mt;
+    __shared__ int s_count[256];
+    __shared__ int s_ok;
+    __shared__ long long s_tmp[CH / 32];
+    const int64_t u = blockIdx.x;
+    load_map_table(&s_mt, mt);
+    const spreg_panel_desc d = descs[u];
+    const int nk = s_mt.num_nkern;
+    if (threadIdx.x == 0) {
+        const bool ok = d.num_values >= 0 && d.num_cols >= 0 && d.values_off >= 0 && d.cols_off >= 0 &&
+                        d.counts_off >= 0 && d.values_off % 4 == 0 && d.cols_off % 4 == 0 && d.counts_off % 4 == 0 &&
+                        d.values_off + (int64_t)d.num_values * vb <= arena_bytes &&
+                        d.cols_off + (int64_t)d.num_cols * 4 <= arena_bytes &&
+                        d.counts_off + (int64_t)nk * 4 <= arena_bytes;
+        s_ok = ok ? 1 : 0;
+        if (!ok) raise_err(err, 5, u, 0);
+    }
+    __syncthreads();
+    if (!s_ok) {
+        if (threadIdx.x == 0) stats[u] = UnitStats{0, 0, 0, 0, (int32_t)sizeof(ExecHeader), 0};
+        for (int id = threadIdx.x; id < nk; id += CH) unit_counts[u * nk + id] = 0;
+        return;
+    }
+    const int32_t *counts = reinterpret_cast<const int32_t *>(arena + d.counts_off);
+    for (int id = threadIdx.x; id < 256; id += CH) s_count[id] = id < nk ? counts[id] : 0;
+    __syncthreads();
+    int64_t gp, tj;
+    unit_coords(u, g.ppt, g.T, g.P, &gp, &tj);
+    if (threadIdx.x == 0) {
+        long long ents = 0, vals = 0;
+        bool neg = false;
+        for (int id = 0; id < nk; ++id) {
+            neg |= s_count[id] < 0;
+            ents += s_count[id];
+            vals += (long long)s_count[id] * __popc(s_mt.id_to_pattern[id]);
+        }
+        s_ok = (!neg && ents == d.num_cols && vals == d.num_values) ? 1 : 0;
+        if (!s_ok) raise_err(err, 6, u, (int)ents);
+    }
+    __syncthreads();
+    if (!s_ok) {
+        if (threadIdx.x == 0) stats[u] = UnitStats{0, 0, 0, 0, (int32_t)sizeof(ExecHeader), 0};
+        for (int id = threadIdx.x; id < nk; id += CH) unit_counts[u * nk + id] = 0;
+        return;
+    }
+    const int64_t lo = col_offset + tj * g.kt;
+    const int64_t hi = col_offset + ((tj + 1) * g.kt < g.K ? (tj + 1) * g.kt : g.K);
+    const int32_t *cols = reinterpret_cast<const int32_t *>(arena + d.cols_off);
+    for (int e = threadIdx.x; e < d.num_cols; e += CH)
+        if (cols[e] < lo || cols[e] >= hi) raise_err(err, 7, u, cols[e]);
+    long long zeros = 0;
+    for (int v = threadIdx.x; v < d.num_values; v += CH) {
+        const uint8_t *q = arena + d.values_off + (int64_t)v * vb;
+        bool z;
+        if (vb == 4) z = (*reinterpret_cast<const uint32_t *>(q) & 0x7FFFFFFFu) == 0u;
+        else z = (*reinterpret_cast<const uint16_t *>(q) & 0x7FFFu) == 0u;
+        zeros += z ? 1 : 0;
+    }
+    for (int o = 16; o > 0; o >>= 1) zeros += __shfl_down_sync(0xffffffffu, zeros, o);
+    if ((threadIdx.x & 31) == 0) s_tmp[threadIdx.x >> 5] = zeros;
+    __syncthreads();
+    for (int id = threadIdx.x; id < nk; id += CH) unit_counts[u * nk + id] = s_count[id];
+    if (threadIdx.x == 0) {
+        long long pad = 0;
+        for (int i = 0; i < CH / 32; ++i) pad += s_tmp[i];
+        int32_t xb, xg;
+        exec_size(s_mt, s_count, vb, &xb, &xg);
+        const long long nnz = d.num_values - pad;
+        stats[u] = UnitStats{d.num_cols, d.num_values, (int32_t)pad, (int32_t)nnz, xb, xg};
+        atomicAdd(&tile_nnz[(gp / g.ppt) * g.T + tj], (unsigned long long)nnz);
+    }
+}
+
+// Emit pass of an imported arena: the recomputed descriptor must equal the imported one; the
+// unit's values and columns are copied and its execution block is written group by group (the
+// arena already holds the entries in nanokernel-id order).
+__global__ void __launch_bounds__(CH) arena_emit_kernel(const MapTable *__restrict__ mt,
+                                                        const uint8_t *__restrict__ src,
+                                                        const spreg_panel_desc *__restrict__ src_descs,
+                                                        const int32_t *__restrict__ unit_counts,
+                                                        const spreg_panel_desc *__restrict__ descs,
+                                                        uint8_t *__restrict__ arena, uint8_t *__restrict__ exec,
+                                                        const int64_t *__restrict__ exec_offs, const int vb,
+                                                        DevError *err) {
+    __shared__ MapTable s_mt;
+    __shared__ EmitShared s;
+    __shared__ int s_ok;
+    const int64_t u = blockIdx.x;
+    load_map_table(&s_mt, mt);
+    const spreg_panel_desc sd = src_descs[u], d = descs[u];
+    const int nk = s_mt.num_nkern;
+    if (threadIdx.x == 0) {
+        s_ok = (sd.values_off == d.values_off && sd.cols_off == d.cols_off && sd.counts_off == d.counts_off &&
+                sd.num_values == d.num_values && sd.num_cols == d.num_cols) ? 1 : 0;
+        if (!s_ok) raise_err(err, 8, u, 0);
+    }
+    __syncthreads();
+    if (!s_ok) return;
+    for (int64_t i = threadIdx.x; i < (int64_t)d.num_values * vb; i += CH)
+        arena[d.values_off + i] = src[d.values_off + i];
+    for (int64_t i = threadIdx.x; i < (int64_t)d.num_cols * 4; i += CH) arena[d.cols_off + i] = src[d.cols_off + i];
+    uint8_t *xb = exec + exec_offs[u];
+    emit_prologue(s, s_mt, unit_counts + u * nk, reinterpret_cast<int32_t *>(arena + d.counts_off), xb, vb);
+    __syncthreads();
+    const int32_t *cols = reinterpret_cast<const int32_t *>(src + d.cols_off);
+    const uint8_t *vals = src + d.values_off;
+    for (int id = 0; id < nk; ++id) {
+        const int n = unit_counts[u * nk + id];
+        const int pc = __popc(s_mt.id_to_pattern[id]);
+        for (int r = threadIdx.x; r < n; r += CH) {
+            reinterpret_cast<int32_t *>(xb + s.xcol[id])[r] = cols[s.start[id] + r];
+            for (int q = 0; q < pc * vb; ++q)
+                xb[s.xval[id] + (int64_t)r * pc * vb + q] = vals[((int64_t)s.vstart[id] + (int64_t)r * pc) * vb + q];
+        }
+    }
+}
+
 struct Scratch {
     int32_t *unit_counts = nullptr;
     UnitStats *stats = nullptr;
@@ -671,6 +800,10 @@ const char *dev_error_text(int code) {
     case 2: return "packer invariant num_nnz == padding + count_nonzero(panel) failed (mapping does not cover the pattern exactly once)";
     case 3: return "duplicate (row, column) entry in CSR input";
     case 4: return "column index out of range of the dense panel";
+    case 5: return "imported descriptor addresses bytes outside the arena";
+    case 6: return "imported nkern_counts do not add up to the unit's columns and values";
+    case 7: return "imported column index outside the unit's K tile";
+    case 8: return "imported descriptor differs from the layout of its counts";
     default: return "unknown device check";
     }
 }
@@ -913,7 +1046,79 @@ int pack_lists_impl(const spreg_mapping *m, int64_t rows, int64_t cols, int64_t 
             emit_list_kernel<__half><<<(unsigned)num_panels, CH, 0, stream>>>(src, mt, sc.unit_counts, p->descs,
                                                                                p->arena, p->scales, p->exec, p->exec_offs);
     };
-    return finish_pack(m, g, value_dtype, 0, 0, 0, sc, mt, emit, out, stream);
+    st = finish_pack(m, g, value_dtype, 0, 0, 0, sc, mt, emit, out, stream);
+    if (st == SPREG_OK && *out) (*out)->list_packed = true;
+    return st;
+}
+
+int pack_from_arena_impl(const spreg_mapping *m, const spreg_arena_geom *ag, const void *arena_h,
+                         int64_t arena_bytes, const spreg_panel_desc *descs_h, int64_t num_units,
+                         const float *scales_h, int64_t num_scales, spreg_packed **out, cudaStream_t stream) {
+    SPREG_CHECK_ARG(m && ag && out, "null argument");
+    SPREG_CHECK_ARG(ag->value_dtype >= SPREG_F32 && ag->value_dtype <= SPREG_F16, "bad value dtype %d", ag->value_dtype);
+    spreg_pack_opts o = {ag->m_tile, ag->k_tile, ag->col_offset, ag->value_dtype};
+    Geom g;
+    int st = make_geom(m, ag->rows, ag->cols, &o, &g);
+    if (st != SPREG_OK) return st;
+    SPREG_CHECK_ARG(num_units == g.units, "%lld descriptors for %lld units of this geometry", (long long)num_units,
+                    (long long)g.units);
+    SPREG_CHECK_ARG(arena_bytes >= 0 && (arena_bytes == 0 || arena_h) && (num_units == 0 || descs_h), "null arena");
+    SPREG_CHECK_ARG(ag->value_dtype != SPREG_F16 || (scales_h && num_scales == g.P), "F16 arenas need %lld scales",
+                    (long long)g.P);
+    if (ag->value_dtype == SPREG_F16)
+        for (int64_t i = 0; i < g.P; ++i)
+            SPREG_CHECK_ARG(scales_h[i] > 0.0f && scales_h[i] < INFINITY, "scale %lld is not a finite positive value",
+                            (long long)i);
+    if (g.units > INT32_MAX) SPREG_FAIL(SPREG_ERR_UNSUPPORTED, "too many packed units");
+    const MapTable *mt = mapping_device_table(m, &st);
+    if (st != SPREG_OK) return st;
+    const int vb = dtype_bytes(ag->value_dtype);
+    const int64_t tiles = (g.P > 0 ? (g.P + g.ppt - 1) / g.ppt : 0) * g.T;
+    Scratch sc;
+    if ((st = alloc_scratch(sc, g, m->num_nkern, tiles, stream))) return st;
+    struct DevBuf {
+        void *p = nullptr;
+        cudaStream_t s;
+        ~DevBuf() { if (p) cudaFreeAsync(p, s); }
+    } b_arena{nullptr, stream}, b_descs{nullptr, stream};
+    SPREG_CUDA(cudaMallocAsync(&b_arena.p, (size_t)(arena_bytes > 0 ? arena_bytes : 16), stream));
+    SPREG_CUDA(cudaMallocAsync(&b_descs.p, (size_t)(num_units > 0 ? num_units : 1) * sizeof(spreg_panel_desc), stream));
+    if (arena_bytes) SPREG_CUDA(cudaMemcpyAsync(b_arena.p, arena_h, (size_t)arena_bytes, cudaMemcpyHostToDevice, stream));
+    if (num_units)
+        SPREG_CUDA(cudaMemcpyAsync(b_descs.p, descs_h, (size_t)num_units * sizeof(spreg_panel_desc),
+                                   cudaMemcpyHostToDevice, stream));
+    const uint8_t *src = static_cast<const uint8_t *>(b_arena.p);
+    const spreg_panel_desc *sdesc = static_cast<const spreg_panel_desc *>(b_descs.p);
+    if (g.units > 0) {
+        arena_count_kernel<<<(unsigned)g.units, CH, 0, stream>>>(g, mt, src, arena_bytes, sdesc, vb, ag->col_offset,
+                                                                 sc.unit_counts, sc.stats, sc.tile_nnz, sc.err);
+        SPREG_CUDA(cudaGetLastError());
+    }
+    auto emit = [&](spreg_packed *p) {
+        arena_emit_kernel<<<(unsigned)g.units, CH, 0, stream>>>(mt, src, sdesc, sc.unit_counts, p->descs, p->arena,
+                                                                p->exec, p->exec_offs, vb, sc.err);
+    };
+    spreg_packed *p = nullptr;
+    st = finish_pack(m, g, ag->value_dtype, ag->col_offset, ag->m_tile, ag->k_tile, sc, mt, emit, &p, stream);
+    if (st != SPREG_OK) return st;
+    DevError derr;
+    cudaError_t e = cudaMemcpyAsync(&derr, sc.err, sizeof derr, cudaMemcpyDeviceToHost, stream);
+    if (e == cudaSuccess && ag->value_dtype == SPREG_F16 && g.P > 0)
+        e = cudaMemcpyAsync(p->scales, scales_h, (size_t)g.P * sizeof(float), cudaMemcpyHostToDevice, stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess) { release(p); SPREG_FAIL(SPREG_ERR_CUDA, "arena import: %s", cudaGetErrorString(e)); }
+    if (derr.code != 0) {
+        release(p);
+        SPREG_FAIL(SPREG_ERR_CHECK, "arena import check failed at unit %d (value %d): %s", derr.unit, derr.value,
+                   dev_error_text(derr.code));
+    }
+    if (p->info.arena_bytes != arena_bytes) {
+        const long long want = (long long)p->info.arena_bytes;
+        release(p);
+        SPREG_FAIL(SPREG_ERR_CHECK, "arena holds %lld bytes, its descriptors lay out %lld", (long long)arena_bytes, want);
+    }
+    *out = p;
+    return SPREG_OK;
 }
 
 int sort_encode_impl(const spreg_mapping *m, const int32_t *codes, int64_t n, int32_t *encoded, int32_t *order,

@@ -182,4 +182,5 @@ struct spreg_packed {
     int64_t *exec_offs = nullptr;   // units + 1 block offsets
     int64_t exec_bytes = 0;
     int64_t max_exec_bytes = 0;
+    bool list_packed = false;       // packed panel by panel (per-panel column offsets, no K tiles)
 };

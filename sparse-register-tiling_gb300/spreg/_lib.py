@@ -63,6 +63,11 @@ class PackOpts(C.Structure):
     _fields_ = [("m_tile", C.c_int32), ("k_tile", C.c_int32), ("col_offset", C.c_int64), ("value_dtype", C.c_int32)]
 
 
+class ArenaGeom(C.Structure):
+    _fields_ = [("rows", C.c_int64), ("cols", C.c_int64), ("m_tile", C.c_int32), ("k_tile", C.c_int32),
+                ("col_offset", C.c_int64), ("value_dtype", C.c_int32), ("reserved", C.c_int32)]
+
+
 class ExecArgs(C.Structure):
     _fields_ = [("b", C.c_void_p), ("ldb", C.c_int64), ("c", C.c_void_p), ("ldc", C.c_int64), ("n", C.c_int64),
                 ("b_dtype", C.c_int32), ("c_dtype", C.c_int32), ("load_c", C.c_int32), ("epilogue", C.c_int32),
@@ -99,6 +104,8 @@ PROTOTYPES = {
     "spreg_packed_get_info": (C.c_int, [P, C.POINTER(PackedInfo)]),
     "spreg_packed_device_ptrs": (C.c_int, [P, C.POINTER(P), C.POINTER(P), C.POINTER(P)]),
     "spreg_packed_to_host": (C.c_int, [P, P, C.c_int64, P, C.c_int64, P, C.c_int64, P]),
+    "spreg_pack_from_arena": (C.c_int, [P, C.POINTER(ArenaGeom), P, C.c_int64, P, C.c_int64, P, C.c_int64,
+                                        C.POINTER(P), P]),
     "spreg_tile_create": (C.c_int, [P, C.c_int64, C.c_int64, C.c_int64, C.POINTER(P)]),
     "spreg_tile_pack_panel": (C.c_int, [P, C.c_int64, C.c_int64, P, P, C.c_int64, P, C.c_int64]),
     "spreg_tile_pack": (C.c_int, [P, C.c_int32, P]),

@@ -323,11 +323,13 @@ def test_execute_kernels_bit_exact(cuda, mkey, meta, vd, n, nr):
     assert np.array_equal(Cg.view(np.uint32), want.view(np.uint32))
 
 
-def test_b_staging_request_is_rejected(cuda):
-    m = Mapping.identity(4)
-    pm = gpu_pack(synth.bernoulli(64, 64, 0.5, seed=1), m)
-    with pytest.raises(_lib.SpregError, match="not offered"):
-        pm.execute(torch.ones((64, 64), device="cuda"), staging=1)
+def test_b_staging_panel_by_panel_pack_is_rejected(cuda):
+    """Shared-memory B tiles need one column range per K tile; SOPTile packs have per-panel offsets."""
+    module = make_sop_module(Acc(4, 64), list(range(1, 16)), lambda p: p)
+    A = torch.from_numpy(synth.bernoulli(64, 64, 0.5, seed=1))
+    tile = module.make_sop_tile(A)
+    with pytest.raises(_lib.SpregError, match="dense/CSR pack"):
+        tile.packed.execute(torch.ones((64, 64), device="cuda"), staging=1)
 
 
 @pytest.mark.parametrize("meta", [1, 2])
