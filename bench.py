@@ -50,7 +50,8 @@ def parse():
     ap.add_argument("--n", type=int, default=512)
     ap.add_argument("--sparsity", type=float, default=0.9)
     ap.add_argument("--nr", type=int, default=0)
-    ap.add_argument("--staging", type=int, default=0, help="0 auto, 1 shared-memory B strips, 2 L1/L2")
+    ap.add_argument("--staging", type=int, default=0, help="0 auto, 1 shared-memory B tiles, 2 L1/L2")
+    ap.add_argument("--k-tile", type=int, default=0, help="K tile (K_c) of the packing; 0 = one tile")
     ap.add_argument("--meta", type=int, default=0, help="0 auto, 1 execution-layout kernel, 2 register streams")
     ap.add_argument("--dtype", choices=["f32", "bf16"], default="f32",
                     help="storage of A values and B (FP32 accumulation and FP32 C either way)")
@@ -59,6 +60,9 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline budget; 0 skips it")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end leg")
     ap.add_argument("--serving", type=int, default=1, help="1: add the serving-loop measurement to the line")
+    ap.add_argument("--precision", type=int, default=1, help="1: add the storage-precision sweep to the line")
+    ap.add_argument("--layers", type=int, default=1,
+                    help="1: add the batched uneven transformer-layer measurement to the line")
     ap.add_argument("--serve-requests", type=int, default=768)
     ap.add_argument("--serve-slots", type=int, default=128)
     ap.add_argument("--serve-budget-mb", type=int, default=1024)
@@ -238,6 +242,132 @@ def serving_bench(args, dev) -> dict:
             "capacity_note": "capacity = all requests queued at t=0; latency = arrival to output in host memory"}
 
 
+def precision_suite(dev) -> list:
+    """1x1-conv-shaped SpMMs (B = K x 3136: batch 1, 56 x 56 spatial) at sparsity 0.8-0.95 with
+    log-normal row skew: rel err against FP64 of FP32, BF16 and FP16 (per-panel scaled) storage,
+    FP32 accumulation, and the FP32 kernel time of each layer."""
+    import torch
+    from oracle import oracle as O
+    from spreg import BF16, F16, F32, Mapping, PackedMatrix, synth
+    m = Mapping.identity(4)
+    rows = []
+    for i, (M, K) in enumerate(((64, 256), (128, 512), (256, 1024), (512, 2048), (2048, 512))):
+        sp = (0.8, 0.85, 0.9, 0.95, 0.9)[i]
+        A = synth.row_skew(M, K, sp, seed=300 + i, sigma=0.5, std=0.02)
+        B = synth.dense(K, 3136, seed=400 + i)
+        ref = O.dense_fp64(A, B)
+        At = torch.from_numpy(A).to(dev)
+        row = {"shape": [M, K], "sparsity": sp, "n": 3136}
+        for name, vd, tdt in (("fp32", F32, torch.float32), ("bf16", BF16, torch.bfloat16), ("fp16", F16, torch.float16)):
+            pm = PackedMatrix.from_dense(At, m, value_dtype=vd)
+            Bt = torch.from_numpy(B).to(dev).to(tdt)
+            C = pm.execute(Bt)
+            row[f"rel_err_{name}"] = float(O.rel_err(C.cpu().numpy(), ref))
+            if name == "fp32":
+                Cf = torch.empty((M, 3136), device=dev)
+                t = pm.execute_timed(Bt, Cf, num_runs=1)
+                row["fp32_us"] = t / 1e3
+                row["fp32_gflops"] = 2 * int(pm.info["nnz"]) * 3136 / t
+            if name != "fp32":
+                # the same storage with its own inputs rounded: the error the kernel adds
+                Bq = Bt.float().cpu().numpy()
+                row[f"rel_err_{name}_vs_rounded_inputs"] = float(O.rel_err(
+                    C.cpu().numpy(), O.dense_fp64(_rounded(A, vd, pm), Bq)))
+        rows.append(row)
+    return rows
+
+
+def _rounded(A, vd, pm):
+    """A's values as the packed storage holds them (BF16 / FP16 with the per-panel scale)."""
+    import torch
+    from spreg import BF16
+    if vd == BF16:
+        return torch.from_numpy(A).to(torch.bfloat16).float().numpy()
+    arena, descs, scales = pm.to_host()
+    mr = pm.info["mr"]
+    out = np.zeros_like(A)
+    for p in range(pm.info["num_panels"]):
+        s = float(scales[p])
+        blk = A[p * mr:(p + 1) * mr]
+        out[p * mr:(p + 1) * mr] = torch.from_numpy(blk / s).to(torch.float16).float().numpy() * s
+    return out
+
+
+def layers_suite(dev, steps: int = 50) -> dict:
+    """The 36 sparse linear layers of a 6-layer transformer (Q/K/V/O 512x512, FFN 2048x512 and
+    512x2048) at 90 % row-skew sparsity, BF16 values and B, FP32 output, N per instance uniform in
+    16..1024: the fixed-tile plain path (one launch per SpMM: M_r = 4, N_r = 64, untiled) against
+    one batched launch per step of autotuned packings, replayed from a CUDA graph."""
+    import torch
+    from spreg import BF16, Mapping, PackedMatrix, execute_batched, synth
+    from spreg.autotune import mapping_of, tune
+    g = synth.rng(900)
+    shapes = []
+    for _ in range(6):
+        shapes += [(512, 512)] * 4 + [(2048, 512), (512, 2048)]
+    ns = [int(x) for x in g.integers(16, 1025, size=len(shapes))]
+    As = [synth.row_skew(M, K, 0.9, seed=1000 + i, sigma=0.5, std=0.02) for i, (M, K) in enumerate(shapes)]
+    Bs = [torch.from_numpy(synth.dense(K, n, seed=2000 + i)).to(dev).to(torch.bfloat16)
+          for i, ((M, K), n) in enumerate(zip(shapes, ns))]
+    Cp = [torch.empty((M, n), device=dev) for (M, K), n in zip(shapes, ns)]
+    Cb = [torch.empty((M, n), device=dev) for (M, K), n in zip(shapes, ns)]
+    m4 = Mapping.identity(4)
+    plain = [PackedMatrix.from_dense(torch.from_numpy(A).to(dev), m4, value_dtype=BF16) for A in As]
+    flops = sum(2 * int(p.info["nnz"]) * n for p, n in zip(plain, ns))
+    t0 = time.perf_counter()
+    tuned, cfg = [], []
+    cache = {}
+    for A, n, (M, K) in zip(As, ns, shapes):
+        key = (M, K, min(1024, 1 << max(4, int(n - 1).bit_length())))  # tune once per shape and N octave
+        if key not in cache:
+            cache[key] = tune(A, n, "bf16", top=6, device=dev).best
+        c = cache[key]
+        cfg.append(c)
+        tuned.append(PackedMatrix.from_dense(torch.from_numpy(A).to(dev), mapping_of(c.mr, c.mapping),
+                                             k_tile=c.k_tile, value_dtype=BF16))
+    t_tune = time.perf_counter() - t0
+
+    def plain_step():
+        for p, B, C in zip(plain, Bs, Cp):
+            p.execute(B, C, nr=64)
+
+    work = [(p, B, C, dict(nr=c.nr)) for p, B, C, c in zip(tuned, Bs, Cb, cfg)]
+
+    def batched_step():
+        execute_batched(work)
+
+    def time_it(fn):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps * 1e3
+
+    t_plain = time_it(plain_step)
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        batched_step()
+    torch.cuda.current_stream().wait_stream(s)
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        batched_step()
+    t_batched = time_it(graph.replay)
+    err = max(float((a - b).norm() / max(b.norm(), 1e-30)) for a, b in zip(Cb, Cp))
+    return {"workload": "36 layers (6 x Q/K/V/O 512x512, FFN 2048x512, 512x2048) @90% row-skew, BF16 values and B, "
+                        "FP32 out, N uniform 16..1024 per layer",
+            "plain_fixed_tile_us": t_plain, "batched_autotuned_graph_us": t_batched, "speedup": t_plain / t_batched,
+            "plain_tflops": flops / t_plain / 1e6, "batched_tflops": flops / t_batched / 1e6,
+            "plain_launches_per_step": len(plain), "tune_seconds": t_tune,
+            "configs": sorted({c.name() for c in cfg}),
+            "max_rel_diff_batched_vs_plain": err}
+
+
 def _stat(st) -> dict:
     return {"req_s": st.req_per_s, "tokens_s": st.tokens_per_s, "p50_ms": st.p50_ms, "p99_ms": st.p99_ms,
             "mean_ms": st.mean_ms, "requests": st.requests}
@@ -332,7 +462,7 @@ def main():
     tdt = torch.float32 if args.dtype == "f32" else torch.bfloat16
     packs, Bd, Cd = [], [], []
     for A, B in zip(As, Bs):
-        packs.append(PackedMatrix.from_dense(torch.from_numpy(A).to(dev), m, value_dtype=vd))
+        packs.append(PackedMatrix.from_dense(torch.from_numpy(A).to(dev), m, k_tile=args.k_tile, value_dtype=vd))
         Bd.append(torch.from_numpy(B).to(dev).to(tdt))
         Cd.append(torch.empty((args.m, args.n), device=dev))
     torch.cuda.synchronize()
@@ -343,14 +473,14 @@ def main():
     working_set = step_bytes
 
     # parity spot check of replica 0 against the oracle before timing anything
-    ref0 = O.Packed(O.Tables.of(m), As[0], value_dtype=spreg_dtype)
+    ref0 = O.Packed(O.Tables.of(m), As[0], k_tile=args.k_tile, value_dtype=spreg_dtype)
     got0 = packs[0].execute(Bd[0], Cd[0], nr=args.nr, staging=args.staging, meta=args.meta).cpu().numpy()
     B0ref = Bs[0] if args.dtype == "f32" else Bd[0].cpu().view(torch.int16).numpy().view(np.uint16)
     parity_ok = bool(np.array_equal(got0.view(np.uint32), ref0.execute(B0ref).view(np.uint32)))
 
     stream = torch.cuda.current_stream()
     from spreg.packed import execute_batched
-    work = [(p, B, C, dict(nr=args.nr, meta=args.meta)) for p, B, C in zip(packs, Bd, Cd)]
+    work = [(p, B, C, dict(nr=args.nr, meta=args.meta, staging=args.staging)) for p, B, C in zip(packs, Bd, Cd)]
 
     def step():
         if args.batched:
@@ -445,6 +575,8 @@ def main():
     serving = None
     if args.serving:
         serving = serving_bench(args, dev)
+    precision = precision_suite(dev) if args.precision else None
+    layers = layers_suite(dev) if args.layers else None
 
     cpu = None
     if rank == 0 and args.cpu_seconds > 0:
@@ -457,12 +589,14 @@ def main():
                 "config": {"workload": f"spmm_{args.dtype}_{args.m}x{args.k}_s{args.sparsity}_n{args.n}_x{args.replicas}",
                            "replicas": args.replicas, "m": args.m, "k": args.k, "n": args.n,
                            "sparsity": args.sparsity, "mr": 4, "mapping": "61fee", "nr": args.nr or "auto",
-                           "b_staging": {0: "auto", 1: "shared-memory strips", 2: "L1/L2"}[args.staging],
+                           "b_staging": {0: "auto", 1: "shared-memory B tiles", 2: "L1/L2"}[args.staging],
+                           "k_tile": args.k_tile,
                            "cuda_graph": graph is not None, "batched_launch": bool(args.batched),
                            "l2": f"inputs larger than L2: working set {working_set / 2**20:.0f} MiB per step "
                                  f"vs {L2_BYTES / 2**20:.0f} MiB L2",
                            "parallelism": f"replicas x{ws}"},
                 "gflops": gflops, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "serving": serving,
+                "precision": precision, "batched_layers": layers,
                 "clocks": clk.summary(), "gpu_launches": launches_per_step * args.steps,
                 "parity_bit_exact_vs_oracle": parity_ok}
         print(json.dumps(line))
