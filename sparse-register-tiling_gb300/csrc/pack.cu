@@ -665,6 +665,7 @@ __global__ void __launch_bounds__(CH) arena_count_kernel(const Geom g, const Map
     __shared__ long long s_tmp[CH / 32];
     const int64_t u = blockIdx.x;
     load_map_table(&s_mt, mt);
+    __syncthreads();  // the table is read below by every thread
     const spreg_panel_desc d = descs[u];
     const int nk = s_mt.num_nkern;
     if (threadIdx.x == 0) {
@@ -748,6 +749,7 @@ __global__ void __launch_bounds__(CH) arena_emit_kernel(const MapTable *__restri
     __shared__ int s_ok;
     const int64_t u = blockIdx.x;
     load_map_table(&s_mt, mt);
+    __syncthreads();  // the table is read below by every thread
     const spreg_panel_desc sd = src_descs[u], d = descs[u];
     const int nk = s_mt.num_nkern;
     if (threadIdx.x == 0) {
