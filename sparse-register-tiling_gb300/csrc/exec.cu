@@ -9,6 +9,8 @@
 // shared-memory B-tile kernel (exec_tile_kernel), grouped the same way.
 #include "exec_tile.cuh"
 
+#include <cudaTypedefs.h>
+
 #include <algorithm>
 #include <atomic>
 #include <map>
@@ -162,6 +164,39 @@ int auto_nv(int64_t n, int64_t panels, int sms) {
 // Largest B tile (K tile rows x strip bytes) the shared-memory B kernel stages per stage.
 constexpr int64_t kTileMaxStageB = 96 * 1024;
 
+// cuTensorMapEncodeTiled from the driver, looked up once through the runtime.
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            p = nullptr;
+        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }();
+    return fn;
+}
+
+// Tensor map of B for the tile kernel: columns [0, cols) x rows [0, rows), a box of box_cols x
+// box_rows elements, zeros outside.
+int encode_b_map(CUtensorMap *map, const void *b, int dtype, int64_t cols, int64_t rows, int64_t ldb, int box_cols,
+                 int box_rows) {
+    auto enc = tensor_map_encoder();
+    SPREG_CHECK_ARG(enc, "cuTensorMapEncodeTiled is not available from the driver");
+    const CUtensorMapDataType t = dtype == SPREG_F32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32
+                                 : dtype == SPREG_BF16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16
+                                                       : CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
+    const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)(ldb * (int64_t)dtype_bytes(dtype))};
+    const cuuint32_t box[2] = {(cuuint32_t)box_cols, (cuuint32_t)box_rows};
+    const cuuint32_t es[2] = {1, 1};
+    CUresult r = enc(map, t, 2, const_cast<void *>(b), dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                     CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    SPREG_CHECK_ARG(r == CUDA_SUCCESS, "cuTensorMapEncodeTiled failed (%d) for B of %lld x %lld, ldb %lld", (int)r,
+                    (long long)rows, (long long)cols, (long long)ldb);
+    return SPREG_OK;
+}
+
 struct CallPlan {
     int mr, combo, nv;
     bool stream_kernel;      // run exec_kernel (register streams) instead of the batch kernel
@@ -223,17 +258,16 @@ int plan_call(const spreg_packed *a, const spreg_exec_args *args, CallPlan *cp) 
     // reads rounded up to 16 bytes stay inside each row of B), a tile that fits a stage, and the
     // column ranges of K tiles (not the per-panel offsets of panel-by-panel packs).
     const int64_t kt_rows = a->geom.kt;
-    auto tile_rows_ok = [&](int nvv, int64_t col_end) {
-        const int64_t stage_b = kt_rows * 32 * nvv * (int64_t)bsz;
-        const int64_t need = (col_end * (int64_t)bsz + 15) / 16 * 16;
-        return stage_b <= kTileMaxStageB && need <= args->ldb * (int64_t)bsz;
-    };
+    const int box_rows = (int)std::min<int64_t>(kt_rows, kTileBoxRows);
+    const int64_t staged_rows = (kt_rows + box_rows - 1) / box_rows * box_rows;
+    auto tile_rows_ok = [&](int nvv) { return staged_rows * 32 * nvv * (int64_t)bsz <= kTileMaxStageB; };
     const bool tile_base_ok = a->exec && !a->list_packed && aligned(args->b, 16) &&
                               (args->ldb * (int64_t)bsz) % 16 == 0 && 1024 + 2 * cp->xbuf <= f->smem_optin;
     if (args->b_staging == 1) {
         SPREG_CHECK_ARG(tile_base_ok, "shared-memory B tiles need a dense/CSR pack, a 16-byte aligned B with "
                         "16-byte aligned rows, and execution blocks that fit shared memory");
         SPREG_CHECK_ARG(args->meta_staging != 2, "b_staging = 1 runs the execution-layout metadata path");
+        SPREG_CHECK_ARG(args->n <= INT32_MAX, "n out of range for shared-memory B tiles");
     }
 
     XProblem base = {};
@@ -263,11 +297,11 @@ int plan_call(const spreg_packed *a, const spreg_exec_args *args, CallPlan *cp) 
 
     cp->tile = false;
     if (args->b_staging == 1) {
-        const bool main_ok = !cp->has_main || tile_rows_ok(nv, n_main);
-        const bool tail_ok = !cp->has_tail || tile_rows_ok(1, args->n);
+        const bool main_ok = !cp->has_main || tile_rows_ok(nv);
+        const bool tail_ok = !cp->has_tail || tile_rows_ok(1);
         SPREG_CHECK_ARG(main_ok && tail_ok, "shared-memory B tiles: a K tile of %lld rows x %d columns exceeds a "
-                        "stage (%lld bytes), or the last columns round past ldb; pack with a smaller k_tile",
-                        (long long)kt_rows, 32 * nv, (long long)kTileMaxStageB);
+                        "stage (%lld bytes); pack with a smaller k_tile", (long long)kt_rows, 32 * nv,
+                        (long long)kTileMaxStageB);
         cp->tile = true;
         cp->stream_kernel = false;
         TProblem tb = {};
@@ -287,16 +321,24 @@ int plan_call(const spreg_packed *a, const spreg_exec_args *args, CallPlan *cp) 
         tb.kt = (int32_t)kt_rows;
         tb.krows = (int32_t)a->geom.K;
         tb.col_offset = (int32_t)in.col_offset;
+        tb.box_rows = box_rows;
+        const int64_t brows = in.col_offset + a->geom.K;
         cp->tmain = tb;
         cp->tmain.col_begin = 0;
-        cp->tmain.col_end = n_main;
+        cp->tmain.col_end = (int32_t)n_main;
         cp->tmain.S = cp->main.S;
+        if (cp->has_main && (st = encode_b_map(&cp->tmain.tmap, args->b, args->b_dtype, n_main, brows, args->ldb,
+                                               32 * nv, box_rows)))
+            return st;
         cp->ttail = tb;
-        cp->ttail.col_begin = n_main;
-        cp->ttail.col_end = args->n;
+        cp->ttail.col_begin = (int32_t)n_main;
+        cp->ttail.col_end = (int32_t)args->n;
         cp->ttail.S = cp->tail.S;
-        cp->stage_b_main = (kt_rows * 32 * nv * (int64_t)bsz + 127) / 128 * 128;
-        cp->stage_b_tail = (kt_rows * 32 * (int64_t)bsz + 127) / 128 * 128;
+        if (cp->has_tail && (st = encode_b_map(&cp->ttail.tmap, args->b, args->b_dtype, args->n, brows, args->ldb, 32,
+                                               box_rows)))
+            return st;
+        cp->stage_b_main = (staged_rows * 32 * nv * (int64_t)bsz + 127) / 128 * 128;
+        cp->stage_b_tail = (staged_rows * 32 * (int64_t)bsz + 127) / 128 * 128;
     }
 
     ExecParams &p = cp->sp;
@@ -409,8 +451,8 @@ int launch_tile_groups(std::map<std::tuple<int, int, int>, TileGroup> &groups, c
                         (long long)smem_for(W));
         const size_t smem = (size_t)smem_for(W);
         const int threads = 32 * (W + 1);
-        for (size_t first = 0; first < g.probs.size(); first += kMaxBatchProblems) {
-            const size_t cnt = std::min<size_t>(kMaxBatchProblems, g.probs.size() - first);
+        for (size_t first = 0; first < g.probs.size(); first += kTileMaxProblems) {
+            const size_t cnt = std::min<size_t>(kTileMaxProblems, g.probs.size() - first);
             TileParams tp;
             tp.nprob = (int32_t)cnt;
             int64_t jobs = 0;

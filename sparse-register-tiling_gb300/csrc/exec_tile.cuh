@@ -2,9 +2,11 @@
 //
 // A job is (problem, group of W row panels, strip of 32 * NV columns).  One CTA runs W consumer
 // warps (warp w owns panel group * W + w, its accumulators in registers as in exec_batch_kernel)
-// and one producer warp.  For every K tile t of the job the producer bulk-copies
-//   * the tile's B rows [col_offset + t * K_c, ... + K_c) x the strip's columns, and
-//   * the execution block of unit (panel, t) of every consumer warp
+// and one producer warp.  For every K tile t of the job the producer copies
+//   * the tile's B rows [col_offset + t * K_c, ... + K_c) x the strip's columns: one 2-D tensor
+//     copy (TMA, a tensor map of B per problem) per 256 rows, zero-filled outside B, and
+//   * the execution blocks of units (panel, t) of all consumer warps: one bulk copy when the
+//     blocks are adjacent in memory (panels of one row tile), else one per warp
 // into one stage of a ring of kTileStages stages, and arrives on the stage's "full" barrier
 // (expect_tx of all bytes).  Consumers gather B rows out of shared memory (one broadcast-free
 // 4 * NV-byte load per lane per entry) and arrive on the stage's "empty" barrier when done; the
@@ -21,12 +23,18 @@
 // Every wait is bounded; a wait that gives up records a code in the device status word and the
 // warp stops, the producer first waiting (bounded) for the copies it issued.
 #pragma once
+#include <cuda.h>
+
+#include <cstddef>
+
 #include "exec_kernel.cuh"
 
 namespace spreg {
 
 constexpr int kTileStages = 2;
-constexpr int kTileMaxWarps = 16;  // consumer warps per CTA
+constexpr int kTileMaxWarps = 16;    // consumer warps per CTA
+constexpr int kTileMaxProblems = 96; // problems per launch (a tensor map each; kernel parameters <= 32 KB)
+constexpr int kTileBoxRows = 256;    // rows of one tensor copy (TMA box limit)
 
 struct TProblem {
     const uint8_t *exec;        // execution layout of the packed matrix
@@ -35,15 +43,17 @@ struct TProblem {
     const void *B;
     void *C;
     int64_t ldb, ldc, M;
-    int64_t col_begin;          // first column of the problem's strips
-    int64_t col_end;            // columns >= col_end are not computed
     int64_t job_begin;          // first global job
+    int32_t col_begin;          // first column of the problem's strips
+    int32_t col_end;            // columns >= col_end are not computed
     int32_t P, S, T, ppt;       // row panels, strips, K tiles, panels per row tile
     int32_t load_c, epilogue;
     int32_t kt, krows;          // B rows per K tile, B rows of all tiles (columns of A)
     int32_t col_offset, groups; // first B row of tile 0; panel groups of W panels
+    int32_t box_rows, pad0;     // rows of one tensor copy (K tile copied in ceil(kt / box_rows) copies)
+    CUtensorMap tmap;           // B as a 2-D tensor: columns [0, col_end) x rows [0, col_offset + krows)
 };
-static_assert(sizeof(TProblem) == 128, "TProblem is 128 bytes");
+static_assert(sizeof(TProblem) == 256 && offsetof(TProblem, tmap) == 128, "TProblem layout");
 
 struct TileParams {
     int *counter;               // job counter, zero at launch
@@ -53,8 +63,9 @@ struct TileParams {
     int32_t xbuf;               // bytes of one consumer's metadata slot
     int32_t warps;              // consumer warps W
     int32_t stage_b;            // bytes of one stage's B tile
-    TProblem prob[kMaxBatchProblems];
+    TProblem prob[kTileMaxProblems];
 };
+static_assert(sizeof(TileParams) <= 32764, "kernel parameters are limited to 32764 bytes");
 
 __device__ __forceinline__ int find_tproblem(const TileParams &tp, int64_t job) {
     int lo = 0, hi = tp.nprob - 1;
@@ -66,8 +77,18 @@ __device__ __forceinline__ int find_tproblem(const TileParams &tp, int64_t job) 
     return lo;
 }
 
+// One box of a 2-D tensor map (columns x, rows y) into shared memory; rows and columns outside
+// the tensor read as zero.
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int x, int y, uint32_t bar) {
+    asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+                 ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar) : "memory");
+}
+
 __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void sts_u32(uint32_t a, uint32_t v) {
+    asm volatile("st.shared.b32 [%0], %1;" ::"r"(a), "r"(v) : "memory");
 }
 __device__ __forceinline__ void sts_v4(uint32_t a, int x, int y, int z, int w) {
     asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(a), "r"(x), "r"(y), "r"(z), "r"(w) : "memory");
@@ -162,7 +183,8 @@ __device__ __forceinline__ void t_store(const TProblem &pr, int64_t gp, int64_t 
 }
 
 // Shared memory: [0, 64) full / empty barriers, [256, 256 + 16 * stages) job of each stage,
-// from 1024 the stages: B tile (stage_b bytes) then W metadata slots (xbuf bytes each).
+// [512, 512 + 4 * 16 * stages) each consumer's block offset in each stage's metadata area, from
+// 1024 the stages: B tile (stage_b bytes) then the metadata area (W * xbuf bytes).
 template <int MR, int NV, class TV, class TB, class TC>
 __global__ void __launch_bounds__(32 * (kTileMaxWarps + 1), 1) exec_tile_kernel(const __grid_constant__ TileParams tp) {
     extern __shared__ __align__(128) unsigned char smem[];
@@ -170,7 +192,7 @@ __global__ void __launch_bounds__(32 * (kTileMaxWarps + 1), 1) exec_tile_kernel(
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int W = tp.warps;
     const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(smem);
-    const uint32_t full0 = sbase, empty0 = sbase + 8u * kTileStages, jobs0 = sbase + 256u;
+    const uint32_t full0 = sbase, empty0 = sbase + 8u * kTileStages, jobs0 = sbase + 256u, moffs0 = sbase + 512u;
     const uint32_t stage_bytes = (uint32_t)tp.stage_b + (uint32_t)W * (uint32_t)tp.xbuf;
     const uint32_t stage0 = sbase + 1024u;
     if (threadIdx.x == 0) {
@@ -221,36 +243,41 @@ __global__ void __launch_bounds__(32 * (kTileMaxWarps + 1), 1) exec_tile_kernel(
                 break;
             }
             const TProblem &pr = tp.prob[pi];
-            const int64_t r0 = (int64_t)pr.col_offset + (int64_t)t * pr.kt;
-            const int64_t rl = (int64_t)pr.krows - (int64_t)t * pr.kt;
-            const int nrows = (int)(rl < pr.kt ? rl : pr.kt);
-            const int64_t c0 = pr.col_begin + (int64_t)strip * (32 * NV);
-            const int64_t ncols = (pr.col_end - c0) < 32 * NV ? (pr.col_end - c0) : 32 * NV;
-            const uint32_t wbytes = (uint32_t)((ncols * (int64_t)sizeof(TB) + 15) & ~(int64_t)15);
-            uint32_t mbytes = 0;
+            const int r0 = pr.col_offset + t * pr.kt;
+            const int c0 = pr.col_begin + strip * (32 * NV);
+            const int nbox = (pr.kt + pr.box_rows - 1) / pr.box_rows;
+            // metadata: lane w < W holds the block of unit (group * W + w, t)
             int64_t moff = 0;
+            uint32_t mbytes = 0;
             const int64_t gp = (int64_t)group * W + lane;
-            if (lane < W && gp < pr.P) {
+            const bool act = lane < W && gp < pr.P;
+            if (act) {
                 const int64_t u = unit_index(gp, t, pr.ppt, pr.T, pr.P);
                 moff = pr.exec_offs[u];
                 mbytes = (uint32_t)(pr.exec_offs[u + 1] - moff);
             }
-            uint32_t total = mbytes;
+            const int nact = __popc(__ballot_sync(0xffffffffu, act));  // active lanes are 0 .. nact - 1
+            const int64_t m0 = __shfl_sync(0xffffffffu, moff, 0);
+            const int64_t nxt = __shfl_down_sync(0xffffffffu, moff, 1);
+            const bool contig = __all_sync(0xffffffffu, !(act && lane + 1 < nact) || moff + mbytes == nxt);
+            uint32_t mtotal = mbytes;
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) total += __shfl_xor_sync(0xffffffffu, total, o);
-            total += wbytes * (uint32_t)nrows;
+            for (int o = 16; o > 0; o >>= 1) mtotal += __shfl_xor_sync(0xffffffffu, mtotal, o);
+            if (lane < W)
+                sts_u32(moffs0 + 4u * (uint32_t)(s * kTileMaxWarps + lane),
+                        contig ? (uint32_t)(moff - m0) : (uint32_t)lane * (uint32_t)tp.xbuf);
+            const uint32_t sb = stage0 + (uint32_t)s * stage_bytes;
             if (lane == 0) {
                 sts_v4(jobs0 + 16u * s, pi, group, strip, t);
-                mbar_arrive_expect_tx(full, total);
+                mbar_arrive_expect_tx(full, (uint32_t)nbox * (uint32_t)pr.box_rows * ROWB + mtotal);
+                for (int b = 0; b < nbox; ++b)
+                    tma_load_2d(sb + (uint32_t)(b * pr.box_rows) * ROWB, &pr.tmap, c0, r0 + b * pr.box_rows, full);
+                if (contig && mtotal) bulk_copy_g2s(sb + (uint32_t)tp.stage_b, pr.exec + m0, mtotal, full);
             }
+            if (!contig && mbytes)
+                bulk_copy_g2s(sb + (uint32_t)tp.stage_b + (uint32_t)lane * (uint32_t)tp.xbuf, pr.exec + moff, mbytes,
+                              full);
             __syncwarp();
-            const uint32_t sb = stage0 + (uint32_t)s * stage_bytes;
-            const char *bsrc = reinterpret_cast<const char *>(pr.B) + c0 * (int64_t)sizeof(TB);
-            const int64_t ldb_bytes = pr.ldb * (int64_t)sizeof(TB);
-            for (int r = lane; r < nrows; r += 32)
-                bulk_copy_g2s(sb + (uint32_t)r * ROWB, bsrc + (r0 + r) * ldb_bytes, wbytes, full);
-            if (mbytes) bulk_copy_g2s(sb + (uint32_t)tp.stage_b + (uint32_t)lane * (uint32_t)tp.xbuf, pr.exec + moff,
-                                      mbytes, full);
             last_seq[s] = seq;
             if (++t == pr.T) fetch();
         }
@@ -281,7 +308,8 @@ __global__ void __launch_bounds__(32 * (kTileMaxWarps + 1), 1) exec_tile_kernel(
             const bool valid = col0 < pr.col_end;
             if (t == 0) t_acc_init<MR, NV, TV, TC>(pr, row0, col0, valid, acc);
             const uint32_t sb = stage0 + (uint32_t)s * stage_bytes;
-            const uint32_t buf = sb + (uint32_t)tp.stage_b + (uint32_t)warp * (uint32_t)tp.xbuf;
+            const uint32_t buf =
+                sb + (uint32_t)tp.stage_b + lds_u32(moffs0 + 4u * (uint32_t)(s * kTileMaxWarps + warp));
             const SmemB<NV, TB> bl{sb + (uint32_t)lane * (uint32_t)(NV * sizeof(TB)),
                                    (int32_t)(pr.col_offset + (int64_t)t * pr.kt), ROWB};
             const uint32_t G = lds_u32(buf);
