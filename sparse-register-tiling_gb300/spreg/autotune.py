@@ -15,6 +15,9 @@ panel, stands for the critical path of one warp when there are too few items to 
 GPU.  One coefficient set per (M_r, NV, value/B type); `fit_costs` solves non-negative least
 squares over measured samples.
 
+For M_r = 8 the candidates also include a nanokernel set built for the matrix from its pattern
+histogram (`kernel_sets.greedy_kernel_set`, the reference's set-cover model in greedy form).
+
 `tune` ranks every candidate with the model, times the best few on the device with the reference's
 timing protocol (`execute_timed`: median of repeated runs), and returns the fastest, so a poor
 model costs tuning time, not speed.
@@ -56,8 +59,27 @@ class Candidate:
         return f"M{self.mr}N{self.nr}_{self.mapping}" + (f"_K{self.k_tile}" if self.k_tile else "")
 
 
+# Mappings built in this process (greedy sets from a matrix's histogram), by mapping id.
+GENERATED: Dict[str, Mapping] = {}
+
+
 def mapping_of(mr: int, name: str) -> Mapping:
-    return Mapping.identity(mr) if name == "identity" else Mapping.load(name)
+    if name == "identity":
+        return Mapping.identity(mr)
+    if name in GENERATED:
+        return GENERATED[name]
+    return Mapping.load(name)
+
+
+def greedy_mapping(mask: np.ndarray, mr: int, budget: int = 19, k_c: int = 128) -> Mapping:
+    """Nanokernel set for this matrix from its pattern histogram (`kernel_sets`), registered under
+    its mapping id so that `mapping_of` finds it."""
+    from .kernel_sets import executor_penalty, greedy_kernel_set
+    hist = np.bincount(panel_codes(mask, mr).ravel(), minlength=2 ** mr)
+    units = ((mask.shape[0] + mr - 1) // mr) * max(1, math.ceil(mask.shape[1] / k_c))
+    m = greedy_kernel_set(hist, mr, budget, units, penalty=executor_penalty(mr))
+    GENERATED[m.mapping_id] = m
+    return m
 
 
 # ---------------------------------------------------------------------------- statistics
@@ -241,13 +263,17 @@ class TuneResult:
 
 
 def rank(mask: np.ndarray, n: int, dtype: str = "f32", costs: Optional[Costs] = None,
-         mrs: Iterable[int] = (2, 4, 8), k_tiles: Iterable[int] = K_TILES
+         mrs: Iterable[int] = (2, 4, 8), k_tiles: Iterable[int] = K_TILES, greedy: bool = True
          ) -> Tuple[List[Tuple[float, Candidate]], Dict[Tuple[int, str], PanelStats]]:
     """Candidates sorted by predicted time, and the statistics they were predicted from."""
     costs = costs if costs is not None else Costs.load()
     stats: Dict[Tuple[int, str], PanelStats] = {}
     ranked = []
-    for c in candidates(n, mrs, mask.shape[1], k_tiles):
+    cands = candidates(n, mrs, mask.shape[1], k_tiles)
+    if greedy and 8 in tuple(mrs):
+        gid = greedy_mapping(mask, 8).mapping_id
+        cands += [Candidate(c.mr, gid, c.nr, c.k_tile) for c in cands if c.mr == 8 and c.mapping == "identity"]
+    for c in cands:
         key = (c.mr, c.mapping)
         if key not in stats:
             stats[key] = panel_stats(mask, c.mr, mapping_of(c.mr, c.mapping))

@@ -72,7 +72,7 @@ def test_costs_save_load(tmp_path):
 
 def test_rank_orders_all_candidates():
     A = synth.row_skew(512, 512, 0.9, seed=1)
-    ranked, stats = rank(A != 0, 48, "f32", Costs.default())
+    ranked, stats = rank(A != 0, 48, "f32", Costs.default(), greedy=False)
     ts = [t for t, _ in ranked]
     assert ts == sorted(ts)
     names = {c.name() for _, c in ranked}
@@ -101,3 +101,14 @@ def test_tune_picks_a_measured_candidate_and_it_is_exact(cuda):
     got = pm.execute(torch.from_numpy(B).cuda(), nr=res.best.nr).cpu().numpy()
     want = O.Packed(O.Tables.of(m), A).execute(B)
     np.testing.assert_array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
+def test_rank_adds_greedy_nanokernel_set_for_mr8():
+    from spreg.autotune import GENERATED
+    A = synth.row_skew(256, 384, 0.9, seed=2)
+    ranked, stats = rank(A != 0, 64, "f32", Costs.default())
+    gen = {c.mapping for _, c in ranked if c.mapping in GENERATED}
+    assert len(gen) == 1
+    gid = gen.pop()
+    assert all(c.mr == 8 for _, c in ranked if c.mapping == gid)
+    assert (8, gid) in stats and mapping_of(8, gid).mapping_id == gid
