@@ -1,10 +1,11 @@
 """Benchmark of the sparse-register-tiling SpMM on GB300.
 
 Workload (default): the FFN-shaped plain-FP32 SpMM -- A 2048 x 512 at 90 % sparsity with
-log-normal row skew (sigma 0.5), values N(0, 0.02), packed with M_r = 4 and the identity
-nanokernel set (mapping 61fee); B 512 x 512 FP32 N(0, 1).  One step runs the SpMM on R
-independent replicas (distinct seeds) whose working set (R x ~6 MB) is several times the L2,
-so every step streams A, B and C from HBM.
+log-normal row skew (sigma 0.5), values N(0, 0.02); B 512 x 512 FP32 N(0, 1).  Packed with
+M_r = 4, K tiles of 128 and the nanokernel set chosen from replica 0's pattern histogram
+(greedy set cover: the single rows plus the all-rows kernel), executed by the shared-memory
+B-tile kernel.  One step runs the SpMM on R independent replicas (distinct seeds) whose working
+set (R x ~6 MB) is several times the L2, so every step streams A, B and C from HBM.
 
   python bench.py [--steps K] [--warmup W] [--gpus N] [--impl spreg|reference]
 
@@ -33,7 +34,7 @@ for _p in (ROOT, PKG):
 import numpy as np  # noqa: E402
 
 METRIC = ("SpMM %HBM peak (plain FP32 sparse-register-tiling SpMM, A 2048x512 @90% row-skew, "
-          "N=512, M_r=4 identity): algorithmic GB/s")
+          "N=512): algorithmic GB/s")
 UNIT = "GB/s"
 L2_BYTES = 129 * 2 ** 20
 
@@ -50,8 +51,11 @@ def parse():
     ap.add_argument("--n", type=int, default=512)
     ap.add_argument("--sparsity", type=float, default=0.9)
     ap.add_argument("--nr", type=int, default=0)
-    ap.add_argument("--staging", type=int, default=0, help="0 auto, 1 shared-memory B tiles, 2 L1/L2")
-    ap.add_argument("--k-tile", type=int, default=0, help="K tile (K_c) of the packing; 0 = one tile")
+    ap.add_argument("--staging", type=int, default=1, help="0 auto, 1 shared-memory B tiles, 2 L1/L2")
+    ap.add_argument("--k-tile", type=int, default=128, help="K tile (K_c) of the packing; 0 = one tile")
+    ap.add_argument("--mr", type=int, default=4, help="panel height M_r")
+    ap.add_argument("--mapping", default="greedy",
+                    help="identity, a mapping id, or greedy (set cover on replica 0's pattern histogram)")
     ap.add_argument("--meta", type=int, default=0, help="0 auto, 1 execution-layout kernel, 2 register streams")
     ap.add_argument("--dtype", choices=["f32", "bf16"], default="f32",
                     help="storage of A values and B (FP32 accumulation and FP32 C either way)")
@@ -76,6 +80,18 @@ def dist_env():
     return ws, rank, local
 
 
+def bench_mapping(args, A0):
+    from spreg import Mapping
+    if args.mapping == "identity":
+        return Mapping.identity(args.mr)
+    if args.mapping == "greedy":
+        from spreg.kernel_sets import executor_penalty, greedy_kernel_set, pattern_histogram
+        units = ((A0.shape[0] + args.mr - 1) // args.mr) * max(1, -(-A0.shape[1] // (args.k_tile or 128)))
+        return greedy_kernel_set(pattern_histogram(A0, args.mr), args.mr, 2 ** args.mr - 1, units,
+                                 penalty=executor_penalty(args.mr))
+    return Mapping.load(args.mapping)
+
+
 def make_inputs(args, rank: int):
     from spreg import synth
     As, Bs = [], []
@@ -94,7 +110,8 @@ def algorithmic_bytes_oracle(pk, n: int) -> int:
 
 
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled every 200 ms while running."""
+    """nvidia-smi clocks / throttle reasons sampled every 50 ms; `summary` keeps the samples that
+    arrived between `mark_start` and `mark_end` (the timed region)."""
 
     QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -103,13 +120,21 @@ class ClockSampler:
     def __init__(self, index: int):
         self.index = index
         self.proc = None
-        self.lines: list[str] = []
+        self.lines: list[tuple] = []
         self.t = None
+        self.t0 = None
+        self.t1 = None
+
+    def mark_start(self):
+        self.t0 = time.perf_counter()
+
+    def mark_end(self):
+        self.t1 = time.perf_counter()
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -119,7 +144,7 @@ class ClockSampler:
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.perf_counter(), line.strip()))
 
     def __exit__(self, *exc):
         if self.proc is not None:
@@ -134,7 +159,13 @@ class ClockSampler:
     def summary(self) -> dict:
         mhz, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        t0 = self.t0 if self.t0 is not None else float("-inf")
+        t1 = self.t1 if self.t1 is not None else float("inf")
+        inside = [ln for t, ln in self.lines if t0 <= t <= t1]
+        if not inside and self.lines:  # a region shorter than one sampling interval: the nearest sample
+            mid = (t0 + t1) / 2 if self.t0 is not None and self.t1 is not None else self.lines[-1][0]
+            inside = [min(self.lines, key=lambda x: abs(x[0] - mid))[1]]
+        for ln in inside:
             f = [x.strip() for x in ln.split(",")]
             if len(f) < 9:
                 continue
@@ -151,15 +182,16 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(mhz), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(mhz)}
 
 
-def load_traffic():
-    path = os.path.join(ROOT, "profiles", "exec_fp32_2048x512_n512.json")
-    if os.path.exists(path):
-        try:
-            with open(path) as f:
-                return json.load(f).get("dram_bytes_per_launch")
-        except (OSError, ValueError):
-            return None
-    return None
+def load_traffic(key: str, spmms_per_launch: int):
+    """DRAM bytes per launch from the ncu summaries in profiles/traffic.json (per-SpMM figure of the
+    captured launch x SpMMs per launch), or None when that kernel and workload were not captured."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as f:
+            e = json.load(f).get(key)
+    except (OSError, ValueError):
+        return None
+    return None if not e else e["dram_bytes_per_spmm"] * spmms_per_launch
 
 
 def measured_peaks():
@@ -373,11 +405,11 @@ def _stat(st) -> dict:
             "mean_ms": st.mean_ms, "requests": st.requests}
 
 
-def cpu_baseline(As, Bs, args, seconds: float, threads: int = 0):
+def cpu_baseline(As, Bs, args, seconds: float, threads: int = 0, mapping=None):
     """Restated reference executor (oracle, OpenMP) on a bounded sample of the same workload."""
     from oracle import oracle as O
     from spreg.mapping import Mapping
-    t = O.Tables.of(Mapping.identity(4))
+    t = O.Tables.of(mapping if mapping is not None else Mapping.identity(args.mr))
     done_bytes, done_flops, runs, i = 0, 0, 0, 0
     packs = {}
     t0 = time.perf_counter()
@@ -385,7 +417,7 @@ def cpu_baseline(As, Bs, args, seconds: float, threads: int = 0):
     while elapsed < seconds and runs < 10000:
         r = i % len(As)
         if r not in packs:
-            packs[r] = O.Packed(t, As[r])
+            packs[r] = O.Packed(t, As[r], k_tile=args.k_tile)
         pk = packs[r]
         s = time.perf_counter()
         pk.execute(Bs[r], threads=threads)
@@ -411,9 +443,8 @@ def run_reference(args):
     from oracle import oracle as O
     O.build(with_reference=False) if not os.path.exists(O.LIB_PATH) else None
     As, Bs = make_inputs(args, 0)
-    from spreg.mapping import Mapping
-    t = O.Tables.of(Mapping.identity(4))
-    packs = [O.Packed(t, A) for A in As]
+    t = O.Tables.of(bench_mapping(args, As[0]))
+    packs = [O.Packed(t, A, k_tile=args.k_tile) for A in As]
     per_step = sum(algorithmic_bytes_oracle(p, args.n) for p in packs)
     for _ in range(args.warmup):
         for p, B in zip(packs, Bs):
@@ -431,7 +462,7 @@ def run_reference(args):
             "data": "synthetic (seeded row-skew sparse A, N(0,1) B)",
             "config": {"workload": f"spmm_fp32_{args.m}x{args.k}_s{args.sparsity}_n{args.n}_x{args.replicas}",
                        "replicas": args.replicas, "m": args.m, "k": args.k, "n": args.n, "sparsity": args.sparsity,
-                       "mr": 4, "mapping": "61fee"},
+                       "mr": args.mr, "mapping": args.mapping, "k_tile": args.k_tile},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                              "sample": f"the full workload ({args.replicas} replicas) per step, restated reference "
                                        "executor (oracle/spreg_oracle.c), OpenMP over all host threads"},
@@ -456,8 +487,8 @@ def main():
     from oracle import oracle as O
     from spreg import Mapping, MatMulSpecialized, PackedMatrix, TileConfig, synth
 
-    m = Mapping.identity(4)
     As, Bs = make_inputs(args, rank)
+    m = bench_mapping(args, As[0])
     vd = spreg_dtype = (0 if args.dtype == "f32" else 1)
     tdt = torch.float32 if args.dtype == "f32" else torch.bfloat16
     packs, Bd, Cd = [], [], []
@@ -508,19 +539,21 @@ def main():
             graph = None
 
     run = graph.replay if graph is not None else step
-    for _ in range(max(args.warmup, 3)):
-        run()
-    torch.cuda.synchronize()
-    if ws > 1:
-        torch.distributed.barrier()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(dev.index) as clk:
+    with ClockSampler(dev.index) as clk:  # sampling starts before the warm-up steps
+        for _ in range(max(args.warmup, 3)):
+            run()
         torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        clk.mark_start()
         ev0.record(stream)
         for _ in range(args.steps):
             run()
         ev1.record(stream)
         torch.cuda.synchronize()
+        clk.mark_end()
     ms = ev0.elapsed_time(ev1)
     if ws > 1:
         t = torch.tensor([ms], device=dev)
@@ -537,11 +570,14 @@ def main():
     launch_s = sec / (args.steps * launches_per_step)
     achieved = (step_bytes / launches_per_step) / launch_s / 1e9
     spmm_us = sec / (args.steps * len(packs)) * 1e6
-    traffic = load_traffic()
+    kname = "exec_tile_kernel" if args.staging == 1 else "exec_batch_kernel"
+    traffic_key = (f"{kname}/{args.dtype}/{args.m}x{args.k}/s{args.sparsity}/n{args.n}/kt{args.k_tile}/"
+                   f"{'identity' if args.mapping == 'identity' else args.mapping}")
+    traffic = load_traffic(traffic_key, len(packs) // launches_per_step)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "peak_source": f"{peak_kind} hbm_gbs", "traffic": traffic,
-                "kernel": "spreg::exec_batch_kernel<4,NV,%s>" % ("float,float,float" if args.dtype == "f32" else
-                                                                  "bf16,bf16,float"),
+                "peak_source": f"{peak_kind} hbm_gbs", "traffic": traffic, "traffic_key": traffic_key,
+                "kernel": "spreg::%s<%d,NV,%s>" % (kname, args.mr, "float,float,float" if args.dtype == "f32" else
+                                                    "bf16,bf16,float"),
                 "spmm_us": spmm_us, "launches_per_step": launches_per_step,
                 "algorithmic_bytes_per_launch": step_bytes / launches_per_step,
                 "flops_per_launch": step_flops / launches_per_step, "gflops": gflops,
@@ -552,7 +588,8 @@ def main():
     mms, Bh, Ch = [], [], []
     for A, B in zip(As[:e2e_n], Bs[:e2e_n]):
         rp, ci, v = synth.to_csr(A)
-        mms.append(MatMulSpecialized(args.m, args.k, args.n, v, rp, ci, TileConfig(nr=args.nr), 1, "", m))
+        mms.append(MatMulSpecialized(args.m, args.k, args.n, v, rp, ci, TileConfig(K_c=args.k_tile, nr=args.nr), 1, "",
+                                     m))
         Bh.append(torch.from_numpy(B).pin_memory())
         Ch.append(torch.empty((args.m, args.n), dtype=torch.float32).pin_memory())
     for mm, B, C in zip(mms, Bh, Ch):
@@ -580,7 +617,7 @@ def main():
 
     cpu = None
     if rank == 0 and args.cpu_seconds > 0:
-        cpu = cpu_baseline(As, Bs, args, args.cpu_seconds)
+        cpu = cpu_baseline(As, Bs, args, args.cpu_seconds, mapping=m)
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -588,7 +625,8 @@ def main():
                 "vs_baseline": None, "dtype": args.dtype, "data": "synthetic (seeded row-skew sparse A, N(0,1) B)",
                 "config": {"workload": f"spmm_{args.dtype}_{args.m}x{args.k}_s{args.sparsity}_n{args.n}_x{args.replicas}",
                            "replicas": args.replicas, "m": args.m, "k": args.k, "n": args.n,
-                           "sparsity": args.sparsity, "mr": 4, "mapping": "61fee", "nr": args.nr or "auto",
+                           "sparsity": args.sparsity, "mr": args.mr, "mapping": m.mapping_id,
+                           "nanokernels": m.nanokernels if args.mapping != "identity" else "all", "nr": args.nr or "auto",
                            "b_staging": {0: "auto", 1: "shared-memory B tiles", 2: "L1/L2"}[args.staging],
                            "k_tile": args.k_tile,
                            "cuda_graph": graph is not None, "batched_launch": bool(args.batched),
