@@ -234,6 +234,17 @@ int spreg_execute_batched(const spreg_work_item *items_host, int32_t num_items, 
 #define SPREG_NOALLOC_MAX_LAUNCHES 64
 int spreg_execute_batched_noalloc(const spreg_work_item *items_host, int32_t num_items, spreg_stream_t stream);
 
+/* Dense row panels on the tensor cores: C[row_index[i], 0:n] (+)= A_rows[i, 0:k] . B[0:k, 0:n] for
+ * i < rows, with tcgen05 BF16 MMAs accumulating in FP32 tensor memory (all pointers on the device).
+ * A_rows is rows x k BF16 (16-byte aligned, lda a multiple of 8), B is k x n BF16 (row stride ldb), C
+ * is F32 or BF16 (row stride ldc); load_c adds C, epilogue 1 applies ReLU.  For the panels of a
+ * pruned matrix dense enough that a dense product beats the register-tiled executors (the
+ * reference's executor runs every panel register-tiled, spmm/nano/SpMM_SOP.h:174-178).  Results
+ * are not bit-identical to the register-tiled order: the accumulation order is the tensor core's. */
+int spreg_dense_rows_bf16(const void *a_rows, int64_t rows, int64_t k, int64_t lda, const int32_t *row_index,
+                          const void *b, int64_t ldb, void *c, int64_t ldc, int64_t n, int32_t c_dtype,
+                          int32_t load_c, int32_t epilogue, spreg_stream_t stream);
+
 /* Status word of the current device: nonzero once a kernel gave up a bounded wait (its results
  * are then incomplete).  Synchronous; reset != 0 clears it. */
 int spreg_device_status(int32_t *status_host, int32_t reset);

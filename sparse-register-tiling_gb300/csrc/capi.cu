@@ -15,6 +15,8 @@ void set_error(const std::string &msg) { g_last_error = msg; }
 void clear_error() { g_last_error.clear(); }
 
 // Implemented in pack.cu / exec.cu.
+int dense_rows_bf16_impl(const void *, int64_t, int64_t, int64_t, const int32_t *, const void *, int64_t, void *,
+                         int64_t, int64_t, int32_t, int32_t, int32_t, cudaStream_t);
 int pack_from_arena_impl(const spreg_mapping *, const spreg_arena_geom *, const void *, int64_t,
                          const spreg_panel_desc *, int64_t, const float *, int64_t, spreg_packed **, cudaStream_t);
 int pack_dense_impl(const spreg_mapping *, const float *, int64_t, int64_t, int64_t, const spreg_pack_opts *,
@@ -211,6 +213,14 @@ int spreg_pack_from_arena(const spreg_mapping *m, const spreg_arena_geom *geom, 
     clear_error();
     if (out) *out = nullptr;
     return pack_from_arena_impl(m, geom, arena_host, arena_bytes, descs_host, num_units, scales_host, num_scales, out,
+                                (cudaStream_t)stream);
+}
+
+int spreg_dense_rows_bf16(const void *a_rows, int64_t rows, int64_t k, int64_t lda, const int32_t *row_index,
+                          const void *b, int64_t ldb, void *c, int64_t ldc, int64_t n, int32_t c_dtype,
+                          int32_t load_c, int32_t epilogue, spreg_stream_t stream) {
+    clear_error();
+    return dense_rows_bf16_impl(a_rows, rows, k, lda, row_index, b, ldb, c, ldc, n, c_dtype, load_c, epilogue,
                                 (cudaStream_t)stream);
 }
 

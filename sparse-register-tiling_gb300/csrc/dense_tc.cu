@@ -1,0 +1,319 @@
+// dense_tc.cu -- dense row panels on the 5th-generation tensor cores (tcgen05 MMA, tensor memory,
+// TMA).
+//
+// C[row_index[i], 0:n] (+)= A_rows[i, 0:K] . B[0:K, 0:n] for the rows of a pruned matrix whose panels
+// are dense enough that a BF16 tensor-core product beats the register-tiled executors.  BF16 operands,
+// FP32 accumulation in tensor memory (TMEM), FP32 or BF16 output with load_c and the ReLU epilogue.
+//
+// One CTA computes a 128 x 128 output tile with 4 warps:
+//   * B is first transposed into a K-contiguous BF16 buffer Bt (n x K8, K8 = K rounded up to 8), so
+//     both MMA operands are K-major;
+//   * lane 0 of warp 0 loads 128 x 64 tiles of A_rows and Bt with 2-D tensor copies (TMA, 128-byte
+//     swizzle) into a ring of 4 stages ("full" mbarriers with expected bytes);
+//   * lane 0 of warp 1 issues, per 64-wide K block, four tcgen05.mma.kind::f16 (M 128, N 128, K 16)
+//     into a 128-column TMEM accumulator, and tcgen05.commit releases the stage ("empty" mbarrier);
+//     a last commit signals "done";
+//   * all 4 warps read the accumulator with tcgen05.ld (warp w owns TMEM lanes 32w .. 32w + 31, i.e.
+//     output rows), apply load_c / ReLU and store to row row_index[i] of C.
+// Rows past R and columns past n are zero-filled by the tensor copies and never stored; K past the
+// end of A_rows / Bt reads as zero.  Every wait is bounded: a wait that gives up records a code in
+// the device status word; TMEM is released on every path.
+#include "spreg_common.cuh"
+
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+namespace spreg {
+
+int *device_status_word(int *st);  // exec.cu
+
+namespace {
+
+constexpr int TC_BM = 128, TC_BN = 128, TC_BK = 64, TC_STAGES = 4;
+constexpr uint32_t TC_TILE_A = TC_BM * TC_BK * 2;  // 16 KB
+constexpr uint32_t TC_TILE_B = TC_BN * TC_BK * 2;  // 16 KB
+constexpr uint32_t TC_STAGE = TC_TILE_A + TC_TILE_B;
+constexpr uint32_t TC_TMEM_COLS = 128;
+constexpr size_t TC_SMEM = 1024 /* alignment slack */ + TC_STAGES * TC_STAGE + 256 /* barriers, TMEM slot */;
+
+struct TcParams {
+    CUtensorMap a_map;           // A_rows: columns [0, K) x rows [0, R), box 64 x 128, 128-byte swizzle
+    CUtensorMap b_map;           // Bt: columns [0, K) x rows [0, n), box 64 x 128, 128-byte swizzle
+    const int32_t *row_index;    // output row of each A row
+    void *C;
+    int64_t ldc;
+    int32_t R, n, kblocks, c_dtype;
+    int32_t load_c, epilogue, pad0, pad1;
+    int *status;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void tc_mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ bool tc_try_wait(uint32_t bar, uint32_t phase) {
+    uint32_t ok;
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(ok) : "r"(bar), "r"(phase) : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ bool tc_wait(uint32_t bar, uint32_t phase, int *status, int code) {
+    for (uint32_t it = 0; it < (1u << 22); ++it)
+        if (tc_try_wait(bar, phase)) return true;
+    if (status) atomicCAS(status, 0, code);
+    return false;
+}
+__device__ __forceinline__ void tc_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void tc_tma_2d(uint32_t dst, const CUtensorMap *map, int x, int y, uint32_t bar) {
+    asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+                 ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar) : "memory");
+}
+
+// Shared-memory matrix descriptor of a K-major operand tile stored with the 128-byte swizzle: rows of
+// 128 bytes (64 BF16), 8-row groups 1024 bytes apart.
+__device__ __forceinline__ uint64_t tc_desc(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);  // start address, 16-byte units
+    d |= (uint64_t)1 << 16;                    // leading-dimension byte offset (unused for this layout)
+    d |= (uint64_t)(1024 >> 4) << 32;          // stride-dimension byte offset: next 8-row group
+    d |= (uint64_t)1 << 46;                    // descriptor version of tcgen05
+    d |= (uint64_t)2 << 61;                    // layout: 128-byte swizzle
+    return d;
+}
+
+// Instruction descriptor of kind::f16: D FP32, A and B BF16, both K-major, M x N.
+__host__ __device__ constexpr uint32_t tc_idesc(int M, int N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc) {
+    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %4, 0;\n\t"
+                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+                 ::"r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc) : "memory");
+}
+__device__ __forceinline__ void tc_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, float (&v)[16]) {
+    uint32_t r[16];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+                 "%14, %15}, [%16];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                   "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                   "=r"(r[15])
+                 : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__global__ void __launch_bounds__(128, 1) tc_rows_kernel(const __grid_constant__ TcParams p) {
+    extern __shared__ unsigned char smem_raw[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t raw = smem_u32(smem_raw);
+    const uint32_t sbase = (raw + 1023u) & ~1023u;  // the swizzle atoms need 1024-byte alignment
+    const uint32_t bars = sbase + TC_STAGES * TC_STAGE;
+    const uint32_t full0 = bars, empty0 = bars + 8u * TC_STAGES, done = bars + 16u * TC_STAGES;
+    const uint32_t tmem_slot = done + 8u;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < TC_STAGES; ++s) {
+            tc_mbar_init(full0 + 8u * s, 1);
+            tc_mbar_init(empty0 + 8u * s, 1);
+        }
+        tc_mbar_init(done, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tmem_slot),
+                     "r"(TC_TMEM_COLS) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    uint32_t tmem;
+    asm volatile("ld.shared.b32 %0, [%1];" : "=r"(tmem) : "r"(tmem_slot) : "memory");
+
+    const int m0 = blockIdx.x * TC_BM, n0 = blockIdx.y * TC_BN;
+    if (warp == 0 && lane == 0) {
+        // producer: A and Bt tiles of each K block
+        int issued = 0;
+        for (int kb = 0; kb < p.kblocks; ++kb) {
+            const int s = kb % TC_STAGES;
+            if (kb >= TC_STAGES && !tc_wait(empty0 + 8u * s, (uint32_t)(((kb / TC_STAGES) - 1) & 1), p.status, 21))
+                break;
+            const uint32_t st = sbase + (uint32_t)s * TC_STAGE;
+            tc_expect_tx(full0 + 8u * s, TC_STAGE);
+            tc_tma_2d(st, &p.a_map, kb * TC_BK, m0, full0 + 8u * s);
+            tc_tma_2d(st + TC_TILE_A, &p.b_map, kb * TC_BK, n0, full0 + 8u * s);
+            issued = kb + 1;
+        }
+        // before the CTA can finish, every copy issued has landed
+        for (int kb = issued - TC_STAGES > 0 ? issued - TC_STAGES : 0; kb < issued; ++kb)
+            tc_wait(full0 + 8u * (kb % TC_STAGES), (uint32_t)((kb / TC_STAGES) & 1), p.status, 22);
+    } else if (warp == 1 && lane == 0) {
+        // MMA issuer
+        constexpr uint32_t idesc = tc_idesc(TC_BM, TC_BN);
+        for (int kb = 0; kb < p.kblocks; ++kb) {
+            const int s = kb % TC_STAGES;
+            if (!tc_wait(full0 + 8u * s, (uint32_t)((kb / TC_STAGES) & 1), p.status, 23)) break;
+            tc_fence_after();
+            const uint32_t st = sbase + (uint32_t)s * TC_STAGE;
+#pragma unroll
+            for (int k = 0; k < TC_BK / 16; ++k)
+                tc_mma(tmem, tc_desc(st + 32u * k), tc_desc(st + TC_TILE_A + 32u * k), idesc, (kb | k) != 0);
+            tc_commit(empty0 + 8u * s);  // the stage is free once these MMAs have read it
+        }
+        tc_commit(done);  // arrives when every MMA issued above has completed
+    }
+    __syncwarp();
+    const bool ok = __all_sync(0xffffffffu, tc_wait(done, 0u, p.status, 24));  // tcgen05.ld is warp-wide
+    tc_fence_after();
+
+    // epilogue: warp w reads TMEM lanes (rows) 32w .. 32w + 31
+    const int r = m0 + 32 * warp + lane;
+    const bool row_ok = ok && r < p.R;
+    const int64_t orow = row_ok ? p.row_index[r] : 0;
+    if (ok) {
+        for (int c = 0; c < TC_BN; c += 16) {
+            float v[16];
+            tc_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c, v);  // every lane takes part
+            if (!row_ok) continue;
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                const int col = n0 + c + j;
+                if (col >= p.n) break;
+                float o = v[j];
+                if (p.c_dtype == SPREG_F32) {
+                    float *cp = reinterpret_cast<float *>(p.C) + orow * p.ldc + col;
+                    if (p.load_c) o += *cp;
+                    if (p.epilogue == SPREG_EPILOGUE_RELU) o = fmaxf(o, 0.0f);
+                    *cp = o;
+                } else {
+                    __nv_bfloat16 *cp = reinterpret_cast<__nv_bfloat16 *>(p.C) + orow * p.ldc + col;
+                    if (p.load_c) o += __bfloat162float(*cp);
+                    if (p.epilogue == SPREG_EPILOGUE_RELU) o = fmaxf(o, 0.0f);
+                    *cp = __float2bfloat16_rn(o);
+                }
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_TMEM_COLS) : "memory");
+    }
+}
+
+// Bt[j][k] = B[k][j] for k < K (zero for K <= k < K8), j < n: 32 x 32 tiles through shared memory.
+__global__ void transpose_b_kernel(const __nv_bfloat16 *__restrict__ B, int64_t ldb, int K, int n, int K8,
+                                   __nv_bfloat16 *__restrict__ Bt) {
+    __shared__ __nv_bfloat16 tile[32][33];
+    const int k0 = blockIdx.x * 32, j0 = blockIdx.y * 32;
+    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+        const int k = k0 + i, j = j0 + threadIdx.x;
+        tile[i][threadIdx.x] = (k < K && j < n) ? B[(int64_t)k * ldb + j] : __float2bfloat16_rn(0.0f);
+    }
+    __syncthreads();
+    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+        const int j = j0 + i, k = k0 + threadIdx.x;
+        if (j < n && k < K8) Bt[(int64_t)j * K8 + k] = tile[threadIdx.x][i];
+    }
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 tc_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+        void *q = nullptr;
+        cudaDriverEntryPointQueryResult r;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &q, 12000, cudaEnableDefault, &r) != cudaSuccess ||
+            r != cudaDriverEntryPointSuccess)
+            q = nullptr;
+        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(q);
+    }();
+    return fn;
+}
+
+// BF16 matrix of `rows` x `cols` (row stride ld elements) as 64 x 128 boxes with the 128-byte swizzle.
+int tc_map(CUtensorMap *map, const void *base, int64_t cols, int64_t rows, int64_t ld) {
+    auto enc = tc_encoder();
+    SPREG_CHECK_ARG(enc, "cuTensorMapEncodeTiled is not available from the driver");
+    const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)(ld * 2)};
+    const cuuint32_t box[2] = {(cuuint32_t)TC_BK, (cuuint32_t)TC_BM};
+    const cuuint32_t es[2] = {1, 1};
+    CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), dims, strides, box, es,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    SPREG_CHECK_ARG(r == CUDA_SUCCESS, "cuTensorMapEncodeTiled failed (%d) for a %lld x %lld BF16 operand", (int)r,
+                    (long long)rows, (long long)cols);
+    return SPREG_OK;
+}
+
+}  // namespace
+
+int dense_rows_bf16_impl(const void *a_rows, int64_t R, int64_t K, int64_t lda, const int32_t *row_index,
+                         const void *b, int64_t ldb, void *c, int64_t ldc, int64_t n, int32_t c_dtype, int32_t load_c,
+                         int32_t epilogue, cudaStream_t stream) {
+    SPREG_CHECK_ARG(R >= 0 && K >= 0 && n >= 0, "negative size");
+    if (R == 0 || n == 0) return SPREG_OK;
+    SPREG_CHECK_ARG(a_rows && row_index && c && (b || K == 0), "null pointer");
+    SPREG_CHECK_ARG(R <= INT32_MAX && K <= INT32_MAX && n <= INT32_MAX, "size out of range");
+    SPREG_CHECK_ARG(c_dtype == SPREG_F32 || c_dtype == SPREG_BF16, "C must be F32 or BF16");
+    SPREG_CHECK_ARG(epilogue == SPREG_EPILOGUE_NONE || epilogue == SPREG_EPILOGUE_RELU, "bad epilogue");
+    SPREG_CHECK_ARG(lda >= K && (lda * 2) % 16 == 0 && reinterpret_cast<uintptr_t>(a_rows) % 16 == 0,
+                    "A rows must be 16-byte aligned with a row stride of a multiple of 8 elements (lda %lld)",
+                    (long long)lda);
+    SPREG_CHECK_ARG(ldb >= n && ldc >= n, "ldb / ldc smaller than n");
+    SPREG_CHECK_ARG(K > 0, "K must be positive");
+    SPREG_CHECK_ARG((n + TC_BN - 1) / TC_BN <= 65535, "n too large for one launch");
+    int st = SPREG_OK;
+    int *status = device_status_word(&st);
+    if (st != SPREG_OK) return st;
+    const int64_t K8 = (K + 7) / 8 * 8;
+    TcParams p = {};
+    p.row_index = row_index;
+    p.C = c;
+    p.ldc = ldc;
+    p.R = (int32_t)R;
+    p.n = (int32_t)n;
+    p.kblocks = (int32_t)((K + TC_BK - 1) / TC_BK);
+    p.c_dtype = c_dtype;
+    p.load_c = load_c ? 1 : 0;
+    p.epilogue = epilogue;
+    p.status = status;
+    static bool configured[64] = {};
+    int dev = 0;
+    SPREG_CUDA(cudaGetDevice(&dev));
+    if (dev >= 0 && dev < 64 && !configured[dev]) {
+        SPREG_CUDA(cudaFuncSetAttribute(tc_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM));
+        configured[dev] = true;
+    }
+    void *bt = nullptr;
+    SPREG_CUDA(cudaMallocAsync(&bt, (size_t)(n * K8 * 2), stream));
+    transpose_b_kernel<<<dim3((unsigned)((K8 + 31) / 32), (unsigned)((n + 31) / 32)), dim3(32, 8), 0, stream>>>(
+        static_cast<const __nv_bfloat16 *>(b), ldb, (int)K, (int)n, (int)K8, static_cast<__nv_bfloat16 *>(bt));
+    cudaError_t te = cudaGetLastError();
+    if (te != cudaSuccess) {
+        cudaFreeAsync(bt, stream);
+        SPREG_FAIL(SPREG_ERR_CUDA, "transpose launch: %s", cudaGetErrorString(te));
+    }
+    if ((st = tc_map(&p.a_map, a_rows, K, R, lda)) || (st = tc_map(&p.b_map, bt, K, n, K8))) {
+        cudaFreeAsync(bt, stream);
+        return st;
+    }
+    tc_rows_kernel<<<dim3((unsigned)((R + TC_BM - 1) / TC_BM), (unsigned)((n + TC_BN - 1) / TC_BN)), 128, TC_SMEM,
+                     stream>>>(p);
+    cudaError_t e = cudaGetLastError();
+    cudaFreeAsync(bt, stream);
+    if (e != cudaSuccess) SPREG_FAIL(SPREG_ERR_CUDA, "tensor-core launch: %s", cudaGetErrorString(e));
+    return SPREG_OK;
+}
+
+}  // namespace spreg

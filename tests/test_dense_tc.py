@@ -1,0 +1,109 @@
+"""Dense row panels on the tensor cores (tcgen05): products against torch FP32 of the same BF16
+operands, and the hybrid split (tensor-core panels + register-tiled panels) against the oracle."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from spreg import _lib, synth
+
+pytestmark = pytest.mark.gpu
+
+FP32_ACC_TOL = 1e-5   # FP32 accumulation of BF16 products, any order
+BF16_OUT_TOL = 1e-2   # output rounded to BF16
+
+
+def _rel(a, b):
+    import torch
+    return float((a.double() - b.double()).norm() / max(float(b.double().norm()), 1e-300))
+
+
+@pytest.mark.parametrize("R,K,n", [(1, 8, 1), (128, 64, 128), (300, 100, 200), (77, 1000, 16), (256, 4096, 96),
+                                   (129, 520, 257)])
+@pytest.mark.parametrize("c_bf16,load_c,relu", [(False, False, False), (False, True, True), (True, False, True)])
+def test_dense_rows_match_torch(cuda, R, K, n, c_bf16, load_c, relu):
+    import torch
+    from spreg.hybrid import dense_rows_bf16
+    g = torch.Generator(device="cuda").manual_seed(R * 7 + K + n)
+    M = R + 37
+    k8 = (K + 7) // 8 * 8
+    a = torch.zeros((R, k8), device="cuda", dtype=torch.bfloat16)
+    a[:, :K] = torch.randn((R, K), device="cuda", generator=g).to(torch.bfloat16)
+    B = torch.randn((K, n), device="cuda", generator=g).to(torch.bfloat16)
+    rows = torch.randperm(M, device="cuda", generator=g)[:R].to(torch.int32)
+    dt = torch.bfloat16 if c_bf16 else torch.float32
+    C0 = torch.randn((M, n), device="cuda", generator=g).to(dt)
+    C = C0.clone()
+    dense_rows_bf16(a, rows, B, C, load_c=load_c, epilogue=1 if relu else 0)
+    want = a[:, :K].float() @ B.float()
+    if load_c:
+        want = want + C0[rows.long()].float()
+    if relu:
+        want = torch.relu(want)
+    got = C[rows.long()].float()
+    assert _rel(got, want) <= (BF16_OUT_TOL if c_bf16 else FP32_ACC_TOL)
+    others = torch.ones(M, dtype=torch.bool, device="cuda")
+    others[rows.long()] = False
+    assert torch.equal(C[others], C0[others])  # rows the product does not own are untouched
+    from spreg.packed import device_status
+    assert device_status() == 0
+
+
+def test_dense_rows_argument_checks(cuda):
+    import torch
+    from spreg.hybrid import dense_rows_bf16
+    a = torch.zeros((4, 12), device="cuda", dtype=torch.bfloat16)  # row stride 24 bytes
+    B = torch.zeros((12, 8), device="cuda", dtype=torch.bfloat16)
+    C = torch.zeros((4, 8), device="cuda")
+    idx = torch.arange(4, device="cuda", dtype=torch.int32)
+    with pytest.raises(_lib.SpregError, match="16-byte aligned"):
+        dense_rows_bf16(a, idx, B, C)
+
+
+def _hybrid_case(tc_fill, load_c, relu, seed=3):
+    import torch
+    from spreg import Mapping
+    from spreg.hybrid import HybridMatrix, panel_fill
+    M, K, n = 260, 384, 72
+    A = synth.row_skew(M, K, 0.9, seed=seed, std=1.0)
+    A[40:48] = synth.bernoulli(8, K, 0.4, seed=seed + 1, std=1.0)    # two dense panels
+    A[200:204] = synth.bernoulli(4, K, 0.1, seed=seed + 2, std=1.0)  # one very dense panel
+    A = synth.round_bf16(A)
+    m = Mapping.identity(4)
+    At = torch.from_numpy(A).cuda()
+    h = HybridMatrix.from_dense(At, m, tc_fill, k_tile=128)
+    B = synth.round_bf16(synth.dense(K, n, seed=seed + 3))
+    Bt = torch.from_numpy(B).cuda().to(torch.bfloat16)
+    C0 = synth.dense(M, n, seed=seed + 4)
+    C = torch.from_numpy(C0).cuda().clone()
+    h.execute(Bt, C, load_c=load_c, epilogue=1 if relu else 0)
+    want = A.astype(np.float64) @ B.astype(np.float64) + (C0 if load_c else 0)
+    if relu:
+        want = np.maximum(want, 0)
+    return h, C.cpu().numpy(), want, A, B, C0
+
+
+@pytest.mark.parametrize("load_c,relu", [(False, False), (True, False), (False, True), (True, True)])
+def test_hybrid_split_matches_fp64(cuda, load_c, relu):
+    h, got, want, A, B, C0 = _hybrid_case(0.3, load_c, relu)
+    assert h.tc_rows == 12  # panels 10, 11 (rows 40..47) and 50 (rows 200..203)
+    assert O.rel_err(got, want) <= FP32_ACC_TOL
+    # the register-tiled rows are bit-identical to the oracle's execution of the sparse part
+    import torch
+    A_sp = A.copy()
+    A_sp[40:48] = 0
+    A_sp[200:204] = 0
+    from spreg import Mapping
+    ref = O.Packed(O.Tables.of(Mapping.identity(4)), A_sp, k_tile=128, value_dtype=_lib.BF16)
+    Bu = torch.from_numpy(B).to(torch.bfloat16).view(torch.int16).numpy().view(np.uint16)
+    Cr = C0.copy() if load_c else np.zeros_like(C0)
+    ref.execute(Bu, Cr, load_c=load_c, epilogue=1 if relu else 0)
+    keep = np.ones(A.shape[0], bool)
+    keep[40:48] = keep[200:204] = False
+    assert np.array_equal(got[keep].view(np.uint32), Cr[keep].view(np.uint32))
+
+
+@pytest.mark.parametrize("fill", [0.0, 1.01])
+def test_hybrid_all_or_no_panels_on_tensor_cores(cuda, fill):
+    h, got, want, *_ = _hybrid_case(fill, True, True)
+    assert h.tc_rows == (260 if fill == 0.0 else 0)
+    assert O.rel_err(got, want) <= FP32_ACC_TOL
