@@ -65,6 +65,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end leg")
     ap.add_argument("--serving", type=int, default=1, help="1: add the serving-loop measurement to the line")
     ap.add_argument("--precision", type=int, default=1, help="1: add the storage-precision sweep to the line")
+    ap.add_argument("--tensor-cores", type=int, default=1, help="1: add the tensor-core (tcgen05) leg to the line")
     ap.add_argument("--layers", type=int, default=1,
                     help="1: add the batched uneven transformer-layer measurement to the line")
     ap.add_argument("--serve-requests", type=int, default=768)
@@ -400,6 +401,49 @@ def layers_suite(dev, steps: int = 50) -> dict:
             "max_rel_diff_batched_vs_plain": err}
 
 
+def tensor_core_suite(dev, reps: int = 20) -> dict:
+    """The tcgen05 dense-rows kernel: a dense BF16 product (4096 x 4096 x 4096, FP32 accumulation)
+    against the measured bf16 peak, and the hybrid threshold of the serving layers (90 % row-skew,
+    BF16) timed on the device."""
+    import torch
+    from spreg import Mapping, synth
+    from spreg.hybrid import dense_rows_bf16, tune_tc_fill
+    M = K = N = 4096
+    g = torch.Generator(device=dev).manual_seed(0)
+    a = torch.randn((M, K), device=dev, generator=g).to(torch.bfloat16)
+    b = torch.randn((K, N), device=dev, generator=g).to(torch.bfloat16)
+    c = torch.empty((M, N), device=dev)
+    idx = torch.arange(M, device=dev, dtype=torch.int32)
+    dense_rows_bf16(a, idx, b, c)  # checks the row indices once
+    for _ in range(3):
+        dense_rows_bf16(a, idx, b, c, check_rows=False)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        dense_rows_bf16(a, idx, b, c, check_rows=False)
+    e1.record()
+    torch.cuda.synchronize()
+    us = e0.elapsed_time(e1) / reps * 1e3
+    ref = a[:256].float() @ b.float()
+    err = float((c[:256] - ref).norm() / ref.norm())
+    tflops = 2.0 * M * N * K / us / 1e6
+    peak = None
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peak = float(json.load(f)["bf16_tflops"])
+    except (OSError, ValueError, KeyError):
+        pass
+    hyb = {}
+    for (m, k, kt, n) in ((4096, 1024, 512, 128), (1024, 4096, 1024, 128)):
+        A = torch.from_numpy(synth.round_bf16(synth.row_skew(m, k, 0.9, seed=3, sigma=0.5, std=0.02))).to(dev)
+        hyb[f"{m}x{k}_n{n}"] = tune_tc_fill(A, Mapping.identity(2), n, k_tile=kt)
+    return {"dense_bf16_4096^3_us": us, "tflops": tflops, "peak_tflops": peak,
+            "frac_of_measured_peak": (tflops / peak) if peak else None,
+            "rel_err_vs_fp32_of_bf16_inputs": err, "includes": "B transpose into K-major + tcgen05 kernel",
+            "hybrid_threshold_serving_layers": hyb}
+
+
 def _stat(st) -> dict:
     return {"req_s": st.req_per_s, "tokens_s": st.tokens_per_s, "p50_ms": st.p50_ms, "p99_ms": st.p99_ms,
             "mean_ms": st.mean_ms, "requests": st.requests}
@@ -613,6 +657,7 @@ def main():
     if args.serving:
         serving = serving_bench(args, dev)
     precision = precision_suite(dev) if args.precision else None
+    tensor_cores = tensor_core_suite(dev) if args.tensor_cores else None
     layers = layers_suite(dev) if args.layers else None
 
     cpu = None
@@ -634,7 +679,7 @@ def main():
                                  f"vs {L2_BYTES / 2**20:.0f} MiB L2",
                            "parallelism": f"replicas x{ws}"},
                 "gflops": gflops, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "serving": serving,
-                "precision": precision, "batched_layers": layers,
+                "precision": precision, "batched_layers": layers, "tensor_cores": tensor_cores,
                 "clocks": clk.summary(), "gpu_launches": launches_per_step * args.steps,
                 "parity_bit_exact_vs_oracle": parity_ok}
         print(json.dumps(line))

@@ -25,9 +25,12 @@ from .packed import PackedMatrix
 
 
 def dense_rows_bf16(a_rows, row_index, B, C, n: Optional[int] = None, load_c: bool = False,
-                    epilogue: int = _lib.EPILOGUE_NONE, stream=None):
+                    epilogue: int = _lib.EPILOGUE_NONE, stream=None, check_rows: bool = True):
     """C[row_index[i], :n] (+)= a_rows[i, :K] . B[:, :n] with K = B's rows, on the tensor cores (CUDA
-    tensors; a_rows (at least K columns) and B BF16, row_index int32 rows of C, C float32 or BF16)."""
+    tensors; a_rows (at least K columns) and B BF16, row_index int32 rows of C, C float32 or BF16).
+
+    check_rows reads the row indices back to check them against C (a device synchronisation);
+    callers whose indices are known to be in range pass False."""
     import torch
     n = B.shape[1] if n is None else int(n)
     k = B.shape[0]
@@ -46,7 +49,7 @@ def dense_rows_bf16(a_rows, row_index, B, C, n: Optional[int] = None, load_c: bo
         raise ValueError("operands need unit column stride")
     if row_index.numel() != a_rows.shape[0]:
         raise ValueError("one row index per A row")
-    if row_index.numel() and (int(row_index.min()) < 0 or int(row_index.max()) >= C.shape[0]):
+    if check_rows and row_index.numel() and (int(row_index.min()) < 0 or int(row_index.max()) >= C.shape[0]):
         raise ValueError("a row index lies outside C")
     cd = _lib.F32 if C.dtype == torch.float32 else _lib.BF16
     _lib.check(_lib.lib().spreg_dense_rows_bf16(
@@ -112,7 +115,9 @@ class HybridMatrix:
         if B.shape[0] < self.cols or C.shape[0] != self.rows or (n or B.shape[1]) > min(B.shape[1], C.shape[1]):
             raise ValueError(f"B needs {self.cols} rows, C {self.rows} rows, both at least n columns")
         kw = dict(n=n, load_c=load_c, epilogue=epilogue, nr=nr, stream=stream)
-        if self.tc_rows and self.cols > 0:
+        if self.tc_rows == self.rows and self.cols > 0:
+            self._tc(B, C, n, load_c, epilogue, stream)  # every row is a tensor-core row
+        elif self.tc_rows and self.cols > 0:
             if load_c:
                 self._tc(B, C, n, True, epilogue, stream)
                 self.packed.execute(B, C, **kw)
