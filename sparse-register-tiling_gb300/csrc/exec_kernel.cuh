@@ -603,9 +603,57 @@ __device__ __forceinline__ void step_dispatch(const int pat, const uint32_t vs, 
 
 // n entries of one group: full steps of 4 entries (one 16-byte broadcast load of column indices,
 // 4 B rows, the pattern's FMA block), then one predicated step for the last n % 4 entries.
-template <int MR, int NV, class TV, class BL>
+// A group of a pattern known at compile time: no per-step dispatch.
+template <int PAT, int MR, int NV, class TV, class BL>
+__device__ __forceinline__ void run_group_pat(const int n, uint32_t cs, uint32_t vs, const BL &bl,
+                                              float (&acc)[MR][NV]) {
+    constexpr uint32_t VSTEP = 4u * (uint32_t)sizeof(TV) * (uint32_t)cpopc(PAT);
+    const int full = n >> 2;
+#pragma unroll 1
+    for (int s = 0; s < full; ++s) {
+        const uint4 k4 = lds_u128(cs);
+        float b[4][NV];
+        bl.load((int)k4.x, b[0]);
+        bl.load((int)k4.y, b[1]);
+        bl.load((int)k4.z, b[2]);
+        bl.load((int)k4.w, b[3]);
+        step_fma<PAT, MR, NV, TV, true>(vs, 4, b, acc);
+        cs += 16u;
+        vs += VSTEP;
+    }
+    const int m = n & 3;
+    if (m) {
+        const uint4 k4 = lds_u128(cs);
+        const int ks[4] = {(int)k4.x, (int)k4.y, (int)k4.z, (int)k4.w};
+        float b[4][NV];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (u < m) bl.load(ks[u], b[u]);
+        step_fma<PAT, MR, NV, TV, false>(vs, m, b, acc);
+    }
+}
+
+// With HOT (the shared-memory B-tile kernel, which has the registers for it), the single rows and the
+// all-rows nanokernel of M_r = 2 and 4 -- the common groups at high sparsity, and the set the
+// histogram-based selection picks -- run their own loop; every other pattern dispatches per step.
+template <int MR, int NV, class TV, bool HOT = false, class BL>
 __device__ __forceinline__ void run_group_x(const int pat, const int n, uint32_t cs, uint32_t vs, const BL &bl,
                                             float (&acc)[MR][NV]) {
+    if constexpr (HOT && (MR == 2 || MR == 4)) {
+        switch (pat) {
+        case 1: run_group_pat<1, MR, NV, TV>(n, cs, vs, bl, acc); return;
+        case 2: run_group_pat<2, MR, NV, TV>(n, cs, vs, bl, acc); return;
+        case (1 << MR) - 1: run_group_pat<(1 << MR) - 1, MR, NV, TV>(n, cs, vs, bl, acc); return;
+        default: break;
+        }
+        if constexpr (MR == 4) {
+            switch (pat) {
+            case 4: run_group_pat<4, MR, NV, TV>(n, cs, vs, bl, acc); return;
+            case 8: run_group_pat<8, MR, NV, TV>(n, cs, vs, bl, acc); return;
+            default: break;
+            }
+        }
+    }
     const uint32_t vstep = 4u * (uint32_t)sizeof(TV) * (uint32_t)__popc(pat);
     const int full = n >> 2;
 #pragma unroll 1

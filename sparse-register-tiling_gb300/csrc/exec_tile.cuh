@@ -32,7 +32,7 @@
 namespace spreg {
 
 constexpr int kTileStages = 2;
-constexpr int kTileMaxWarps = 16;    // consumer warps per CTA
+constexpr int kTileMaxWarps = 15;    // consumer warps per CTA (with the producer: 512 threads, 128 registers each)
 constexpr int kTileMaxProblems = 96; // problems per launch (a tensor map each; kernel parameters <= 32 KB)
 constexpr int kTileBoxRows = 256;    // rows of one tensor copy (TMA box limit)
 
@@ -316,7 +316,7 @@ __global__ void __launch_bounds__(32 * (kTileMaxWarps + 1), 1) exec_tile_kernel(
 #pragma unroll 1
             for (uint32_t g = 0; g < G; ++g) {
                 const uint4 rec = lds_u128(buf + 16u + 16u * g);
-                run_group_x<MR, NV, TV>((int)rec.x, (int)rec.y, buf + rec.z, buf + rec.w, bl, acc);
+                run_group_x<MR, NV, TV, true>((int)rec.x, (int)rec.y, buf + rec.z, buf + rec.w, bl, acc);
             }
             if (t == pr.T - 1) t_store<MR, NV, TV, TC>(pr, gp, row0, col0, valid, acc);
         }
