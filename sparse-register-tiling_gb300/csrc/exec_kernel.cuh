@@ -609,17 +609,47 @@ __device__ __forceinline__ void run_group_pat(const int n, uint32_t cs, uint32_t
                                               float (&acc)[MR][NV]) {
     constexpr uint32_t VSTEP = 4u * (uint32_t)sizeof(TV) * (uint32_t)cpopc(PAT);
     const int full = n >> 2;
+    if constexpr (NV >= 4) {
+        // registers are short for a second B set: prefetch only the next step's column indices
+        uint4 k4 = full > 0 ? lds_u128(cs) : make_uint4(0, 0, 0, 0);
 #pragma unroll 1
-    for (int s = 0; s < full; ++s) {
-        const uint4 k4 = lds_u128(cs);
+        for (int s = 0; s < full; ++s) {
+            float b[4][NV];
+            bl.load((int)k4.x, b[0]);
+            bl.load((int)k4.y, b[1]);
+            bl.load((int)k4.z, b[2]);
+            bl.load((int)k4.w, b[3]);
+            cs += 16u;
+            if (s + 1 < full) k4 = lds_u128(cs);
+            step_fma<PAT, MR, NV, TV, true>(vs, 4, b, acc);
+            vs += VSTEP;
+        }
+    } else if (full > 0) {
+        // software pipeline: the next step's column indices and B rows load before this step's FMAs
+        uint4 k4 = lds_u128(cs);
         float b[4][NV];
         bl.load((int)k4.x, b[0]);
         bl.load((int)k4.y, b[1]);
         bl.load((int)k4.z, b[2]);
         bl.load((int)k4.w, b[3]);
-        step_fma<PAT, MR, NV, TV, true>(vs, 4, b, acc);
-        cs += 16u;
-        vs += VSTEP;
+#pragma unroll 1
+        for (int s = 0; s < full; ++s) {
+            cs += 16u;
+            float bn[4][NV];
+            if (s + 1 < full) {
+                k4 = lds_u128(cs);
+                bl.load((int)k4.x, bn[0]);
+                bl.load((int)k4.y, bn[1]);
+                bl.load((int)k4.z, bn[2]);
+                bl.load((int)k4.w, bn[3]);
+            }
+            step_fma<PAT, MR, NV, TV, true>(vs, 4, b, acc);
+            vs += VSTEP;
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+#pragma unroll
+                for (int j = 0; j < NV; ++j) b[u][j] = bn[u][j];
+        }
     }
     const int m = n & 3;
     if (m) {
