@@ -242,11 +242,21 @@ def serving_bench(args, dev) -> dict:
     rp = reqs_for(fp, n_plain, float("inf"), 2)
     cap_p = serve_per_request(fp, rp)
 
+    # the same requests on tensor-core layers (every panel a dense BF16 tcgen05 product)
+    tcm = SparseMLP(w, "bf16", device=dev, tc=True)
+    server_tc = Server(tcm, budget_bytes=args.serve_budget_mb << 20, max_slots=args.serve_slots)
+    server_tc.run(reqs_for(tcm, 16, float("inf"), 1))
+    rt = reqs_for(tcm, R, float("inf"), 2)
+    cap_t = server_tc.run(rt)
+    rt_lat = server_tc.run(reqs_for(tcm, min(R, max(64, int(2.0 * cap_p.req_per_s * 0.5))), 2.0 * cap_p.req_per_s, 30))
+
     # accuracy of served outputs against the FP64 stack (three small requests)
     pick = [i for i in np.argsort(ns[:n_plain])[:3]]
     err_b = max(float(np.linalg.norm(output_fp32(rb[i]) - (ref := mlp_reference_fp64(w, xs[i])))
                       / np.linalg.norm(ref)) for i in pick)
     err_p = max(float(np.linalg.norm(output_fp32(rp[i]) - (ref := mlp_reference_fp64(w, xs[i])))
+                      / np.linalg.norm(ref)) for i in pick)
+    err_t = max(float(np.linalg.norm(output_fp32(rt[i]) - (ref := mlp_reference_fp64(w, xs[i])))
                       / np.linalg.norm(ref)) for i in pick)
 
     # latency under Poisson arrivals at rates relative to the per-request path's capacity
@@ -270,6 +280,10 @@ def serving_bench(args, dev) -> dict:
                                   "tune_seconds": t_tune,
                                   "measured_ns_per_spmm": {"up": tuned[0].measured_ns, "down": tuned[1].measured_ns}},
             "req_s_ratio": cap_b.req_per_s / cap_p.req_per_s,
+            "batched_bf16_tensor_cores": _stat(cap_t) | {
+                "req_s_ratio_vs_per_request_fp32": cap_t.req_per_s / cap_p.req_per_s,
+                "rel_err_vs_fp64": err_t, "poisson_at_2x_per_request_capacity": _stat(rt_lat),
+                "note": "every layer as a dense BF16 tcgen05 product: the hybrid split with panel-fill threshold 0"},
             "rel_err_vs_fp64": {"batched_bf16": err_b, "per_request_fp32": err_p, "bf16_tolerance": 1e-2},
             "sweep": sweep,
             "capacity_note": "capacity = all requests queued at t=0; latency = arrival to output in host memory"}

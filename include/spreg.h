@@ -245,6 +245,22 @@ int spreg_dense_rows_bf16(const void *a_rows, int64_t rows, int64_t k, int64_t l
                           const void *b, int64_t ldb, void *c, int64_t ldc, int64_t n, int32_t c_dtype,
                           int32_t load_c, int32_t epilogue, spreg_stream_t stream);
 
+/* One product of spreg_dense_rows_bf16, for the batched call. */
+typedef struct {
+    const void *a_rows;
+    int64_t rows, k, lda;
+    const int32_t *row_index;
+    const void *b;
+    int64_t ldb;
+    void *c;
+    int64_t ldc, n;
+    int32_t c_dtype, load_c, epilogue, reserved;
+} spreg_dense_rows_item;
+
+/* Many dense-rows products (any shapes) in as few launches as possible: the output tiles of up to
+ * 80 products share one launch.  Same arguments and results as spreg_dense_rows_bf16 per item. */
+int spreg_dense_rows_bf16_batched(const spreg_dense_rows_item *items, int32_t num_items, spreg_stream_t stream);
+
 /* Status word of the current device: nonzero once a kernel gave up a bounded wait (its results
  * are then incomplete).  Synchronous; reset != 0 clears it. */
 int spreg_device_status(int32_t *status_host, int32_t reset);

@@ -17,6 +17,7 @@ void clear_error() { g_last_error.clear(); }
 // Implemented in pack.cu / exec.cu.
 int dense_rows_bf16_impl(const void *, int64_t, int64_t, int64_t, const int32_t *, const void *, int64_t, void *,
                          int64_t, int64_t, int32_t, int32_t, int32_t, cudaStream_t);
+int dense_rows_batched_impl(const spreg_dense_rows_item *, int32_t, cudaStream_t);
 int pack_from_arena_impl(const spreg_mapping *, const spreg_arena_geom *, const void *, int64_t,
                          const spreg_panel_desc *, int64_t, const float *, int64_t, spreg_packed **, cudaStream_t);
 int pack_dense_impl(const spreg_mapping *, const float *, int64_t, int64_t, int64_t, const spreg_pack_opts *,
@@ -222,6 +223,11 @@ int spreg_dense_rows_bf16(const void *a_rows, int64_t rows, int64_t k, int64_t l
     clear_error();
     return dense_rows_bf16_impl(a_rows, rows, k, lda, row_index, b, ldb, c, ldc, n, c_dtype, load_c, epilogue,
                                 (cudaStream_t)stream);
+}
+
+int spreg_dense_rows_bf16_batched(const spreg_dense_rows_item *items, int32_t num_items, spreg_stream_t stream) {
+    clear_error();
+    return dense_rows_batched_impl(items, num_items, (cudaStream_t)stream);
 }
 
 void spreg_packed_destroy(spreg_packed *p) { packed_release(p); }

@@ -5,7 +5,10 @@
 // are dense enough that a BF16 tensor-core product beats the register-tiled executors.  BF16 operands,
 // FP32 accumulation in tensor memory (TMEM), FP32 or BF16 output with load_c and the ReLU epilogue.
 //
-// One CTA computes a 128 x 128 output tile with 4 warps:
+// One launch runs up to 80 such products ("problems", a tensor map pair each in the kernel
+// parameters); its CTAs are the output tiles of all of them, and each CTA finds its problem by a
+// binary search over the problems' first tiles.  One CTA computes a 128 x 128 output tile with 4
+// warps:
 //   * B is first transposed into a K-contiguous BF16 buffer Bt (n x K8, K8 = K rounded up to 8), so
 //     both MMA operands are K-major;
 //   * lane 0 of warp 0 loads 128 x 64 tiles of A_rows and Bt with 2-D tensor copies (TMA, 128-byte
@@ -23,6 +26,10 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
 namespace spreg {
 
 int *device_status_word(int *st);  // exec.cu
@@ -36,16 +43,24 @@ constexpr uint32_t TC_STAGE = TC_TILE_A + TC_TILE_B;
 constexpr uint32_t TC_TMEM_COLS = 128;
 constexpr size_t TC_SMEM = 1024 /* alignment slack */ + TC_STAGES * TC_STAGE + 256 /* barriers, TMEM slot */;
 
-struct TcParams {
+constexpr int TC_MAX_PROBLEMS = 80;  // problems per launch (two tensor maps each; parameters <= 32 KB)
+
+struct TcProblem {
     CUtensorMap a_map;           // A_rows: columns [0, K) x rows [0, R), box 64 x 128, 128-byte swizzle
     CUtensorMap b_map;           // Bt: columns [0, K) x rows [0, n), box 64 x 128, 128-byte swizzle
     const int32_t *row_index;    // output row of each A row
     void *C;
     int64_t ldc;
     int32_t R, n, kblocks, c_dtype;
-    int32_t load_c, epilogue, pad0, pad1;
-    int *status;
+    int32_t load_c, epilogue, tile_begin, tiles_n;  // first output tile of the launch, tiles along n
 };
+
+struct TcParams {
+    int *status;
+    int32_t nprob, pad0;
+    TcProblem prob[TC_MAX_PROBLEMS];
+};
+static_assert(sizeof(TcParams) <= 32764, "kernel parameters are limited to 32764 bytes");
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -140,18 +155,27 @@ __global__ void __launch_bounds__(128, 1) tc_rows_kernel(const __grid_constant__
     uint32_t tmem;
     asm volatile("ld.shared.b32 %0, [%1];" : "=r"(tmem) : "r"(tmem_slot) : "memory");
 
-    const int m0 = blockIdx.x * TC_BM, n0 = blockIdx.y * TC_BN;
+    // this CTA's problem and output tile
+    int lo = 0, hi = p.nprob - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (p.prob[mid].tile_begin <= (int)blockIdx.x) lo = mid;
+        else hi = mid - 1;
+    }
+    const TcProblem &q = p.prob[lo];
+    const int local = (int)blockIdx.x - q.tile_begin;
+    const int m0 = (local / q.tiles_n) * TC_BM, n0 = (local % q.tiles_n) * TC_BN;
     if (warp == 0 && lane == 0) {
         // producer: A and Bt tiles of each K block
         int issued = 0;
-        for (int kb = 0; kb < p.kblocks; ++kb) {
+        for (int kb = 0; kb < q.kblocks; ++kb) {
             const int s = kb % TC_STAGES;
             if (kb >= TC_STAGES && !tc_wait(empty0 + 8u * s, (uint32_t)(((kb / TC_STAGES) - 1) & 1), p.status, 21))
                 break;
             const uint32_t st = sbase + (uint32_t)s * TC_STAGE;
             tc_expect_tx(full0 + 8u * s, TC_STAGE);
-            tc_tma_2d(st, &p.a_map, kb * TC_BK, m0, full0 + 8u * s);
-            tc_tma_2d(st + TC_TILE_A, &p.b_map, kb * TC_BK, n0, full0 + 8u * s);
+            tc_tma_2d(st, &q.a_map, kb * TC_BK, m0, full0 + 8u * s);
+            tc_tma_2d(st + TC_TILE_A, &q.b_map, kb * TC_BK, n0, full0 + 8u * s);
             issued = kb + 1;
         }
         // before the CTA can finish, every copy issued has landed
@@ -160,7 +184,7 @@ __global__ void __launch_bounds__(128, 1) tc_rows_kernel(const __grid_constant__
     } else if (warp == 1 && lane == 0) {
         // MMA issuer
         constexpr uint32_t idesc = tc_idesc(TC_BM, TC_BN);
-        for (int kb = 0; kb < p.kblocks; ++kb) {
+        for (int kb = 0; kb < q.kblocks; ++kb) {
             const int s = kb % TC_STAGES;
             if (!tc_wait(full0 + 8u * s, (uint32_t)((kb / TC_STAGES) & 1), p.status, 23)) break;
             tc_fence_after();
@@ -178,8 +202,8 @@ __global__ void __launch_bounds__(128, 1) tc_rows_kernel(const __grid_constant__
 
     // epilogue: warp w reads TMEM lanes (rows) 32w .. 32w + 31
     const int r = m0 + 32 * warp + lane;
-    const bool row_ok = ok && r < p.R;
-    const int64_t orow = row_ok ? p.row_index[r] : 0;
+    const bool row_ok = ok && r < q.R;
+    const int64_t orow = row_ok ? q.row_index[r] : 0;
     if (ok) {
         for (int c = 0; c < TC_BN; c += 16) {
             float v[16];
@@ -188,17 +212,17 @@ __global__ void __launch_bounds__(128, 1) tc_rows_kernel(const __grid_constant__
 #pragma unroll
             for (int j = 0; j < 16; ++j) {
                 const int col = n0 + c + j;
-                if (col >= p.n) break;
+                if (col >= q.n) break;
                 float o = v[j];
-                if (p.c_dtype == SPREG_F32) {
-                    float *cp = reinterpret_cast<float *>(p.C) + orow * p.ldc + col;
-                    if (p.load_c) o += *cp;
-                    if (p.epilogue == SPREG_EPILOGUE_RELU) o = fmaxf(o, 0.0f);
+                if (q.c_dtype == SPREG_F32) {
+                    float *cp = reinterpret_cast<float *>(q.C) + orow * q.ldc + col;
+                    if (q.load_c) o += *cp;
+                    if (q.epilogue == SPREG_EPILOGUE_RELU) o = fmaxf(o, 0.0f);
                     *cp = o;
                 } else {
-                    __nv_bfloat16 *cp = reinterpret_cast<__nv_bfloat16 *>(p.C) + orow * p.ldc + col;
-                    if (p.load_c) o += __bfloat162float(*cp);
-                    if (p.epilogue == SPREG_EPILOGUE_RELU) o = fmaxf(o, 0.0f);
+                    __nv_bfloat16 *cp = reinterpret_cast<__nv_bfloat16 *>(q.C) + orow * q.ldc + col;
+                    if (q.load_c) o += __bfloat162float(*cp);
+                    if (q.epilogue == SPREG_EPILOGUE_RELU) o = fmaxf(o, 0.0f);
                     *cp = __float2bfloat16_rn(o);
                 }
             }
@@ -258,36 +282,35 @@ int tc_map(CUtensorMap *map, const void *base, int64_t cols, int64_t rows, int64
 
 }  // namespace
 
-int dense_rows_bf16_impl(const void *a_rows, int64_t R, int64_t K, int64_t lda, const int32_t *row_index,
-                         const void *b, int64_t ldb, void *c, int64_t ldc, int64_t n, int32_t c_dtype, int32_t load_c,
-                         int32_t epilogue, cudaStream_t stream) {
-    SPREG_CHECK_ARG(R >= 0 && K >= 0 && n >= 0, "negative size");
-    if (R == 0 || n == 0) return SPREG_OK;
-    SPREG_CHECK_ARG(a_rows && row_index && c && (b || K == 0), "null pointer");
-    SPREG_CHECK_ARG(R <= INT32_MAX && K <= INT32_MAX && n <= INT32_MAX, "size out of range");
-    SPREG_CHECK_ARG(c_dtype == SPREG_F32 || c_dtype == SPREG_BF16, "C must be F32 or BF16");
-    SPREG_CHECK_ARG(epilogue == SPREG_EPILOGUE_NONE || epilogue == SPREG_EPILOGUE_RELU, "bad epilogue");
-    SPREG_CHECK_ARG(lda >= K && (lda * 2) % 16 == 0 && reinterpret_cast<uintptr_t>(a_rows) % 16 == 0,
-                    "A rows must be 16-byte aligned with a row stride of a multiple of 8 elements (lda %lld)",
-                    (long long)lda);
-    SPREG_CHECK_ARG(ldb >= n && ldc >= n, "ldb / ldc smaller than n");
-    SPREG_CHECK_ARG(K > 0, "K must be positive");
-    SPREG_CHECK_ARG((n + TC_BN - 1) / TC_BN <= 65535, "n too large for one launch");
+int dense_rows_batched_impl(const spreg_dense_rows_item *items, int32_t count, cudaStream_t stream) {
+    SPREG_CHECK_ARG(count >= 0 && (count == 0 || items), "bad item list");
     int st = SPREG_OK;
+    // checks, and the transposed-B scratch of every item (one allocation)
+    std::vector<int32_t> live;
+    std::vector<int64_t> bt_off((size_t)count, 0);
+    int64_t bt_bytes = 0;
+    for (int32_t i = 0; i < count; ++i) {
+        const spreg_dense_rows_item &it = items[i];
+        SPREG_CHECK_ARG(it.rows >= 0 && it.k >= 0 && it.n >= 0, "item %d: negative size", i);
+        if (it.rows == 0 || it.n == 0) continue;
+        SPREG_CHECK_ARG(it.a_rows && it.row_index && it.c && it.b, "item %d: null pointer", i);
+        SPREG_CHECK_ARG(it.rows <= INT32_MAX && it.k <= INT32_MAX && it.n <= INT32_MAX, "item %d: size out of range", i);
+        SPREG_CHECK_ARG(it.c_dtype == SPREG_F32 || it.c_dtype == SPREG_BF16, "item %d: C must be F32 or BF16", i);
+        SPREG_CHECK_ARG(it.epilogue == SPREG_EPILOGUE_NONE || it.epilogue == SPREG_EPILOGUE_RELU, "item %d: bad epilogue",
+                        i);
+        SPREG_CHECK_ARG(it.lda >= it.k && (it.lda * 2) % 16 == 0 && reinterpret_cast<uintptr_t>(it.a_rows) % 16 == 0,
+                        "A rows must be 16-byte aligned with a row stride of a multiple of 8 elements (item %d, lda "
+                        "%lld)", i, (long long)it.lda);
+        SPREG_CHECK_ARG(it.ldb >= it.n && it.ldc >= it.n, "item %d: ldb / ldc smaller than n", i);
+        SPREG_CHECK_ARG(it.k > 0, "item %d: K must be positive", i);
+        const int64_t K8 = (it.k + 7) / 8 * 8;
+        bt_off[(size_t)i] = bt_bytes;
+        bt_bytes += (it.n * K8 * 2 + 255) / 256 * 256;
+        live.push_back(i);
+    }
+    if (live.empty()) return SPREG_OK;
     int *status = device_status_word(&st);
     if (st != SPREG_OK) return st;
-    const int64_t K8 = (K + 7) / 8 * 8;
-    TcParams p = {};
-    p.row_index = row_index;
-    p.C = c;
-    p.ldc = ldc;
-    p.R = (int32_t)R;
-    p.n = (int32_t)n;
-    p.kblocks = (int32_t)((K + TC_BK - 1) / TC_BK);
-    p.c_dtype = c_dtype;
-    p.load_c = load_c ? 1 : 0;
-    p.epilogue = epilogue;
-    p.status = status;
     static bool configured[64] = {};
     int dev = 0;
     SPREG_CUDA(cudaGetDevice(&dev));
@@ -295,25 +318,71 @@ int dense_rows_bf16_impl(const void *a_rows, int64_t R, int64_t K, int64_t lda, 
         SPREG_CUDA(cudaFuncSetAttribute(tc_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM));
         configured[dev] = true;
     }
-    void *bt = nullptr;
-    SPREG_CUDA(cudaMallocAsync(&bt, (size_t)(n * K8 * 2), stream));
-    transpose_b_kernel<<<dim3((unsigned)((K8 + 31) / 32), (unsigned)((n + 31) / 32)), dim3(32, 8), 0, stream>>>(
-        static_cast<const __nv_bfloat16 *>(b), ldb, (int)K, (int)n, (int)K8, static_cast<__nv_bfloat16 *>(bt));
-    cudaError_t te = cudaGetLastError();
-    if (te != cudaSuccess) {
+    char *bt = nullptr;
+    SPREG_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&bt), (size_t)bt_bytes, stream));
+    auto fail = [&](int code) {
         cudaFreeAsync(bt, stream);
-        SPREG_FAIL(SPREG_ERR_CUDA, "transpose launch: %s", cudaGetErrorString(te));
+        return code;
+    };
+    for (int32_t i : live) {
+        const spreg_dense_rows_item &it = items[i];
+        const int64_t K8 = (it.k + 7) / 8 * 8;
+        transpose_b_kernel<<<dim3((unsigned)((K8 + 31) / 32), (unsigned)((it.n + 31) / 32)), dim3(32, 8), 0, stream>>>(
+            static_cast<const __nv_bfloat16 *>(it.b), it.ldb, (int)it.k, (int)it.n, (int)K8,
+            reinterpret_cast<__nv_bfloat16 *>(bt + bt_off[(size_t)i]));
     }
-    if ((st = tc_map(&p.a_map, a_rows, K, R, lda)) || (st = tc_map(&p.b_map, bt, K, n, K8))) {
-        cudaFreeAsync(bt, stream);
-        return st;
-    }
-    tc_rows_kernel<<<dim3((unsigned)((R + TC_BM - 1) / TC_BM), (unsigned)((n + TC_BN - 1) / TC_BN)), 128, TC_SMEM,
-                     stream>>>(p);
     cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        fail(0);
+        SPREG_FAIL(SPREG_ERR_CUDA, "transpose launch: %s", cudaGetErrorString(e));
+    }
+    static thread_local TcParams p;  // ~31 KB: kept off the stack
+    for (size_t first = 0; first < live.size(); first += TC_MAX_PROBLEMS) {
+        const size_t cnt = std::min<size_t>(TC_MAX_PROBLEMS, live.size() - first);
+        memset(&p, 0, sizeof p);
+        p.status = status;
+        p.nprob = (int32_t)cnt;
+        int64_t tiles = 0;
+        for (size_t j = 0; j < cnt; ++j) {
+            const spreg_dense_rows_item &it = items[live[first + j]];
+            TcProblem &q = p.prob[j];
+            const int64_t K8 = (it.k + 7) / 8 * 8;
+            q.row_index = it.row_index;
+            q.C = it.c;
+            q.ldc = it.ldc;
+            q.R = (int32_t)it.rows;
+            q.n = (int32_t)it.n;
+            q.kblocks = (int32_t)((it.k + TC_BK - 1) / TC_BK);
+            q.c_dtype = it.c_dtype;
+            q.load_c = it.load_c ? 1 : 0;
+            q.epilogue = it.epilogue;
+            q.tiles_n = (int32_t)((it.n + TC_BN - 1) / TC_BN);
+            q.tile_begin = (int32_t)tiles;
+            tiles += ((it.rows + TC_BM - 1) / TC_BM) * q.tiles_n;
+            if ((st = tc_map(&q.a_map, it.a_rows, it.k, it.rows, it.lda)) ||
+                (st = tc_map(&q.b_map, bt + bt_off[(size_t)live[first + j]], it.k, it.n, K8)))
+                return fail(st);
+        }
+        if (tiles > INT32_MAX) {
+            fail(0);
+            SPREG_FAIL(SPREG_ERR_UNSUPPORTED, "too many output tiles in one launch");
+        }
+        tc_rows_kernel<<<(unsigned)tiles, 128, TC_SMEM, stream>>>(p);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) {
+            fail(0);
+            SPREG_FAIL(SPREG_ERR_CUDA, "tensor-core launch: %s", cudaGetErrorString(e));
+        }
+    }
     cudaFreeAsync(bt, stream);
-    if (e != cudaSuccess) SPREG_FAIL(SPREG_ERR_CUDA, "tensor-core launch: %s", cudaGetErrorString(e));
     return SPREG_OK;
+}
+
+int dense_rows_bf16_impl(const void *a_rows, int64_t R, int64_t K, int64_t lda, const int32_t *row_index,
+                         const void *b, int64_t ldb, void *c, int64_t ldc, int64_t n, int32_t c_dtype, int32_t load_c,
+                         int32_t epilogue, cudaStream_t stream) {
+    const spreg_dense_rows_item it = {a_rows, R, K, lda, row_index, b, ldb, c, ldc, n, c_dtype, load_c, epilogue, 0};
+    return dense_rows_batched_impl(&it, 1, stream);
 }
 
 }  // namespace spreg

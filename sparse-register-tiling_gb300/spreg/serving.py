@@ -47,6 +47,13 @@ WORK_ITEM_DTYPE = np.dtype([
     ("warps_per_cta", np.int32), ("b_staging", np.int32), ("meta_staging", np.int32)])
 assert WORK_ITEM_DTYPE.itemsize == C.sizeof(_lib.WorkItem)
 
+# numpy view of spreg_dense_rows_item (include/spreg.h): one tensor-core product
+TC_ITEM_DTYPE = np.dtype([
+    ("a_rows", np.uint64), ("rows", np.int64), ("k", np.int64), ("lda", np.int64), ("row_index", np.uint64),
+    ("b", np.uint64), ("ldb", np.int64), ("c", np.uint64), ("ldc", np.int64), ("n", np.int64),
+    ("c_dtype", np.int32), ("load_c", np.int32), ("epilogue", np.int32), ("reserved", np.int32)])
+assert TC_ITEM_DTYPE.itemsize == 96
+
 
 def _handle_int(h) -> int:
     return int(h.value if hasattr(h, "value") else h)
@@ -225,10 +232,14 @@ class SparseMLP:
 
     ``configs`` (one dict per layer, keys ``mr``, ``mapping``, ``k_tile``; see `tune_mlp`) packs each
     layer with its own panel height, nanokernel set and K tile; by default every layer uses
-    ``mapping`` (M_r = 4 identity) untiled."""
+    ``mapping`` (M_r = 4 identity) untiled.
+
+    ``tc=True`` (BF16 only) keeps every layer as dense BF16 rows for the tensor cores -- the hybrid
+    split with a panel-fill threshold of 0, which `spreg.hybrid.tune_tc_fill` picks for these layer
+    shapes from N = 128 up -- and runs them with ``spreg_dense_rows_bf16(_batched)``."""
 
     def __init__(self, weights, dtype: str = "bf16", mapping: Optional[Mapping] = None, device=None,
-                 configs: Optional[Sequence[dict]] = None):
+                 configs: Optional[Sequence[dict]] = None, tc: bool = False):
         import torch
         from .packed import PackedMatrix
         if dtype not in ("bf16", "f32"):
@@ -243,12 +254,23 @@ class SparseMLP:
         if configs is not None and len(configs) != 2 * len(weights):
             raise ValueError(f"configs needs one entry per layer ({2 * len(weights)}), got {len(configs)}")
         self.configs = list(configs) if configs is not None else None
+        self.tc = bool(tc)
+        if self.tc and dtype != "bf16":
+            raise ValueError("tensor-core layers take BF16 operands")
         self.layers = []
+        self.tc_rows = []   # per layer: (dense BF16 rows M x K8, row index 0 .. M - 1)
         for b, (wu, wd) in enumerate(weights):
             if wu.shape != (self.d_ff, self.d_model) or wd.shape != (self.d_model, self.d_ff):
                 raise ValueError("every block needs W_up d_ff x d_model and W_down d_model x d_ff")
             for j, w in enumerate((wu, wd)):
                 t = torch.from_numpy(np.ascontiguousarray(w, dtype=np.float32)).to(self.device)
+                if self.tc:
+                    M, K = w.shape
+                    a = torch.zeros((M, round_up(K, 8)), dtype=torch.bfloat16, device=self.device)
+                    a[:, :K] = t.to(torch.bfloat16)
+                    self.tc_rows.append((a, torch.arange(M, dtype=torch.int32, device=self.device)))
+                    del t
+                    continue
                 mp, kt = self.mapping, 0
                 if self.configs is not None:
                     from .autotune import mapping_of
@@ -273,8 +295,25 @@ class SparseMLP:
         return self.x_bytes(n) + round_up(self.d_ff * self.ld(n) * self.elem, ARENA_ALIGN)
 
     def work_items(self, x_ptr: int, h_ptr: int, n: int) -> np.ndarray:
-        """The request's SpMMs, one per layer, as spreg_work_item records."""
+        """The request's SpMMs, one per layer, as spreg_work_item records (spreg_dense_rows_item
+        records for tensor-core layers)."""
         ld = self.ld(n)
+        if self.tc:
+            it = np.zeros(self.num_layers, dtype=TC_ITEM_DTYPE)
+            for l, (a, idx) in enumerate(self.tc_rows):
+                up = l % 2 == 0
+                it[l]["a_rows"] = a.data_ptr()
+                it[l]["rows"] = a.shape[0]
+                it[l]["k"] = self.d_model if up else self.d_ff
+                it[l]["lda"] = a.stride(0)
+                it[l]["row_index"] = idx.data_ptr()
+                it[l]["b"], it[l]["c"] = (x_ptr, h_ptr) if up else (h_ptr, x_ptr)
+                it[l]["ldb"] = it[l]["ldc"] = ld
+                it[l]["n"] = n
+                it[l]["c_dtype"] = _lib.BF16
+                it[l]["load_c"] = 0 if up else 1
+                it[l]["epilogue"] = _lib.EPILOGUE_RELU if up else _lib.EPILOGUE_NONE
+            return it
         it = np.zeros(self.num_layers, dtype=WORK_ITEM_DTYPE)
         for l, pm in enumerate(self.layers):
             up = l % 2 == 0
@@ -291,6 +330,14 @@ class SparseMLP:
     def forward(self, x_dev, h_dev, n: Optional[int] = None, stream=None):
         """One request through the stack in place on x_dev (d_model x n), h_dev (d_ff x n) as
         scratch: two spreg_execute launches per block."""
+        if self.tc:
+            from .hybrid import dense_rows_bf16
+            for b in range(self.blocks):
+                (au, iu), (ad, idd) = self.tc_rows[2 * b], self.tc_rows[2 * b + 1]
+                dense_rows_bf16(au, iu, x_dev, h_dev, n=n, epilogue=_lib.EPILOGUE_RELU, stream=stream,
+                                check_rows=False)
+                dense_rows_bf16(ad, idd, h_dev, x_dev, n=n, load_c=True, stream=stream, check_rows=False)
+            return x_dev
         for b in range(self.blocks):
             up, down = self.layers[2 * b], self.layers[2 * b + 1]
             up.execute(x_dev, h_dev, n=n, epilogue=_lib.EPILOGUE_RELU, stream=stream)
@@ -361,7 +408,8 @@ class Server:
         self.base = self.arena_t.data_ptr()
         self.compute = torch.cuda.Stream(model.device)
         self.copy = torch.cuda.Stream(model.device)
-        self._buf = np.zeros(max(self.max_slots, 1), dtype=WORK_ITEM_DTYPE)
+        self._dtype = TC_ITEM_DTYPE if model.tc else WORK_ITEM_DTYPE
+        self._buf = np.zeros(max(self.max_slots, 1), dtype=self._dtype)
         self._lib = _lib.lib()
 
     def _x_view(self, r: Request):
@@ -413,14 +461,15 @@ class Server:
             if sched.active:
                 batch = sched.next_iteration()
                 if len(batch) > self._buf.shape[0]:
-                    self._buf = np.zeros(len(batch), dtype=WORK_ITEM_DTYPE)
+                    self._buf = np.zeros(len(batch), dtype=self._dtype)
                 buf = self._buf
                 for i, r in enumerate(batch):
                     if r._ready is not None:
                         self.compute.wait_event(r._ready)
                         r._ready = None
                     buf[i] = r._items[r.layer - 1]
-                _lib.check(self._lib.spreg_execute_batched(buf.ctypes.data, len(batch), self.compute.cuda_stream))
+                run = self._lib.spreg_dense_rows_bf16_batched if m.tc else self._lib.spreg_execute_batched
+                _lib.check(run(buf.ctypes.data, len(batch), self.compute.cuda_stream))
                 ev = torch.cuda.Event()
                 ev.record(self.compute)
                 inflight.append(ev)

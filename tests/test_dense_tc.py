@@ -107,3 +107,31 @@ def test_hybrid_all_or_no_panels_on_tensor_cores(cuda, fill):
     h, got, want, *_ = _hybrid_case(fill, True, True)
     assert h.tc_rows == (260 if fill == 0.0 else 0)
     assert O.rel_err(got, want) <= FP32_ACC_TOL
+
+
+def test_batched_products_equal_single_calls(cuda):
+    """Products of many shapes in one batched call are bit-identical to one call each."""
+    import torch
+    from spreg.hybrid import dense_rows_bf16
+    from spreg.serving import TC_ITEM_DTYPE
+    g = torch.Generator(device="cuda").manual_seed(5)
+    cases = [(128, 64, 128), (7, 300, 33), (300, 1000, 200), (1, 8, 1), (256, 520, 129)] * 20  # 100 items
+    ops, items = [], np.zeros(len(cases), dtype=TC_ITEM_DTYPE)
+    for i, (R, K, n) in enumerate(cases):
+        k8 = (K + 7) // 8 * 8
+        a = torch.zeros((R, k8), device="cuda", dtype=torch.bfloat16)
+        a[:, :K] = torch.randn((R, K), device="cuda", generator=g).to(torch.bfloat16)
+        B = torch.randn((K, n), device="cuda", generator=g).to(torch.bfloat16)
+        idx = torch.randperm(R + 5, device="cuda", generator=g)[:R].to(torch.int32)
+        C1 = torch.randn((R + 5, n), device="cuda", generator=g)
+        C2 = C1.clone()
+        load_c, epi = i % 2, (i // 2) % 2
+        dense_rows_bf16(a, idx, B, C1, load_c=bool(load_c), epilogue=epi)
+        items[i] = (a.data_ptr(), R, K, a.stride(0), idx.data_ptr(), B.data_ptr(), B.stride(0), C2.data_ptr(),
+                    C2.stride(0), n, _lib.F32, load_c, epi, 0)
+        ops.append((a, idx, B, C1, C2))
+    _lib.check(_lib.lib().spreg_dense_rows_bf16_batched(items.ctypes.data, len(cases),
+                                                       _lib.stream_handle(torch.cuda.current_stream())))
+    torch.cuda.synchronize()
+    for a, idx, B, C1, C2 in ops:
+        assert torch.equal(C1.view(torch.int32), C2.view(torch.int32))

@@ -257,3 +257,28 @@ def test_serving_tiled_mixed_configs(cuda):
         Server(model, budget_bytes=8 << 20, max_slots=1).run([alone], realtime=False)
         np.testing.assert_array_equal(output_fp32(alone), output_fp32(r))
         assert rel_err(output_fp32(r), mlp_reference_fp64(w, r.x)) <= BF16_TOL
+
+
+@pytest.mark.gpu
+def test_serving_tensor_core_layers(cuda):
+    """Tensor-core layers (every panel dense BF16 on tcgen05): alone == mix bit for bit, the FP64
+    tolerance, and the per-request path gives the same outputs."""
+    from spreg.serving import Server, SparseMLP, output_fp32, prepare_requests, serve_per_request
+    w = mlp_weights(128, 512, 2, 0.9, seed=13)
+    model = SparseMLP(w, "bf16", tc=True)
+    g = np.random.default_rng(4)
+    ns = [3, 64, 130, 1, 257]
+    reqs = [Request(i, n, x=synth.round_bf16(g.standard_normal((128, n)).astype(np.float32)), arrival=float(i % 3))
+            for i, n in enumerate(ns)]
+    prepare_requests(model, reqs)
+    Server(model, budget_bytes=32 << 20, max_slots=8).run(reqs, realtime=False)
+    mix = [output_fp32(r).copy() for r in reqs]
+    for r, out in zip(reqs, mix):
+        assert rel_err(out, mlp_reference_fp64(w, r.x)) <= BF16_TOL
+        alone = Request(50 + r.rid, r.n, x=r.x)
+        prepare_requests(model, [alone])
+        Server(model, budget_bytes=8 << 20, max_slots=1).run([alone], realtime=False)
+        np.testing.assert_array_equal(output_fp32(alone), out)
+    serve_per_request(model, reqs, realtime=False)
+    for r, out in zip(reqs, mix):
+        np.testing.assert_array_equal(output_fp32(r), out)
