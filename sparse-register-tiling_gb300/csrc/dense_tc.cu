@@ -7,8 +7,8 @@
 //
 // One launch runs up to 80 such products ("problems", a tensor map pair each in the kernel
 // parameters); its CTAs are the output tiles of all of them, and each CTA finds its problem by a
-// binary search over the problems' first tiles.  One CTA computes a 128 x 128 output tile with 4
-// warps:
+// binary search over the problems' first tiles.  One CTA computes a 128 x BN output tile (BN 256 when
+// every product of the launch has more than 128 columns, else 128) with 4 warps:
 //   * B is first transposed into a K-contiguous BF16 buffer Bt (n x K8, K8 = K rounded up to 8), so
 //     both MMA operands are K-major;
 //   * lane 0 of warp 0 loads 128 x 64 tiles of A_rows and Bt with 2-D tensor copies (TMA, 128-byte
@@ -36,12 +36,14 @@ int *device_status_word(int *st);  // exec.cu
 
 namespace {
 
-constexpr int TC_BM = 128, TC_BN = 128, TC_BK = 64, TC_STAGES = 4;
+constexpr int TC_BM = 128, TC_BK = 64, TC_STAGES = 4;
 constexpr uint32_t TC_TILE_A = TC_BM * TC_BK * 2;  // 16 KB
-constexpr uint32_t TC_TILE_B = TC_BN * TC_BK * 2;  // 16 KB
-constexpr uint32_t TC_STAGE = TC_TILE_A + TC_TILE_B;
-constexpr uint32_t TC_TMEM_COLS = 128;
-constexpr size_t TC_SMEM = 1024 /* alignment slack */ + TC_STAGES * TC_STAGE + 256 /* barriers, TMEM slot */;
+// Output tile width BN (128 or 256): the MMA's N, the TMEM accumulator's columns, B tile rows.
+template <int BN> constexpr uint32_t tc_tile_b() { return (uint32_t)BN * TC_BK * 2; }
+template <int BN> constexpr uint32_t tc_stage() { return TC_TILE_A + tc_tile_b<BN>(); }
+template <int BN> constexpr size_t tc_smem() {
+    return 1024 /* alignment slack */ + TC_STAGES * tc_stage<BN>() + 256 /* barriers, TMEM slot */;
+}
 
 constexpr int TC_MAX_PROBLEMS = 80;  // problems per launch (two tensor maps each; parameters <= 32 KB)
 
@@ -128,7 +130,10 @@ __device__ __forceinline__ void tc_ld16(uint32_t taddr, float (&v)[16]) {
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+template <int BN>
 __global__ void __launch_bounds__(128, 1) tc_rows_kernel(const __grid_constant__ TcParams p) {
+    constexpr uint32_t TC_TILE_B = tc_tile_b<BN>(), TC_STAGE = tc_stage<BN>(), TC_TMEM_COLS = BN;
+    constexpr int TC_BN = BN;
     extern __shared__ unsigned char smem_raw[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t raw = smem_u32(smem_raw);
@@ -264,13 +269,13 @@ PFN_cuTensorMapEncodeTiled_v12000 tc_encoder() {
     return fn;
 }
 
-// BF16 matrix of `rows` x `cols` (row stride ld elements) as 64 x 128 boxes with the 128-byte swizzle.
-int tc_map(CUtensorMap *map, const void *base, int64_t cols, int64_t rows, int64_t ld) {
+// BF16 matrix of `rows` x `cols` (row stride ld elements) as 64 x box_rows boxes with the 128-byte swizzle.
+int tc_map(CUtensorMap *map, const void *base, int64_t cols, int64_t rows, int64_t ld, int box_rows) {
     auto enc = tc_encoder();
     SPREG_CHECK_ARG(enc, "cuTensorMapEncodeTiled is not available from the driver");
     const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
     const cuuint64_t strides[1] = {(cuuint64_t)(ld * 2)};
-    const cuuint32_t box[2] = {(cuuint32_t)TC_BK, (cuuint32_t)TC_BM};
+    const cuuint32_t box[2] = {(cuuint32_t)TC_BK, (cuuint32_t)box_rows};
     const cuuint32_t es[2] = {1, 1};
     CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), dims, strides, box, es,
                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
@@ -315,7 +320,10 @@ int dense_rows_batched_impl(const spreg_dense_rows_item *items, int32_t count, c
     int dev = 0;
     SPREG_CUDA(cudaGetDevice(&dev));
     if (dev >= 0 && dev < 64 && !configured[dev]) {
-        SPREG_CUDA(cudaFuncSetAttribute(tc_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM));
+        SPREG_CUDA(cudaFuncSetAttribute(tc_rows_kernel<128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)tc_smem<128>()));
+        SPREG_CUDA(cudaFuncSetAttribute(tc_rows_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)tc_smem<256>()));
         configured[dev] = true;
     }
     char *bt = nullptr;
@@ -342,6 +350,10 @@ int dense_rows_batched_impl(const spreg_dense_rows_item *items, int32_t count, c
         memset(&p, 0, sizeof p);
         p.status = status;
         p.nprob = (int32_t)cnt;
+        // 256-wide output tiles when every product of the launch is wider than 128 columns
+        int64_t min_n = INT64_MAX;
+        for (size_t j = 0; j < cnt; ++j) min_n = std::min<int64_t>(min_n, items[live[first + j]].n);
+        const int bn = min_n > 128 ? 256 : 128;
         int64_t tiles = 0;
         for (size_t j = 0; j < cnt; ++j) {
             const spreg_dense_rows_item &it = items[live[first + j]];
@@ -356,18 +368,19 @@ int dense_rows_batched_impl(const spreg_dense_rows_item *items, int32_t count, c
             q.c_dtype = it.c_dtype;
             q.load_c = it.load_c ? 1 : 0;
             q.epilogue = it.epilogue;
-            q.tiles_n = (int32_t)((it.n + TC_BN - 1) / TC_BN);
+            q.tiles_n = (int32_t)((it.n + bn - 1) / bn);
             q.tile_begin = (int32_t)tiles;
             tiles += ((it.rows + TC_BM - 1) / TC_BM) * q.tiles_n;
-            if ((st = tc_map(&q.a_map, it.a_rows, it.k, it.rows, it.lda)) ||
-                (st = tc_map(&q.b_map, bt + bt_off[(size_t)live[first + j]], it.k, it.n, K8)))
+            if ((st = tc_map(&q.a_map, it.a_rows, it.k, it.rows, it.lda, TC_BM)) ||
+                (st = tc_map(&q.b_map, bt + bt_off[(size_t)live[first + j]], it.k, it.n, K8, bn)))
                 return fail(st);
         }
         if (tiles > INT32_MAX) {
             fail(0);
             SPREG_FAIL(SPREG_ERR_UNSUPPORTED, "too many output tiles in one launch");
         }
-        tc_rows_kernel<<<(unsigned)tiles, 128, TC_SMEM, stream>>>(p);
+        if (bn == 256) tc_rows_kernel<256><<<(unsigned)tiles, 128, tc_smem<256>(), stream>>>(p);
+        else tc_rows_kernel<128><<<(unsigned)tiles, 128, tc_smem<128>(), stream>>>(p);
         e = cudaGetLastError();
         if (e != cudaSuccess) {
             fail(0);
