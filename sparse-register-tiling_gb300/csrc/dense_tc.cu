@@ -28,6 +28,8 @@
 
 #include <algorithm>
 #include <cstring>
+#include <map>
+#include <tuple>
 #include <vector>
 
 namespace spreg {
@@ -55,6 +57,13 @@ struct TcProblem {
     int64_t ldc;
     int32_t R, n, kblocks, c_dtype;
     int32_t load_c, epilogue, tile_begin, tiles_n;  // first output tile of the launch, tiles along n
+    // Products sharing A (same weight rows, row index and epilogue) are one problem whose columns
+    // are their B's side by side: column j belongs to segment s with seg_start[s] <= j <
+    // seg_start[s + 1] and is column j - seg_start[s] of C seg_c[s] (row stride seg_ldc[s]).
+    const int32_t *seg_start;
+    void *const *seg_c;
+    const int64_t *seg_ldc;
+    int32_t nseg, pad0;
 };
 
 struct TcParams {
@@ -210,6 +219,16 @@ __global__ void __launch_bounds__(128, 1) tc_rows_kernel(const __grid_constant__
     const bool row_ok = ok && r < q.R;
     const int64_t orow = row_ok ? q.row_index[r] : 0;
     if (ok) {
+        int seg = 0;  // segment of the current column (coalesced products)
+        if (q.nseg > 1 && row_ok) {
+            int lo2 = 0, hi2 = q.nseg - 1;
+            while (lo2 < hi2) {
+                const int mid = (lo2 + hi2 + 1) >> 1;
+                if (q.seg_start[mid] <= n0) lo2 = mid;
+                else hi2 = mid - 1;
+            }
+            seg = lo2;
+        }
         for (int c = 0; c < TC_BN; c += 16) {
             float v[16];
             tc_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c, v);  // every lane takes part
@@ -218,14 +237,23 @@ __global__ void __launch_bounds__(128, 1) tc_rows_kernel(const __grid_constant__
             for (int j = 0; j < 16; ++j) {
                 const int col = n0 + c + j;
                 if (col >= q.n) break;
+                void *cbase = q.C;
+                int64_t ldc = q.ldc;
+                int lcol = col;
+                if (q.nseg > 1) {
+                    while (col >= q.seg_start[seg + 1]) ++seg;
+                    cbase = q.seg_c[seg];
+                    ldc = q.seg_ldc[seg];
+                    lcol = col - q.seg_start[seg];
+                }
                 float o = v[j];
                 if (q.c_dtype == SPREG_F32) {
-                    float *cp = reinterpret_cast<float *>(q.C) + orow * q.ldc + col;
+                    float *cp = reinterpret_cast<float *>(cbase) + orow * ldc + lcol;
                     if (q.load_c) o += *cp;
                     if (q.epilogue == SPREG_EPILOGUE_RELU) o = fmaxf(o, 0.0f);
                     *cp = o;
                 } else {
-                    __nv_bfloat16 *cp = reinterpret_cast<__nv_bfloat16 *>(q.C) + orow * q.ldc + col;
+                    __nv_bfloat16 *cp = reinterpret_cast<__nv_bfloat16 *>(cbase) + orow * ldc + lcol;
                     if (q.load_c) o += __bfloat162float(*cp);
                     if (q.epilogue == SPREG_EPILOGUE_RELU) o = fmaxf(o, 0.0f);
                     *cp = __float2bfloat16_rn(o);
@@ -241,19 +269,29 @@ __global__ void __launch_bounds__(128, 1) tc_rows_kernel(const __grid_constant__
     }
 }
 
-// Bt[j][k] = B[k][j] for k < K (zero for K <= k < K8), j < n: 32 x 32 tiles through shared memory.
-__global__ void transpose_b_kernel(const __nv_bfloat16 *__restrict__ B, int64_t ldb, int K, int n, int K8,
-                                   __nv_bfloat16 *__restrict__ Bt) {
-    __shared__ __nv_bfloat16 tile[32][33];
+// One B of a batched call: transposed into dst (n x K8, zero past k).
+struct TransposeItem {
+    const __nv_bfloat16 *b;
+    __nv_bfloat16 *dst;
+    int64_t ldb;
+    int32_t k, n, K8, pad;
+};
+
+// All B of a batched call in one launch: Bt[j][k] = B[k][j] for k < K (zero up to K8), j < n, in
+// 32 x 32 tiles through shared memory; blockIdx.z picks the item, x / y its tile.
+__global__ void transpose_items_kernel(const TransposeItem *__restrict__ items) {
+    const TransposeItem it = items[blockIdx.z];
     const int k0 = blockIdx.x * 32, j0 = blockIdx.y * 32;
+    if (k0 >= it.K8 || j0 >= it.n) return;  // uniform per block
+    __shared__ __nv_bfloat16 tile[32][33];
     for (int i = threadIdx.y; i < 32; i += blockDim.y) {
         const int k = k0 + i, j = j0 + threadIdx.x;
-        tile[i][threadIdx.x] = (k < K && j < n) ? B[(int64_t)k * ldb + j] : __float2bfloat16_rn(0.0f);
+        tile[i][threadIdx.x] = (k < it.k && j < it.n) ? it.b[(int64_t)k * it.ldb + j] : __float2bfloat16_rn(0.0f);
     }
     __syncthreads();
     for (int i = threadIdx.y; i < 32; i += blockDim.y) {
         const int j = j0 + i, k = k0 + threadIdx.x;
-        if (j < n && k < K8) Bt[(int64_t)j * K8 + k] = tile[threadIdx.x][i];
+        if (j < it.n && k < it.K8) it.dst[(int64_t)j * it.K8 + k] = tile[threadIdx.x][i];
     }
 }
 
@@ -290,10 +328,14 @@ int tc_map(CUtensorMap *map, const void *base, int64_t cols, int64_t rows, int64
 int dense_rows_batched_impl(const spreg_dense_rows_item *items, int32_t count, cudaStream_t stream) {
     SPREG_CHECK_ARG(count >= 0 && (count == 0 || items), "bad item list");
     int st = SPREG_OK;
-    // checks, and the transposed-B scratch of every item (one allocation)
-    std::vector<int32_t> live;
-    std::vector<int64_t> bt_off((size_t)count, 0);
-    int64_t bt_bytes = 0;
+    // checks; products with the same A, row index, output type and epilogue become one problem
+    struct Group {
+        const spreg_dense_rows_item *first;
+        std::vector<int32_t> members;
+        int64_t n = 0, bt_off = 0, tab_off = 0;
+    };
+    std::vector<Group> groups;
+    std::map<std::tuple<const void *, int64_t, int64_t, int64_t, const void *, int32_t, int32_t, int32_t>, size_t> key;
     for (int32_t i = 0; i < count; ++i) {
         const spreg_dense_rows_item &it = items[i];
         SPREG_CHECK_ARG(it.rows >= 0 && it.k >= 0 && it.n >= 0, "item %d: negative size", i);
@@ -308,12 +350,78 @@ int dense_rows_batched_impl(const spreg_dense_rows_item *items, int32_t count, c
                         "%lld)", i, (long long)it.lda);
         SPREG_CHECK_ARG(it.ldb >= it.n && it.ldc >= it.n, "item %d: ldb / ldc smaller than n", i);
         SPREG_CHECK_ARG(it.k > 0, "item %d: K must be positive", i);
-        const int64_t K8 = (it.k + 7) / 8 * 8;
-        bt_off[(size_t)i] = bt_bytes;
-        bt_bytes += (it.n * K8 * 2 + 255) / 256 * 256;
-        live.push_back(i);
+        auto kk = std::make_tuple(it.a_rows, it.rows, it.k, it.lda, (const void *)it.row_index, it.c_dtype,
+                                  it.load_c ? 1 : 0, it.epilogue);
+        auto f = key.find(kk);
+        if (f == key.end()) {
+            key.emplace(kk, groups.size());
+            groups.push_back(Group{&it, {i}, it.n});
+        } else {
+            Group &g = groups[f->second];
+            g.members.push_back(i);
+            g.n += it.n;
+        }
     }
-    if (live.empty()) return SPREG_OK;
+    if (groups.empty()) return SPREG_OK;
+    // scratch: each problem's Bt (n x K8, 256-byte aligned), then the segment tables
+    int64_t bytes = 0;
+    for (Group &g : groups) {
+        SPREG_CHECK_ARG(g.n <= INT32_MAX, "coalesced products wider than 2^31 columns");
+        const int64_t K8 = (g.first->k + 7) / 8 * 8;
+        g.bt_off = bytes;
+        bytes += (g.n * K8 * 2 + 255) / 256 * 256;
+    }
+    std::vector<unsigned char> tab;
+    auto put = [&](const void *src, size_t len) {
+        const size_t at = tab.size();
+        tab.resize(at + (len + 7) / 8 * 8);
+        memcpy(tab.data() + at, src, len);
+        return (int64_t)at;
+    };
+    std::vector<int64_t> seg_c_off(groups.size(), 0), seg_ldc_off(groups.size(), 0);
+    for (size_t gi = 0; gi < groups.size(); ++gi) {
+        Group &g = groups[gi];
+        if (g.members.size() < 2) continue;
+        std::vector<int32_t> starts;
+        std::vector<uint64_t> cs;
+        std::vector<int64_t> lds;
+        int32_t o = 0;
+        for (int32_t m : g.members) {
+            starts.push_back(o);
+            o += (int32_t)items[m].n;
+            cs.push_back(reinterpret_cast<uint64_t>(items[m].c));
+            lds.push_back(items[m].ldc);
+        }
+        starts.push_back(o);
+        g.tab_off = put(starts.data(), starts.size() * 4);
+        seg_c_off[gi] = put(cs.data(), cs.size() * 8);
+        seg_ldc_off[gi] = put(lds.data(), lds.size() * 8);
+    }
+    // transpose items (every member of every group), after the segment tables
+    std::vector<TransposeItem> titems;
+    int64_t max_kt = 1, max_nt = 1;
+    for (Group &g : groups) {
+        const int64_t K8 = (g.first->k + 7) / 8 * 8;
+        int64_t o = 0;
+        for (int32_t m : g.members) {
+            const spreg_dense_rows_item &it = items[m];
+            TransposeItem ti;
+            ti.b = static_cast<const __nv_bfloat16 *>(it.b);
+            ti.dst = nullptr;  // set once the scratch base is known
+            ti.ldb = it.ldb;
+            ti.k = (int32_t)it.k;
+            ti.n = (int32_t)it.n;
+            ti.K8 = (int32_t)K8;
+            ti.pad = 0;
+            titems.push_back(ti);
+            max_kt = std::max<int64_t>(max_kt, (K8 + 31) / 32);
+            max_nt = std::max<int64_t>(max_nt, (it.n + 31) / 32);
+            o += it.n;
+        }
+    }
+    SPREG_CHECK_ARG(titems.size() <= 65535 && max_nt <= 65535, "too many products in one call");
+    const int64_t titem_off = put(titems.data(), titems.size() * sizeof(TransposeItem));  // dst filled in below
+    const int64_t tab_base = (bytes + 255) / 256 * 256;
     int *status = device_status_word(&st);
     if (st != SPREG_OK) return st;
     static bool configured[64] = {};
@@ -326,53 +434,73 @@ int dense_rows_batched_impl(const spreg_dense_rows_item *items, int32_t count, c
                                         (int)tc_smem<256>()));
         configured[dev] = true;
     }
-    char *bt = nullptr;
-    SPREG_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&bt), (size_t)bt_bytes, stream));
+    char *scratch = nullptr;
+    SPREG_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&scratch), (size_t)(tab_base + (int64_t)tab.size() + 16),
+                               stream));
     auto fail = [&](int code) {
-        cudaFreeAsync(bt, stream);
+        cudaFreeAsync(scratch, stream);
         return code;
     };
-    for (int32_t i : live) {
-        const spreg_dense_rows_item &it = items[i];
-        const int64_t K8 = (it.k + 7) / 8 * 8;
-        transpose_b_kernel<<<dim3((unsigned)((K8 + 31) / 32), (unsigned)((it.n + 31) / 32)), dim3(32, 8), 0, stream>>>(
-            static_cast<const __nv_bfloat16 *>(it.b), it.ldb, (int)it.k, (int)it.n, (int)K8,
-            reinterpret_cast<__nv_bfloat16 *>(bt + bt_off[(size_t)i]));
+    // B of every product, transposed into its problem's Bt at its segment's row offset: one launch
+    {
+        size_t t = 0;
+        for (Group &g : groups) {
+            const int64_t K8 = (g.first->k + 7) / 8 * 8;
+            int64_t o = 0;
+            for (int32_t m : g.members) {
+                titems[t++].dst = reinterpret_cast<__nv_bfloat16 *>(scratch + g.bt_off) + o * K8;
+                o += items[m].n;
+            }
+        }
     }
-    cudaError_t e = cudaGetLastError();
+    memcpy(tab.data() + titem_off, titems.data(), titems.size() * sizeof(TransposeItem));
+    cudaError_t e = cudaMemcpyAsync(scratch + tab_base, tab.data(), tab.size(), cudaMemcpyHostToDevice, stream);
+    if (e == cudaSuccess) {
+        transpose_items_kernel<<<dim3((unsigned)max_kt, (unsigned)max_nt, (unsigned)titems.size()), dim3(32, 8), 0,
+                                 stream>>>(reinterpret_cast<const TransposeItem *>(scratch + tab_base + titem_off));
+        e = cudaGetLastError();
+    }
     if (e != cudaSuccess) {
         fail(0);
-        SPREG_FAIL(SPREG_ERR_CUDA, "transpose launch: %s", cudaGetErrorString(e));
+        SPREG_FAIL(SPREG_ERR_CUDA, "tensor-core set-up: %s", cudaGetErrorString(e));
     }
     static thread_local TcParams p;  // ~31 KB: kept off the stack
-    for (size_t first = 0; first < live.size(); first += TC_MAX_PROBLEMS) {
-        const size_t cnt = std::min<size_t>(TC_MAX_PROBLEMS, live.size() - first);
+    for (size_t first = 0; first < groups.size(); first += TC_MAX_PROBLEMS) {
+        const size_t cnt = std::min<size_t>(TC_MAX_PROBLEMS, groups.size() - first);
         memset(&p, 0, sizeof p);
         p.status = status;
         p.nprob = (int32_t)cnt;
-        // 256-wide output tiles when every product of the launch is wider than 128 columns
+        // 256-wide output tiles when every problem of the launch is wider than 128 columns
         int64_t min_n = INT64_MAX;
-        for (size_t j = 0; j < cnt; ++j) min_n = std::min<int64_t>(min_n, items[live[first + j]].n);
+        for (size_t j = 0; j < cnt; ++j) min_n = std::min<int64_t>(min_n, groups[first + j].n);
         const int bn = min_n > 128 ? 256 : 128;
         int64_t tiles = 0;
         for (size_t j = 0; j < cnt; ++j) {
-            const spreg_dense_rows_item &it = items[live[first + j]];
+            const size_t gi = first + j;
+            const Group &g = groups[gi];
+            const spreg_dense_rows_item &it = *g.first;
             TcProblem &q = p.prob[j];
             const int64_t K8 = (it.k + 7) / 8 * 8;
             q.row_index = it.row_index;
             q.C = it.c;
             q.ldc = it.ldc;
             q.R = (int32_t)it.rows;
-            q.n = (int32_t)it.n;
+            q.n = (int32_t)g.n;
             q.kblocks = (int32_t)((it.k + TC_BK - 1) / TC_BK);
             q.c_dtype = it.c_dtype;
             q.load_c = it.load_c ? 1 : 0;
             q.epilogue = it.epilogue;
-            q.tiles_n = (int32_t)((it.n + bn - 1) / bn);
+            q.nseg = (int32_t)g.members.size();
+            if (q.nseg > 1) {
+                q.seg_start = reinterpret_cast<const int32_t *>(scratch + tab_base + g.tab_off);
+                q.seg_c = reinterpret_cast<void *const *>(scratch + tab_base + seg_c_off[gi]);
+                q.seg_ldc = reinterpret_cast<const int64_t *>(scratch + tab_base + seg_ldc_off[gi]);
+            }
+            q.tiles_n = (int32_t)((g.n + bn - 1) / bn);
             q.tile_begin = (int32_t)tiles;
             tiles += ((it.rows + TC_BM - 1) / TC_BM) * q.tiles_n;
             if ((st = tc_map(&q.a_map, it.a_rows, it.k, it.rows, it.lda, TC_BM)) ||
-                (st = tc_map(&q.b_map, bt + bt_off[(size_t)live[first + j]], it.k, it.n, K8, bn)))
+                (st = tc_map(&q.b_map, scratch + g.bt_off, it.k, g.n, K8, bn)))
                 return fail(st);
         }
         if (tiles > INT32_MAX) {
@@ -387,7 +515,7 @@ int dense_rows_batched_impl(const spreg_dense_rows_item *items, int32_t count, c
             SPREG_FAIL(SPREG_ERR_CUDA, "tensor-core launch: %s", cudaGetErrorString(e));
         }
     }
-    cudaFreeAsync(bt, stream);
+    cudaFreeAsync(scratch, stream);
     return SPREG_OK;
 }
 

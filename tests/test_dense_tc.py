@@ -135,3 +135,33 @@ def test_batched_products_equal_single_calls(cuda):
     torch.cuda.synchronize()
     for a, idx, B, C1, C2 in ops:
         assert torch.equal(C1.view(torch.int32), C2.view(torch.int32))
+
+
+def test_products_sharing_weights_coalesce_to_same_results(cuda):
+    """Products with the same weight rows (the same layer for many requests) run as one product over
+    their side-by-side B; every output equals its own single call bit for bit."""
+    import torch
+    from spreg.hybrid import dense_rows_bf16
+    from spreg.serving import TC_ITEM_DTYPE
+    g = torch.Generator(device="cuda").manual_seed(9)
+    R, K = 300, 520
+    a = torch.zeros((R, 520), device="cuda", dtype=torch.bfloat16)
+    a[:, :K] = torch.randn((R, K), device="cuda", generator=g).to(torch.bfloat16)
+    idx = torch.randperm(R, device="cuda", generator=g).to(torch.int32)
+    ns = [1, 64, 130, 7, 256, 300, 33, 128, 2, 200] * 3
+    items = np.zeros(len(ns), dtype=TC_ITEM_DTYPE)
+    ops = []
+    for i, n in enumerate(ns):
+        B = torch.randn((K, n + 3), device="cuda", generator=g).to(torch.bfloat16)[:, :n]  # ldb > n
+        C1 = torch.randn((R, n), device="cuda", generator=g)
+        C2 = C1.clone()
+        load_c, epi = i % 2, (i // 3) % 2  # three coalesced groups of mixed widths
+        dense_rows_bf16(a, idx, B, C1, load_c=bool(load_c), epilogue=epi)
+        items[i] = (a.data_ptr(), R, K, a.stride(0), idx.data_ptr(), B.data_ptr(), B.stride(0), C2.data_ptr(),
+                    C2.stride(0), n, _lib.F32, load_c, epi, 0)
+        ops.append((B, C1, C2))
+    _lib.check(_lib.lib().spreg_dense_rows_bf16_batched(items.ctypes.data, len(ns),
+                                                       _lib.stream_handle(torch.cuda.current_stream())))
+    torch.cuda.synchronize()
+    for B, C1, C2 in ops:
+        assert torch.equal(C1.view(torch.int32), C2.view(torch.int32))
