@@ -218,6 +218,9 @@ __global__ void __launch_bounds__(128, 1) tc_rows_kernel(const __grid_constant__
     const int r = m0 + 32 * warp + lane;
     const bool row_ok = ok && r < q.R;
     const int64_t orow = row_ok ? q.row_index[r] : 0;
+    // vector stores need 16-byte (F32) / 8-byte (BF16) aligned row starts of C
+    const int esz = q.c_dtype == SPREG_F32 ? 4 : 2;
+    const bool vec_ok = (reinterpret_cast<uintptr_t>(q.C) % (4 * esz)) == 0 && (q.ldc % 4) == 0;
     if (ok) {
         int seg = 0;  // segment of the current column (coalesced products)
         if (q.nseg > 1 && row_ok) {
@@ -233,6 +236,45 @@ __global__ void __launch_bounds__(128, 1) tc_rows_kernel(const __grid_constant__
             float v[16];
             tc_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c, v);  // every lane takes part
             if (!row_ok) continue;
+            if (q.nseg <= 1 && vec_ok && n0 + c + 16 <= q.n) {
+                // whole 16-column chunk of one output: 16-byte (F32) / 8-byte (BF16) stores
+                if (q.c_dtype == SPREG_F32) {
+                    float4 *cp = reinterpret_cast<float4 *>(reinterpret_cast<float *>(q.C) + orow * q.ldc + n0 + c);
+#pragma unroll
+                    for (int j4 = 0; j4 < 4; ++j4) {
+                        float4 o = make_float4(v[4 * j4], v[4 * j4 + 1], v[4 * j4 + 2], v[4 * j4 + 3]);
+                        if (q.load_c) {
+                            const float4 ci = cp[j4];
+                            o.x += ci.x; o.y += ci.y; o.z += ci.z; o.w += ci.w;
+                        }
+                        if (q.epilogue == SPREG_EPILOGUE_RELU) {
+                            o.x = fmaxf(o.x, 0.0f); o.y = fmaxf(o.y, 0.0f); o.z = fmaxf(o.z, 0.0f); o.w = fmaxf(o.w, 0.0f);
+                        }
+                        cp[j4] = o;
+                    }
+                } else {
+                    uint2 *cp = reinterpret_cast<uint2 *>(reinterpret_cast<__nv_bfloat16 *>(q.C) + orow * q.ldc + n0 + c);
+#pragma unroll
+                    for (int j4 = 0; j4 < 4; ++j4) {
+                        float o[4] = {v[4 * j4], v[4 * j4 + 1], v[4 * j4 + 2], v[4 * j4 + 3]};
+                        if (q.load_c) {
+                            const uint2 ci = cp[j4];
+                            const __nv_bfloat162 c01 = *reinterpret_cast<const __nv_bfloat162 *>(&ci.x);
+                            const __nv_bfloat162 c23 = *reinterpret_cast<const __nv_bfloat162 *>(&ci.y);
+                            o[0] += __low2float(c01); o[1] += __high2float(c01);
+                            o[2] += __low2float(c23); o[3] += __high2float(c23);
+                        }
+                        if (q.epilogue == SPREG_EPILOGUE_RELU)
+                            for (int t = 0; t < 4; ++t) o[t] = fmaxf(o[t], 0.0f);
+                        __nv_bfloat162 w01 = __floats2bfloat162_rn(o[0], o[1]), w23 = __floats2bfloat162_rn(o[2], o[3]);
+                        uint2 w;
+                        w.x = *reinterpret_cast<uint32_t *>(&w01);
+                        w.y = *reinterpret_cast<uint32_t *>(&w23);
+                        cp[j4] = w;
+                    }
+                }
+                continue;
+            }
 #pragma unroll
             for (int j = 0; j < 16; ++j) {
                 const int col = n0 + c + j;

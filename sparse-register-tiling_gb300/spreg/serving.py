@@ -131,7 +131,7 @@ class Request:
     # device-side state kept by the server
     _host_in: object = None
     _host_out: object = None
-    _items: object = None
+    _slot: int = -1
     _ready: object = None
 
     @property
@@ -294,37 +294,40 @@ class SparseMLP:
         """Activation block of one request: x (d_model x ld) then h (d_ff x ld)."""
         return self.x_bytes(n) + round_up(self.d_ff * self.ld(n) * self.elem, ARENA_ALIGN)
 
-    def work_items(self, x_ptr: int, h_ptr: int, n: int) -> np.ndarray:
-        """The request's SpMMs, one per layer, as spreg_work_item records (spreg_dense_rows_item
-        records for tensor-core layers)."""
-        ld = self.ld(n)
+    def _item_template(self) -> np.ndarray:
+        """The per-layer fields that do not depend on the request (built once)."""
+        if getattr(self, "_template", None) is not None:
+            return self._template
+        up = np.arange(self.num_layers) % 2 == 0
         if self.tc:
             it = np.zeros(self.num_layers, dtype=TC_ITEM_DTYPE)
-            for l, (a, idx) in enumerate(self.tc_rows):
-                up = l % 2 == 0
-                it[l]["a_rows"] = a.data_ptr()
-                it[l]["rows"] = a.shape[0]
-                it[l]["k"] = self.d_model if up else self.d_ff
-                it[l]["lda"] = a.stride(0)
-                it[l]["row_index"] = idx.data_ptr()
-                it[l]["b"], it[l]["c"] = (x_ptr, h_ptr) if up else (h_ptr, x_ptr)
-                it[l]["ldb"] = it[l]["ldc"] = ld
-                it[l]["n"] = n
-                it[l]["c_dtype"] = _lib.BF16
-                it[l]["load_c"] = 0 if up else 1
-                it[l]["epilogue"] = _lib.EPILOGUE_RELU if up else _lib.EPILOGUE_NONE
-            return it
-        it = np.zeros(self.num_layers, dtype=WORK_ITEM_DTYPE)
-        for l, pm in enumerate(self.layers):
-            up = l % 2 == 0
-            it[l]["a"] = _handle_int(pm.handle)
-            it[l]["b"], it[l]["c"] = (x_ptr, h_ptr) if up else (h_ptr, x_ptr)
-            it[l]["ldb"] = it[l]["ldc"] = ld
-            it[l]["n"] = n
-            it[l]["b_dtype"] = it[l]["c_dtype"] = self.act_code
-            it[l]["load_c"] = 0 if up else 1
-            it[l]["epilogue"] = _lib.EPILOGUE_RELU if up else _lib.EPILOGUE_NONE
-            it[l]["nr"] = nr_for_tokens(n)
+            it["a_rows"] = [a.data_ptr() for a, _ in self.tc_rows]
+            it["rows"] = [a.shape[0] for a, _ in self.tc_rows]
+            it["k"] = np.where(up, self.d_model, self.d_ff)
+            it["lda"] = [a.stride(0) for a, _ in self.tc_rows]
+            it["row_index"] = [idx.data_ptr() for _, idx in self.tc_rows]
+            it["c_dtype"] = _lib.BF16
+        else:
+            it = np.zeros(self.num_layers, dtype=WORK_ITEM_DTYPE)
+            it["a"] = [_handle_int(pm.handle) for pm in self.layers]
+            it["b_dtype"] = it["c_dtype"] = self.act_code
+        it["load_c"] = np.where(up, 0, 1)
+        it["epilogue"] = np.where(up, _lib.EPILOGUE_RELU, _lib.EPILOGUE_NONE)
+        self._template = it
+        return it
+
+    def work_items(self, x_ptr: int, h_ptr: int, n: int) -> np.ndarray:
+        """The request's SpMMs, one per layer, as spreg_work_item records (spreg_dense_rows_item
+        records for tensor-core layers): layer 2b reads x and writes h, layer 2b + 1 the reverse."""
+        it = self._item_template().copy()
+        ld = self.ld(n)
+        it["b"][0::2], it["c"][0::2] = x_ptr, h_ptr
+        it["b"][1::2], it["c"][1::2] = h_ptr, x_ptr
+        it["ldb"] = ld
+        it["ldc"] = ld
+        it["n"] = n
+        if not self.tc:
+            it["nr"] = nr_for_tokens(n)
         return it
 
     def forward(self, x_dev, h_dev, n: Optional[int] = None, stream=None):
@@ -409,7 +412,8 @@ class Server:
         self.compute = torch.cuda.Stream(model.device)
         self.copy = torch.cuda.Stream(model.device)
         self._dtype = TC_ITEM_DTYPE if model.tc else WORK_ITEM_DTYPE
-        self._buf = np.zeros(max(self.max_slots, 1), dtype=self._dtype)
+        # every admitted request's records at a fixed slot: rows slot * L .. slot * L + L - 1
+        self._table = np.zeros(max(self.max_slots, 1) * model.num_layers, dtype=self._dtype)
         self._lib = _lib.lib()
 
     def _x_view(self, r: Request):
@@ -429,6 +433,8 @@ class Server:
         sched = Scheduler(m.num_layers, lambda r: m.act_bytes(r.n), arena, self.max_slots)
         order = sorted(reqs, key=lambda r: (r.arrival, r.rid))
         inflight: Deque = collections.deque()
+        free_slots = list(range(self.max_slots - 1, -1, -1))
+        L = m.num_layers
         draining: List = []
         nxt, done, it, launches, max_batch = 0, 0, 0, 0, 0
         first_arrival = order[0].arrival if order else 0.0
@@ -444,6 +450,7 @@ class Server:
                 if ev.query():
                     r.t_done = clock() - t0 if realtime else float(it)
                     sched.release(r)
+                    free_slots.append(r._slot)
                     done += 1
                 else:
                     still.append((ev, r))
@@ -452,7 +459,8 @@ class Server:
                 r.t_admit = clock() - t0 if realtime else float(it)
                 r.first_iteration = it
                 x_ptr = self.base + r.offset
-                r._items = m.work_items(x_ptr, x_ptr + m.x_bytes(r.n), r.n)
+                r._slot = free_slots.pop()
+                self._table[r._slot * L:(r._slot + 1) * L] = m.work_items(x_ptr, x_ptr + m.x_bytes(r.n), r.n)
                 with torch.cuda.stream(self.copy):
                     self._x_view(r).copy_(r._host_in, non_blocking=True)
                     ev = torch.cuda.Event()
@@ -460,14 +468,13 @@ class Server:
                 r._ready = ev
             if sched.active:
                 batch = sched.next_iteration()
-                if len(batch) > self._buf.shape[0]:
-                    self._buf = np.zeros(len(batch), dtype=self._dtype)
-                buf = self._buf
+                rows = np.empty(len(batch), dtype=np.int64)
                 for i, r in enumerate(batch):
                     if r._ready is not None:
                         self.compute.wait_event(r._ready)
                         r._ready = None
-                    buf[i] = r._items[r.layer - 1]
+                    rows[i] = r._slot * L + r.layer - 1
+                buf = self._table[rows]  # one gather of this iteration's records
                 run = self._lib.spreg_dense_rows_bf16_batched if m.tc else self._lib.spreg_execute_batched
                 _lib.check(run(buf.ctypes.data, len(batch), self.compute.cuda_stream))
                 ev = torch.cuda.Event()
