@@ -90,6 +90,9 @@ __device__ __forceinline__ bool tc_wait(uint32_t bar, uint32_t phase, int *statu
     if (status) atomicCAS(status, 0, code);
     return false;
 }
+__device__ __forceinline__ void mbar_arrive_tc(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
 __device__ __forceinline__ void tc_expect_tx(uint32_t bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
 }
@@ -139,85 +142,29 @@ __device__ __forceinline__ void tc_ld16(uint32_t taddr, float (&v)[16]) {
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-template <int BN>
-__global__ void __launch_bounds__(128, 1) tc_rows_kernel(const __grid_constant__ TcParams p) {
-    constexpr uint32_t TC_TILE_B = tc_tile_b<BN>(), TC_STAGE = tc_stage<BN>(), TC_TMEM_COLS = BN;
-    constexpr int TC_BN = BN;
-    extern __shared__ unsigned char smem_raw[];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t raw = smem_u32(smem_raw);
-    const uint32_t sbase = (raw + 1023u) & ~1023u;  // the swizzle atoms need 1024-byte alignment
-    const uint32_t bars = sbase + TC_STAGES * TC_STAGE;
-    const uint32_t full0 = bars, empty0 = bars + 8u * TC_STAGES, done = bars + 16u * TC_STAGES;
-    const uint32_t tmem_slot = done + 8u;
-    if (threadIdx.x == 0) {
-        for (int s = 0; s < TC_STAGES; ++s) {
-            tc_mbar_init(full0 + 8u * s, 1);
-            tc_mbar_init(empty0 + 8u * s, 1);
-        }
-        tc_mbar_init(done, 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    if (warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tmem_slot),
-                     "r"(TC_TMEM_COLS) : "memory");
-        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-    }
-    tc_fence_before();
-    __syncthreads();
-    tc_fence_after();
-    uint32_t tmem;
-    asm volatile("ld.shared.b32 %0, [%1];" : "=r"(tmem) : "r"(tmem_slot) : "memory");
-
-    // this CTA's problem and output tile
+// Problem of output tile t of the launch (binary search over the problems' first tiles).
+__device__ __forceinline__ int tc_problem_of(const TcParams &p, int t) {
     int lo = 0, hi = p.nprob - 1;
     while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
-        if (p.prob[mid].tile_begin <= (int)blockIdx.x) lo = mid;
+        if (p.prob[mid].tile_begin <= t) lo = mid;
         else hi = mid - 1;
     }
-    const TcProblem &q = p.prob[lo];
-    const int local = (int)blockIdx.x - q.tile_begin;
-    const int m0 = (local / q.tiles_n) * TC_BM, n0 = (local % q.tiles_n) * TC_BN;
-    if (warp == 0 && lane == 0) {
-        // producer: A and Bt tiles of each K block
-        int issued = 0;
-        for (int kb = 0; kb < q.kblocks; ++kb) {
-            const int s = kb % TC_STAGES;
-            if (kb >= TC_STAGES && !tc_wait(empty0 + 8u * s, (uint32_t)(((kb / TC_STAGES) - 1) & 1), p.status, 21))
-                break;
-            const uint32_t st = sbase + (uint32_t)s * TC_STAGE;
-            tc_expect_tx(full0 + 8u * s, TC_STAGE);
-            tc_tma_2d(st, &q.a_map, kb * TC_BK, m0, full0 + 8u * s);
-            tc_tma_2d(st + TC_TILE_A, &q.b_map, kb * TC_BK, n0, full0 + 8u * s);
-            issued = kb + 1;
-        }
-        // before the CTA can finish, every copy issued has landed
-        for (int kb = issued - TC_STAGES > 0 ? issued - TC_STAGES : 0; kb < issued; ++kb)
-            tc_wait(full0 + 8u * (kb % TC_STAGES), (uint32_t)((kb / TC_STAGES) & 1), p.status, 22);
-    } else if (warp == 1 && lane == 0) {
-        // MMA issuer
-        constexpr uint32_t idesc = tc_idesc(TC_BM, TC_BN);
-        for (int kb = 0; kb < q.kblocks; ++kb) {
-            const int s = kb % TC_STAGES;
-            if (!tc_wait(full0 + 8u * s, (uint32_t)((kb / TC_STAGES) & 1), p.status, 23)) break;
-            tc_fence_after();
-            const uint32_t st = sbase + (uint32_t)s * TC_STAGE;
-#pragma unroll
-            for (int k = 0; k < TC_BK / 16; ++k)
-                tc_mma(tmem, tc_desc(st + 32u * k), tc_desc(st + TC_TILE_A + 32u * k), idesc, (kb | k) != 0);
-            tc_commit(empty0 + 8u * s);  // the stage is free once these MMAs have read it
-        }
-        tc_commit(done);  // arrives when every MMA issued above has completed
-    }
-    __syncwarp();
-    const bool ok = __all_sync(0xffffffffu, tc_wait(done, 0u, p.status, 24));  // tcgen05.ld is warp-wide
-    tc_fence_after();
+    return lo;
+}
 
-    // epilogue: warp w reads TMEM lanes (rows) 32w .. 32w + 31
-    const int r = m0 + 32 * warp + lane;
+// Epilogue of one output tile by one warp: TMEM lanes 32 * quarter .. + 31 (tile rows) of the
+// accumulator at TMEM address tacc (lane 0, its first column); load_c / ReLU; store through the
+// row index (and segments).
+template <int BN>
+__device__ __forceinline__ void tc_store_tile(const TcProblem &q, int m0, int n0, int quarter, int lane, uint32_t tacc,
+                                              bool ok) {
+    constexpr int TC_BN = BN;
+    const int r = m0 + 32 * quarter + lane;
     const bool row_ok = ok && r < q.R;
     const int64_t orow = row_ok ? q.row_index[r] : 0;
+    const uint32_t tmem = tacc;
+    const int warp = quarter;
     // vector stores need 16-byte (F32) / 8-byte (BF16) aligned row starts of C
     const int esz = q.c_dtype == SPREG_F32 ? 4 : 2;
     const bool vec_ok = (reinterpret_cast<uintptr_t>(q.C) % (4 * esz)) == 0 && (q.ldc % 4) == 0;
@@ -301,6 +248,121 @@ __global__ void __launch_bounds__(128, 1) tc_rows_kernel(const __grid_constant__
                     *cp = __float2bfloat16_rn(o);
                 }
             }
+        }
+    }
+}
+
+// Persistent: CTA b takes output tiles b, b + gridDim.x, ...  Warp 0 (lane 0) loads the operand tiles
+// of every K block of those tiles into the stage ring; warp 1 (lane 0) issues the MMAs of tile j into
+// TMEM accumulator j % 2 (2 x BN columns) and commits "acc full"; warps 2..5 read an accumulator
+// (warp w reads TMEM lane quarter w % 4), store the tile and arrive on "acc empty", so the next
+// tile's MMAs overlap this tile's stores.
+template <int BN>
+__global__ void __launch_bounds__(192, 1) tc_rows_kernel(const __grid_constant__ TcParams p, const int total_tiles) {
+    constexpr uint32_t TC_TILE_B = tc_tile_b<BN>(), TC_STAGE = tc_stage<BN>(), TC_TMEM_COLS = 2 * BN;
+    constexpr int TC_BN = BN;
+    extern __shared__ unsigned char smem_raw[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t raw = smem_u32(smem_raw);
+    const uint32_t sbase = (raw + 1023u) & ~1023u;  // the swizzle atoms need 1024-byte alignment
+    const uint32_t bars = sbase + TC_STAGES * TC_STAGE;
+    const uint32_t full0 = bars, empty0 = bars + 8u * TC_STAGES;
+    const uint32_t accf0 = bars + 16u * TC_STAGES, acce0 = accf0 + 16u;  // acc full / empty, 2 each
+    const uint32_t tmem_slot = acce0 + 16u;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < TC_STAGES; ++s) {
+            tc_mbar_init(full0 + 8u * s, 1);
+            tc_mbar_init(empty0 + 8u * s, 1);
+        }
+        for (int a = 0; a < 2; ++a) {
+            tc_mbar_init(accf0 + 8u * a, 1);
+            tc_mbar_init(acce0 + 8u * a, 4);  // the 4 epilogue warps
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tmem_slot),
+                     "r"(TC_TMEM_COLS) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    uint32_t tmem;
+    asm volatile("ld.shared.b32 %0, [%1];" : "=r"(tmem) : "r"(tmem_slot) : "memory");
+
+    if (warp == 0) {
+        if (lane == 0) {
+            // producer: operand tiles of every K block of every tile of this CTA
+            int64_t g = 0;  // K blocks issued so far (stage g % STAGES)
+            bool ok = true;
+            for (int t = blockIdx.x; t < total_tiles && ok; t += gridDim.x) {
+                const TcProblem &q = p.prob[tc_problem_of(p, t)];
+                const int local = t - q.tile_begin;
+                const int m0 = (local / q.tiles_n) * TC_BM, n0 = (local % q.tiles_n) * TC_BN;
+                for (int kb = 0; kb < q.kblocks; ++kb, ++g) {
+                    const int s = (int)(g % TC_STAGES);
+                    if (g >= TC_STAGES &&
+                        !tc_wait(empty0 + 8u * s, (uint32_t)(((g / TC_STAGES) - 1) & 1), p.status, 21)) {
+                        ok = false;
+                        break;
+                    }
+                    const uint32_t st = sbase + (uint32_t)s * TC_STAGE;
+                    tc_expect_tx(full0 + 8u * s, TC_STAGE);
+                    tc_tma_2d(st, &q.a_map, kb * TC_BK, m0, full0 + 8u * s);
+                    tc_tma_2d(st + TC_TILE_A, &q.b_map, kb * TC_BK, n0, full0 + 8u * s);
+                }
+            }
+            // before the CTA can finish, every copy issued has landed
+            for (int64_t k = g - TC_STAGES > 0 ? g - TC_STAGES : 0; k < g; ++k)
+                tc_wait(full0 + 8u * (uint32_t)(k % TC_STAGES), (uint32_t)((k / TC_STAGES) & 1), p.status, 22);
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            // MMA issuer
+            constexpr uint32_t idesc = tc_idesc(TC_BM, TC_BN);
+            int64_t g = 0;
+            int j = 0;  // this CTA's tile count
+            bool ok = true;
+            for (int t = blockIdx.x; t < total_tiles && ok; t += gridDim.x, ++j) {
+                const TcProblem &q = p.prob[tc_problem_of(p, t)];
+                const int a = j & 1;
+                if (j >= 2 && !tc_wait(acce0 + 8u * a, (uint32_t)(((j >> 1) - 1) & 1), p.status, 25)) break;
+                tc_fence_after();
+                const uint32_t dacc = tmem + (uint32_t)(a * TC_BN);
+                for (int kb = 0; kb < q.kblocks; ++kb, ++g) {
+                    const int s = (int)(g % TC_STAGES);
+                    if (!tc_wait(full0 + 8u * s, (uint32_t)((g / TC_STAGES) & 1), p.status, 23)) {
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t st = sbase + (uint32_t)s * TC_STAGE;
+#pragma unroll
+                    for (int k = 0; k < TC_BK / 16; ++k)
+                        tc_mma(dacc, tc_desc(st + 32u * k), tc_desc(st + TC_TILE_A + 32u * k), idesc, (kb | k) != 0);
+                    tc_commit(empty0 + 8u * s);  // the stage is free once these MMAs have read it
+                }
+                tc_commit(accf0 + 8u * a);  // accumulator a holds tile j once these MMAs complete
+            }
+        }
+    } else {
+        // epilogue warps 2..5
+        const int quarter = warp & 3;
+        int j = 0;
+        bool ok = true;
+        for (int t = blockIdx.x; t < total_tiles; t += gridDim.x, ++j) {
+            const TcProblem &q = p.prob[tc_problem_of(p, t)];
+            const int local = t - q.tile_begin;
+            const int m0 = (local / q.tiles_n) * TC_BM, n0 = (local % q.tiles_n) * TC_BN;
+            const int a = j & 1;
+            ok = ok && __all_sync(0xffffffffu, tc_wait(accf0 + 8u * a, (uint32_t)((j >> 1) & 1), p.status, 24));
+            tc_fence_after();
+            if (!ok) break;
+            tc_store_tile<BN>(q, m0, n0, quarter, lane, tmem + (uint32_t)(a * TC_BN), ok);  // adds the lane quarter
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive_tc(acce0 + 8u * a);
         }
     }
     tc_fence_before();
@@ -476,6 +538,9 @@ int dense_rows_batched_impl(const spreg_dense_rows_item *items, int32_t count, c
                                         (int)tc_smem<256>()));
         configured[dev] = true;
     }
+    static int sms_of[64] = {};
+    if (dev >= 0 && dev < 64 && !sms_of[dev]) SPREG_CUDA(cudaDeviceGetAttribute(&sms_of[dev], cudaDevAttrMultiProcessorCount, dev));
+    const int sms = (dev >= 0 && dev < 64 && sms_of[dev] > 0) ? sms_of[dev] : 148;
     char *scratch = nullptr;
     SPREG_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&scratch), (size_t)(tab_base + (int64_t)tab.size() + 16),
                                stream));
@@ -549,8 +614,9 @@ int dense_rows_batched_impl(const spreg_dense_rows_item *items, int32_t count, c
             fail(0);
             SPREG_FAIL(SPREG_ERR_UNSUPPORTED, "too many output tiles in one launch");
         }
-        if (bn == 256) tc_rows_kernel<256><<<(unsigned)tiles, 128, tc_smem<256>(), stream>>>(p);
-        else tc_rows_kernel<128><<<(unsigned)tiles, 128, tc_smem<128>(), stream>>>(p);
+        const unsigned grid = (unsigned)std::min<int64_t>(tiles, sms);
+        if (bn == 256) tc_rows_kernel<256><<<grid, 192, tc_smem<256>(), stream>>>(p, (int)tiles);
+        else tc_rows_kernel<128><<<grid, 192, tc_smem<128>(), stream>>>(p, (int)tiles);
         e = cudaGetLastError();
         if (e != cudaSuccess) {
             fail(0);
