@@ -382,20 +382,45 @@ struct TransposeItem {
 };
 
 // All B of a batched call in one launch: Bt[j][k] = B[k][j] for k < K (zero up to K8), j < n, in
-// 32 x 32 tiles through shared memory; blockIdx.z picks the item, x / y its tile.
-__global__ void transpose_items_kernel(const TransposeItem *__restrict__ items) {
+// 64 x 64 tiles through shared memory; blockIdx.z picks the item, x / y its tile.  Rows of B are
+// read 16 bytes at a time when they are 16-byte aligned, rows of Bt are written 16 bytes at a time
+// (K8 and the tile's K offset are multiples of 8).
+__global__ void __launch_bounds__(256) transpose_items_kernel(const TransposeItem *__restrict__ items) {
     const TransposeItem it = items[blockIdx.z];
-    const int k0 = blockIdx.x * 32, j0 = blockIdx.y * 32;
+    const int k0 = blockIdx.x * 64, j0 = blockIdx.y * 64;
     if (k0 >= it.K8 || j0 >= it.n) return;  // uniform per block
-    __shared__ __nv_bfloat16 tile[32][33];
-    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
-        const int k = k0 + i, j = j0 + threadIdx.x;
-        tile[i][threadIdx.x] = (k < it.k && j < it.n) ? it.b[(int64_t)k * it.ldb + j] : __float2bfloat16_rn(0.0f);
+    __shared__ uint16_t tile[64][66];        // [k][j]; a 33-word row stride spreads the column reads
+    const uint16_t *B = reinterpret_cast<const uint16_t *>(it.b);
+    const bool vec_in = ((reinterpret_cast<uintptr_t>(B) | (uintptr_t)(it.ldb * 2)) % 16) == 0;
+    for (int c = threadIdx.x; c < 512; c += 256) {
+        const int kr = c >> 3, jc = (c & 7) * 8;
+        const int k = k0 + kr, j = j0 + jc;
+        uint16_t v[8];
+        if (k < it.k && vec_in && j + 8 <= it.n) {
+            const uint4 w = *reinterpret_cast<const uint4 *>(B + (int64_t)k * it.ldb + j);
+            const uint32_t ws[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                v[2 * e] = (uint16_t)(ws[e] & 0xFFFFu);
+                v[2 * e + 1] = (uint16_t)(ws[e] >> 16);
+            }
+        } else {
+#pragma unroll
+            for (int e = 0; e < 8; ++e) v[e] = (k < it.k && j + e < it.n) ? B[(int64_t)k * it.ldb + j + e] : (uint16_t)0;
+        }
+#pragma unroll
+        for (int e = 0; e < 8; ++e) tile[kr][jc + e] = v[e];
     }
     __syncthreads();
-    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
-        const int j = j0 + i, k = k0 + threadIdx.x;
-        if (j < it.n && k < it.K8) it.dst[(int64_t)j * it.K8 + k] = tile[threadIdx.x][i];
+    uint16_t *D = reinterpret_cast<uint16_t *>(it.dst);
+    for (int c = threadIdx.x; c < 512; c += 256) {
+        const int jr = c >> 3, kc = (c & 7) * 8;
+        const int j = j0 + jr, k = k0 + kc;
+        if (j >= it.n || k >= it.K8) continue;  // k + 8 <= K8: both are multiples of 8
+        uint32_t w[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) w[e] = (uint32_t)tile[kc + 2 * e][jr] | ((uint32_t)tile[kc + 2 * e + 1][jr] << 16);
+        *reinterpret_cast<uint4 *>(D + (int64_t)j * it.K8 + k) = make_uint4(w[0], w[1], w[2], w[3]);
     }
 }
 
@@ -518,8 +543,8 @@ int dense_rows_batched_impl(const spreg_dense_rows_item *items, int32_t count, c
             ti.K8 = (int32_t)K8;
             ti.pad = 0;
             titems.push_back(ti);
-            max_kt = std::max<int64_t>(max_kt, (K8 + 31) / 32);
-            max_nt = std::max<int64_t>(max_nt, (it.n + 31) / 32);
+            max_kt = std::max<int64_t>(max_kt, (K8 + 63) / 64);
+            max_nt = std::max<int64_t>(max_nt, (it.n + 63) / 64);
             o += it.n;
         }
     }
@@ -563,7 +588,7 @@ int dense_rows_batched_impl(const spreg_dense_rows_item *items, int32_t count, c
     memcpy(tab.data() + titem_off, titems.data(), titems.size() * sizeof(TransposeItem));
     cudaError_t e = cudaMemcpyAsync(scratch + tab_base, tab.data(), tab.size(), cudaMemcpyHostToDevice, stream);
     if (e == cudaSuccess) {
-        transpose_items_kernel<<<dim3((unsigned)max_kt, (unsigned)max_nt, (unsigned)titems.size()), dim3(32, 8), 0,
+        transpose_items_kernel<<<dim3((unsigned)max_kt, (unsigned)max_nt, (unsigned)titems.size()), 256, 0,
                                  stream>>>(reinterpret_cast<const TransposeItem *>(scratch + tab_base + titem_off));
         e = cudaGetLastError();
     }
