@@ -95,9 +95,10 @@ def bench_mapping(args, A0):
 
 def make_inputs(args, rank: int):
     from spreg import synth
+    from spreg.replicas import shard_seed
     As, Bs = [], []
     for r in range(args.replicas):
-        seed = 1000 * (rank + 1) + r
+        seed = shard_seed(rank, r)
         As.append(synth.row_skew(args.m, args.k, args.sparsity, seed=seed, sigma=0.5, std=0.02))
         Bs.append(synth.dense(args.k, args.n, seed=seed + 500000))
     return As, Bs
@@ -544,6 +545,7 @@ def main():
 
     from oracle import oracle as O
     from spreg import Mapping, MatMulSpecialized, PackedMatrix, TileConfig, synth
+    from spreg.replicas import max_over_ranks, whole_job_rate
 
     As, Bs = make_inputs(args, rank)
     m = bench_mapping(args, As[0])
@@ -612,15 +614,12 @@ def main():
         ev1.record(stream)
         torch.cuda.synchronize()
         clk.mark_end()
-    ms = ev0.elapsed_time(ev1)
+    ms = max_over_ranks(ev0.elapsed_time(ev1), dev)  # replicas: the job takes as long as its slowest rank
     if ws > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
         torch.distributed.barrier()
     sec = ms / 1e3
-    value = step_bytes * args.steps * ws / sec / 1e9
-    gflops = step_flops * args.steps * ws / sec / 1e9
+    value = whole_job_rate(step_bytes, args.steps, ws, ms) / 1e9
+    gflops = whole_job_rate(step_flops, args.steps, ws, ms) / 1e9
     ms_per_step = ms / args.steps
 
     # roofline of the executor kernel (one launch per replica per step)
@@ -655,24 +654,26 @@ def main():
     e2e_ok = bool(np.array_equal(Ch[0].numpy(), ref0.execute(Bs[0]))) if (parity_ok and e2e_n) else False
     e2e_steps = max(2, args.steps // 4)
     torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         for mm, B, C in zip(mms, Bh, Ch):
             mm(C, B)
-    e2e_sec = time.perf_counter() - t0
-    e2e_bytes = sum(bytes_per[:e2e_n]) * e2e_steps
-    e2e = {"value": e2e_bytes / e2e_sec / 1e9 if e2e_n else None, "unit": UNIT,
+    e2e_ms = max_over_ranks((time.perf_counter() - t0) * 1e3, dev)
+    e2e = {"value": whole_job_rate(sum(bytes_per[:e2e_n]), e2e_steps, ws, e2e_ms) / 1e9 if e2e_n else None,
+           "unit": UNIT,
            "h2d_bytes_per_step": e2e_n * args.k * args.n * 4, "d2h_bytes_per_step": e2e_n * args.m * args.n * 4,
            "path": "spreg_matmul_run (host B in, host C out, synchronous per SpMM)", "replicas_per_step": e2e_n,
            "bit_exact_vs_oracle": e2e_ok}
     del mms
 
-    serving = None
-    if args.serving:
-        serving = serving_bench(args, dev)
-    precision = precision_suite(dev) if args.precision else None
-    tensor_cores = tensor_core_suite(dev) if args.tensor_cores else None
-    layers = layers_suite(dev) if args.layers else None
+    # the secondary legs describe one GPU: rank 0 alone runs them, the other ranks are done
+    lead = rank == 0
+    serving = serving_bench(args, dev) if (lead and args.serving) else None
+    precision = precision_suite(dev) if (lead and args.precision) else None
+    tensor_cores = tensor_core_suite(dev) if (lead and args.tensor_cores) else None
+    layers = layers_suite(dev) if (lead and args.layers) else None
 
     cpu = None
     if rank == 0 and args.cpu_seconds > 0:
