@@ -196,6 +196,33 @@ def load_traffic(key: str, spmms_per_launch: int):
     return None if not e else e["dram_bytes_per_spmm"] * spmms_per_launch
 
 
+def smem_roofline(packs, n: int, bsz: int, k_tile: int, spmm_s: float, sm_mhz, sms: int = 152, warps: int = 15):
+    """Shared-memory roofline of the B-tile executor (the bound it actually meets at FP32).
+
+    Per SpMM the consumers read, for every packed entry (panel, column) and every strip of
+    32 * NV columns, one B row segment of 32 * NV * bsz bytes out of shared memory, and the tensor
+    copies write each K tile's strip of B once per job (W panels).  The peak is 128 bytes per clock
+    per SM at the sampled SM clock.
+    """
+    if not sm_mhz or not k_tile:
+        return None
+    nv = 4 if n >= 128 else (2 if n >= 64 else 1)
+    strip = 32 * nv
+    strips = -(-n // strip)
+    gathers = fills = 0
+    for p in packs:
+        i = p.info
+        tiles = -(-(i["cols"]) // k_tile)
+        gathers += i["num_col_indices"] * strips * strip * bsz
+        fills += -(-(i["num_panels"]) // warps) * strips * tiles * k_tile * strip * bsz
+    per_spmm = (gathers + fills) / len(packs)
+    peak = sms * 128 * sm_mhz * 1e6 / 1e9
+    achieved = per_spmm / spmm_s / 1e9
+    return {"bound": "shared memory", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "bytes_per_spmm": per_spmm, "gather_bytes_per_spmm": gathers / len(packs),
+            "fill_bytes_per_spmm": fills / len(packs), "peak_basis": f"{sms} SMs x 128 B/clk at {sm_mhz:.0f} MHz"}
+
+
 def measured_peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -679,6 +706,9 @@ def main():
     if rank == 0 and args.cpu_seconds > 0:
         cpu = cpu_baseline(As, Bs, args, args.cpu_seconds, mapping=m)
 
+    clocks = clk.summary()
+    if args.staging == 1:
+        roofline["smem"] = smem_roofline(packs, args.n, bsz, args.k_tile, spmm_us / 1e6, clocks.get("sm_mhz"))
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
@@ -695,7 +725,7 @@ def main():
                            "parallelism": f"replicas x{ws}"},
                 "gflops": gflops, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "serving": serving,
                 "precision": precision, "batched_layers": layers, "tensor_cores": tensor_cores,
-                "clocks": clk.summary(), "gpu_launches": launches_per_step * args.steps,
+                "clocks": clocks, "gpu_launches": launches_per_step * args.steps,
                 "parity_bit_exact_vs_oracle": parity_ok}
         print(json.dumps(line))
     if ws > 1:
