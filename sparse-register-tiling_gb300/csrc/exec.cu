@@ -280,6 +280,7 @@ int plan_call(const spreg_packed *a, const spreg_exec_args *args, CallPlan *cp) 
     XProblem base = {};
     base.exec = a->exec;
     base.exec_offs = a->exec_offs;
+    base.panel_rank = a->panel_rank;
     base.scales = a->scales;
     base.B = args->b;
     base.C = args->c;
@@ -320,6 +321,7 @@ int plan_call(const spreg_packed *a, const spreg_exec_args *args, CallPlan *cp) 
         TProblem tb = {};
         tb.exec = a->exec;
         tb.exec_offs = a->exec_offs;
+        tb.panel_order = a->panel_order;
         tb.scales = a->scales;
         tb.B = args->b;
         tb.C = args->c;
@@ -472,9 +474,8 @@ int launch_tile_groups(std::map<std::tuple<int, int, int>, TileGroup> &groups, c
             for (size_t i = 0; i < cnt; ++i) {
                 TProblem &pr = tp.prob[i];
                 pr = g.probs[first + i];
-                pr.groups = (pr.P + W - 1) / W;
                 pr.job_begin = jobs;
-                jobs += (int64_t)pr.groups * pr.S;
+                jobs += (int64_t)((pr.P + W - 1) / W) * pr.S;
             }
             if (jobs == 0) continue;
             SPREG_CHECK_ARG(jobs <= INT32_MAX, "too many jobs in one launch");

@@ -770,7 +770,7 @@ constexpr int kMaxBatchProblems = 224;
 
 struct XProblem {
     const uint8_t *exec;        // execution layout of the packed matrix
-    const int64_t *exec_offs;   // units + 1 block offsets
+    const int64_t *exec_offs;   // units + 1 block offsets in slot order (exec_slot)
     const float *scales;        // per-row-panel F16 scales (else null)
     const void *B;
     void *C;
@@ -779,8 +779,10 @@ struct XProblem {
     int64_t col_end;            // columns >= col_end are not computed (NV = 1 tails)
     int64_t item_begin;         // first global item
     int32_t P, S, T, ppt;       // row panels, strips, K tiles, panels per row tile
-    int32_t load_c, epilogue, pad0, pad1;
+    int32_t load_c, epilogue;
+    const int32_t *panel_rank;  // panel -> position in the work order (exec_slot)
 };
+static_assert(sizeof(XProblem) == 120, "XProblem layout");
 
 struct BatchParams {
     int *counter;               // work counter, zero at launch
@@ -822,9 +824,9 @@ __device__ __forceinline__ XJob next_job(const BatchParams &bp, const XJob &j, i
 __device__ __forceinline__ void issue_job(const BatchParams &bp, const XJob &j, uint32_t buf, uint32_t bar, int lane) {
     if (lane == 0 && j.pi >= 0) {
         const XProblem &pr = bp.prob[j.pi];
-        const int64_t u = unit_index(j.gp, j.t, pr.ppt, pr.T, pr.P);
-        const int64_t off = pr.exec_offs[u];
-        const uint32_t bytes = (uint32_t)(pr.exec_offs[u + 1] - off);
+        const int64_t slot = exec_slot(j.gp, j.t, pr.P, pr.panel_rank);
+        const int64_t off = pr.exec_offs[slot];
+        const uint32_t bytes = (uint32_t)(pr.exec_offs[slot + 1] - off);
         fence_proxy_async_smem();
         mbar_arrive_expect_tx(bar, bytes);
         bulk_copy_g2s(buf, pr.exec + off, bytes, bar);

@@ -14,6 +14,10 @@
 // the same ring, so the producer fetches the next job's first tile while consumers finish the
 // last tile of the current one.
 //
+// The W panels of a job are consecutive in the pack's work order (panels by descending work), so
+// a job's warps finish each K tile at about the same time and the stage is refilled without a
+// long wait on the slowest warp; their execution blocks of one K tile are adjacent in memory.
+//
 // B rows are read from L2 once per job instead of once per packed entry: for the W panels of a
 // job a B row is copied once, while the gathers of exec_batch_kernel fetch it once per entry
 // that references it (about W * (1 - sparsity^M_r) times).  Per output element the FMA chain is
@@ -38,7 +42,8 @@ constexpr int kTileBoxRows = 256;    // rows of one tensor copy (TMA box limit)
 
 struct TProblem {
     const uint8_t *exec;        // execution layout of the packed matrix
-    const int64_t *exec_offs;   // units + 1 block offsets
+    const int64_t *exec_offs;   // units + 1 block offsets in slot order (exec_slot)
+    const int32_t *panel_order; // panels by descending work: job group g runs panel_order[g * W + w] on warp w
     const float *scales;        // per-row-panel F16 scales (else null)
     const void *B;
     void *C;
@@ -49,8 +54,8 @@ struct TProblem {
     int32_t P, S, T, ppt;       // row panels, strips, K tiles, panels per row tile
     int32_t load_c, epilogue;
     int32_t kt, krows;          // B rows per K tile, B rows of all tiles (columns of A)
-    int32_t col_offset, groups; // first B row of tile 0; panel groups of W panels
-    int32_t box_rows, pad0;     // rows of one tensor copy (K tile copied in ceil(kt / box_rows) copies)
+    int32_t col_offset;         // first B row of tile 0
+    int32_t box_rows;           // rows of one tensor copy (K tile copied in ceil(kt / box_rows) copies)
     CUtensorMap tmap;           // B as a 2-D tensor: columns [0, col_end) x rows [0, col_offset + krows)
 };
 static_assert(sizeof(TProblem) == 256 && offsetof(TProblem, tmap) == 128, "TProblem layout");
@@ -249,12 +254,12 @@ __global__ void __launch_bounds__(32 * (kTileMaxWarps + 1), 1) exec_tile_kernel(
             // metadata: lane w < W holds the block of unit (group * W + w, t)
             int64_t moff = 0;
             uint32_t mbytes = 0;
-            const int64_t gp = (int64_t)group * W + lane;
-            const bool act = lane < W && gp < pr.P;
+            const int64_t pos = (int64_t)group * W + lane;  // position in the work order
+            const bool act = lane < W && pos < pr.P;
             if (act) {
-                const int64_t u = unit_index(gp, t, pr.ppt, pr.T, pr.P);
-                moff = pr.exec_offs[u];
-                mbytes = (uint32_t)(pr.exec_offs[u + 1] - moff);
+                const int64_t slot = (int64_t)t * pr.P + pos;
+                moff = pr.exec_offs[slot];
+                mbytes = (uint32_t)(pr.exec_offs[slot + 1] - moff);
             }
             const int nact = __popc(__ballot_sync(0xffffffffu, act));  // active lanes are 0 .. nact - 1
             const int64_t m0 = __shfl_sync(0xffffffffu, moff, 0);
@@ -300,9 +305,10 @@ __global__ void __launch_bounds__(32 * (kTileMaxWarps + 1), 1) exec_tile_kernel(
         const int4 ji = lds_v4(jobs0 + 16u * s);
         if (ji.x < 0) break;
         const TProblem &pr = tp.prob[ji.x];
-        const int64_t gp = (int64_t)ji.y * W + warp;
+        const int64_t pos = (int64_t)ji.y * W + warp;
         const int t = ji.w;
-        if (gp < pr.P) {
+        if (pos < pr.P) {
+            const int64_t gp = pr.panel_order[pos];
             const int64_t row0 = gp * MR;
             const int64_t col0 = pr.col_begin + (int64_t)ji.z * (32 * NV) + (int64_t)lane * NV;
             const bool valid = col0 < pr.col_end;

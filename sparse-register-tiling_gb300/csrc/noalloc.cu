@@ -158,6 +158,7 @@ extern "C" int spreg_execute_batched_noalloc(const spreg_work_item *items, int32
         XProblem base = {};
         base.exec = a->exec;
         base.exec_offs = a->exec_offs;
+        base.panel_rank = a->panel_rank;
         base.scales = a->scales;
         base.B = args->b;
         base.C = args->c;

@@ -13,6 +13,7 @@
 //                popcount.  Values of an entry are written in ascending row order (template:192-207).
 #include "spreg_common.cuh"
 
+#include <algorithm>
 #include <vector>
 
 namespace spreg {
@@ -266,8 +267,7 @@ __global__ void __launch_bounds__(1024) layout_kernel(const int64_t units, const
                                                       const int64_t ppt, const int64_t T, const int64_t P,
                                                       const UnitStats *__restrict__ stats,
                                                       const unsigned long long *__restrict__ tile_nnz,
-                                                      spreg_panel_desc *__restrict__ descs, PackTotals *tot,
-                                                      int64_t *__restrict__ exec_offs) {
+                                                      spreg_panel_desc *__restrict__ descs, PackTotals *tot) {
     __shared__ long long s_scan[1024];
     __shared__ long long s_xscan[1024];
     __shared__ long long s_carry, s_xcarry;
@@ -306,7 +306,6 @@ __global__ void __launch_bounds__(1024) layout_kernel(const int64_t units, const
             s_xscan[t] += xadd;
             __syncthreads();
         }
-        if (u < units) exec_offs[u] = s_xcarry + s_xscan[t] - xsize;
         if (u < units) {
             const long long off = s_carry + s_scan[t] - size;
             spreg_panel_desc d;
@@ -352,8 +351,61 @@ __global__ void __launch_bounds__(1024) layout_kernel(const int64_t units, const
         tot->empty_units = (long long)s_acc[5];
         tot->exec_bytes = s_xcarry;
         tot->max_exec_bytes = (long long)s_acc[7];
-        exec_offs[units] = s_xcarry;
     }
+}
+
+// Work estimate of each row panel over its K tiles: the executor's cost per entry (index, B row
+// load, loop), per value (FMA) and per nanokernel group (record, dispatch).
+__global__ void panel_work_kernel(const int64_t P, const int64_t T, const int64_t ppt,
+                                  const UnitStats *__restrict__ stats, int64_t *__restrict__ work) {
+    const int64_t gp = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gp >= P) return;
+    int64_t w = 0;
+    for (int64_t t = 0; t < T; ++t) {
+        const UnitStats st = stats[unit_index(gp, t, ppt, T, P)];
+        w += 3 * (int64_t)st.num_cols + st.num_values + 8 * (int64_t)st.num_groups;
+    }
+    work[gp] = w;
+}
+
+// Offsets of the execution blocks in slot order (exec_slot): exec_offs[slot] for the executors,
+// unit_xoff[unit] for the emit kernels.
+__global__ void __launch_bounds__(1024) exec_slots_kernel(const int64_t units, const int64_t P, const int64_t T,
+                                                          const int64_t ppt, const int32_t *__restrict__ order,
+                                                          const UnitStats *__restrict__ stats,
+                                                          int64_t *__restrict__ exec_offs,
+                                                          int64_t *__restrict__ unit_xoff) {
+    __shared__ long long s_scan[1024];
+    __shared__ long long s_carry;
+    const int t = threadIdx.x;
+    if (t == 0) s_carry = 0;
+    __syncthreads();
+    for (int64_t base = 0; base < units; base += 1024) {
+        const int64_t s = base + t;
+        int64_t u = -1;
+        long long xsize = 0;
+        if (s < units) {
+            u = unit_index(order[s % P], s / P, ppt, T, P);
+            xsize = stats[u].exec_bytes;
+        }
+        s_scan[t] = xsize;
+        __syncthreads();
+        for (int o = 1; o < 1024; o <<= 1) {
+            const long long add = t >= o ? s_scan[t - o] : 0;
+            __syncthreads();
+            s_scan[t] += add;
+            __syncthreads();
+        }
+        if (u >= 0) {
+            const long long off = s_carry + s_scan[t] - xsize;
+            exec_offs[s] = off;
+            unit_xoff[u] = off;
+        }
+        __syncthreads();
+        if (t == 0) s_carry += s_scan[1023];
+        __syncthreads();
+    }
+    if (t == 0) exec_offs[units] = s_carry;
 }
 
 // Power-of-two F16 scale per row panel: 2^e with max|v| = m * 2^e, m in [0.5, 1); 1 if max is 0.
@@ -785,8 +837,12 @@ struct Scratch {
     unsigned long long *tile_nnz = nullptr;
     PackTotals *totals = nullptr;
     DevError *err = nullptr;
+    int64_t *panel_work = nullptr;  // P work estimates
+    int64_t *unit_xoff = nullptr;   // units execution-block offsets by unit
     cudaStream_t s = nullptr;
     ~Scratch() {
+        if (panel_work) cudaFreeAsync(panel_work, s);
+        if (unit_xoff) cudaFreeAsync(unit_xoff, s);
         if (unit_counts) cudaFreeAsync(unit_counts, s);
         if (stats) cudaFreeAsync(stats, s);
         if (panel_maxabs) cudaFreeAsync(panel_maxabs, s);
@@ -817,6 +873,8 @@ void release(spreg_packed *p) {
     if (p->scales) cudaFree(p->scales);
     if (p->exec) cudaFree(p->exec);
     if (p->exec_offs) cudaFree(p->exec_offs);
+    if (p->panel_order) cudaFree(p->panel_order);
+    if (p->panel_rank) cudaFree(p->panel_rank);
     delete p;
 }
 
@@ -834,9 +892,15 @@ int finish_pack(const spreg_mapping *m, const Geom &g, int value_dtype, int64_t 
     const int64_t units = g.units;
     cudaError_t e = cudaMalloc(&p->descs, (size_t)(units > 0 ? units : 1) * sizeof(spreg_panel_desc));
     if (e == cudaSuccess) e = cudaMalloc(&p->exec_offs, (size_t)(units + 1) * sizeof(int64_t));
+    if (e == cudaSuccess) e = cudaMalloc(&p->panel_order, (size_t)(g.P > 0 ? g.P : 1) * sizeof(int32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&p->panel_rank, (size_t)(g.P > 0 ? g.P : 1) * sizeof(int32_t));
     if (e != cudaSuccess) { release(p); SPREG_FAIL(SPREG_ERR_NOMEM, "cudaMalloc(descs): %s", cudaGetErrorString(e)); }
-    layout_kernel<<<1, 1024, 0, stream>>>(units, nk, vb, g.ppt, g.T, g.P, sc.stats, sc.tile_nnz, p->descs, sc.totals,
-                                          p->exec_offs);
+    layout_kernel<<<1, 1024, 0, stream>>>(units, nk, vb, g.ppt, g.T, g.P, sc.stats, sc.tile_nnz, p->descs, sc.totals);
+    std::vector<int64_t> work((size_t)g.P);
+    if (g.P > 0) {
+        panel_work_kernel<<<(unsigned)((g.P + 255) / 256), 256, 0, stream>>>(g.P, g.T, g.ppt, sc.stats, sc.panel_work);
+        cudaMemcpyAsync(work.data(), sc.panel_work, (size_t)g.P * sizeof(int64_t), cudaMemcpyDeviceToHost, stream);
+    }
     PackTotals tot;
     DevError derr;
     cudaMemcpyAsync(&tot, sc.totals, sizeof tot, cudaMemcpyDeviceToHost, stream);
@@ -848,6 +912,26 @@ int finish_pack(const spreg_mapping *m, const Geom &g, int value_dtype, int64_t 
         SPREG_FAIL(SPREG_ERR_CHECK, "packer check failed at unit %d (value %d): %s", derr.unit, derr.value,
                    dev_error_text(derr.code));
     }
+    // Panels by descending work (ties by index): the tile executor gives consecutive panels of this
+    // order to the warps of one job, so a job's warps finish their K tiles at about the same time.
+    {
+        std::vector<int32_t> order((size_t)g.P), rank((size_t)g.P);
+        for (int64_t i = 0; i < g.P; ++i) order[(size_t)i] = (int32_t)i;
+        std::stable_sort(order.begin(), order.end(),
+                         [&](int32_t x, int32_t y) { return work[(size_t)x] > work[(size_t)y]; });
+        for (int64_t i = 0; i < g.P; ++i) rank[(size_t)order[(size_t)i]] = (int32_t)i;
+        if (g.P > 0) {
+            e = cudaMemcpyAsync(p->panel_order, order.data(), (size_t)g.P * sizeof(int32_t), cudaMemcpyHostToDevice,
+                                stream);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(p->panel_rank, rank.data(), (size_t)g.P * sizeof(int32_t), cudaMemcpyHostToDevice,
+                                    stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(stream);  // the host vectors end with this scope
+            if (e != cudaSuccess) { release(p); SPREG_FAIL(SPREG_ERR_CUDA, "panel order: %s", cudaGetErrorString(e)); }
+        }
+    }
+    exec_slots_kernel<<<1, 1024, 0, stream>>>(units, g.P, g.T, g.ppt, p->panel_order, sc.stats, p->exec_offs,
+                                              sc.unit_xoff);
     const int64_t arena_bytes = tot.arena_bytes;
     e = cudaMalloc(&p->arena, (size_t)(arena_bytes > 0 ? arena_bytes : 64));
     if (e != cudaSuccess) { release(p); SPREG_FAIL(SPREG_ERR_NOMEM, "cudaMalloc(arena %lld B): %s", (long long)arena_bytes, cudaGetErrorString(e)); }
@@ -900,6 +984,8 @@ int alloc_scratch(Scratch &sc, const Geom &g, int nk, int64_t tiles, cudaStream_
     SPREG_CUDA(cudaMallocAsync(&sc.tile_nnz, (size_t)(tiles > 0 ? tiles : 1) * sizeof(unsigned long long), stream));
     SPREG_CUDA(cudaMallocAsync(&sc.totals, sizeof(PackTotals), stream));
     SPREG_CUDA(cudaMallocAsync(&sc.err, sizeof(DevError), stream));
+    SPREG_CUDA(cudaMallocAsync(&sc.panel_work, (size_t)(g.P > 0 ? g.P : 1) * sizeof(int64_t), stream));
+    SPREG_CUDA(cudaMallocAsync(&sc.unit_xoff, (size_t)units * sizeof(int64_t), stream));
     SPREG_CUDA(cudaMemsetAsync(sc.panel_maxabs, 0, (size_t)(g.P > 0 ? g.P : 1) * sizeof(unsigned), stream));
     SPREG_CUDA(cudaMemsetAsync(sc.tile_nnz, 0, (size_t)(tiles > 0 ? tiles : 1) * sizeof(unsigned long long), stream));
     SPREG_CUDA(cudaMemsetAsync(sc.err, 0, sizeof(DevError), stream));
@@ -948,13 +1034,13 @@ int pack_columns(const spreg_mapping *m, const Geom &g, const Loader &ld, const 
     auto emit = [&](spreg_packed *p) {
         if (value_dtype == SPREG_F32)
             emit_cols_kernel<Loader, float><<<(unsigned)g.units, CH, 0, stream>>>(
-                g, ld, mt, sc.unit_counts, p->descs, p->arena, nullptr, col_offset, p->exec, p->exec_offs);
+                g, ld, mt, sc.unit_counts, p->descs, p->arena, nullptr, col_offset, p->exec, sc.unit_xoff);
         else if (value_dtype == SPREG_BF16)
             emit_cols_kernel<Loader, __nv_bfloat16><<<(unsigned)g.units, CH, 0, stream>>>(
-                g, ld, mt, sc.unit_counts, p->descs, p->arena, nullptr, col_offset, p->exec, p->exec_offs);
+                g, ld, mt, sc.unit_counts, p->descs, p->arena, nullptr, col_offset, p->exec, sc.unit_xoff);
         else
             emit_cols_kernel<Loader, __half><<<(unsigned)g.units, CH, 0, stream>>>(
-                g, ld, mt, sc.unit_counts, p->descs, p->arena, p->scales, col_offset, p->exec, p->exec_offs);
+                g, ld, mt, sc.unit_counts, p->descs, p->arena, p->scales, col_offset, p->exec, sc.unit_xoff);
     };
     return finish_pack(m, g, value_dtype, col_offset, o ? o->m_tile : 0, o ? o->k_tile : 0, sc, mt, emit, out, stream);
 }
@@ -1040,13 +1126,13 @@ int pack_lists_impl(const spreg_mapping *m, int64_t rows, int64_t cols, int64_t 
     auto emit = [&](spreg_packed *p) {
         if (value_dtype == SPREG_F32)
             emit_list_kernel<float><<<(unsigned)num_panels, CH, 0, stream>>>(src, mt, sc.unit_counts, p->descs,
-                                                                              p->arena, nullptr, p->exec, p->exec_offs);
+                                                                              p->arena, nullptr, p->exec, sc.unit_xoff);
         else if (value_dtype == SPREG_BF16)
             emit_list_kernel<__nv_bfloat16><<<(unsigned)num_panels, CH, 0, stream>>>(
-                src, mt, sc.unit_counts, p->descs, p->arena, nullptr, p->exec, p->exec_offs);
+                src, mt, sc.unit_counts, p->descs, p->arena, nullptr, p->exec, sc.unit_xoff);
         else
             emit_list_kernel<__half><<<(unsigned)num_panels, CH, 0, stream>>>(src, mt, sc.unit_counts, p->descs,
-                                                                               p->arena, p->scales, p->exec, p->exec_offs);
+                                                                               p->arena, p->scales, p->exec, sc.unit_xoff);
     };
     st = finish_pack(m, g, value_dtype, 0, 0, 0, sc, mt, emit, out, stream);
     if (st == SPREG_OK && *out) (*out)->list_packed = true;
@@ -1098,7 +1184,7 @@ int pack_from_arena_impl(const spreg_mapping *m, const spreg_arena_geom *ag, con
     }
     auto emit = [&](spreg_packed *p) {
         arena_emit_kernel<<<(unsigned)g.units, CH, 0, stream>>>(mt, src, sdesc, sc.unit_counts, p->descs, p->arena,
-                                                                p->exec, p->exec_offs, vb, sc.err);
+                                                                p->exec, sc.unit_xoff, vb, sc.err);
     };
     spreg_packed *p = nullptr;
     st = finish_pack(m, g, ag->value_dtype, ag->col_offset, ag->m_tile, ag->k_tile, sc, mt, emit, &p, stream);

@@ -77,6 +77,12 @@ __host__ __device__ inline int64_t unit_index(int64_t gp, int64_t tj, int64_t pp
     return p_lo * T + tj * n_in + (gp - p_lo);
 }
 
+// Execution blocks lie in slot order: K tile major, then panels by descending work (panel_rank),
+// so the blocks of consecutive panels in that order at one K tile are adjacent in memory.
+__host__ __device__ inline int64_t exec_slot(int64_t gp, int64_t tj, int64_t P, const int32_t *panel_rank) {
+    return tj * P + panel_rank[gp];
+}
+
 // Inverse of unit_index: unit -> (global panel, K tile).
 __host__ __device__ inline void unit_coords(int64_t u, int64_t ppt, int64_t T, int64_t P, int64_t *gp, int64_t *tj) {
     const int64_t per_tile = ppt * T;
@@ -179,7 +185,9 @@ struct spreg_packed {
     float *scales = nullptr;
     uint8_t id_to_pattern[256] = {};
     uint8_t *exec = nullptr;        // execution layout (derived from the arena by the packer)
-    int64_t *exec_offs = nullptr;   // units + 1 block offsets
+    int64_t *exec_offs = nullptr;   // units + 1 block offsets, in slot order (exec_slot)
+    int32_t *panel_order = nullptr; // P panels by descending work: slot t * P + i holds unit (panel_order[i], t)
+    int32_t *panel_rank = nullptr;  // inverse of panel_order
     int64_t exec_bytes = 0;
     int64_t max_exec_bytes = 0;
     bool list_packed = false;       // packed panel by panel (per-panel column offsets, no K tiles)
