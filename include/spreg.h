@@ -289,6 +289,14 @@ int spreg_matmul_create(int32_t m, int32_t k, int32_t n, const float *values_hos
 int spreg_matmul_allocate_executor(spreg_matmul *mm, int32_t n);
 /* operator()(C, B) with HOST buffers: copy B in, C = A.B, copy C out (synchronous). */
 int spreg_matmul_run(spreg_matmul *mm, float *c_host, const float *b_host);
+/* operator()(C, B) with HOST buffers, enqueued on the matmul's own stream without waiting: the copy in,
+ * the product and the copy out run in order there, overlapping other matmuls' copies and products.
+ * b_host and c_host must stay valid until spreg_matmul_sync; pinned buffers make the copies
+ * asynchronous (pageable ones are staged synchronously by the driver).  Same result as
+ * spreg_matmul_run. */
+int spreg_matmul_run_async(spreg_matmul *mm, float *c_host, const float *b_host);
+/* Wait for every call enqueued on the matmul's stream; then c_host of those calls holds C. */
+int spreg_matmul_sync(spreg_matmul *mm);
 /* Same on device buffers (ldb = ldc = n), asynchronous on `stream`. */
 int spreg_matmul_run_device(spreg_matmul *mm, float *c, const float *b, spreg_stream_t stream);
 int spreg_matmul_get_config(const spreg_matmul *mm, spreg_tile_config *cfg);

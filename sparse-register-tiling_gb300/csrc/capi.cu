@@ -483,8 +483,7 @@ static int matmul_exec(spreg_matmul *mm, float *c, const float *b, cudaStream_t 
     return execute_impl(mm->packed, &a, s);
 }
 
-int spreg_matmul_run(spreg_matmul *mm, float *c_host, const float *b_host) {
-    clear_error();
+static int matmul_enqueue(spreg_matmul *mm, float *c_host, const float *b_host) {
     SPREG_CHECK_ARG(mm, "null matmul");
     SPREG_CHECK_ARG(mm->cfg.value_dtype == SPREG_F32, "host operator() takes FP32 buffers; use run_device for 16-bit B");
     if (!mm->dB || mm->alloc_n < mm->n) {
@@ -497,6 +496,25 @@ int spreg_matmul_run(spreg_matmul *mm, float *c_host, const float *b_host) {
     int st = matmul_exec(mm, mm->dC, mm->dB, mm->stream);
     if (st) return st;
     if (cb) SPREG_CUDA(cudaMemcpyAsync(c_host, mm->dC, cb, cudaMemcpyDeviceToHost, mm->stream));
+    return SPREG_OK;
+}
+
+int spreg_matmul_run_async(spreg_matmul *mm, float *c_host, const float *b_host) {
+    clear_error();
+    return matmul_enqueue(mm, c_host, b_host);
+}
+
+int spreg_matmul_sync(spreg_matmul *mm) {
+    clear_error();
+    SPREG_CHECK_ARG(mm, "null matmul");
+    SPREG_CUDA(cudaStreamSynchronize(mm->stream));
+    return SPREG_OK;
+}
+
+int spreg_matmul_run(spreg_matmul *mm, float *c_host, const float *b_host) {
+    clear_error();
+    int st = matmul_enqueue(mm, c_host, b_host);
+    if (st) return st;
     SPREG_CUDA(cudaStreamSynchronize(mm->stream));
     return SPREG_OK;
 }

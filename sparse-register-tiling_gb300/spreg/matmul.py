@@ -116,20 +116,42 @@ class MatMulSpecialized:
             _lib.check(_lib.lib().spreg_matmul_run_device(self._h, C_out.data_ptr(), B.data_ptr(),
                                                           _lib.stream_handle(stream)))
             return C_out
+        b, ptr = self._host_args(C_out, B)
+        _lib.check(_lib.lib().spreg_matmul_run(self._h, ptr, b.ctypes.data))
+        return C_out
+
+    def run_async(self, C_out, B):
+        """operator()(C, B) on host buffers, enqueued without waiting (copy in, product, copy out on
+        this matmul's stream).  C_out and B must stay alive and unchanged until sync(); pin them
+        (torch pin_memory) for copies that overlap other matmuls' work."""
+        b, ptr = self._host_args(C_out, B)
+        src = B.data_ptr() if hasattr(B, "data_ptr") else (B.ctypes.data if isinstance(B, np.ndarray) else None)
+        if b.ctypes.data != src:  # a converted copy would be freed before the enqueued copy reads it
+            raise ValueError("run_async needs B as a contiguous float32 host buffer (no conversion copy)")
+        _lib.check(_lib.lib().spreg_matmul_run_async(self._h, ptr, b.ctypes.data))
+        return C_out
+
+    def sync(self) -> None:
+        """Wait for this matmul's enqueued calls; their C buffers then hold the results."""
+        _lib.check(_lib.lib().spreg_matmul_sync(self._h))
+
+    def _host_args(self, C_out, B):
         b = _host_f32(B)
         if b.shape != (self.k, self.n):
             raise ValueError(f"expected B {self.k}x{self.n}, got {b.shape}")
-        out = C_out
         if hasattr(C_out, "numpy"):  # CPU tensor
             if not C_out.is_contiguous() or C_out.dtype.__str__() != "torch.float32":
                 raise ValueError("C must be a contiguous float32 CPU tensor")
+            if tuple(C_out.shape) != (self.m, self.n):
+                raise ValueError(f"expected C {self.m}x{self.n}")
             ptr = C_out.data_ptr()
         else:
             if C_out.dtype != np.float32 or not C_out.flags["C_CONTIGUOUS"]:
                 raise ValueError("C must be a contiguous float32 array")
+            if C_out.shape != (self.m, self.n):
+                raise ValueError(f"expected C {self.m}x{self.n}")
             ptr = C_out.ctypes.data
-        _lib.check(_lib.lib().spreg_matmul_run(self._h, ptr, b.ctypes.data))
-        return out
+        return b, ptr
 
     def __del__(self):
         try:

@@ -16,7 +16,7 @@ from oracle import oracle as O
 from spreg import _lib, synth
 from spreg.mapping import Mapping
 from spreg.matmul import MatMulSpecialized, TileConfig
-from spreg.packed import PackedMatrix, execute_batched
+from spreg.packed import PackedMatrix, device_status, execute_batched
 from spreg.sop_driver import Acc, make_sop_module, sort_and_encode_patterns
 
 pytestmark = pytest.mark.gpu
@@ -269,6 +269,32 @@ def test_matmul_specialized_host_and_device(cuda):
     mm2(C2, B)
     ref2 = O.Packed(O.Tables.of(Mapping.identity(4)), A, m_tile=16, k_tile=256).execute(B)
     assert np.array_equal(C2, ref2)
+
+
+def test_matmul_specialized_async_host_calls_overlap_and_match(cuda):
+    """Host-buffer calls enqueued on several matmuls' streams, then synced: each C equals the oracle,
+    also when one matmul runs two calls back to back before its sync."""
+    mms, Bs, Cs, refs = [], [], [], []
+    for i in range(6):
+        A = synth.row_skew(200 + 8 * i, 256, 0.9, seed=40 + i, std=1.0)
+        B = synth.dense(256, 160, seed=50 + i)
+        rp, ci, v = synth.to_csr(A)
+        mms.append(MatMulSpecialized(A.shape[0], 256, 160, v, rp, ci, TileConfig(K_c=128), 1, "", "61fee"))
+        Bs.append(torch.from_numpy(B).pin_memory())
+        Cs.append(torch.zeros((A.shape[0], 160)).pin_memory())
+        refs.append(O.Packed(O.Tables.of(Mapping.identity(4)), A, k_tile=128).execute(B))
+    C0b = torch.zeros_like(Cs[0]).pin_memory()
+    for mm, B, C in zip(mms, Bs, Cs):
+        mm.run_async(C, B)
+    mms[0].run_async(C0b, Bs[0])  # second call on the same stream: runs after the first
+    for mm in mms:
+        mm.sync()
+    for C, ref in zip(Cs, refs):
+        assert np.array_equal(C.numpy(), ref)
+    assert np.array_equal(C0b.numpy(), refs[0])
+    with pytest.raises(ValueError, match="no conversion copy"):
+        mms[1].run_async(Cs[1], Bs[1].double())  # a converted B would be freed before its copy runs
+    assert device_status() == 0
 
 
 def test_execute_batched_equals_individual(cuda):
