@@ -68,6 +68,8 @@ def parse():
     ap.add_argument("--tensor-cores", type=int, default=1, help="1: add the tensor-core (tcgen05) leg to the line")
     ap.add_argument("--layers", type=int, default=1,
                     help="1: add the batched uneven transformer-layer measurement to the line")
+    ap.add_argument("--ffn-sweep", type=int, default=1,
+                    help="1: add the FFN-shaped FP32 sweep (2048x512 / 512x2048 at sparsity 0.7-0.98) to the line")
     ap.add_argument("--serve-requests", type=int, default=768)
     ap.add_argument("--serve-slots", type=int, default=128)
     ap.add_argument("--serve-budget-mb", type=int, default=1024)
@@ -349,6 +351,61 @@ def precision_suite(dev) -> list:
                 row[f"rel_err_{name}_vs_rounded_inputs"] = float(O.rel_err(
                     C.cpu().numpy(), O.dense_fp64(_rounded(A, vd, pm), Bq)))
         rows.append(row)
+    return rows
+
+
+def ffn_sweep(dev, replicas: int = 32, steps: int = 20) -> list:
+    """The FFN-shaped FP32 workload across its sparsities: A 2048 x 512 and 512 x 2048 at 0.7, 0.8,
+    0.9, 0.95 and 0.98 (log-normal row skew, sigma 0.5, values N(0, 0.02)), B K x 512 N(0, 1).
+
+    Each point runs `replicas` distinct replicas (working set larger than L2) in one launch of the
+    default packing (M_r = 4, K_c = 128, nanokernel set from replica 0's histogram), replayed from
+    a CUDA graph. It reports algorithmic GB/s and GFLOP/s (2 nnz N), and checks replica 0 bit for
+    bit against the oracle and against FP64 (rel err).
+    """
+    import torch
+    from oracle import oracle as O
+    from spreg import PackedMatrix, execute_batched, synth
+    from spreg.kernel_sets import executor_penalty, greedy_kernel_set, pattern_histogram
+    peak, _ = measured_peaks()
+    rows = []
+    for M, K in ((2048, 512), (512, 2048)):
+        for sp in (0.7, 0.8, 0.9, 0.95, 0.98):
+            As = [synth.row_skew(M, K, sp, seed=7000 + 10 * r + int(sp * 100), sigma=0.5, std=0.02)
+                  for r in range(replicas)]
+            B0 = synth.dense(K, 512, seed=7500 + K)
+            m = greedy_kernel_set(pattern_histogram(As[0], 4), 4, 15, ((M + 3) // 4) * (-(-K // 128)),
+                                  penalty=executor_penalty(4))
+            packs = [PackedMatrix.from_dense(torch.from_numpy(A).to(dev), m, k_tile=128) for A in As]
+            Bd = [torch.from_numpy(B0).to(dev).roll(r, 0) for r in range(replicas)]  # distinct B per replica
+            Cd = [torch.empty((M, 512), device=dev) for _ in range(replicas)]
+            work = [(p, b, c, {}) for p, b, c in zip(packs, Bd, Cd)]
+            execute_batched(work)
+            torch.cuda.synchronize()
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g):
+                execute_batched(work)
+            for _ in range(3):
+                g.replay()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record()
+            for _ in range(steps):
+                g.replay()
+            e1.record()
+            torch.cuda.synchronize()
+            sec = e0.elapsed_time(e1) / 1e3 / steps
+            nbytes = sum(p.algorithmic_bytes(512) for p in packs)
+            flops = sum(p.flops(512) for p in packs)
+            got = Cd[0].cpu().numpy()
+            B0r = Bd[0].cpu().numpy()
+            want = O.Packed(O.Tables.of(m), As[0], k_tile=128).execute(B0r)
+            rows.append({"shape": [M, K], "sparsity": sp, "n": 512, "replicas": replicas,
+                         "spmm_us": sec / replicas * 1e6, "gbs": nbytes / sec / 1e9,
+                         "frac_of_measured_hbm": nbytes / sec / 1e9 / peak, "gflops": flops / sec / 1e9,
+                         "nanokernels": m.nanokernels, "bit_exact_vs_oracle": bool(np.array_equal(got, want)),
+                         "rel_err_vs_fp64": float(O.rel_err(got, O.dense_fp64(As[0], B0r)))})
+            del packs, Bd, Cd, work, g
     return rows
 
 
@@ -721,6 +778,7 @@ def main():
     precision = precision_suite(dev) if (lead and args.precision) else None
     tensor_cores = tensor_core_suite(dev) if (lead and args.tensor_cores) else None
     layers = layers_suite(dev) if (lead and args.layers) else None
+    sweep = ffn_sweep(dev) if (lead and args.ffn_sweep) else None
 
     cpu = None
     if rank == 0 and args.cpu_seconds > 0:
@@ -745,6 +803,7 @@ def main():
                            "parallelism": f"replicas x{ws}"},
                 "gflops": gflops, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "serving": serving,
                 "precision": precision, "batched_layers": layers, "tensor_cores": tensor_cores,
+                "ffn_sparsity_sweep": sweep,
                 "clocks": clocks, "gpu_launches": launches_per_step * args.steps,
                 "parity_bit_exact_vs_oracle": parity_ok}
         print(json.dumps(line))

@@ -158,13 +158,19 @@ int device_status_impl(int32_t *status, int reset) {
 }
 
 // Columns per lane (strip width / 32) chosen automatically: wide strips amortise the per-entry
-// index and value loads over more columns, narrow strips give more items when the problem is small.
-int auto_nv(int64_t n, int64_t panels, int sms) {
+// index and value loads over more columns, narrow strips give more items when the launch is small.
+// `others1` = the (panel, 32-column strip) items of the other SpMMs that share the launch, so a
+// small SpMM in a large batch keeps wide strips.
+int auto_nv(int64_t n, int64_t panels, int sms, int64_t others1) {
     int nv = 1;
     if (n >= 64) nv = 2;
     if (n >= 128) nv = 4;
-    while (nv > 1 && panels * (n / (32 * nv)) < (int64_t)sms * 8) nv >>= 1;
+    while (nv > 1 && panels * (n / (32 * nv)) + others1 / nv < (int64_t)sms * 8) nv >>= 1;
     return nv;
+}
+
+int64_t strip_items1(const spreg_packed *a, const spreg_exec_args *args) {
+    return (a && args) ? a->info.num_panels * (args->n / 32) : 0;
 }
 
 // ------------------------------------------------------------------ one call -> problems
@@ -217,7 +223,7 @@ struct CallPlan {
     int warps;
 };
 
-int plan_call(const spreg_packed *a, const spreg_exec_args *args, CallPlan *cp) {
+int plan_call(const spreg_packed *a, const spreg_exec_args *args, CallPlan *cp, int64_t others1) {
     SPREG_CHECK_ARG(a && args, "null packed matrix or args");
     const spreg_packed_info &in = a->info;
     const int combo = combo_of(in.value_dtype, args->b_dtype, args->c_dtype);
@@ -239,7 +245,7 @@ int plan_call(const spreg_packed *a, const spreg_exec_args *args, CallPlan *cp) 
     if (st) return st;
     int nv;
     switch (args->nr) {
-    case 0: nv = auto_nv(args->n, in.num_panels, f->sms); break;
+    case 0: nv = auto_nv(args->n, in.num_panels, f->sms, others1); break;
     case 32: nv = 1; break;
     case 64: nv = 2; break;
     case 128: nv = 4; break;
@@ -526,9 +532,11 @@ int run_calls(const spreg_packed *const *as, const spreg_exec_args *const *args,
     std::map<std::tuple<int, int, int>, Group> groups;
     std::map<std::tuple<int, int, int>, TileGroup> tgroups;
     std::vector<CallPlan> streams;
+    int64_t items1 = 0;
+    for (int32_t i = 0; i < n; ++i) items1 += strip_items1(as[i], args[i]);
     for (int32_t i = 0; i < n; ++i) {
         CallPlan cp;
-        int st = plan_call(as[i], args[i], &cp);
+        int st = plan_call(as[i], args[i], &cp, items1 - strip_items1(as[i], args[i]));
         if (st != SPREG_OK) return st;
         if (cp.tile) add_tile_call(tgroups, cp);
         else if (cp.stream_kernel) streams.push_back(cp);

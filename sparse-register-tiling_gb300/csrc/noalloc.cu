@@ -27,7 +27,8 @@
 
 namespace spreg {
 
-int auto_nv(int64_t n, int64_t panels, int sms);  // exec.cu
+int auto_nv(int64_t n, int64_t panels, int sms, int64_t others1);  // exec.cu
+int64_t strip_items1(const spreg_packed *a, const spreg_exec_args *args);  // exec.cu
 
 constexpr int kNoAllocLaunches = 64;
 static __device__ __align__(256) int g_noalloc_scratch[1 + kNoAllocLaunches];
@@ -121,6 +122,8 @@ extern "C" int spreg_execute_batched_noalloc(const spreg_work_item *items, int32
 
     // Plan every SpMM as the batched kernel's problems (whole strips + an NV = 1 remainder).
     std::map<std::tuple<int, int, int>, NoAllocGroup> groups;
+    int64_t items1 = 0;
+    for (int32_t i = 0; i < num_items; ++i) items1 += strip_items1(items[i].a, &items[i].args);
     for (int32_t i = 0; i < num_items; ++i) {
         const spreg_packed *a = items[i].a;
         const spreg_exec_args *args = &items[i].args;
@@ -144,7 +147,7 @@ extern "C" int spreg_execute_batched_noalloc(const spreg_work_item *items, int32
                         (long long)a->max_exec_bytes);
         int nv;
         switch (args->nr) {
-        case 0: nv = auto_nv(args->n, in.num_panels, d->sms); break;
+        case 0: nv = auto_nv(args->n, in.num_panels, d->sms, items1 - strip_items1(a, args)); break;
         case 32: nv = 1; break;
         case 64: nv = 2; break;
         case 128: nv = 4; break;
