@@ -355,57 +355,66 @@ def precision_suite(dev) -> list:
 
 
 def ffn_sweep(dev, replicas: int = 32, steps: int = 20) -> list:
-    """The FFN-shaped FP32 workload across its sparsities: A 2048 x 512 and 512 x 2048 at 0.7, 0.8,
-    0.9, 0.95 and 0.98 (log-normal row skew, sigma 0.5, values N(0, 0.02)), B K x 512 N(0, 1).
+    """The FFN-shaped workload across its sparsities and storage types: A 2048 x 512 and 512 x 2048
+    at 0.7, 0.8, 0.9, 0.95 and 0.98 (log-normal row skew, sigma 0.5, values N(0, 0.02)), B K x 512
+    N(0, 1); FP32, BF16 and FP16 (per-panel scaled) storage of A values and B, FP32 accumulation
+    and FP32 C.
 
     Each point runs `replicas` distinct replicas (working set larger than L2) in one launch of the
     default packing (M_r = 4, K_c = 128, nanokernel set from replica 0's histogram), replayed from
-    a CUDA graph. It reports algorithmic GB/s and GFLOP/s (2 nnz N), and checks replica 0 bit for
-    bit against the oracle and against FP64 (rel err).
+    a CUDA graph. It reports algorithmic GB/s (2-byte values and B for the 16-bit forms) and
+    GFLOP/s (2 nnz N), and checks replica 0 bit for bit against the oracle and against FP64.
     """
     import torch
     from oracle import oracle as O
-    from spreg import PackedMatrix, execute_batched, synth
+    from spreg import BF16, F16, F32, PackedMatrix, execute_batched, synth
     from spreg.kernel_sets import executor_penalty, greedy_kernel_set, pattern_histogram
     peak, _ = measured_peaks()
+    forms = (("fp32", F32, torch.float32), ("bf16", BF16, torch.bfloat16), ("fp16", F16, torch.float16))
     rows = []
     for M, K in ((2048, 512), (512, 2048)):
         for sp in (0.7, 0.8, 0.9, 0.95, 0.98):
             As = [synth.row_skew(M, K, sp, seed=7000 + 10 * r + int(sp * 100), sigma=0.5, std=0.02)
                   for r in range(replicas)]
-            B0 = synth.dense(K, 512, seed=7500 + K)
+            B0 = torch.from_numpy(synth.dense(K, 512, seed=7500 + K)).to(dev)
             m = greedy_kernel_set(pattern_histogram(As[0], 4), 4, 15, ((M + 3) // 4) * (-(-K // 128)),
                                   penalty=executor_penalty(4))
-            packs = [PackedMatrix.from_dense(torch.from_numpy(A).to(dev), m, k_tile=128) for A in As]
-            Bd = [torch.from_numpy(B0).to(dev).roll(r, 0) for r in range(replicas)]  # distinct B per replica
-            Cd = [torch.empty((M, 512), device=dev) for _ in range(replicas)]
-            work = [(p, b, c, {}) for p, b, c in zip(packs, Bd, Cd)]
-            execute_batched(work)
-            torch.cuda.synchronize()
-            g = torch.cuda.CUDAGraph()
-            with torch.cuda.graph(g):
+            exact = O.dense_fp64(As[0], B0.cpu().numpy())
+            row = {"shape": [M, K], "sparsity": sp, "n": 512, "replicas": replicas, "nanokernels": m.nanokernels}
+            for name, vd, tdt in forms:
+                packs = [PackedMatrix.from_dense(torch.from_numpy(A).to(dev), m, k_tile=128, value_dtype=vd)
+                         for A in As]
+                Bd = [B0.roll(r, 0).to(tdt) for r in range(replicas)]  # a distinct B per replica
+                Cd = [torch.empty((M, 512), device=dev) for _ in range(replicas)]
+                work = [(p, b, c, {}) for p, b, c in zip(packs, Bd, Cd)]
                 execute_batched(work)
-            for _ in range(3):
-                g.replay()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            torch.cuda.synchronize()
-            e0.record()
-            for _ in range(steps):
-                g.replay()
-            e1.record()
-            torch.cuda.synchronize()
-            sec = e0.elapsed_time(e1) / 1e3 / steps
-            nbytes = sum(p.algorithmic_bytes(512) for p in packs)
-            flops = sum(p.flops(512) for p in packs)
-            got = Cd[0].cpu().numpy()
-            B0r = Bd[0].cpu().numpy()
-            want = O.Packed(O.Tables.of(m), As[0], k_tile=128).execute(B0r)
-            rows.append({"shape": [M, K], "sparsity": sp, "n": 512, "replicas": replicas,
-                         "spmm_us": sec / replicas * 1e6, "gbs": nbytes / sec / 1e9,
-                         "frac_of_measured_hbm": nbytes / sec / 1e9 / peak, "gflops": flops / sec / 1e9,
-                         "nanokernels": m.nanokernels, "bit_exact_vs_oracle": bool(np.array_equal(got, want)),
-                         "rel_err_vs_fp64": float(O.rel_err(got, O.dense_fp64(As[0], B0r)))})
-            del packs, Bd, Cd, work, g
+                torch.cuda.synchronize()
+                g = torch.cuda.CUDAGraph()
+                with torch.cuda.graph(g):
+                    execute_batched(work)
+                for _ in range(3):
+                    g.replay()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                torch.cuda.synchronize()
+                e0.record()
+                for _ in range(steps):
+                    g.replay()
+                e1.record()
+                torch.cuda.synchronize()
+                sec = e0.elapsed_time(e1) / 1e3 / steps
+                bsz = 4 if vd == F32 else 2
+                nbytes = sum(p.algorithmic_bytes(512, b_bytes=bsz) for p in packs)
+                flops = sum(p.flops(512) for p in packs)
+                got = Cd[0].cpu().numpy()
+                Bq = Bd[0].cpu()
+                Bref = Bq.numpy() if vd == F32 else Bq.view(torch.int16).numpy().view(np.uint16)
+                want = O.Packed(O.Tables.of(m), As[0], k_tile=128, value_dtype=vd).execute(Bref)
+                row[name] = {"spmm_us": sec / replicas * 1e6, "gbs": nbytes / sec / 1e9,
+                             "frac_of_measured_hbm": nbytes / sec / 1e9 / peak, "gflops": flops / sec / 1e9,
+                             "bit_exact_vs_oracle": bool(np.array_equal(got.view(np.uint32), want.view(np.uint32))),
+                             "rel_err_vs_fp64": float(O.rel_err(got, exact))}
+                del packs, Bd, Cd, work, g
+            rows.append(row)
     return rows
 
 

@@ -249,7 +249,8 @@ int plan_call(const spreg_packed *a, const spreg_exec_args *args, CallPlan *cp, 
     case 32: nv = 1; break;
     case 64: nv = 2; break;
     case 128: nv = 4; break;
-    default: SPREG_FAIL(SPREG_ERR_INVALID_ARG, "nr must be 0, 32, 64 or 128 (got %d)", args->nr);
+    case 256: nv = 4; break;  // 256-column strips where the B-tile kernel takes 16-bit B (below), else 128
+    default: SPREG_FAIL(SPREG_ERR_INVALID_ARG, "nr must be 0, 32, 64, 128 or 256 (got %d)", args->nr);
     }
     const size_t bsz = dtype_bytes(args->b_dtype), csz = dtype_bytes(args->c_dtype);
     while (nv > 1 && !(aligned(args->b, bsz * nv) && args->ldb % nv == 0 && aligned(args->c, csz * nv) &&
@@ -257,10 +258,8 @@ int plan_call(const spreg_packed *a, const spreg_exec_args *args, CallPlan *cp, 
         nv >>= 1;
     cp->mr = in.mr;
     cp->combo = combo;
-    cp->nv = nv;
     cp->warps = args->warps_per_cta > 0 ? args->warps_per_cta : 4;
     SPREG_CHECK_ARG(cp->warps >= 1 && cp->warps <= 8, "warps_per_cta must be in [1, 8]");
-    const int64_t n_main = (args->n / (32 * nv)) * (32 * nv);
     cp->xbuf = (a->max_exec_bytes + 127) / 128 * 128;
     const bool x_fits = a->exec && 1024 + 2 * cp->xbuf <= f->smem_optin;
     SPREG_CHECK_ARG(args->meta_staging != 1 || x_fits, "the execution-layout kernel cannot run this pack "
@@ -282,6 +281,31 @@ int plan_call(const spreg_packed *a, const spreg_exec_args *args, CallPlan *cp, 
         SPREG_CHECK_ARG(args->meta_staging != 2, "b_staging = 1 runs the execution-layout metadata path");
         SPREG_CHECK_ARG(args->n <= INT32_MAX, "n out of range for shared-memory B tiles");
     }
+
+    // Wide strips for 16-bit B in the B-tile kernel: NV = 8 (256 columns, one 16-byte shared-memory
+    // load per lane and entry) spreads each entry's index and value loads over twice the columns.
+    // Taken when that kernel runs, the stage still holds 64 KB, the launch keeps enough
+    // (panel, strip) items, and at least 85 % of the entries are in groups with their own loop there
+    // (the single rows and the all-rows kernel; other patterns dispatch per half step, slower than
+    // NV = 4 where they are common: BF16 2048 x 512 at 70-80 % sparsity) -- or when nr = 256 asks.
+    int64_t hot = 0, all = 0;
+    for (int i = 0; i < in.num_nkern; ++i) {
+        const int p = a->id_to_pattern[i];
+        all += a->id_entries[i];
+        if ((p & (p - 1)) == 0 || p == (1 << in.mr) - 1) hot += a->id_entries[i];
+    }
+    const bool hot_set = all > 0 && 100 * hot >= 85 * all;
+    const bool tile_kernel =
+        args->b_staging == 1 || (args->b_staging == 0 && tile_base_ok && args->meta_staging != 2 &&
+                                 !cp->stream_kernel && a->geom.T > 1 && args->n <= INT32_MAX &&
+                                 staged_rows * 32 * nv * (int64_t)bsz <= 64 * 1024);
+    if (tile_kernel && bsz == 2 && in.mr <= 4 && nv == 4 && (args->nr == 0 || args->nr == 256) && args->n >= 256 &&
+        staged_rows * 256 * (int64_t)bsz <= 64 * 1024 && aligned(args->b, 16) && args->ldb % 8 == 0 &&
+        aligned(args->c, csz * 8) && args->ldc % 8 == 0 &&
+        (args->nr == 256 || (hot_set && in.num_panels * (args->n / 256) + others1 / 8 >= (int64_t)f->sms * 8)))
+        nv = 8;
+    cp->nv = nv;
+    const int64_t n_main = (args->n / (32 * nv)) * (32 * nv);
 
     XProblem base = {};
     base.exec = a->exec;

@@ -469,6 +469,9 @@ __device__ __forceinline__ unsigned short lds_u16(uint32_t a) {
 template <class TV> __device__ __forceinline__ float word_val(uint32_t w, int half) {
     if constexpr (sizeof(TV) == 4) {
         return __uint_as_float(w);
+    } else if constexpr (std::is_same<TV, __nv_bfloat16>::value) {
+        // BF16 is the upper half of an FP32 word: the widening is exact, one logical op per value
+        return __uint_as_float(half ? (w & 0xFFFF0000u) : (w << 16));
     } else {
         const unsigned short h = (unsigned short)(half ? (w >> 16) : (w & 0xFFFFu));
         return DT<TV>::to_f32(*reinterpret_cast<const TV *>(&h));
@@ -601,6 +604,96 @@ __device__ __forceinline__ void step_dispatch(const int pat, const uint32_t vs, 
     if (!done) step_fma_nibbles<MR, NV, TV>(pat, vs, FULL ? 4 : m, b, acc);
 }
 
+// ------------------------------------------------------------------ 256-column strips (NV = 8)
+// With NV = 8 a step of 4 entries runs as two halves of 2 entries, so that only 2 B rows of 8
+// columns (16 registers) are live beside the 4 x 8 accumulators.  M_r <= 4 (every pattern has its
+// own FMA block); values are 16-bit, read as 32-bit words (a half starts 4 * popcount bytes in).
+template <int PAT, int MR, int NV, class TV, bool FULL>
+__device__ __forceinline__ void half_fma(const uint32_t vs, const int m, const float (&b)[2][NV],
+                                         float (&acc)[MR][NV]) {
+    constexpr int PC = cpopc(PAT);
+    constexpr int VB = (int)sizeof(TV);
+    static_assert(VB == 2 && MR <= 4, "256-column strips take 16-bit values and M_r <= 4");
+    uint32_t vw[PC];  // 2 entries x PC values x 2 bytes
+#pragma unroll
+    for (int i = 0; i < PC; ++i) vw[i] = lds_u32(vs + 4u * i);
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+        if (FULL || u < m) {
+            int q = 0;
+#pragma unroll
+            for (int r = 0; r < MR; ++r) {
+                if ((PAT >> r) & 1) {
+                    const int vi = u * PC + q;
+                    const float a = word_val<TV>(vw[vi >> 1], vi & 1);
+                    ++q;
+#pragma unroll
+                    for (int j = 0; j < NV; ++j) acc[r][j] = fmaf(a, b[u][j], acc[r][j]);
+                }
+            }
+        }
+    }
+}
+
+// The same with the pattern known at run time (groups of patterns without their own loop).
+template <int MR, int NV, class TV, bool FULL>
+__device__ __forceinline__ void half_dispatch(const int pat, const uint32_t vs, const int m, const float (&b)[2][NV],
+                                              float (&acc)[MR][NV]) {
+#define SPREG_HCASE(P)                                                                          \
+    case (P):                                                                                   \
+        if constexpr ((P) > 0 && (P) < (1 << MR)) half_fma<(P), MR, NV, TV, FULL>(vs, m, b, acc); \
+        break;
+    switch (pat) {
+        SPREG_C16(SPREG_HCASE, 0)
+    default:
+        break;
+    }
+#undef SPREG_HCASE
+}
+
+// n entries of one group at NV = 8; PAT > 0 is the group's pattern known at compile time, PAT = 0
+// dispatches on `pat` once per half step.  The B rows are loaded before the FMA block is chosen
+// (a switch around whole steps spilled).
+template <int PAT, int MR, int NV, class TV, class BL>
+__device__ __forceinline__ void run_group_wide(const int pat, const int n, uint32_t cs, uint32_t vs, const BL &bl,
+                                               float (&acc)[MR][NV]) {
+    const uint32_t pc = PAT > 0 ? (uint32_t)cpopc(PAT) : (uint32_t)__popc(pat);
+    const uint32_t vhalf = 2u * (uint32_t)sizeof(TV) * pc, vstep = 2u * vhalf;
+    auto half = [&](uint32_t v, int m, const float (&b)[2][NV], auto full_tag) {
+        constexpr bool FULL = decltype(full_tag)::value;
+        if constexpr (PAT > 0) half_fma<PAT, MR, NV, TV, FULL>(v, m, b, acc);
+        else half_dispatch<MR, NV, TV, FULL>(pat, v, m, b, acc);
+    };
+    const int full = n >> 2;
+    uint4 k4 = full > 0 ? lds_u128(cs) : make_uint4(0, 0, 0, 0);
+#pragma unroll 1
+    for (int s = 0; s < full; ++s) {
+        const uint4 kk = k4;
+        cs += 16u;
+        if (s + 1 < full) k4 = lds_u128(cs);
+        float b[2][NV];
+        bl.load((int)kk.x, b[0]);
+        bl.load((int)kk.y, b[1]);
+        half(vs, 2, b, std::true_type{});
+        bl.load((int)kk.z, b[0]);
+        bl.load((int)kk.w, b[1]);
+        half(vs + vhalf, 2, b, std::true_type{});
+        vs += vstep;
+    }
+    const int m = n & 3;
+    if (m) {
+        const uint4 kk = lds_u128(cs);
+        float b[2][NV];
+        bl.load((int)kk.x, b[0]);
+        if (m > 1) bl.load((int)kk.y, b[1]);
+        half(vs, m < 2 ? m : 2, b, std::false_type{});
+        if (m > 2) {
+            bl.load((int)kk.z, b[0]);
+            half(vs + vhalf, m - 2, b, std::false_type{});
+        }
+    }
+}
+
 // n entries of one group: full steps of 4 entries (one 16-byte broadcast load of column indices,
 // 4 B rows, the pattern's FMA block), then one predicated step for the last n % 4 entries.
 // A group of a pattern known at compile time: no per-step dispatch.
@@ -609,7 +702,10 @@ __device__ __forceinline__ void run_group_pat(const int n, uint32_t cs, uint32_t
                                               float (&acc)[MR][NV]) {
     constexpr uint32_t VSTEP = 4u * (uint32_t)sizeof(TV) * (uint32_t)cpopc(PAT);
     const int full = n >> 2;
-    if constexpr (NV >= 4) {
+    if constexpr (NV >= 8) {
+        run_group_wide<PAT, MR, NV, TV>(PAT, n, cs, vs, bl, acc);
+        return;
+    } else if constexpr (NV >= 4) {
         // registers are short for a second B set: prefetch only the next step's column indices
         uint4 k4 = full > 0 ? lds_u128(cs) : make_uint4(0, 0, 0, 0);
 #pragma unroll 1
@@ -683,6 +779,10 @@ __device__ __forceinline__ void run_group_x(const int pat, const int n, uint32_t
             default: break;
             }
         }
+    }
+    if constexpr (NV >= 8) {
+        run_group_wide<0, MR, NV, TV>(pat, n, cs, vs, bl, acc);
+        return;
     }
     const uint32_t vstep = 4u * (uint32_t)sizeof(TV) * (uint32_t)__popc(pat);
     const int full = n >> 2;

@@ -119,9 +119,12 @@ template <int NV, class TB> struct SmemB {
                 const uint2 v = lds_u64(a);
                 b[0] = __uint_as_float(v.x); b[1] = __uint_as_float(v.y);
             } else {
-                const uint4 v = lds_u128(a);
-                b[0] = __uint_as_float(v.x); b[1] = __uint_as_float(v.y);
-                b[2] = __uint_as_float(v.z); b[3] = __uint_as_float(v.w);
+#pragma unroll
+                for (int i = 0; i < NV / 4; ++i) {
+                    const uint4 v = lds_u128(a + 16u * i);
+                    b[4 * i] = __uint_as_float(v.x); b[4 * i + 1] = __uint_as_float(v.y);
+                    b[4 * i + 2] = __uint_as_float(v.z); b[4 * i + 3] = __uint_as_float(v.w);
+                }
             }
         } else {
             if constexpr (NV == 1) {
@@ -129,10 +132,16 @@ template <int NV, class TB> struct SmemB {
             } else if constexpr (NV == 2) {
                 const uint32_t w = lds_u32(a);
                 b[0] = word_val<TB>(w, 0); b[1] = word_val<TB>(w, 1);
-            } else {
+            } else if constexpr (NV == 4) {
                 const uint2 v = lds_u64(a);
                 b[0] = word_val<TB>(v.x, 0); b[1] = word_val<TB>(v.x, 1);
                 b[2] = word_val<TB>(v.y, 0); b[3] = word_val<TB>(v.y, 1);
+            } else {
+                const uint4 v = lds_u128(a);
+                b[0] = word_val<TB>(v.x, 0); b[1] = word_val<TB>(v.x, 1);
+                b[2] = word_val<TB>(v.y, 0); b[3] = word_val<TB>(v.y, 1);
+                b[4] = word_val<TB>(v.z, 0); b[5] = word_val<TB>(v.z, 1);
+                b[6] = word_val<TB>(v.w, 0); b[7] = word_val<TB>(v.w, 1);
             }
         }
     }
@@ -331,6 +340,13 @@ __global__ void __launch_bounds__(32 * (kTileMaxWarps + 1), 1) exec_tile_kernel(
     }
 }
 
+// 256-column strips (NV = 8) are built for 16-bit B and M_r <= 4 only.
+using TileKernelPtr = void (*)(TileParams);
+template <int MR, class V, class B, class C> inline TileKernelPtr tile_nv8_kernel() {
+    if constexpr (sizeof(B) == 2 && MR <= 4) return exec_tile_kernel<MR, 8, V, B, C>;
+    else return nullptr;
+}
+
 template <int MR, int COMBO>
 cudaError_t launch_exec_tile(const TileParams &p, int nv, unsigned grid, int threads, size_t smem, cudaStream_t s);
 
@@ -341,7 +357,7 @@ cudaError_t launch_exec_tile(const TileParams &p, int nv, unsigned grid, int thr
         using V = ComboTypes<COMBO>::V;                                                               \
         using B = ComboTypes<COMBO>::B;                                                               \
         using C = ComboTypes<COMBO>::C;                                                               \
-        static bool configured[64][5] = {};                                                           \
+        static bool configured[64][9] = {};                                                           \
         int dev = 0;                                                                                  \
         cudaGetDevice(&dev);                                                                          \
         auto run = [&](auto kern) -> cudaError_t {                                                    \
@@ -358,6 +374,10 @@ cudaError_t launch_exec_tile(const TileParams &p, int nv, unsigned grid, int thr
         case 1: return run(exec_tile_kernel<MR, 1, V, B, C>);                                         \
         case 2: return run(exec_tile_kernel<MR, 2, V, B, C>);                                         \
         case 4: return run(exec_tile_kernel<MR, 4, V, B, C>);                                         \
+        case 8: {                                                                                     \
+            auto k8 = tile_nv8_kernel<MR, V, B, C>();                                                 \
+            return k8 ? run(k8) : cudaErrorInvalidValue;                                              \
+        }                                                                                             \
         default: return cudaErrorInvalidValue;                                                        \
         }                                                                                             \
     }

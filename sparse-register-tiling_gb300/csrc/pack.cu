@@ -368,6 +368,23 @@ __global__ void panel_work_kernel(const int64_t P, const int64_t T, const int64_
     work[gp] = w;
 }
 
+// Entries of each nanokernel id over all units (block = id).
+__global__ void id_totals_kernel(const int32_t *__restrict__ unit_counts, const int64_t units, const int nk,
+                                 unsigned long long *__restrict__ totals) {
+    __shared__ unsigned long long s_sum[32];
+    const int id = blockIdx.x;
+    unsigned long long sum = 0;
+    for (int64_t u = threadIdx.x; u < units; u += blockDim.x) sum += (unsigned)unit_counts[u * nk + id];
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
+    if ((threadIdx.x & 31) == 0) s_sum[threadIdx.x >> 5] = sum;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long t = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += s_sum[w];
+        totals[id] = t;
+    }
+}
+
 // Offsets of the execution blocks in slot order (exec_slot): exec_offs[slot] for the executors,
 // unit_xoff[unit] for the emit kernels.
 __global__ void __launch_bounds__(1024) exec_slots_kernel(const int64_t units, const int64_t P, const int64_t T,
@@ -839,8 +856,10 @@ struct Scratch {
     DevError *err = nullptr;
     int64_t *panel_work = nullptr;  // P work estimates
     int64_t *unit_xoff = nullptr;   // units execution-block offsets by unit
+    unsigned long long *id_totals = nullptr;  // 256 entry counts by nanokernel id
     cudaStream_t s = nullptr;
     ~Scratch() {
+        if (id_totals) cudaFreeAsync(id_totals, s);
         if (panel_work) cudaFreeAsync(panel_work, s);
         if (unit_xoff) cudaFreeAsync(unit_xoff, s);
         if (unit_counts) cudaFreeAsync(unit_counts, s);
@@ -901,6 +920,11 @@ int finish_pack(const spreg_mapping *m, const Geom &g, int value_dtype, int64_t 
         panel_work_kernel<<<(unsigned)((g.P + 255) / 256), 256, 0, stream>>>(g.P, g.T, g.ppt, sc.stats, sc.panel_work);
         cudaMemcpyAsync(work.data(), sc.panel_work, (size_t)g.P * sizeof(int64_t), cudaMemcpyDeviceToHost, stream);
     }
+    unsigned long long id_totals[256] = {};
+    if (units > 0 && nk > 0) {
+        id_totals_kernel<<<(unsigned)nk, 256, 0, stream>>>(sc.unit_counts, units, nk, sc.id_totals);
+        cudaMemcpyAsync(id_totals, sc.id_totals, 256 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, stream);
+    }
     PackTotals tot;
     DevError derr;
     cudaMemcpyAsync(&tot, sc.totals, sizeof tot, cudaMemcpyDeviceToHost, stream);
@@ -912,6 +936,7 @@ int finish_pack(const spreg_mapping *m, const Geom &g, int value_dtype, int64_t 
         SPREG_FAIL(SPREG_ERR_CHECK, "packer check failed at unit %d (value %d): %s", derr.unit, derr.value,
                    dev_error_text(derr.code));
     }
+    for (int i = 0; i < 256; ++i) p->id_entries[i] = (int64_t)id_totals[i];
     // Panels by descending work (ties by index): the tile executor gives consecutive panels of this
     // order to the warps of one job, so a job's warps finish their K tiles at about the same time.
     {
@@ -986,6 +1011,8 @@ int alloc_scratch(Scratch &sc, const Geom &g, int nk, int64_t tiles, cudaStream_
     SPREG_CUDA(cudaMallocAsync(&sc.err, sizeof(DevError), stream));
     SPREG_CUDA(cudaMallocAsync(&sc.panel_work, (size_t)(g.P > 0 ? g.P : 1) * sizeof(int64_t), stream));
     SPREG_CUDA(cudaMallocAsync(&sc.unit_xoff, (size_t)units * sizeof(int64_t), stream));
+    SPREG_CUDA(cudaMallocAsync(&sc.id_totals, 256 * sizeof(unsigned long long), stream));
+    SPREG_CUDA(cudaMemsetAsync(sc.id_totals, 0, 256 * sizeof(unsigned long long), stream));
     SPREG_CUDA(cudaMemsetAsync(sc.panel_maxabs, 0, (size_t)(g.P > 0 ? g.P : 1) * sizeof(unsigned), stream));
     SPREG_CUDA(cudaMemsetAsync(sc.tile_nnz, 0, (size_t)(tiles > 0 ? tiles : 1) * sizeof(unsigned long long), stream));
     SPREG_CUDA(cudaMemsetAsync(sc.err, 0, sizeof(DevError), stream));

@@ -188,6 +188,7 @@ struct spreg_packed {
     int64_t *exec_offs = nullptr;   // units + 1 block offsets, in slot order (exec_slot)
     int32_t *panel_order = nullptr; // P panels by descending work: slot t * P + i holds unit (panel_order[i], t)
     int32_t *panel_rank = nullptr;  // inverse of panel_order
+    int64_t id_entries[256] = {};   // packed entries (columns) of each nanokernel id, all units
     int64_t exec_bytes = 0;
     int64_t max_exec_bytes = 0;
     bool list_packed = false;       // packed panel by panel (per-panel column offsets, no K tiles)

@@ -142,3 +142,51 @@ def test_tile_kernel_refusals(cuda):
     with pytest.raises(_lib.SpregError, match="16-byte aligned"):
         pt.execute(torch.ones((512, 65), device="cuda")[:, 1:], staging=1)  # B base not 16-byte aligned
     assert device_status() == 0
+
+
+@pytest.mark.parametrize("vd,cd", [(_lib.BF16, _lib.F32), (_lib.BF16, _lib.BF16), (_lib.F16, _lib.F32)])
+@pytest.mark.parametrize("n,ld", [(512, 512), (300, 304), (256, 264)])
+@pytest.mark.parametrize("mr,mp", [(2, None), (4, None), (4, "75a1b")])
+def test_tile_kernel_256_column_strips(cuda, vd, cd, n, ld, mr, mp):
+    """nr = 256 with 16-bit B: 256-column strips (two half steps of 2 entries), ragged columns on
+    the 32-column kernel, load_c and the ReLU epilogue; bit-exact with the oracle."""
+    m = Mapping.load(mp) if mp else Mapping.identity(mr)
+    A = synth.row_skew(203, 384, 0.9, seed=n + mr, std=0.5)
+    B = synth.dense(384, n, seed=n + 1)
+    C0 = synth.dense(203, n, seed=7)
+    got, want = run_pair(A, m, B, k_tile=128, value_dtype=vd, c_dtype=cd, nr=256, ld=ld, load_c=True, epilogue=1,
+                         C0=C0)
+    assert same_bits(got, want)
+    assert device_status() == 0
+
+
+def test_tile_kernel_256_column_strips_in_a_batch(cuda):
+    """Automatic strip width: BF16 SpMMs of several shapes in one launch take 256-column strips where
+    the launch has the items for them; every result equals its own call and the oracle."""
+    m = Mapping.identity(4)
+    work, refs = [], []
+    for i in range(24):
+        M, K, n = (512, 256, 512) if i % 2 else (256, 512, 384)
+        A = synth.row_skew(M, K, 0.9, seed=300 + i, std=1.0)
+        B = synth.dense(K, n, seed=400 + i)
+        pm = PackedMatrix.from_dense(torch.from_numpy(A).cuda(), m, k_tile=128, value_dtype=_lib.BF16)
+        tb = torch.from_numpy(B).to(torch.bfloat16).cuda()
+        C = torch.zeros((M, n), device="cuda")
+        work.append((pm, tb, C, {}))
+        Bq = tb.cpu().view(torch.int16).numpy().view(np.uint16)
+        refs.append(O.Packed(O.Tables.of(m), A, k_tile=128, value_dtype=_lib.BF16).execute(Bq))
+    execute_batched(work)
+    for (pm, tb, C, kw), want in zip(work, refs):
+        assert same_bits(C.cpu().numpy(), want)
+    pm, tb, C, _ = work[1]
+    C1 = pm.execute(tb, staging=1, nr=128)
+    assert same_bits(C1.cpu().numpy(), C.cpu().numpy())
+    assert device_status() == 0
+
+
+def test_nr_256_with_fp32_b_runs_128_column_strips(cuda):
+    m = Mapping.identity(4)
+    A = synth.row_skew(64, 256, 0.9, seed=3, std=1.0)
+    B = synth.dense(256, 512, seed=4)
+    got, want = run_pair(A, m, B, k_tile=128, nr=256)
+    assert same_bits(got, want)
