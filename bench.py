@@ -587,6 +587,59 @@ def cpu_baseline(As, Bs, args, seconds: float, threads: int = 0, mapping=None):
                       "executor time, restated reference executor (oracle/spreg_oracle.c) with OpenMP over panels"}
 
 
+def host_cpu() -> dict:
+    """Model and logical CPUs of this host (lscpu where present, else /proc/cpuinfo)."""
+    model = ""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.split(":")[0].strip() in ("Model name", "Model"):
+                model = model or ln.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    if not model and os.path.exists("/proc/cpuinfo"):
+        for ln in open("/proc/cpuinfo"):
+            if ln.lower().startswith(("model name", "cpu part")):
+                model = ln.split(":", 1)[1].strip()
+                break
+    return {"model": model or "unknown", "nproc": os.cpu_count()}
+
+
+def cpu_baselines(As, Bs, args, mapping, seconds: float = 2.0) -> dict:
+    """The CPU protocol around the headline workload, each on a bounded sample (about `seconds` of
+    compute per entry): the restated reference executor and the restated CSR baseline
+    (pytorch_csr_wrapper.cpp / spmm_csr_c.cpp row x N-tile loop), on 1 thread and on all threads,
+    median of 7 repetitions of one SpMM (SPMM_demo.cpp's protocol) after one warm-up."""
+    from oracle import oracle as O
+    from spreg import synth
+    t = O.Tables.of(mapping)
+    pk = O.Packed(t, As[0], k_tile=args.k_tile)
+    rp, ci, v = synth.to_csr(As[0])
+    nbytes = algorithmic_bytes_oracle(pk, args.n)
+    flops = 2 * pk.sizes["nnz"] * args.n
+    csr_bytes = v.size * 8 + rp.size * 4 + args.k * args.n * 4 + args.m * args.n * 4
+    out = {"host": host_cpu(), "sample": "replica 0 of the headline workload, median of 7 runs after 1 warm-up"}
+    legs = [("sop_executor", lambda th: pk.execute(Bs[0], threads=th), nbytes, (1, O.max_threads())),
+            ("csr_baseline", lambda th: O.csr_spmm(rp, ci, v, Bs[0], threads=th), csr_bytes, (1, O.max_threads()))]
+    if O.has_ref():  # the reference's own scalar CSR SpMM, compiled from its source where that exists
+        legs.append(("spmm_naive", lambda th: O.ref_naive(rp, ci, v, Bs[0]), csr_bytes, (1,)))
+    else:
+        out["spmm_naive"] = "not built on this host: the reference's source is absent here"
+    for name, run, b, thread_counts in legs:
+        for th in thread_counts:
+            run(th)
+            ts = []
+            t_end = time.perf_counter() + seconds
+            while len(ts) < 7 and (not ts or time.perf_counter() < t_end):
+                s = time.perf_counter()
+                run(th)
+                ts.append(time.perf_counter() - s)
+            med = statistics.median(ts)
+            out[f"{name}_{th}t"] = {"ms": med * 1e3, "gbs": b / med / 1e9, "gflops": flops / med / 1e9,
+                                    "threads": th, "runs": len(ts)}
+    return out
+
+
 def run_reference(args):
     """--impl reference: the reference's CPU algorithm (restated; its own executor source is absent)."""
     ws, rank, _ = dist_env()
@@ -792,6 +845,7 @@ def main():
     cpu = None
     if rank == 0 and args.cpu_seconds > 0:
         cpu = cpu_baseline(As, Bs, args, args.cpu_seconds, mapping=m)
+        cpu["protocol"] = cpu_baselines(As, Bs, args, m)
 
     clocks = clk.summary()
     if args.staging == 1:
