@@ -91,7 +91,7 @@ def bench_mapping(args, A0):
         from spreg.kernel_sets import executor_penalty, greedy_kernel_set, pattern_histogram
         units = ((A0.shape[0] + args.mr - 1) // args.mr) * max(1, -(-A0.shape[1] // (args.k_tile or 128)))
         return greedy_kernel_set(pattern_histogram(A0, args.mr), args.mr, 2 ** args.mr - 1, units,
-                                 penalty=executor_penalty(args.mr))
+                                 penalty=executor_penalty(args.mr, tile=bool(args.k_tile)))
     return Mapping.load(args.mapping)
 
 
@@ -378,7 +378,7 @@ def ffn_sweep(dev, replicas: int = 32, steps: int = 20) -> list:
                   for r in range(replicas)]
             B0 = torch.from_numpy(synth.dense(K, 512, seed=7500 + K)).to(dev)
             m = greedy_kernel_set(pattern_histogram(As[0], 4), 4, 15, ((M + 3) // 4) * (-(-K // 128)),
-                                  penalty=executor_penalty(4))
+                                  penalty=executor_penalty(4, tile=True))
             exact = O.dense_fp64(As[0], B0.cpu().numpy())
             row = {"shape": [M, K], "sparsity": sp, "n": 512, "replicas": replicas, "nanokernels": m.nanokernels}
             for name, vd, tdt in forms:

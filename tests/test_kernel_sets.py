@@ -75,6 +75,23 @@ def test_executor_penalty_marks_slow_kernels():
     assert all(popcount(k) >= 1 for k in m.nanokernels)
 
 
+def test_tile_penalty_keeps_the_b_tile_kernel_hot_set():
+    """For K-tiled packs the B-tile executor has its own loop only for the single rows and the
+    all-rows kernel: with the tile penalty the 70 %-sparse FFN weight keeps to those (without it
+    the reference cost model adds six two- and three-row kernels)."""
+    from spreg.kernel_sets import tile_hot
+    assert tile_hot(4, 0b1000) and tile_hot(4, 0b1111) and not tile_hot(4, 0b0110) and tile_hot(2, 0b11)
+    assert not tile_hot(8, 1)
+    pen = executor_penalty(4, tile=True)
+    assert pen(0b0110) == 0.5 and pen(0b0100) == 0.0 and executor_penalty(8, 2.0, tile=True)(0b111) == 2.0
+    A = synth.row_skew(2048, 512, 0.7, seed=7070, sigma=0.5, std=0.02)
+    h = pattern_histogram(A, 4)
+    plain = greedy_kernel_set(h, 4, 15, 512 * 4, penalty=executor_penalty(4))
+    tiled = greedy_kernel_set(h, 4, 15, 512 * 4, penalty=executor_penalty(4, tile=True))
+    assert any(not tile_hot(4, k) for k in plain.nanokernels)
+    assert all(tile_hot(4, k) for k in tiled.nanokernels)
+
+
 @pytest.mark.gpu
 def test_greedy_set_packs_and_executes_bit_exact(cuda):
     import torch
