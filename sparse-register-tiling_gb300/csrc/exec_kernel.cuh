@@ -606,15 +606,40 @@ __device__ __forceinline__ void step_dispatch(const int pat, const uint32_t vs, 
 
 // ------------------------------------------------------------------ 256-column strips (NV = 8)
 // With NV = 8 a step of 4 entries runs as two halves of 2 entries, so that only 2 B rows of 8
-// columns (16 registers) are live beside the 4 x 8 accumulators.  M_r <= 4 (every pattern has its
-// own FMA block); values are 16-bit, read as 32-bit words (a half starts 4 * popcount bytes in).
-template <int PAT, int MR, int NV, class TV, bool FULL>
-__device__ __forceinline__ void half_fma(const uint32_t vs, const int m, const float (&b)[2][NV],
+// columns are live beside the 4 x 8 accumulators.  M_r <= 4 (every pattern has its own FMA block).
+// Values and B stay packed as 16-bit pairs in 32-bit words: the mixed-precision FMA
+// (fma.rn.f32.bf16 / .f16: 16-bit a and b, FP32 c and d) widens its operands itself.  The product
+// of two 16-bit values is exact in FP32, so each step equals fmaf(float(a), float(b), c).
+#define SPREG_FMA_MIXED(T, A, B)                                                                     \
+    asm("{\n\t.reg .b16 a0, a1, b0, b1;\n\tmov.b32 {a0, a1}, %1;\n\tmov.b32 {b0, b1}, %2;\n\t" \
+        "fma.rn.f32." T " %0, " A ", " B ", %3;\n\t}"                                            \
+        : "=f"(d) : "r"(aw), "r"(bw), "f"(c))
+template <class TV, int HA, int HB>
+__device__ __forceinline__ float fma_mixed(const uint32_t aw, const uint32_t bw, const float c) {
+    float d;
+    if constexpr (std::is_same<TV, __nv_bfloat16>::value) {
+        if constexpr (HA == 0 && HB == 0) SPREG_FMA_MIXED("bf16", "a0", "b0");
+        else if constexpr (HA == 0) SPREG_FMA_MIXED("bf16", "a0", "b1");
+        else if constexpr (HB == 0) SPREG_FMA_MIXED("bf16", "a1", "b0");
+        else SPREG_FMA_MIXED("bf16", "a1", "b1");
+    } else {
+        if constexpr (HA == 0 && HB == 0) SPREG_FMA_MIXED("f16", "a0", "b0");
+        else if constexpr (HA == 0) SPREG_FMA_MIXED("f16", "a0", "b1");
+        else if constexpr (HB == 0) SPREG_FMA_MIXED("f16", "a1", "b0");
+        else SPREG_FMA_MIXED("f16", "a1", "b1");
+    }
+    return d;
+}
+#undef SPREG_FMA_MIXED
+
+// 2 entries of pattern PAT: B rows as packed words b[u][NV / 2], values from shared address vs
+// (2 x PC 16-bit values, PC words; a half starts 4 * PC bytes into its step).
+template <int PAT, int MR, int NV, class TV, bool FULL, int I0 = 0>
+__device__ __forceinline__ void half_fma(const uint32_t vs, const int m, const uint32_t (&b)[2][NV / 2],
                                          float (&acc)[MR][NV]) {
     constexpr int PC = cpopc(PAT);
-    constexpr int VB = (int)sizeof(TV);
-    static_assert(VB == 2 && MR <= 4, "256-column strips take 16-bit values and M_r <= 4");
-    uint32_t vw[PC];  // 2 entries x PC values x 2 bytes
+    static_assert(sizeof(TV) == 2 && MR <= 4, "256-column strips take 16-bit values and M_r <= 4");
+    uint32_t vw[PC];
 #pragma unroll
     for (int i = 0; i < PC; ++i) vw[i] = lds_u32(vs + 4u * i);
 #pragma unroll
@@ -625,10 +650,17 @@ __device__ __forceinline__ void half_fma(const uint32_t vs, const int m, const f
             for (int r = 0; r < MR; ++r) {
                 if ((PAT >> r) & 1) {
                     const int vi = u * PC + q;
-                    const float a = word_val<TV>(vw[vi >> 1], vi & 1);
                     ++q;
 #pragma unroll
-                    for (int j = 0; j < NV; ++j) acc[r][j] = fmaf(a, b[u][j], acc[r][j]);
+                    for (int j = 0; j < NV; j += 2) {
+                        if (vi & 1) {
+                            acc[r][j] = fma_mixed<TV, 1, 0>(vw[vi >> 1], b[u][j >> 1], acc[r][j]);
+                            acc[r][j + 1] = fma_mixed<TV, 1, 1>(vw[vi >> 1], b[u][j >> 1], acc[r][j + 1]);
+                        } else {
+                            acc[r][j] = fma_mixed<TV, 0, 0>(vw[vi >> 1], b[u][j >> 1], acc[r][j]);
+                            acc[r][j + 1] = fma_mixed<TV, 0, 1>(vw[vi >> 1], b[u][j >> 1], acc[r][j + 1]);
+                        }
+                    }
                 }
             }
         }
@@ -637,7 +669,7 @@ __device__ __forceinline__ void half_fma(const uint32_t vs, const int m, const f
 
 // The same with the pattern known at run time (groups of patterns without their own loop).
 template <int MR, int NV, class TV, bool FULL>
-__device__ __forceinline__ void half_dispatch(const int pat, const uint32_t vs, const int m, const float (&b)[2][NV],
+__device__ __forceinline__ void half_dispatch(const int pat, const uint32_t vs, const int m, const uint32_t (&b)[2][NV / 2],
                                               float (&acc)[MR][NV]) {
 #define SPREG_HCASE(P)                                                                          \
     case (P):                                                                                   \
@@ -659,7 +691,7 @@ __device__ __forceinline__ void run_group_wide(const int pat, const int n, uint3
                                                float (&acc)[MR][NV]) {
     const uint32_t pc = PAT > 0 ? (uint32_t)cpopc(PAT) : (uint32_t)__popc(pat);
     const uint32_t vhalf = 2u * (uint32_t)sizeof(TV) * pc, vstep = 2u * vhalf;
-    auto half = [&](uint32_t v, int m, const float (&b)[2][NV], auto full_tag) {
+    auto half = [&](uint32_t v, int m, const uint32_t (&b)[2][NV / 2], auto full_tag) {
         constexpr bool FULL = decltype(full_tag)::value;
         if constexpr (PAT > 0) half_fma<PAT, MR, NV, TV, FULL>(v, m, b, acc);
         else half_dispatch<MR, NV, TV, FULL>(pat, v, m, b, acc);
@@ -671,24 +703,24 @@ __device__ __forceinline__ void run_group_wide(const int pat, const int n, uint3
         const uint4 kk = k4;
         cs += 16u;
         if (s + 1 < full) k4 = lds_u128(cs);
-        float b[2][NV];
-        bl.load((int)kk.x, b[0]);
-        bl.load((int)kk.y, b[1]);
+        uint32_t b[2][NV / 2];
+        bl.load_raw((int)kk.x, b[0]);
+        bl.load_raw((int)kk.y, b[1]);
         half(vs, 2, b, std::true_type{});
-        bl.load((int)kk.z, b[0]);
-        bl.load((int)kk.w, b[1]);
+        bl.load_raw((int)kk.z, b[0]);
+        bl.load_raw((int)kk.w, b[1]);
         half(vs + vhalf, 2, b, std::true_type{});
         vs += vstep;
     }
     const int m = n & 3;
     if (m) {
         const uint4 kk = lds_u128(cs);
-        float b[2][NV];
-        bl.load((int)kk.x, b[0]);
-        if (m > 1) bl.load((int)kk.y, b[1]);
+        uint32_t b[2][NV / 2];
+        bl.load_raw((int)kk.x, b[0]);
+        if (m > 1) bl.load_raw((int)kk.y, b[1]);
         half(vs, m < 2 ? m : 2, b, std::false_type{});
         if (m > 2) {
-            bl.load((int)kk.z, b[0]);
+            bl.load_raw((int)kk.z, b[0]);
             half(vs + vhalf, m - 2, b, std::false_type{});
         }
     }

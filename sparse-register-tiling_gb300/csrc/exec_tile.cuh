@@ -110,6 +110,12 @@ template <int NV, class TB> struct SmemB {
     uint32_t base;       // tile + this lane's first column
     int32_t r0;          // B row of tile row 0
     uint32_t row_bytes;  // 32 * NV * sizeof(TB)
+    // 16-bit B, NV = 8: the lane's 8 columns as 4 packed words (for the mixed-precision FMA)
+    __device__ __forceinline__ void load_raw(int k, uint32_t (&w)[NV / 2]) const {
+        static_assert(sizeof(TB) == 2 && NV == 8, "packed B rows are 16-bit, 8 columns per lane");
+        const uint4 v = lds_u128(base + (uint32_t)(k - r0) * row_bytes);
+        w[0] = v.x; w[1] = v.y; w[2] = v.z; w[3] = v.w;
+    }
     __device__ __forceinline__ void load(int k, float (&b)[NV]) const {
         const uint32_t a = base + (uint32_t)(k - r0) * row_bytes;
         if constexpr (sizeof(TB) == 4) {

@@ -190,3 +190,30 @@ def test_nr_256_with_fp32_b_runs_128_column_strips(cuda):
     B = synth.dense(256, 512, seed=4)
     got, want = run_pair(A, m, B, k_tile=128, nr=256)
     assert same_bits(got, want)
+
+
+@pytest.mark.parametrize("vd", [_lib.BF16, _lib.F16])
+def test_tile_kernel_256_column_strips_ragged_k_and_row_tiles(cuda, vd):
+    """256-column strips on a ragged last K tile (K = 400, K_c = 128), row tiles (m_tile 48) and a
+    column offset into B."""
+    m = Mapping.identity(4)
+    A = synth.row_skew(301, 400, 0.92, seed=21, std=0.5)
+    off = 8
+    B = synth.dense(400 + off, 512, seed=22)
+    got, want = run_pair(A, m, B, k_tile=128, m_tile=48, col_offset=off, value_dtype=vd, nr=256)
+    assert same_bits(got, want)
+
+
+def test_work_order_single_panel_and_empty_rows(cuda):
+    """Work-ordered execution blocks with one panel, and with all-zero panels between dense ones."""
+    m = Mapping.identity(4)
+    A1 = synth.row_skew(3, 256, 0.5, seed=1, std=1.0)
+    B1 = synth.dense(256, 128, seed=2)
+    got, want = run_pair(A1, m, B1, k_tile=64)
+    assert same_bits(got, want)
+    A2 = synth.row_skew(96, 256, 0.8, seed=3, std=1.0)
+    A2[8:40] = 0.0
+    A2[60:64] = 0.0
+    B2 = synth.dense(256, 256, seed=4)
+    got, want = run_pair(A2, m, B2, k_tile=128)
+    assert same_bits(got, want)
