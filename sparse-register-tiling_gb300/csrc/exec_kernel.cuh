@@ -143,6 +143,12 @@ template <int NV> struct VecIO<NV, __nv_bfloat16> : VecIO16<NV, __nv_bfloat16> {
 template <int NV> struct VecIO<NV, __half> : VecIO16<NV, __half> {};
 
 // ------------------------------------------------------------------ B row sources
+// One lane's NV columns of a B row in registers: FP32 as floats; 16-bit B as the packed raw values
+// (pairs per 32-bit word), which the mixed-precision FMA (fma_vb) widens itself.
+template <int NV, class TB> struct BSeg { float f[NV]; };
+template <int NV> struct BSeg<NV, __nv_bfloat16> { uint32_t w[(NV + 1) / 2]; };
+template <int NV> struct BSeg<NV, __half> { uint32_t w[(NV + 1) / 2]; };
+
 // GlobalB reads the B rows of one lane's columns through L1/L2.
 template <int NV, class TB> struct GlobalB {
     const TB *p;  // B + this lane's first column
@@ -153,6 +159,24 @@ template <int NV, class TB> struct GlobalB {
             b[0] = valid ? DT<TB>::to_f32(__ldg(p + (int64_t)k * ld)) : 0.0f;
         } else {
             VecIO<NV, TB>::load(p + (int64_t)k * ld, b);
+        }
+    }
+    __device__ __forceinline__ void load(int k, BSeg<NV, TB> &b) const {
+        if constexpr (sizeof(TB) == 4) {
+            load(k, b.f);
+        } else {
+            const TB *q = p + (int64_t)k * ld;
+            if constexpr (NV == 1) {
+                b.w[0] = valid ? (uint32_t)__ldg(reinterpret_cast<const unsigned short *>(q)) : 0u;
+            } else if constexpr (NV == 2) {
+                b.w[0] = __ldg(reinterpret_cast<const unsigned int *>(q));
+            } else if constexpr (NV == 4) {
+                const uint2 v = __ldg(reinterpret_cast<const uint2 *>(q));
+                b.w[0] = v.x; b.w[1] = v.y;
+            } else {
+                const uint4 v = __ldg(reinterpret_cast<const uint4 *>(q));
+                b.w[0] = v.x; b.w[1] = v.y; b.w[2] = v.z; b.w[3] = v.w;
+            }
         }
     }
 };
@@ -477,6 +501,50 @@ template <class TV> __device__ __forceinline__ float word_val(uint32_t w, int ha
         return DT<TV>::to_f32(*reinterpret_cast<const TV *>(&h));
     }
 }
+// Mixed-precision FMA (fma.rn.f32.bf16 / .f16): d = a * b + c with a, b the 16-bit halves HA / HB
+// (0 = low) of two 32-bit words and c, d FP32.  The product of two 16-bit values is exact in FP32,
+// so the result equals fmaf(float(a), float(b), c) bit for bit, without the two widening ops.
+#define SPREG_FMA_MIXED(T, A, B)                                                                     \
+    asm("{\n\t.reg .b16 a0, a1, b0, b1;\n\tmov.b32 {a0, a1}, %1;\n\tmov.b32 {b0, b1}, %2;\n\t" \
+        "fma.rn.f32." T " %0, " A ", " B ", %3;\n\t}"                                            \
+        : "=f"(d) : "r"(aw), "r"(bw), "f"(c))
+template <class TV, int HA, int HB>
+__device__ __forceinline__ float fma_mixed(const uint32_t aw, const uint32_t bw, const float c) {
+    float d;
+    if constexpr (std::is_same<TV, __nv_bfloat16>::value) {
+        if constexpr (HA == 0 && HB == 0) SPREG_FMA_MIXED("bf16", "a0", "b0");
+        else if constexpr (HA == 0) SPREG_FMA_MIXED("bf16", "a0", "b1");
+        else if constexpr (HB == 0) SPREG_FMA_MIXED("bf16", "a1", "b0");
+        else SPREG_FMA_MIXED("bf16", "a1", "b1");
+    } else {
+        if constexpr (HA == 0 && HB == 0) SPREG_FMA_MIXED("f16", "a0", "b0");
+        else if constexpr (HA == 0) SPREG_FMA_MIXED("f16", "a0", "b1");
+        else if constexpr (HB == 0) SPREG_FMA_MIXED("f16", "a1", "b0");
+        else SPREG_FMA_MIXED("f16", "a1", "b1");
+    }
+    return d;
+}
+#undef SPREG_FMA_MIXED
+
+// acc + a * b[j]: a = half `ha` of value word aw (the word itself for FP32), b[j] = column j of the
+// lane's B segment.  ha and j are compile-time after unrolling.
+template <class TV, int NV>
+__device__ __forceinline__ float fma_vb(const uint32_t aw, const int ha, const BSeg<NV, TV> &b, const int j,
+                                        const float c) {
+    if constexpr (sizeof(TV) == 4) {
+        return fmaf(__uint_as_float(aw), b.f[j], c);
+    } else {
+        const uint32_t bw = b.w[j >> 1];
+        if (ha == 0) return (j & 1) ? fma_mixed<TV, 0, 1>(aw, bw, c) : fma_mixed<TV, 0, 0>(aw, bw, c);
+        return (j & 1) ? fma_mixed<TV, 1, 1>(aw, bw, c) : fma_mixed<TV, 1, 0>(aw, bw, c);
+    }
+}
+// Column j of a B segment as FP32 (paths that multiply by an FP32 value).
+template <class TV, int NV> __device__ __forceinline__ float bseg_f32(const BSeg<NV, TV> &b, const int j) {
+    if constexpr (sizeof(TV) == 4) return b.f[j];
+    else return word_val<TV>(b.w[j >> 1], j & 1);
+}
+
 // Value i (compile-time after unrolling) of a block of quads.
 template <class TV, int NQ> __device__ __forceinline__ float quad_val(const uint4 (&q)[NQ], int i) {
     constexpr int PER_WORD = 4 / sizeof(TV);
@@ -500,7 +568,8 @@ __device__ __forceinline__ uint2 lds_u64(uint32_t a) {
 // broadcast loads of 16 (FP32) or 8 (16-bit) bytes; entry u's values follow in ascending row
 // order.  FULL steps have 4 entries; the last step of a group has m < 4 (entries u >= m skipped).
 template <int PAT, int MR, int NV, class TV, bool FULL>
-__device__ __forceinline__ void step_fma(const uint32_t vs, const int m, const float (&b)[4][NV], float (&acc)[MR][NV]) {
+__device__ __forceinline__ void step_fma(const uint32_t vs, const int m, const BSeg<NV, TV> (&b)[4],
+                                         float (&acc)[MR][NV]) {
     constexpr int PC = cpopc(PAT);
     constexpr int VB = (int)sizeof(TV);
     uint32_t vw[PC * VB];
@@ -522,10 +591,10 @@ __device__ __forceinline__ void step_fma(const uint32_t vs, const int m, const f
             for (int r = 0; r < MR; ++r) {
                 if ((PAT >> r) & 1) {
                     const int vi = u * PC + q;
-                    const float a = word_val<TV>(vw[vi * VB / 4], (vi * VB / 2) & 1);
                     ++q;
 #pragma unroll
-                    for (int j = 0; j < NV; ++j) acc[r][j] = fmaf(a, b[u][j], acc[r][j]);
+                    for (int j = 0; j < NV; ++j)
+                        acc[r][j] = fma_vb<TV, NV>(vw[vi * VB / 4], (vi * VB / 2) & 1, b[u], j, acc[r][j]);
                 }
             }
         }
@@ -534,7 +603,7 @@ __device__ __forceinline__ void step_fma(const uint32_t vs, const int m, const f
 
 // Rows BASE .. BASE+3 of the 4-bit sub-pattern Q of one entry (values from shared address va).
 template <int Q, int BASE, int MR, int NV, class TV>
-__device__ __forceinline__ void fma_nibble_x(uint32_t va, const float (&b)[NV], float (&acc)[MR][NV]) {
+__device__ __forceinline__ void fma_nibble_x(uint32_t va, const BSeg<NV, TV> &b, float (&acc)[MR][NV]) {
     int q = 0;
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
@@ -542,7 +611,7 @@ __device__ __forceinline__ void fma_nibble_x(uint32_t va, const float (&b)[NV], 
             const float a = lds_val<TV>(va + (uint32_t)(q * sizeof(TV)));
             ++q;
 #pragma unroll
-            for (int j = 0; j < NV; ++j) acc[BASE + r][j] = fmaf(a, b[j], acc[BASE + r][j]);
+            for (int j = 0; j < NV; ++j) acc[BASE + r][j] = fmaf(a, bseg_f32<TV, NV>(b, j), acc[BASE + r][j]);
         }
     }
 }
@@ -550,7 +619,7 @@ __device__ __forceinline__ void fma_nibble_x(uint32_t va, const float (&b)[NV], 
 // One step of a pattern without its own FMA block (M_r 6 and 8): entry by entry, rows 0-3 then
 // rows 4-7 through 16-way switches.
 template <int MR, int NV, class TV>
-__device__ __forceinline__ void step_fma_nibbles(const int pat, const uint32_t vs, const int m, const float (&b)[4][NV],
+__device__ __forceinline__ void step_fma_nibbles(const int pat, const uint32_t vs, const int m, const BSeg<NV, TV> (&b)[4],
                                                  float (&acc)[MR][NV]) {
     if constexpr (MR > 4) {
         const int lo = pat & 15, hi = (pat >> 4) & 15;
@@ -582,7 +651,7 @@ __device__ __forceinline__ void step_fma_nibbles(const int pat, const uint32_t v
 
 // The FMA block of one step, selected by one uniform switch on the pattern.
 template <int MR, int NV, class TV, bool FULL>
-__device__ __forceinline__ void step_dispatch(const int pat, const uint32_t vs, const int m, const float (&b)[4][NV],
+__device__ __forceinline__ void step_dispatch(const int pat, const uint32_t vs, const int m, const BSeg<NV, TV> (&b)[4],
                                               float (&acc)[MR][NV]) {
     bool done = false;
 #define SPREG_CASE(P)                                                                \
@@ -610,27 +679,6 @@ __device__ __forceinline__ void step_dispatch(const int pat, const uint32_t vs, 
 // Values and B stay packed as 16-bit pairs in 32-bit words: the mixed-precision FMA
 // (fma.rn.f32.bf16 / .f16: 16-bit a and b, FP32 c and d) widens its operands itself.  The product
 // of two 16-bit values is exact in FP32, so each step equals fmaf(float(a), float(b), c).
-#define SPREG_FMA_MIXED(T, A, B)                                                                     \
-    asm("{\n\t.reg .b16 a0, a1, b0, b1;\n\tmov.b32 {a0, a1}, %1;\n\tmov.b32 {b0, b1}, %2;\n\t" \
-        "fma.rn.f32." T " %0, " A ", " B ", %3;\n\t}"                                            \
-        : "=f"(d) : "r"(aw), "r"(bw), "f"(c))
-template <class TV, int HA, int HB>
-__device__ __forceinline__ float fma_mixed(const uint32_t aw, const uint32_t bw, const float c) {
-    float d;
-    if constexpr (std::is_same<TV, __nv_bfloat16>::value) {
-        if constexpr (HA == 0 && HB == 0) SPREG_FMA_MIXED("bf16", "a0", "b0");
-        else if constexpr (HA == 0) SPREG_FMA_MIXED("bf16", "a0", "b1");
-        else if constexpr (HB == 0) SPREG_FMA_MIXED("bf16", "a1", "b0");
-        else SPREG_FMA_MIXED("bf16", "a1", "b1");
-    } else {
-        if constexpr (HA == 0 && HB == 0) SPREG_FMA_MIXED("f16", "a0", "b0");
-        else if constexpr (HA == 0) SPREG_FMA_MIXED("f16", "a0", "b1");
-        else if constexpr (HB == 0) SPREG_FMA_MIXED("f16", "a1", "b0");
-        else SPREG_FMA_MIXED("f16", "a1", "b1");
-    }
-    return d;
-}
-#undef SPREG_FMA_MIXED
 
 // 2 entries of pattern PAT: B rows as packed words b[u][NV / 2], values from shared address vs
 // (2 x PC 16-bit values, PC words; a half starts 4 * PC bytes into its step).
@@ -742,7 +790,7 @@ __device__ __forceinline__ void run_group_pat(const int n, uint32_t cs, uint32_t
         uint4 k4 = full > 0 ? lds_u128(cs) : make_uint4(0, 0, 0, 0);
 #pragma unroll 1
         for (int s = 0; s < full; ++s) {
-            float b[4][NV];
+            BSeg<NV, TV> b[4];
             bl.load((int)k4.x, b[0]);
             bl.load((int)k4.y, b[1]);
             bl.load((int)k4.z, b[2]);
@@ -755,7 +803,7 @@ __device__ __forceinline__ void run_group_pat(const int n, uint32_t cs, uint32_t
     } else if (full > 0) {
         // software pipeline: the next step's column indices and B rows load before this step's FMAs
         uint4 k4 = lds_u128(cs);
-        float b[4][NV];
+        BSeg<NV, TV> b[4];
         bl.load((int)k4.x, b[0]);
         bl.load((int)k4.y, b[1]);
         bl.load((int)k4.z, b[2]);
@@ -763,7 +811,7 @@ __device__ __forceinline__ void run_group_pat(const int n, uint32_t cs, uint32_t
 #pragma unroll 1
         for (int s = 0; s < full; ++s) {
             cs += 16u;
-            float bn[4][NV];
+            BSeg<NV, TV> bn[4];
             if (s + 1 < full) {
                 k4 = lds_u128(cs);
                 bl.load((int)k4.x, bn[0]);
@@ -774,16 +822,14 @@ __device__ __forceinline__ void run_group_pat(const int n, uint32_t cs, uint32_t
             step_fma<PAT, MR, NV, TV, true>(vs, 4, b, acc);
             vs += VSTEP;
 #pragma unroll
-            for (int u = 0; u < 4; ++u)
-#pragma unroll
-                for (int j = 0; j < NV; ++j) b[u][j] = bn[u][j];
+            for (int u = 0; u < 4; ++u) b[u] = bn[u];
         }
     }
     const int m = n & 3;
     if (m) {
         const uint4 k4 = lds_u128(cs);
         const int ks[4] = {(int)k4.x, (int)k4.y, (int)k4.z, (int)k4.w};
-        float b[4][NV];
+        BSeg<NV, TV> b[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u)
             if (u < m) bl.load(ks[u], b[u]);
@@ -821,7 +867,7 @@ __device__ __forceinline__ void run_group_x(const int pat, const int n, uint32_t
 #pragma unroll 1
     for (int s = 0; s < full; ++s) {
         const uint4 k4 = lds_u128(cs);
-        float b[4][NV];
+        BSeg<NV, TV> b[4];
         bl.load((int)k4.x, b[0]);
         bl.load((int)k4.y, b[1]);
         bl.load((int)k4.z, b[2]);
@@ -834,7 +880,7 @@ __device__ __forceinline__ void run_group_x(const int pat, const int n, uint32_t
     if (m) {
         const uint4 k4 = lds_u128(cs);
         const int ks[4] = {(int)k4.x, (int)k4.y, (int)k4.z, (int)k4.w};
-        float b[4][NV];
+        BSeg<NV, TV> b[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u)
             if (u < m) bl.load(ks[u], b[u]);

@@ -151,6 +151,23 @@ template <int NV, class TB> struct SmemB {
             }
         }
     }
+    __device__ __forceinline__ void load(int k, BSeg<NV, TB> &b) const {
+        if constexpr (sizeof(TB) == 4) {
+            load(k, b.f);
+        } else {
+            const uint32_t a = base + (uint32_t)(k - r0) * row_bytes;
+            if constexpr (NV == 1) {
+                b.w[0] = (uint32_t)lds_u16(a);
+            } else if constexpr (NV == 2) {
+                b.w[0] = lds_u32(a);
+            } else if constexpr (NV == 4) {
+                const uint2 v = lds_u64(a);
+                b.w[0] = v.x; b.w[1] = v.y;
+            } else {
+                load_raw(k, b.w);
+            }
+        }
+    }
 };
 
 // C tile init / store of one (problem, panel, strip), as x_acc_init / x_store.
