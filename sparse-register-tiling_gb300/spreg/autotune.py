@@ -46,7 +46,7 @@ MAPPINGS_FOR_MR = {2: ("identity",), 4: ("identity",), 8: ("identity", "400fa", 
 class Candidate:
     mr: int
     mapping: str     # "identity" or a mapping id
-    nr: int          # strip width: 32, 64 or 128 columns
+    nr: int          # strip width: 32, 64, 128 or (16-bit B, K_c <= 128) 256 columns
     k_tile: int = 0  # K_c of the packing (0: one K tile)
 
     @property
@@ -235,20 +235,24 @@ def fit_costs(samples: Sequence[Tuple[str, PanelStats, int, int, float]], sms: i
 
 
 # ---------------------------------------------------------------------------- tuning
-K_TILES = (0, 512, 1024)
+K_TILES = (0, 128, 512, 1024)
 
 
 def candidates(n: int, mrs: Iterable[int] = (2, 4, 8), k: int = 0,
-               k_tiles: Iterable[int] = K_TILES) -> List[Candidate]:
-    """Every (M_r, mapping, N_r, K_c) worth trying for n columns of B and K = k (K_c < K only)."""
+               k_tiles: Iterable[int] = K_TILES, wide: bool = False) -> List[Candidate]:
+    """Every (M_r, mapping, N_r, K_c) worth trying for n columns of B and K = k (K_c < K only).
+    `wide` (16-bit B) adds 256-column strips for M_r <= 4 packs with K_c <= 128: the B-tile
+    executor runs them, its stage holding K_c x 256 16-bit values."""
     out = []
     for mr in mrs:
         for mp in MAPPINGS_FOR_MR.get(mr, ("identity",)):
-            for nr in (32, 64, 128):
+            for nr in (32, 64, 128, 256):
                 if nr > 32 and n < nr // 2:
                     continue  # a strip wider than twice the columns only adds masked lanes
                 for kt in k_tiles:
                     if kt and not (0 < kt < k):
+                        continue
+                    if nr == 256 and not (wide and mr <= 4 and 0 < kt <= 128):
                         continue
                     out.append(Candidate(mr, mp, nr, kt))
     return out
@@ -269,7 +273,7 @@ def rank(mask: np.ndarray, n: int, dtype: str = "f32", costs: Optional[Costs] = 
     costs = costs if costs is not None else Costs.load()
     stats: Dict[Tuple[int, str], PanelStats] = {}
     ranked = []
-    cands = candidates(n, mrs, mask.shape[1], k_tiles)
+    cands = candidates(n, mrs, mask.shape[1], k_tiles, wide=dtype != "f32")
     if greedy and 8 in tuple(mrs):
         gid = greedy_mapping(mask, 8).mapping_id
         cands += [Candidate(c.mr, gid, c.nr, c.k_tile) for c in cands if c.mr == 8 and c.mapping == "identity"]
@@ -279,7 +283,11 @@ def rank(mask: np.ndarray, n: int, dtype: str = "f32", costs: Optional[Costs] = 
             stats[key] = panel_stats(mask, c.mr, mapping_of(c.mr, c.mapping))
         # the model has no K_c term: K tiles only shrink per-warp metadata buffers (occupancy),
         # which the device timing decides; a tiny tie-break keeps untiled first among equals
-        ranked.append((costs.predict_ns(stats[key], n, c.nv, dtype) * (1.0 + 1e-6 * (c.k_tile > 0)), c))
+        # 256-column strips have no fitted coefficients: the 128-column prediction, just ahead of
+        # it, so the device timing of the top candidates compares the two
+        nv = min(c.nv, 4)
+        ranked.append((costs.predict_ns(stats[key], n, nv, dtype) * (1.0 + 1e-6 * (c.k_tile > 0)) *
+                       (0.999 if c.nv > 4 else 1.0), c))
     ranked.sort(key=lambda x: x[0])
     return ranked, stats
 

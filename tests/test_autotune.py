@@ -76,14 +76,20 @@ def test_rank_orders_all_candidates():
     ts = [t for t, _ in ranked]
     assert ts == sorted(ts)
     names = {c.name() for _, c in ranked}
-    assert names == {c.name() for c in candidates(48)}
+    assert names == {c.name() for c in candidates(48, k=512)}
     assert "M4N64_identity" in names and "M8N32_400fa" in names and "M4N128_identity" not in names
     assert set(stats) == {(2, "identity"), (4, "identity"), (8, "identity"), (8, "400fa"), (8, "747f9")}
     assert Candidate(4, "identity", 64).name() == "M4N64_identity"
     assert Candidate(2, "identity", 32, 1024).name() == "M2N32_identity_K1024"
     wide = {c.name() for c in candidates(64, (2,), k=2048)}
     assert {"M2N64_identity", "M2N64_identity_K512", "M2N64_identity_K1024"} <= wide
-    assert not any("_K" in c.name() for c in candidates(64, (4,), k=512))
+    assert not any("_K" in c.name() for c in candidates(64, (4,), k=128))
+    assert {c.k_tile for c in candidates(64, (4,), k=512)} == {0, 128}
+    # 256-column strips: 16-bit B, M_r <= 4, K_c <= 128, n >= 128
+    w = {c.name() for c in candidates(512, (4, 8), k=1024, wide=True)}
+    assert "M4N256_identity_K128" in w and not any(n.startswith("M8N256") for n in w)
+    assert not any("N256" in n for n in w if "_K128" not in n)
+    assert not any(c.nr == 256 for c in candidates(512, (4,), k=1024))
 
 
 @pytest.mark.gpu
