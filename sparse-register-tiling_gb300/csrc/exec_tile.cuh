@@ -107,17 +107,17 @@ __device__ __forceinline__ int4 lds_v4(uint32_t a) {
 
 // B rows of one lane's columns out of a shared-memory tile: row c of B is tile row c - r0.
 template <int NV, class TB> struct SmemB {
-    uint32_t base;       // tile + this lane's first column
-    int32_t r0;          // B row of tile row 0
+    uint32_t base;       // tile + this lane's first column - r0 * row_bytes (mod 2^32): B row c is at
+                         // base + c * row_bytes, one shift-add per entry
     uint32_t row_bytes;  // 32 * NV * sizeof(TB)
     // 16-bit B, NV = 8: the lane's 8 columns as 4 packed words (for the mixed-precision FMA)
     __device__ __forceinline__ void load_raw(int k, uint32_t (&w)[NV / 2]) const {
         static_assert(sizeof(TB) == 2 && NV == 8, "packed B rows are 16-bit, 8 columns per lane");
-        const uint4 v = lds_u128(base + (uint32_t)(k - r0) * row_bytes);
+        const uint4 v = lds_u128(base + (uint32_t)k * row_bytes);
         w[0] = v.x; w[1] = v.y; w[2] = v.z; w[3] = v.w;
     }
     __device__ __forceinline__ void load(int k, float (&b)[NV]) const {
-        const uint32_t a = base + (uint32_t)(k - r0) * row_bytes;
+        const uint32_t a = base + (uint32_t)k * row_bytes;
         if constexpr (sizeof(TB) == 4) {
             if constexpr (NV == 1) {
                 b[0] = __uint_as_float(lds_u32(a));
@@ -155,7 +155,7 @@ template <int NV, class TB> struct SmemB {
         if constexpr (sizeof(TB) == 4) {
             load(k, b.f);
         } else {
-            const uint32_t a = base + (uint32_t)(k - r0) * row_bytes;
+            const uint32_t a = base + (uint32_t)k * row_bytes;
             if constexpr (NV == 1) {
                 b.w[0] = (uint32_t)lds_u16(a);
             } else if constexpr (NV == 2) {
@@ -348,8 +348,8 @@ __global__ void __launch_bounds__(32 * (kTileMaxWarps + 1), 1) exec_tile_kernel(
             const uint32_t sb = stage0 + (uint32_t)s * stage_bytes;
             const uint32_t buf =
                 sb + (uint32_t)tp.stage_b + lds_u32(moffs0 + 4u * (uint32_t)(s * kTileMaxWarps + warp));
-            const SmemB<NV, TB> bl{sb + (uint32_t)lane * (uint32_t)(NV * sizeof(TB)),
-                                   (int32_t)(pr.col_offset + (int64_t)t * pr.kt), ROWB};
+            const uint32_t r0 = (uint32_t)(pr.col_offset + t * pr.kt);  // B row of tile row 0
+            const SmemB<NV, TB> bl{sb + (uint32_t)lane * (uint32_t)(NV * sizeof(TB)) - r0 * ROWB, ROWB};
             const uint32_t G = lds_u32(buf);
 #pragma unroll 1
             for (uint32_t g = 0; g < G; ++g) {
