@@ -354,6 +354,33 @@ def precision_suite(dev) -> list:
     return rows
 
 
+def csr_baseline_leg(A, B_dev, pack, args, batched_spmm_us: float) -> dict:
+    """The reference's CSR baseline (csr.executor, row x N-tile) on the GPU beside the register-tiled
+    executor, as sop_bench.py:197 times them: replica 0, one SpMM per launch, the reference's
+    protocol (median of 150 x num_runs runs); bit-exact check against the restated baseline."""
+    import ctypes as C
+
+    import torch
+    from oracle import oracle as O
+    from spreg import _lib, synth
+    rp, ci, v = synth.to_csr(A)
+    dev = B_dev.device
+    trp, tci, tv = (torch.from_numpy(x).to(dev) for x in (rp, ci, v))
+    Cc = torch.empty((args.m, args.n), device=dev)
+    t = C.c_double()
+    _lib.check(_lib.lib().spreg_csr_spmm_timed(args.m, args.k, args.n, int(v.size), trp.data_ptr(), tci.data_ptr(),
+                                               tv.data_ptr(), B_dev.data_ptr(), args.n, Cc.data_ptr(), args.n, 64, 10,
+                                               C.byref(t), _lib.stream_handle(None)))
+    torch.cuda.synchronize()
+    exact = bool(np.array_equal(Cc.cpu().numpy(), O.csr_spmm(rp, ci, v, B_dev.cpu().numpy())))
+    Cs = torch.empty((args.m, args.n), device=dev)
+    sop_ns = pack.execute_timed(B_dev, Cs, num_runs=10)
+    nbytes = v.size * 8 + rp.size * 4 + args.k * args.n * 4 + args.m * args.n * 4
+    return {"csr_us": t.value / 1e3, "csr_gbs": nbytes / t.value, "csr_bit_exact_vs_oracle": exact,
+            "sop_single_us": sop_ns / 1e3, "sop_batched_us": batched_spmm_us,
+            "note": "replica 0; one SpMM per launch (median of 150 x 10 runs), except sop_batched_us (96 per launch)"}
+
+
 def ffn_sweep(dev, replicas: int = 32, steps: int = 20) -> list:
     """The FFN-shaped workload across its sparsities and storage types: A 2048 x 512 and 512 x 2048
     at 0.7, 0.8, 0.9, 0.95 and 0.98 (log-normal row skew, sigma 0.5, values N(0, 0.02)), B K x 512
@@ -836,6 +863,7 @@ def main():
 
     # the secondary legs describe one GPU: rank 0 alone runs them, the other ranks are done
     lead = rank == 0
+    csr_leg = csr_baseline_leg(As[0], Bd[0], packs[0], args, spmm_us) if (lead and args.dtype == "f32") else None
     serving = serving_bench(args, dev) if (lead and args.serving) else None
     precision = precision_suite(dev) if (lead and args.precision) else None
     tensor_cores = tensor_core_suite(dev) if (lead and args.tensor_cores) else None
@@ -866,7 +894,7 @@ def main():
                            "parallelism": f"replicas x{ws}"},
                 "gflops": gflops, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "serving": serving,
                 "precision": precision, "batched_layers": layers, "tensor_cores": tensor_cores,
-                "ffn_sparsity_sweep": sweep,
+                "ffn_sparsity_sweep": sweep, "gpu_csr_baseline": csr_leg,
                 "clocks": clocks, "gpu_launches": launches_per_step * args.steps,
                 "parity_bit_exact_vs_oracle": parity_ok}
         print(json.dumps(line))

@@ -270,6 +270,22 @@ int spreg_device_status(int32_t *status_host, int32_t reset);
 int spreg_execute_timed(const spreg_packed *a, const spreg_exec_args *args, int64_t num_runs,
                         double *median_ns, spreg_stream_t stream);
 
+/* ------------------------------------------- CSR baseline (the reference's csr module) */
+/* C = A.B for a CSR A (rows x cols, nnz entries, device arrays) and B (cols x n, ldb), FP32,
+ * row x N-tile FMAs in CSR order from zero: pytorch_csr_wrapper.cpp:70-191 (kernel) and :314-353
+ * (csr.executor, as sbench/SOP/sop_bench.py:197 calls it).  n_tile is the reference's tile of
+ * 16 / 32 / 64 / 128 floats; it sets the strip width, never the result.  Row pointers are clamped
+ * to [0, nnz]; a column index outside [0, cols) contributes nothing and sets the device status
+ * word (20). */
+int spreg_csr_spmm(int64_t rows, int64_t cols, int64_t n, int64_t nnz, const int32_t *row_ptrs,
+                   const int32_t *col_inds, const float *values, const float *b, int64_t ldb, float *c, int64_t ldc,
+                   int32_t n_tile, spreg_stream_t stream);
+/* profile() of pytorch_csr_wrapper.cpp:200-232: num_runs warm-up runs, then 150 x num_runs timed
+ * runs; *median_ns = the median per run (ns).  C holds one product afterwards. */
+int spreg_csr_spmm_timed(int64_t rows, int64_t cols, int64_t n, int64_t nnz, const int32_t *row_ptrs,
+                         const int32_t *col_inds, const float *values, const float *b, int64_t ldb, float *c,
+                         int64_t ldc, int32_t n_tile, int64_t num_runs, double *median_ns, spreg_stream_t stream);
+
 /* ------------------------------------------- MatMulSpecialized (C++ path, host buffers) */
 typedef struct {
     int32_t m_tile, k_tile, n_tile; /* M_c, K_c, N_c (SOPConfig m_tile/k_tile/n_tile) */

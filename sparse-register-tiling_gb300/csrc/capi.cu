@@ -33,6 +33,10 @@ int execute_impl(const spreg_packed *, const spreg_exec_args *, cudaStream_t);
 int execute_timed_impl(const spreg_packed *, const spreg_exec_args *, int64_t, double *, cudaStream_t);
 int execute_batched_impl(const spreg_work_item *, int32_t, cudaStream_t);
 int device_status_impl(int32_t *, int);
+int csr_spmm_impl(int64_t, int64_t, int64_t, int64_t, const int32_t *, const int32_t *, const float *, const float *,
+                  int64_t, float *, int64_t, int32_t, cudaStream_t);
+int csr_spmm_timed_impl(int64_t, int64_t, int64_t, int64_t, const int32_t *, const int32_t *, const float *,
+                        const float *, int64_t, float *, int64_t, int32_t, int64_t, double *, cudaStream_t);
 
 static std::mutex g_map_mu;
 
@@ -388,6 +392,22 @@ int spreg_execute_timed(const spreg_packed *a, const spreg_exec_args *args, int6
                         spreg_stream_t stream) {
     clear_error();
     return execute_timed_impl(a, args, num_runs, median_ns, (cudaStream_t)stream);
+}
+
+// ---------------------------------------------------------------------- CSR baseline
+int spreg_csr_spmm(int64_t rows, int64_t cols, int64_t n, int64_t nnz, const int32_t *row_ptrs,
+                   const int32_t *col_inds, const float *values, const float *b, int64_t ldb, float *c, int64_t ldc,
+                   int32_t n_tile, spreg_stream_t stream) {
+    clear_error();
+    return csr_spmm_impl(rows, cols, n, nnz, row_ptrs, col_inds, values, b, ldb, c, ldc, n_tile, (cudaStream_t)stream);
+}
+
+int spreg_csr_spmm_timed(int64_t rows, int64_t cols, int64_t n, int64_t nnz, const int32_t *row_ptrs,
+                         const int32_t *col_inds, const float *values, const float *b, int64_t ldb, float *c,
+                         int64_t ldc, int32_t n_tile, int64_t num_runs, double *median_ns, spreg_stream_t stream) {
+    clear_error();
+    return csr_spmm_timed_impl(rows, cols, n, nnz, row_ptrs, col_inds, values, b, ldb, c, ldc, n_tile, num_runs,
+                               median_ns, (cudaStream_t)stream);
 }
 
 // ---------------------------------------------------------------------- MatMulSpecialized

@@ -194,6 +194,50 @@ class SOPModule:
         return t_ns, (Cd if B.is_cuda else Cd.cpu())
 
 
+class CsrModule:
+    """The reference's `csr` torch module (sbench/SOP/sop_driver.py:33-34, built from
+    _C/pytorch_csr_wrapper.cpp): the CSR baseline that the register-tiled executor is timed against
+    (sop_bench.py:197).  Here it runs as a CUDA kernel (`spreg_csr_spmm`): row x N-tile FMAs in CSR
+    order, bit-identical to the restated baseline."""
+
+    def executor(self, mat, B, num_runs: int = 1024, n_tile: int = 64):
+        """(time, C) = executor(mat, B, num_runs, n_tile) (pytorch_csr_wrapper.cpp:314-353): C = mat . B
+        for a 2-D sparse CSR tensor and a contiguous B; time = median ns per run of 150 x num_runs
+        runs after num_runs warm-up runs.  C is on B's device."""
+        import torch
+        if not getattr(mat, "is_sparse_csr", False) and getattr(mat, "layout", None) != torch.sparse_csr:
+            raise RuntimeError("mat must be a sparse CSR tensor (TORCH_INTERNAL_ASSERT mat.is_sparse_csr())")
+        if mat.dim() != 2:
+            raise RuntimeError("mat must be 2-D")
+        rows, cols = int(mat.shape[0]), int(mat.shape[1])
+        if cols != B.shape[0]:
+            raise RuntimeError(f"mat.size(1) size mismatch with B.size(0) ({cols} vs {B.shape[0]})")
+        if not B.is_contiguous():
+            raise RuntimeError("B must be contiguous")
+        nnz = int(mat._nnz())
+        if nnz > 2 ** 31 - 1:
+            raise RuntimeError("nnz out of range for int32 indices")
+        dev = B.device if B.is_cuda else torch.device("cuda", torch.cuda.current_device())
+        rp = mat.crow_indices().to(dev, torch.int32).contiguous()
+        ci = mat.col_indices().to(dev, torch.int32).contiguous()
+        v = mat.values().to(dev, torch.float32).contiguous()
+        dB = B.to(dev, torch.float32).contiguous()
+        n = int(dB.shape[1])
+        Cd = torch.zeros((rows, n), dtype=torch.float32, device=dev)
+        stream = _lib.stream_handle(None)
+        args = (rows, cols, n, nnz, rp.data_ptr(), ci.data_ptr() if nnz else None, v.data_ptr() if nnz else None,
+                dB.data_ptr(), n, Cd.data_ptr(), n, int(n_tile))
+        t = C.c_double()
+        _lib.check(_lib.lib().spreg_csr_spmm_timed(*args, int(num_runs), C.byref(t), stream))
+        Cd.zero_()
+        _lib.check(_lib.lib().spreg_csr_spmm(*args, stream))
+        torch.cuda.synchronize(dev)
+        return float(t.value), (Cd if B.is_cuda else Cd.cpu())
+
+
+csr = CsrModule()
+
+
 def sort_and_encode_patterns(mapping: Mapping, pat_codes):
     """(encoded, order) of template:84-98, computed by a GPU kernel; returns int32 tensors on pat_codes' device."""
     import torch
