@@ -575,7 +575,7 @@ def tensor_core_suite(dev, reps: int = 20) -> dict:
         hyb[f"{m}x{k}_n{n}"] = tune_tc_fill(A, Mapping.identity(2), n, k_tile=kt)
     return {"dense_bf16_4096^3_us": us, "tflops": tflops, "peak_tflops": peak,
             "frac_of_measured_peak": (tflops / peak) if peak else None,
-            "rel_err_vs_fp32_of_bf16_inputs": err, "includes": "B transpose into K-major + tcgen05 kernel",
+            "rel_err_vs_fp32_of_bf16_inputs": err, "includes": "API call: tcgen05 kernel reading B in place (N-major operand), set-up and launch",
             "hybrid_threshold_serving_layers": hyb}
 
 

@@ -51,7 +51,8 @@ constexpr int TC_MAX_PROBLEMS = 80;  // problems per launch (two tensor maps eac
 
 struct TcProblem {
     CUtensorMap a_map;           // A_rows: columns [0, K) x rows [0, R), box 64 x 128, 128-byte swizzle
-    CUtensorMap b_map;           // Bt: columns [0, K) x rows [0, n), box 64 x 128, 128-byte swizzle
+    CUtensorMap b_map;           // Bt: columns [0, K) x rows [0, n), box 64 x BN, 128-byte swizzle; or
+                                 // (b_mn) B itself: columns [0, n) x rows [0, K), box 64 x 64
     const int32_t *row_index;    // output row of each A row
     void *C;
     int64_t ldc;
@@ -63,7 +64,8 @@ struct TcProblem {
     const int32_t *seg_start;
     void *const *seg_c;
     const int64_t *seg_ldc;
-    int32_t nseg, pad0;
+    int32_t nseg;
+    int32_t b_mn;                // B read in place (N-major operand), no transpose
 };
 
 struct TcParams {
@@ -108,6 +110,19 @@ __device__ __forceinline__ uint64_t tc_desc(uint32_t saddr) {
     d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);  // start address, 16-byte units
     d |= (uint64_t)1 << 16;                    // leading-dimension byte offset (unused for this layout)
     d |= (uint64_t)(1024 >> 4) << 32;          // stride-dimension byte offset: next 8-row group
+    d |= (uint64_t)1 << 46;                    // descriptor version of tcgen05
+    d |= (uint64_t)2 << 61;                    // layout: 128-byte swizzle
+    return d;
+}
+
+// Shared-memory matrix descriptor of an N-major (MN-major) operand tile with the 128-byte swizzle:
+// each K row holds 64 BF16 of N in 128 bytes, 8-row K groups are 1024 bytes apart (stride), and
+// 64-column N blocks (one tensor copy of 64 K rows each) are 8192 bytes apart (leading dimension).
+__device__ __forceinline__ uint64_t tc_desc_mn(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);  // start address, 16-byte units
+    d |= (uint64_t)(8192 >> 4) << 16;          // leading-dimension byte offset: next 64-column N block
+    d |= (uint64_t)(1024 >> 4) << 32;          // stride-dimension byte offset: next 8-row K group
     d |= (uint64_t)1 << 46;                    // descriptor version of tcgen05
     d |= (uint64_t)2 << 61;                    // layout: 128-byte swizzle
     return d;
@@ -310,7 +325,13 @@ __global__ void __launch_bounds__(192, 1) tc_rows_kernel(const __grid_constant__
                     const uint32_t st = sbase + (uint32_t)s * TC_STAGE;
                     tc_expect_tx(full0 + 8u * s, TC_STAGE);
                     tc_tma_2d(st, &q.a_map, kb * TC_BK, m0, full0 + 8u * s);
-                    tc_tma_2d(st + TC_TILE_A, &q.b_map, kb * TC_BK, n0, full0 + 8u * s);
+                    if (q.b_mn) {
+                        // B in place: BN / 64 copies of 64 columns x 64 K rows, 8 KB apart
+                        for (int jb = 0; jb < TC_BN / 64; ++jb)
+                            tc_tma_2d(st + TC_TILE_A + 8192u * jb, &q.b_map, n0 + 64 * jb, kb * TC_BK, full0 + 8u * s);
+                    } else {
+                        tc_tma_2d(st + TC_TILE_A, &q.b_map, kb * TC_BK, n0, full0 + 8u * s);
+                    }
                 }
             }
             // before the CTA can finish, every copy issued has landed
@@ -338,9 +359,19 @@ __global__ void __launch_bounds__(192, 1) tc_rows_kernel(const __grid_constant__
                     }
                     tc_fence_after();
                     const uint32_t st = sbase + (uint32_t)s * TC_STAGE;
+                    if (q.b_mn) {
+                        // N-major B (transpose-B bit of the instruction descriptor); a 16-deep K step is
+                        // 16 rows of 128 bytes
 #pragma unroll
-                    for (int k = 0; k < TC_BK / 16; ++k)
-                        tc_mma(dacc, tc_desc(st + 32u * k), tc_desc(st + TC_TILE_A + 32u * k), idesc, (kb | k) != 0);
+                        for (int k = 0; k < TC_BK / 16; ++k)
+                            tc_mma(dacc, tc_desc(st + 32u * k), tc_desc_mn(st + TC_TILE_A + 2048u * k),
+                                   idesc | (1u << 16), (kb | k) != 0);
+                    } else {
+#pragma unroll
+                        for (int k = 0; k < TC_BK / 16; ++k)
+                            tc_mma(dacc, tc_desc(st + 32u * k), tc_desc(st + TC_TILE_A + 32u * k), idesc,
+                                   (kb | k) != 0);
+                    }
                     tc_commit(empty0 + 8u * s);  // the stage is free once these MMAs have read it
                 }
                 tc_commit(accf0 + 8u * a);  // accumulator a holds tile j once these MMAs complete
@@ -462,6 +493,7 @@ int dense_rows_batched_impl(const spreg_dense_rows_item *items, int32_t count, c
         const spreg_dense_rows_item *first;
         std::vector<int32_t> members;
         int64_t n = 0, bt_off = 0, tab_off = 0;
+        bool mn = false;  // one product whose B is read in place (16-byte aligned rows): no transpose
     };
     std::vector<Group> groups;
     std::map<std::tuple<const void *, int64_t, int64_t, int64_t, const void *, int32_t, int32_t, int32_t>, size_t> key;
@@ -492,11 +524,14 @@ int dense_rows_batched_impl(const spreg_dense_rows_item *items, int32_t count, c
         }
     }
     if (groups.empty()) return SPREG_OK;
-    // scratch: each problem's Bt (n x K8, 256-byte aligned), then the segment tables
+    // scratch: each transposed problem's Bt (n x K8, 256-byte aligned), then the segment tables
     int64_t bytes = 0;
     for (Group &g : groups) {
         SPREG_CHECK_ARG(g.n <= INT32_MAX, "coalesced products wider than 2^31 columns");
-        const int64_t K8 = (g.first->k + 7) / 8 * 8;
+        const spreg_dense_rows_item &f = *g.first;
+        g.mn = g.members.size() == 1 && reinterpret_cast<uintptr_t>(f.b) % 16 == 0 && (f.ldb * 2) % 16 == 0;
+        if (g.mn) continue;
+        const int64_t K8 = (f.k + 7) / 8 * 8;
         g.bt_off = bytes;
         bytes += (g.n * K8 * 2 + 255) / 256 * 256;
     }
@@ -530,6 +565,7 @@ int dense_rows_batched_impl(const spreg_dense_rows_item *items, int32_t count, c
     std::vector<TransposeItem> titems;
     int64_t max_kt = 1, max_nt = 1;
     for (Group &g : groups) {
+        if (g.mn) continue;
         const int64_t K8 = (g.first->k + 7) / 8 * 8;
         int64_t o = 0;
         for (int32_t m : g.members) {
@@ -577,6 +613,7 @@ int dense_rows_batched_impl(const spreg_dense_rows_item *items, int32_t count, c
     {
         size_t t = 0;
         for (Group &g : groups) {
+            if (g.mn) continue;
             const int64_t K8 = (g.first->k + 7) / 8 * 8;
             int64_t o = 0;
             for (int32_t m : g.members) {
@@ -587,7 +624,7 @@ int dense_rows_batched_impl(const spreg_dense_rows_item *items, int32_t count, c
     }
     memcpy(tab.data() + titem_off, titems.data(), titems.size() * sizeof(TransposeItem));
     cudaError_t e = cudaMemcpyAsync(scratch + tab_base, tab.data(), tab.size(), cudaMemcpyHostToDevice, stream);
-    if (e == cudaSuccess) {
+    if (e == cudaSuccess && !titems.empty()) {
         transpose_items_kernel<<<dim3((unsigned)max_kt, (unsigned)max_nt, (unsigned)titems.size()), 256, 0,
                                  stream>>>(reinterpret_cast<const TransposeItem *>(scratch + tab_base + titem_off));
         e = cudaGetLastError();
@@ -631,8 +668,10 @@ int dense_rows_batched_impl(const spreg_dense_rows_item *items, int32_t count, c
             q.tiles_n = (int32_t)((g.n + bn - 1) / bn);
             q.tile_begin = (int32_t)tiles;
             tiles += ((it.rows + TC_BM - 1) / TC_BM) * q.tiles_n;
+            q.b_mn = g.mn ? 1 : 0;
             if ((st = tc_map(&q.a_map, it.a_rows, it.k, it.rows, it.lda, TC_BM)) ||
-                (st = tc_map(&q.b_map, scratch + g.bt_off, it.k, g.n, K8, bn)))
+                (st = g.mn ? tc_map(&q.b_map, it.b, g.n, it.k, it.ldb, 64)
+                           : tc_map(&q.b_map, scratch + g.bt_off, it.k, g.n, K8, bn)))
                 return fail(st);
         }
         if (tiles > INT32_MAX) {
