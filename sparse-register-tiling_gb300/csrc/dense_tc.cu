@@ -6,18 +6,19 @@
 // FP32 accumulation in tensor memory (TMEM), FP32 or BF16 output with load_c and the ReLU epilogue.
 //
 // One launch runs up to 80 such products ("problems", a tensor map pair each in the kernel
-// parameters); its CTAs are the output tiles of all of them, and each CTA finds its problem by a
-// binary search over the problems' first tiles.  One CTA computes a 128 x BN output tile (BN 256 when
-// every product of the launch has more than 128 columns, else 128) with 4 warps:
-//   * B is first transposed into a K-contiguous BF16 buffer Bt (n x K8, K8 = K rounded up to 8), so
-//     both MMA operands are K-major;
-//   * lane 0 of warp 0 loads 128 x 64 tiles of A_rows and Bt with 2-D tensor copies (TMA, 128-byte
-//     swizzle) into a ring of 4 stages ("full" mbarriers with expected bytes);
-//   * lane 0 of warp 1 issues, per 64-wide K block, four tcgen05.mma.kind::f16 (M 128, N 128, K 16)
-//     into a 128-column TMEM accumulator, and tcgen05.commit releases the stage ("empty" mbarrier);
-//     a last commit signals "done";
-//   * all 4 warps read the accumulator with tcgen05.ld (warp w owns TMEM lanes 32w .. 32w + 31, i.e.
-//     output rows), apply load_c / ReLU and store to row row_index[i] of C.
+// parameters).  Its output tiles (128 rows x BN columns; BN 256 when every product of the launch has
+// more than 128 columns, else 128) are shared out over persistent CTAs of 6 warps, at most one per
+// SM, each finding a tile's problem by a binary search over the problems' first tiles:
+//   * warp 0 (one lane) loads 64-deep K blocks of A_rows (128 x 64, K-major) and of B into a ring of
+//     4 stages with 2-D tensor copies (TMA, 128-byte swizzle; "full" mbarriers with expected bytes).
+//     A single product's B is read in place as an N-major operand (BN / 64 copies of 64 columns x
+//     64 K rows); products coalesced over several B are first transposed into one K-major buffer;
+//   * warp 1 (one lane) issues four tcgen05.mma.kind::f16 (M 128, N BN, K 16) per K block into one
+//     of two TMEM accumulators, tcgen05.commit releasing the stage ("empty") and, per tile, the
+//     accumulator ("acc full");
+//   * warps 2-5 each read one 32-lane quarter of the accumulator with tcgen05.ld (the tile's rows),
+//     apply load_c / ReLU, store through the row index (and the segment table of coalesced products)
+//     and release the accumulator ("acc empty"), so the next tile's MMAs overlap these stores.
 // Rows past R and columns past n are zero-filled by the tensor copies and never stored; K past the
 // end of A_rows / Bt reads as zero.  Every wait is bounded: a wait that gives up records a code in
 // the device status word; TMEM is released on every path.
