@@ -116,6 +116,10 @@ class MatMulSpecialized:
             _lib.check(_lib.lib().spreg_matmul_run_device(self._h, C_out.data_ptr(), B.data_ptr(),
                                                           _lib.stream_handle(stream)))
             return C_out
+        fast = self._torch_host_ptrs(C_out, B)
+        if fast is not None:
+            _lib.check(_lib.lib().spreg_matmul_run(self._h, fast[0], fast[1]))
+            return C_out
         b, ptr = self._host_args(C_out, B)
         _lib.check(_lib.lib().spreg_matmul_run(self._h, ptr, b.ctypes.data))
         return C_out
@@ -124,12 +128,30 @@ class MatMulSpecialized:
         """operator()(C, B) on host buffers, enqueued without waiting (copy in, product, copy out on
         this matmul's stream).  C_out and B must stay alive and unchanged until sync(); pin them
         (torch pin_memory) for copies that overlap other matmuls' work."""
+        fast = self._torch_host_ptrs(C_out, B)  # contiguous float32 CPU tensors: no numpy round trip
+        if fast is not None:
+            _lib.check(_lib.lib().spreg_matmul_run_async(self._h, fast[0], fast[1]))
+            return C_out
         b, ptr = self._host_args(C_out, B)
         src = B.data_ptr() if hasattr(B, "data_ptr") else (B.ctypes.data if isinstance(B, np.ndarray) else None)
         if b.ctypes.data != src:  # a converted copy would be freed before the enqueued copy reads it
             raise ValueError("run_async needs B as a contiguous float32 host buffer (no conversion copy)")
         _lib.check(_lib.lib().spreg_matmul_run_async(self._h, ptr, b.ctypes.data))
         return C_out
+
+    def _torch_host_ptrs(self, C_out, B):
+        """(C, B) data pointers when both are contiguous float32 CPU torch tensors of the right
+        shapes, else None (the general path converts and checks)."""
+        import torch
+        if not (isinstance(B, torch.Tensor) and isinstance(C_out, torch.Tensor)):
+            return None
+        if B.is_cuda or C_out.is_cuda or B.dtype != torch.float32 or C_out.dtype != torch.float32:
+            return None
+        if not (B.is_contiguous() and C_out.is_contiguous()):
+            return None
+        if tuple(B.shape) != (self.k, self.n) or tuple(C_out.shape) != (self.m, self.n):
+            return None
+        return C_out.data_ptr(), B.data_ptr()
 
     def sync(self) -> None:
         """Wait for this matmul's enqueued calls; their C buffers then hold the results."""
