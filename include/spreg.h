@@ -265,6 +265,12 @@ int spreg_dense_rows_bf16_batched(const spreg_dense_rows_item *items, int32_t nu
  * are then incomplete).  Synchronous; reset != 0 clears it. */
 int spreg_device_status(int32_t *status_host, int32_t reset);
 
+/* Self-test of the bounded waits every kernel uses: one CTA waits on an mbarrier that nothing
+ * arrives on, polling `limit` times (1 .. 2^22).  The wait gives up, the kernel records 30 in the
+ * device status word and returns; *status_host receives the status word and *polls_host the polls
+ * made.  Synchronous.  The context stays usable (clear the word with spreg_device_status(.., 1)). */
+int spreg_selftest_wait_timeout(uint32_t limit, int32_t *status_host, uint32_t *polls_host, spreg_stream_t stream);
+
 /* execute_tile (template:351-392): C = A.B over n_c columns, timed: warm-up num_runs runs,
  * then 150 x num_runs timed runs; *median_ns = median per-run time in nanoseconds. */
 int spreg_execute_timed(const spreg_packed *a, const spreg_exec_args *args, int64_t num_runs,

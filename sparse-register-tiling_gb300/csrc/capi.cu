@@ -33,6 +33,7 @@ int execute_impl(const spreg_packed *, const spreg_exec_args *, cudaStream_t);
 int execute_timed_impl(const spreg_packed *, const spreg_exec_args *, int64_t, double *, cudaStream_t);
 int execute_batched_impl(const spreg_work_item *, int32_t, cudaStream_t);
 int device_status_impl(int32_t *, int);
+int selftest_wait_impl(uint32_t, int32_t *, uint32_t *, cudaStream_t);
 int csr_spmm_impl(int64_t, int64_t, int64_t, int64_t, const int32_t *, const int32_t *, const float *, const float *,
                   int64_t, float *, int64_t, int32_t, cudaStream_t);
 int csr_spmm_timed_impl(int64_t, int64_t, int64_t, int64_t, const int32_t *, const int32_t *, const float *,
@@ -386,6 +387,11 @@ int spreg_execute_batched(const spreg_work_item *items, int32_t num_items, spreg
 int spreg_device_status(int32_t *status, int32_t reset) {
     clear_error();
     return device_status_impl(status, reset);
+}
+
+int spreg_selftest_wait_timeout(uint32_t limit, int32_t *status_host, uint32_t *polls_host, spreg_stream_t stream) {
+    clear_error();
+    return selftest_wait_impl(limit, status_host, polls_host, (cudaStream_t)stream);
 }
 
 int spreg_execute_timed(const spreg_packed *a, const spreg_exec_args *args, int64_t num_runs, double *median_ns,

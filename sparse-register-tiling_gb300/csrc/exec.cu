@@ -146,6 +146,43 @@ int *next_counter(DevFacts *f) {
     return f->counters + (next.fetch_add(1) % kCounters);
 }
 
+// Self-test of the bounded waits: one CTA waits on an mbarrier that nothing arrives on, with a
+// limit of `limit` polls, exactly as the executors wait on their stages.  The wait gives up, records
+// kSelftestWaitCode in the device status word and the kernel returns; *polled receives how many polls
+// were made (the limit).
+constexpr int kSelftestWaitCode = 30;
+__global__ void selftest_wait_kernel(int *status, uint32_t limit, uint32_t *polled) {
+    __shared__ __align__(8) unsigned long long bar;
+    const uint32_t b = (uint32_t)__cvta_generic_to_shared(&bar);
+    if (threadIdx.x == 0) mbar_init(b, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    __syncthreads();
+    const bool ok = mbar_wait_bounded(b, 0, status, kSelftestWaitCode, limit);
+    if (threadIdx.x == 0) *polled = ok ? 0u : limit;
+}
+
+int selftest_wait_impl(uint32_t limit, int32_t *status_out, uint32_t *polled_out, cudaStream_t stream) {
+    SPREG_CHECK_ARG(status_out && polled_out, "null output");
+    SPREG_CHECK_ARG(limit >= 1 && limit <= (1u << 22), "limit must be in [1, 2^22]");
+    DevFacts *f;
+    int st = dev_facts(&f);
+    if (st) return st;
+    uint32_t *polled = nullptr;
+    SPREG_CUDA(cudaMallocAsync(&polled, sizeof(uint32_t), stream));
+    selftest_wait_kernel<<<1, 32, 0, stream>>>(f->status, limit, polled);
+    cudaError_t e = cudaGetLastError();
+    int32_t v = 0;
+    uint32_t p = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&p, polled, sizeof p, cudaMemcpyDeviceToHost, stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&v, f->status, sizeof v, cudaMemcpyDeviceToHost, stream);
+    cudaFreeAsync(polled, stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess) SPREG_FAIL(SPREG_ERR_CUDA, "selftest: %s", cudaGetErrorString(e));
+    *status_out = v;
+    *polled_out = p;
+    return SPREG_OK;
+}
+
 int device_status_impl(int32_t *status, int reset) {
     DevFacts *f;
     int st = dev_facts(&f);

@@ -466,9 +466,10 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t phase) {
     return ok != 0;
 }
 
-// Bounded wait on an mbarrier phase; false after the limit (then *status records `code`).
-__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t phase, int *status, int code) {
-    for (uint32_t it = 0; it < (1u << 22); ++it)
+// Bounded wait on an mbarrier phase; false after `limit` polls (then *status records `code`).
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t phase, int *status, int code,
+                                                  uint32_t limit = 1u << 22) {
+    for (uint32_t it = 0; it < limit; ++it)
         if (mbar_try_wait(bar, phase)) return true;
     if (status) atomicCAS(status, 0, code);
     return false;

@@ -183,6 +183,15 @@ def device_status(reset: bool = False) -> int:
     return int(v.value)
 
 
+def selftest_wait_timeout(limit: int = 1000) -> tuple:
+    """(status word, polls) after a kernel waited `limit` polls on an mbarrier nothing arrives on:
+    the bounded wait every executor uses gives up and records 30 instead of hanging."""
+    st, polls = C.c_int32(), C.c_uint32()
+    _lib.check(_lib.lib().spreg_selftest_wait_timeout(int(limit), C.byref(st), C.byref(polls),
+                                                      _lib.stream_handle(None)))
+    return int(st.value), int(polls.value)
+
+
 def execute_batched(items, stream=None) -> None:
     """Run [(PackedMatrix, B, C, kwargs), ...] as one work list."""
     arr = (_lib.WorkItem * max(len(items), 1))()

@@ -389,3 +389,23 @@ def test_execute_tiled_kernels(cuda, tiles, meta):
 def test_device_status_clear(cuda):
     from spreg.packed import device_status
     assert device_status(reset=True) == 0
+
+
+def test_bounded_wait_gives_up_and_the_context_stays_usable(cuda):
+    """A wait on an mbarrier that nothing arrives on (short limit) ends with status 30 instead of a
+    hang; afterwards the status clears and an SpMM still runs bit-exact."""
+    import time
+    from spreg.packed import selftest_wait_timeout
+    device_status(reset=True)
+    t0 = time.perf_counter()
+    status, polls = selftest_wait_timeout(1000)
+    assert status == 30 and polls == 1000
+    assert time.perf_counter() - t0 < 5.0
+    assert device_status(reset=True) == 30 and device_status() == 0
+    m = Mapping.identity(4)
+    A = synth.row_skew(64, 256, 0.9, seed=5, std=1.0)
+    B = synth.dense(256, 64, seed=6)
+    got = gpu_pack(A, m, k_tile=128).execute(torch.from_numpy(B).cuda(), staging=1).cpu().numpy()
+    assert np.array_equal(got.view(np.uint32), O.Packed(O.Tables.of(m), A, k_tile=128).execute(B).view(np.uint32))
+    with pytest.raises(_lib.SpregError, match="limit"):
+        selftest_wait_timeout(0)
