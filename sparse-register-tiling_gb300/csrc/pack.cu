@@ -263,27 +263,53 @@ __global__ void __launch_bounds__(CH) count_list_kernel(const ListSrc src, const
 }
 
 // ------------------------------------------------------------------ layout pass
+// Inclusive prefix sum of one value per thread of a 1024-thread block (shuffles within warps, one
+// warp over the 32 warp totals); *total = the block's sum.  s_warp holds 32 entries.
+__device__ __forceinline__ long long block_incl_scan(long long v, long long *s_warp, long long *total) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const long long t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += t;
+    }
+    if (lane == 31) s_warp[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        long long x = s_warp[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const long long t = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += t;
+        }
+        s_warp[lane] = x;
+    }
+    __syncthreads();
+    if (w > 0) v += s_warp[w - 1];
+    *total = s_warp[31];
+    __syncthreads();  // s_warp is reused by the next call
+    return v;
+}
+
 __global__ void __launch_bounds__(1024) layout_kernel(const int64_t units, const int nk, const int vb,
                                                       const int64_t ppt, const int64_t T, const int64_t P,
                                                       const UnitStats *__restrict__ stats,
                                                       const unsigned long long *__restrict__ tile_nnz,
                                                       spreg_panel_desc *__restrict__ descs, PackTotals *tot) {
-    __shared__ long long s_scan[1024];
-    __shared__ long long s_xscan[1024];
-    __shared__ long long s_carry, s_xcarry;
+    __shared__ long long s_warp[32];
     __shared__ unsigned long long s_acc[8];
     const int t = threadIdx.x;
-    if (t == 0) { s_carry = 0; s_xcarry = 0; }
     if (t < 8) s_acc[t] = 0;
     __syncthreads();
+    long long carry = 0, xtotal = 0;
     long long my_v = 0, my_u = 0, my_pad = 0, my_nnz = 0, my_req = 0, my_empty = 0, my_xmax = 0;
     for (int64_t base = 0; base < units; base += 1024) {
         const int64_t u = base + t;
-        long long size = 0, xsize = 0;
+        long long size = 0;
         UnitStats st = {0, 0, 0, 0, 0, 0};
         if (u < units) {
             st = stats[u];
-            xsize = st.exec_bytes;
+            const long long xsize = st.exec_bytes;
+            xtotal += xsize;
             my_xmax = xsize > my_xmax ? xsize : my_xmax;
             size = align64((int64_t)st.num_values * vb) + align64((int64_t)st.num_cols * 4) + align64((int64_t)nk * 4);
             my_v += st.num_values;
@@ -295,19 +321,10 @@ __global__ void __launch_bounds__(1024) layout_kernel(const int64_t units, const
             unit_coords(u, ppt, T, P, &gp, &tj);
             if (tile_nnz[(gp / ppt) * T + tj] == 0) my_empty++;
         }
-        s_scan[t] = size;
-        s_xscan[t] = xsize;
-        __syncthreads();
-        for (int o = 1; o < 1024; o <<= 1) {
-            const long long add = t >= o ? s_scan[t - o] : 0;
-            const long long xadd = t >= o ? s_xscan[t - o] : 0;
-            __syncthreads();
-            s_scan[t] += add;
-            s_xscan[t] += xadd;
-            __syncthreads();
-        }
+        long long chunk = 0;
+        const long long incl = block_incl_scan(size, s_warp, &chunk);
         if (u < units) {
-            const long long off = s_carry + s_scan[t] - size;
+            const long long off = carry + incl - size;
             spreg_panel_desc d;
             d.values_off = off;
             d.cols_off = off + align64((int64_t)st.num_values * vb);
@@ -316,10 +333,9 @@ __global__ void __launch_bounds__(1024) layout_kernel(const int64_t units, const
             d.num_cols = st.num_cols;
             descs[u] = d;
         }
-        __syncthreads();
-        if (t == 0) { s_carry += s_scan[1023]; s_xcarry += s_xscan[1023]; }
-        __syncthreads();
+        carry += chunk;
     }
+    long long my_x = xtotal;
     // warp sums first: one shared atomic per warp instead of 1024 contending ones
     for (int o = 16; o > 0; o >>= 1) {
         my_v += __shfl_down_sync(0xffffffffu, my_v, o);
@@ -328,6 +344,7 @@ __global__ void __launch_bounds__(1024) layout_kernel(const int64_t units, const
         my_nnz += __shfl_down_sync(0xffffffffu, my_nnz, o);
         my_req += __shfl_down_sync(0xffffffffu, my_req, o);
         my_empty += __shfl_down_sync(0xffffffffu, my_empty, o);
+        my_x += __shfl_down_sync(0xffffffffu, my_x, o);
         const long long xm = __shfl_down_sync(0xffffffffu, my_xmax, o);
         my_xmax = xm > my_xmax ? xm : my_xmax;
     }
@@ -338,18 +355,19 @@ __global__ void __launch_bounds__(1024) layout_kernel(const int64_t units, const
         atomicAdd(&s_acc[3], (unsigned long long)my_nnz);
         atomicAdd(&s_acc[4], (unsigned long long)my_req);
         atomicAdd(&s_acc[5], (unsigned long long)my_empty);
+        atomicAdd(&s_acc[6], (unsigned long long)my_x);
         atomicMax(&s_acc[7], (unsigned long long)my_xmax);
     }
     __syncthreads();
     if (t == 0) {
-        tot->arena_bytes = s_carry;
+        tot->arena_bytes = carry;
         tot->num_values = (long long)s_acc[0];
         tot->num_cols = (long long)s_acc[1];
         tot->padding = (long long)s_acc[2];
         tot->nnz = (long long)s_acc[3];
         tot->required_storage = (long long)s_acc[4];
         tot->empty_units = (long long)s_acc[5];
-        tot->exec_bytes = s_xcarry;
+        tot->exec_bytes = (long long)s_acc[6];
         tot->max_exec_bytes = (long long)s_acc[7];
     }
 }
@@ -392,11 +410,9 @@ __global__ void __launch_bounds__(1024) exec_slots_kernel(const int64_t units, c
                                                           const UnitStats *__restrict__ stats,
                                                           int64_t *__restrict__ exec_offs,
                                                           int64_t *__restrict__ unit_xoff) {
-    __shared__ long long s_scan[1024];
-    __shared__ long long s_carry;
+    __shared__ long long s_warp[32];
     const int t = threadIdx.x;
-    if (t == 0) s_carry = 0;
-    __syncthreads();
+    long long carry = 0;
     for (int64_t base = 0; base < units; base += 1024) {
         const int64_t s = base + t;
         int64_t u = -1;
@@ -405,24 +421,16 @@ __global__ void __launch_bounds__(1024) exec_slots_kernel(const int64_t units, c
             u = unit_index(order[s % P], s / P, ppt, T, P);
             xsize = stats[u].exec_bytes;
         }
-        s_scan[t] = xsize;
-        __syncthreads();
-        for (int o = 1; o < 1024; o <<= 1) {
-            const long long add = t >= o ? s_scan[t - o] : 0;
-            __syncthreads();
-            s_scan[t] += add;
-            __syncthreads();
-        }
+        long long chunk = 0;
+        const long long incl = block_incl_scan(xsize, s_warp, &chunk);
         if (u >= 0) {
-            const long long off = s_carry + s_scan[t] - xsize;
+            const long long off = carry + incl - xsize;
             exec_offs[s] = off;
             unit_xoff[u] = off;
         }
-        __syncthreads();
-        if (t == 0) s_carry += s_scan[1023];
-        __syncthreads();
+        carry += chunk;
     }
-    if (t == 0) exec_offs[units] = s_carry;
+    if (t == 0) exec_offs[units] = carry;
 }
 
 // Power-of-two F16 scale per row panel: 2^e with max|v| = m * 2^e, m in [0.5, 1); 1 if max is 0.
