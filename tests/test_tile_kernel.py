@@ -217,3 +217,21 @@ def test_work_order_single_panel_and_empty_rows(cuda):
     B2 = synth.dense(256, 256, seed=4)
     got, want = run_pair(A2, m, B2, k_tile=128)
     assert same_bits(got, want)
+
+
+def test_large_matrix_bit_exact(cuda):
+    """16384 x 4096 at 95 % (3.4 M nonzeros, 32 K tiles of 128), N = 96 with a ragged strip: the packed
+    arena, the work order and both executors (B tiles and L1/L2 gathers) at a larger scale."""
+    m = Mapping.load("75a1b")
+    A = synth.row_skew(16384, 4096, 0.95, seed=77, std=1.0)
+    B = synth.dense(4096, 96, seed=78)
+    pm = PackedMatrix.from_dense(torch.from_numpy(A).cuda(), m, k_tile=128)
+    ref = O.Packed(O.Tables.of(m), A, k_tile=128)
+    assert pm.info["arena_bytes"] == ref.sizes["arena_bytes"] and pm.info["nnz"] == ref.sizes["nnz"]
+    want = ref.execute(B)
+    tb = torch.from_numpy(B).cuda()
+    for staging in (1, 2):
+        got = pm.execute(tb, staging=staging).cpu().numpy()
+        assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), staging
+    assert O.rel_err(want, O.dense_fp64(A, B)) <= 1e-5
+    assert device_status() == 0
