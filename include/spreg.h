@@ -254,7 +254,9 @@ typedef struct {
     int64_t ldb;
     void *c;
     int64_t ldc, n;
-    int32_t c_dtype, load_c, epilogue, reserved;
+    int32_t c_dtype, load_c, epilogue;
+    int32_t tile_n;          /* output tile width: 0 = automatic, 128 or 256 (a launch takes the first
+                                nonzero hint of its items) */
 } spreg_dense_rows_item;
 
 /* Many dense-rows products (any shapes) in as few launches as possible: the output tiles of up to

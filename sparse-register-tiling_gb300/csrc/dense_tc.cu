@@ -512,6 +512,8 @@ int dense_rows_batched_impl(const spreg_dense_rows_item *items, int32_t count, c
                         "%lld)", i, (long long)it.lda);
         SPREG_CHECK_ARG(it.ldb >= it.n && it.ldc >= it.n, "item %d: ldb / ldc smaller than n", i);
         SPREG_CHECK_ARG(it.k > 0, "item %d: K must be positive", i);
+        SPREG_CHECK_ARG(it.tile_n == 0 || it.tile_n == 128 || it.tile_n == 256, "item %d: tile_n must be 0, 128 or 256",
+                        i);
         auto kk = std::make_tuple(it.a_rows, it.rows, it.k, it.lda, (const void *)it.row_index, it.c_dtype,
                                   it.load_c ? 1 : 0, it.epilogue);
         auto f = key.find(kk);
@@ -640,10 +642,16 @@ int dense_rows_batched_impl(const spreg_dense_rows_item *items, int32_t count, c
         memset(&p, 0, sizeof p);
         p.status = status;
         p.nprob = (int32_t)cnt;
-        // 256-wide output tiles when every problem of the launch is wider than 128 columns
+        // 256-wide output tiles when every problem of the launch is wider than 128 columns, unless an
+        // item asks for a width
         int64_t min_n = INT64_MAX;
-        for (size_t j = 0; j < cnt; ++j) min_n = std::min<int64_t>(min_n, groups[first + j].n);
-        const int bn = min_n > 128 ? 256 : 128;
+        int hint = 0;
+        for (size_t j = 0; j < cnt; ++j) {
+            min_n = std::min<int64_t>(min_n, groups[first + j].n);
+            for (int32_t m : groups[first + j].members)
+                if (!hint && (items[m].tile_n == 128 || items[m].tile_n == 256)) hint = items[m].tile_n;
+        }
+        const int bn = hint ? hint : (min_n > 128 ? 256 : 128);
         int64_t tiles = 0;
         for (size_t j = 0; j < cnt; ++j) {
             const size_t gi = first + j;

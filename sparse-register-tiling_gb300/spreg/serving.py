@@ -51,7 +51,7 @@ assert WORK_ITEM_DTYPE.itemsize == C.sizeof(_lib.WorkItem)
 TC_ITEM_DTYPE = np.dtype([
     ("a_rows", np.uint64), ("rows", np.int64), ("k", np.int64), ("lda", np.int64), ("row_index", np.uint64),
     ("b", np.uint64), ("ldb", np.int64), ("c", np.uint64), ("ldc", np.int64), ("n", np.int64),
-    ("c_dtype", np.int32), ("load_c", np.int32), ("epilogue", np.int32), ("reserved", np.int32)])
+    ("c_dtype", np.int32), ("load_c", np.int32), ("epilogue", np.int32), ("tile_n", np.int32)])
 assert TC_ITEM_DTYPE.itemsize == 96
 
 

@@ -165,3 +165,28 @@ def test_products_sharing_weights_coalesce_to_same_results(cuda):
     torch.cuda.synchronize()
     for B, C1, C2 in ops:
         assert torch.equal(C1.view(torch.int32), C2.view(torch.int32))
+
+
+def test_tile_width_hint_gives_the_same_products(cuda):
+    """tile_n = 128 / 256 / automatic: the same FP32 sums of BF16 products (the MMA's K order does not
+    depend on the tile width), and a bad hint is refused."""
+    import torch
+    from spreg.serving import TC_ITEM_DTYPE
+    M, K, N = 300, 200, 400
+    A = torch.randn(M, K, device="cuda").to(torch.bfloat16)
+    B = torch.randn(K, N, device="cuda").to(torch.bfloat16)
+    ri = torch.arange(M, dtype=torch.int32, device="cuda")
+    outs = []
+    for tn in (0, 128, 256):
+        C = torch.empty(M, N, device="cuda")
+        it = np.zeros(1, dtype=TC_ITEM_DTYPE)
+        it[0] = (A.data_ptr(), M, K, K, ri.data_ptr(), B.data_ptr(), N, C.data_ptr(), N, N, _lib.F32, 0, 0, tn)
+        _lib.check(_lib.lib().spreg_dense_rows_bf16_batched(it.ctypes.data, 1, _lib.stream_handle(None)))
+        outs.append(C)
+    torch.cuda.synchronize()
+    assert torch.equal(outs[0], outs[1]) and torch.equal(outs[0], outs[2])
+    ref = A.float() @ B.float()
+    assert float((outs[0] - ref).norm() / ref.norm()) <= 1e-5
+    it[0]["tile_n"] = 64
+    with pytest.raises(_lib.SpregError, match="tile_n"):
+        _lib.check(_lib.lib().spreg_dense_rows_bf16_batched(it.ctypes.data, 1, _lib.stream_handle(None)))
