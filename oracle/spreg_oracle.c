@@ -442,7 +442,23 @@ void orc_execute(int mr, int num_nkern, const int32_t *id_to_pattern, const uint
                 const int32_t *cols = (const int32_t *)(arena + d->cols_off);
                 const uint8_t *vals = arena + d->values_off;
                 int64_t c = 0, v = 0;
-                for (int id = 0; id < num_nkern; ++id) {
+                /* FP32 values and B over a whole strip: the same fmaf chain per element, with fixed-length
+                 * inner loops the compiler turns into vector FMAs (the reference's executor is SIMD too) */
+                const int fast = b_dtype == ORC_F32 && value_dtype == ORC_F32 && w == STRIP;
+                for (int id = 0; fast && id < num_nkern; ++id) {
+                    const int32_t n = cnt[id];
+                    const uint32_t pat = (uint32_t)id_to_pattern[id];
+                    const float *vp = (const float *)vals;
+                    for (int32_t e = 0; e < n; ++e, ++c) {
+                        const float *bp = (const float *)B + cols[c] * ldb + j0;
+                        for (int r = 0; r < mr; ++r) {
+                            if (!((pat >> r) & 1u)) continue;
+                            const float a = vp[v++];
+                            for (int j = 0; j < 16; ++j) acc[r][j] = fmaf(a, bp[j], acc[r][j]);
+                        }
+                    }
+                }
+                for (int id = 0; !fast && id < num_nkern; ++id) {
                     int32_t n = cnt[id];
                     uint32_t pat = (uint32_t)id_to_pattern[id];
                     for (int32_t e = 0; e < n; ++e, ++c) {
