@@ -506,10 +506,18 @@ void orc_csr_spmm(int64_t M, int64_t N, const int32_t *row_ptrs, const int32_t *
         for (int64_t j0 = 0; j0 < N; j0 += NT) {
             int64_t w = N - j0 < NT ? N - j0 : NT;
             for (int64_t j = 0; j < w; ++j) acc[j] = 0.0f;
-            for (int32_t p = row_ptrs[i]; p < row_ptrs[i + 1]; ++p) {
-                float a = values[p];
-                const float *b = B + (int64_t)col_inds[p] * ldb + j0;
-                for (int64_t j = 0; j < w; ++j) acc[j] = fmaf(a, b[j], acc[j]);
+            if (w == NT) { /* whole tile: fixed-length loop, vectorised by the compiler */
+                for (int32_t p = row_ptrs[i]; p < row_ptrs[i + 1]; ++p) {
+                    const float a = values[p];
+                    const float *b = B + (int64_t)col_inds[p] * ldb + j0;
+                    for (int j = 0; j < NT; ++j) acc[j] = fmaf(a, b[j], acc[j]);
+                }
+            } else {
+                for (int32_t p = row_ptrs[i]; p < row_ptrs[i + 1]; ++p) {
+                    float a = values[p];
+                    const float *b = B + (int64_t)col_inds[p] * ldb + j0;
+                    for (int64_t j = 0; j < w; ++j) acc[j] = fmaf(a, b[j], acc[j]);
+                }
             }
             for (int64_t j = 0; j < w; ++j) C[i * ldc + j0 + j] = acc[j];
         }
