@@ -17,6 +17,14 @@
  *   - cpp_testbed/src/spmm/nano/SpMM_SOP.h:107-178 (sop::MatMulSpecialized constructor,
  *     get_config, allocate_executor, operator()(C, B), require_storage)
  *   - cpp_testbed/demo/count_nkerns.cpp:52-128 (tiled packer: M_c x K_c tiles, load_c)
+ *   - sbench/SOP/_C/pytorch_csr_wrapper.cpp:70-191, 314-353 (the csr module's executor: the CSR
+ *     baseline that sbench/SOP/sop_bench.py:197 times beside the register-tiled executor)
+ *
+ * Device status word: kernels never trap.  A bounded wait that gives up, or an index a kernel's
+ * own bounds check refuses, records a nonzero code in a per-device word instead (read and clear it
+ * with spreg_device_status):
+ *   2, 5-7   executor waits (batched and B-tile kernels);   20  CSR column index out of range;
+ *   21-25    tensor-core kernel waits;                        30  spreg_selftest_wait_timeout.
  */
 #ifndef SPREG_H
 #define SPREG_H
