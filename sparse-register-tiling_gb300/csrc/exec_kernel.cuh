@@ -546,14 +546,6 @@ template <class TV, int NV> __device__ __forceinline__ float bseg_f32(const BSeg
     else return word_val<TV>(b.w[j >> 1], j & 1);
 }
 
-// Value i (compile-time after unrolling) of a block of quads.
-template <class TV, int NQ> __device__ __forceinline__ float quad_val(const uint4 (&q)[NQ], int i) {
-    constexpr int PER_WORD = 4 / sizeof(TV);
-    const int w = i / PER_WORD;
-    const uint4 &qq = q[w / 4];
-    const uint32_t word = (w % 4 == 0) ? qq.x : (w % 4 == 1) ? qq.y : (w % 4 == 2) ? qq.z : qq.w;
-    return word_val<TV>(word, i % PER_WORD);
-}
 template <class TV> __device__ __forceinline__ float lds_val(uint32_t a) {
     if constexpr (sizeof(TV) == 4) return __uint_as_float(lds_u32(a));
     else return word_val<TV>(lds_u16(a), 0);
