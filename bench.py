@@ -855,8 +855,9 @@ def main():
     rate = (lambda ms_: whole_job_rate(sum(bytes_per[:e2e_n]), e2e_steps, ws, ms_) / 1e9) if e2e_n else (lambda ms_: None)
     e2e = {"value": rate(e2e_ms), "unit": UNIT, "synchronous_calls_value": rate(e2e_sync_ms),
            "h2d_bytes_per_step": e2e_n * args.k * args.n * 4, "d2h_bytes_per_step": e2e_n * args.m * args.n * 4,
-           "path": "spreg_matmul_run_async per replica (host B in, C = A.B, host C out on the matmul's own stream), "
-                   "then spreg_matmul_sync of every replica; synchronous_calls_value: spreg_matmul_run per replica",
+           "path": "spreg_matmul_run_async per replica (host B copied in, C = A.B stored by the kernel straight "
+                   "into the pinned host C, on the matmul's own stream), then spreg_matmul_sync of every replica; "
+                   "synchronous_calls_value: spreg_matmul_run per replica",
            "replicas_per_step": e2e_n,
            "bit_exact_vs_oracle": e2e_ok, "all_replicas_equal_device_results": e2e_all}
     del mms

@@ -329,6 +329,11 @@ int spreg_matmul_run(spreg_matmul *mm, float *c_host, const float *b_host);
 int spreg_matmul_run_async(spreg_matmul *mm, float *c_host, const float *b_host);
 /* Wait for every call enqueued on the matmul's stream; then c_host of those calls holds C. */
 int spreg_matmul_sync(spreg_matmul *mm);
+/* direct != 0 (the default): host-buffer calls whose c_host is page-locked host memory the device
+ * maps at the same address (cudaHostAlloc, torch pin_memory) have the kernel store C straight into
+ * it: no device C and no copy out.  Any other c_host takes the copy path (device C, then a copy).
+ * Results are identical either way; direct = 0 keeps the copy path for every call. */
+int spreg_matmul_set_direct_output(spreg_matmul *mm, int32_t direct);
 /* Same on device buffers (ldb = ldc = n), asynchronous on `stream`. */
 int spreg_matmul_run_device(spreg_matmul *mm, float *c, const float *b, spreg_stream_t stream);
 int spreg_matmul_get_config(const spreg_matmul *mm, spreg_tile_config *cfg);

@@ -91,7 +91,18 @@ struct spreg_matmul {
     cudaStream_t stream = nullptr;
     float *dB = nullptr, *dC = nullptr;
     int32_t alloc_n = 0;
+    int32_t direct_output = 1;  // store C straight into mapped page-locked host C (no copy out)
 };
+
+// True when p is page-locked host memory that the device addresses at the same pointer.
+static bool host_mapped(const void *p) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();  // not memory CUDA knows: clear the (non-sticky) error it reported
+        return false;
+    }
+    return at.type == cudaMemoryTypeHost && at.devicePointer == p;
+}
 
 extern "C" {
 
@@ -519,9 +530,19 @@ static int matmul_enqueue(spreg_matmul *mm, float *c_host, const float *b_host) 
     SPREG_CHECK_ARG(c_host && (b_host || mm->k == 0 || mm->n == 0), "null host buffers");
     const size_t bb = (size_t)mm->k * mm->n * 4, cb = (size_t)mm->m * mm->n * 4;
     if (bb) SPREG_CUDA(cudaMemcpyAsync(mm->dB, b_host, bb, cudaMemcpyHostToDevice, mm->stream));
-    int st = matmul_exec(mm, mm->dC, mm->dB, mm->stream);
+    // direct output: the kernel's stores of C cross to host memory themselves, beside the copy
+    // engines that carry the other calls' C
+    const bool direct = mm->direct_output && cb && host_mapped(c_host);
+    int st = matmul_exec(mm, direct ? c_host : mm->dC, mm->dB, mm->stream);
     if (st) return st;
-    if (cb) SPREG_CUDA(cudaMemcpyAsync(c_host, mm->dC, cb, cudaMemcpyDeviceToHost, mm->stream));
+    if (cb && !direct) SPREG_CUDA(cudaMemcpyAsync(c_host, mm->dC, cb, cudaMemcpyDeviceToHost, mm->stream));
+    return SPREG_OK;
+}
+
+int spreg_matmul_set_direct_output(spreg_matmul *mm, int32_t direct) {
+    clear_error();
+    SPREG_CHECK_ARG(mm, "null matmul");
+    mm->direct_output = direct ? 1 : 0;
     return SPREG_OK;
 }
 

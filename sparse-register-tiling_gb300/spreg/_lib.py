@@ -131,6 +131,7 @@ PROTOTYPES = {
     "spreg_matmul_run": (C.c_int, [P, P, P]),
     "spreg_matmul_run_async": (C.c_int, [P, P, P]),
     "spreg_matmul_sync": (C.c_int, [P]),
+    "spreg_matmul_set_direct_output": (C.c_int, [P, C.c_int32]),
     "spreg_matmul_run_device": (C.c_int, [P, P, P, P]),
     "spreg_matmul_get_config": (C.c_int, [P, C.POINTER(TileConfig)]),
     "spreg_matmul_required_storage": (C.c_int64, [P]),

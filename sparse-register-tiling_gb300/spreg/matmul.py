@@ -153,6 +153,11 @@ class MatMulSpecialized:
             return None
         return C_out.data_ptr(), B.data_ptr()
 
+    def set_direct_output(self, direct: bool = True) -> None:
+        """Host-buffer calls with a pinned C store C straight into it from the kernel (no copy out);
+        other C buffers keep the copy path.  Results are identical."""
+        _lib.check(_lib.lib().spreg_matmul_set_direct_output(self._h, int(bool(direct))))
+
     def sync(self) -> None:
         """Wait for this matmul's enqueued calls; their C buffers then hold the results."""
         _lib.check(_lib.lib().spreg_matmul_sync(self._h))

@@ -297,6 +297,27 @@ def test_matmul_specialized_async_host_calls_overlap_and_match(cuda):
     assert device_status() == 0
 
 
+def test_matmul_direct_host_output_matches_the_copy_path(cuda):
+    """C stored by the kernel straight into pinned host memory (the default), C through device memory
+    and a copy (direct output off), and a pageable C (always the copy path): the same bits."""
+    A = synth.row_skew(300, 384, 0.9, seed=61, std=1.0)
+    B = torch.from_numpy(synth.dense(384, 200, seed=62)).pin_memory()
+    rp, ci, v = synth.to_csr(A)
+    mm = MatMulSpecialized(300, 384, 200, v, rp, ci, TileConfig(K_c=128), 1, "", "61fee")
+    want = O.Packed(O.Tables.of(Mapping.identity(4)), A, k_tile=128).execute(B.numpy())
+    C_direct = torch.full((300, 200), -1.0).pin_memory()
+    mm(C_direct, B)
+    mm.set_direct_output(False)
+    C_copy = torch.full((300, 200), -1.0).pin_memory()
+    mm(C_copy, B)
+    mm.set_direct_output(True)
+    C_pageable = np.full((300, 200), -1.0, dtype=np.float32)
+    mm(C_pageable, B)
+    for C in (C_direct.numpy(), C_copy.numpy(), C_pageable):
+        assert np.array_equal(C.view(np.uint32), want.view(np.uint32))
+    assert device_status() == 0
+
+
 def test_execute_batched_equals_individual(cuda):
     """Uneven SpMMs (mappings, M_r, dtypes, N with tails, K tiles) in one call: each result is the
     same as its own call and as the oracle."""
