@@ -322,7 +322,8 @@ def serving_bench(args, dev) -> dict:
 def precision_suite(dev) -> list:
     """1x1-conv-shaped SpMMs (B = K x 3136: batch 1, 56 x 56 spatial) at sparsity 0.8-0.95 with
     log-normal row skew: rel err against FP64 of FP32, BF16 and FP16 (per-panel scaled) storage,
-    FP32 accumulation, and the FP32 kernel time of each layer."""
+    FP32 accumulation, and the kernel time of each layer in each storage (one SpMM per launch,
+    the reference's timing protocol)."""
     import torch
     from oracle import oracle as O
     from spreg import BF16, F16, F32, Mapping, PackedMatrix, synth
@@ -340,11 +341,10 @@ def precision_suite(dev) -> list:
             Bt = torch.from_numpy(B).to(dev).to(tdt)
             C = pm.execute(Bt)
             row[f"rel_err_{name}"] = float(O.rel_err(C.cpu().numpy(), ref))
-            if name == "fp32":
-                Cf = torch.empty((M, 3136), device=dev)
-                t = pm.execute_timed(Bt, Cf, num_runs=1)
-                row["fp32_us"] = t / 1e3
-                row["fp32_gflops"] = 2 * int(pm.info["nnz"]) * 3136 / t
+            Cf = torch.empty((M, 3136), device=dev)
+            t = pm.execute_timed(Bt, Cf, num_runs=1)
+            row[f"{name}_us"] = t / 1e3
+            row[f"{name}_gflops"] = 2 * int(pm.info["nnz"]) * 3136 / t
             if name != "fp32":
                 # the same storage with its own inputs rounded: the error the kernel adds
                 Bq = Bt.float().cpu().numpy()
