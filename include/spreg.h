@@ -271,6 +271,13 @@ typedef struct {
  * 80 products share one launch.  Same arguments and results as spreg_dense_rows_bf16 per item. */
 int spreg_dense_rows_bf16_batched(const spreg_dense_rows_item *items, int32_t num_items, spreg_stream_t stream);
 
+/* Thread-block clusters of the dense-rows launches that follow (process-wide): 0 = automatic, 1 =
+ * one CTA per output tile, 2 = CTA pairs on two row blocks of one column block, each loading half of
+ * the shared B tile into both CTAs (TMA multicast).  Automatic takes pairs when a launch has at
+ * least a full wave of them and odd row block counts pad at most 1/8 of its tiles.  Results are the
+ * same either way.  Returns SPREG_ERR_ARG for another mode. */
+int spreg_tc_set_cluster(int32_t mode);
+
 /* Status word of the current device: nonzero once a kernel gave up a bounded wait (its results
  * are then incomplete).  Synchronous; reset != 0 clears it. */
 int spreg_device_status(int32_t *status_host, int32_t reset);

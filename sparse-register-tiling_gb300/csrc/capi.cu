@@ -18,6 +18,7 @@ void clear_error() { g_last_error.clear(); }
 int dense_rows_bf16_impl(const void *, int64_t, int64_t, int64_t, const int32_t *, const void *, int64_t, void *,
                          int64_t, int64_t, int32_t, int32_t, int32_t, cudaStream_t);
 int dense_rows_batched_impl(const spreg_dense_rows_item *, int32_t, cudaStream_t);
+void tc_set_cluster(int mode);
 int pack_from_arena_impl(const spreg_mapping *, const spreg_arena_geom *, const void *, int64_t,
                          const spreg_panel_desc *, int64_t, const float *, int64_t, spreg_packed **, cudaStream_t);
 int pack_dense_impl(const spreg_mapping *, const float *, int64_t, int64_t, int64_t, const spreg_pack_opts *,
@@ -244,6 +245,13 @@ int spreg_dense_rows_bf16(const void *a_rows, int64_t rows, int64_t k, int64_t l
 int spreg_dense_rows_bf16_batched(const spreg_dense_rows_item *items, int32_t num_items, spreg_stream_t stream) {
     clear_error();
     return dense_rows_batched_impl(items, num_items, (cudaStream_t)stream);
+}
+
+int spreg_tc_set_cluster(int32_t mode) {
+    clear_error();
+    SPREG_CHECK_ARG(mode == 0 || mode == 1 || mode == 2, "cluster mode must be 0, 1 or 2 (got %d)", (int)mode);
+    tc_set_cluster(mode);
+    return SPREG_OK;
 }
 
 void spreg_packed_destroy(spreg_packed *p) { packed_release(p); }

@@ -28,6 +28,7 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <map>
 #include <tuple>
@@ -104,6 +105,51 @@ __device__ __forceinline__ void tc_tma_2d(uint32_t dst, const CUtensorMap *map, 
                  ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar) : "memory");
 }
 
+// The same copy delivered to every CTA of `mask` in the cluster: the data lands at offset dst of each
+// CTA's shared memory and each CTA's barrier at offset bar receives the completed bytes.
+__device__ __forceinline__ void tc_tma_2d_mc(uint32_t dst, const CUtensorMap *map, int x, int y, uint32_t bar,
+                                             uint16_t mask) {
+    asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes.multicast::cluster "
+                 "[%0], [%1, {%2, %3}], [%4], %5;"
+                 ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar), "h"(mask) : "memory");
+}
+__device__ __forceinline__ uint32_t tc_cluster_rank() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ uint32_t tc_cluster_id() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%clusterid.x;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ uint32_t tc_cluster_count() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%nclusterid.x;" : "=r"(r));
+    return r;
+}
+// All threads of all CTAs of the cluster (every thread reaches it once, right after the set-up).
+__device__ __forceinline__ void tc_cluster_sync() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+// Arrive on the barrier at offset bar of CTA `cta` of the cluster.
+__device__ __forceinline__ void tc_remote_arrive(uint32_t bar, uint32_t cta) {
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(bar), "r"(cta));
+    asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(r) : "memory");
+}
+__device__ __forceinline__ bool tc_wait_cluster(uint32_t bar, uint32_t phase, int *status, int code) {
+    for (uint32_t it = 0; it < (1u << 22); ++it) {
+        uint32_t ok;
+        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
+                     "selp.u32 %0, 1, 0, p;\n\t}"
+                     : "=r"(ok) : "r"(bar), "r"(phase) : "memory");
+        if (ok) return true;
+    }
+    if (status) atomicCAS(status, 0, code);
+    return false;
+}
+
 // Shared-memory matrix descriptor of a K-major operand tile stored with the 128-byte swizzle: rows of
 // 128 bytes (64 BF16), 8-row groups 1024 bytes apart.
 __device__ __forceinline__ uint64_t tc_desc(uint32_t saddr) {
@@ -141,6 +187,11 @@ __device__ __forceinline__ void tc_mma(uint32_t tmem_d, uint64_t adesc, uint64_t
 }
 __device__ __forceinline__ void tc_commit(uint32_t bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+// The same arrival on the barrier at offset bar of every CTA of `mask` in the cluster.
+__device__ __forceinline__ void tc_commit_mc(uint32_t bar, uint16_t mask) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;"
+                 ::"r"(bar), "h"(mask) : "memory");
 }
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
@@ -268,15 +319,28 @@ __device__ __forceinline__ void tc_store_tile(const TcProblem &q, int m0, int n0
     }
 }
 
-// Persistent: CTA b takes output tiles b, b + gridDim.x, ...  Warp 0 (lane 0) loads the operand tiles
-// of every K block of those tiles into the stage ring; warp 1 (lane 0) issues the MMAs of tile j into
-// TMEM accumulator j % 2 (2 x BN columns) and commits "acc full"; warps 2..5 read an accumulator
-// (warp w reads TMEM lane quarter w % 4), store the tile and arrive on "acc empty", so the next
-// tile's MMAs overlap this tile's stores.
-template <int BN>
-__global__ void __launch_bounds__(192, 1) tc_rows_kernel(const __grid_constant__ TcParams p, const int total_tiles) {
+// Persistent.  The scheduling unit is CL output tiles stacked along the rows: (row block pair (CL = 2)
+// or row block, column block).  Cluster c (a single CTA when CL = 1) takes units c, c + clusters, ...;
+// CTA `rank` of the cluster computes row block CL * pair + rank of each unit.  Warp 0 (lane 0) loads
+// the operand tiles of every K block of those tiles into the stage ring; warp 1 (lane 0) issues the
+// MMAs of tile j into TMEM accumulator j % 2 (2 x BN columns) and commits "acc full"; warps 2..5 read
+// an accumulator (warp w reads TMEM lane quarter w % 4), store the tile and arrive on "acc empty", so
+// the next tile's MMAs overlap this tile's stores.
+//
+// CL = 2: both CTAs of a unit need the same B tile.  Each producer loads its own A tile and one half
+// of B, multicast into both CTAs at the same shared-memory offset, so a B tile leaves L2 once per
+// pair (64 KB per K block and pair instead of 96 KB).  A stage is free for refilling once the MMAs
+// of both CTAs have read it: every MMA issuer commits to the "empty" barrier of both CTAs (2 arrivals
+// a phase).  Before a CTA exits, its producer waits until the peer's last commits have reached this
+// CTA, then both producers exchange an arrival on a "done" barrier, so that no CTA leaves while the
+// other still signals into its shared memory.  Rows past R (the second tile of a pair at an odd row
+// block count) are zero-filled and never stored.
+template <int BN, int CL>
+__global__ void __launch_bounds__(192, 1) tc_rows_kernel(const __grid_constant__ TcParams p, const int total_units) {
+    static_assert(CL == 1 || CL == 2, "clusters of 1 or 2 CTAs");
     constexpr uint32_t TC_TILE_B = tc_tile_b<BN>(), TC_STAGE = tc_stage<BN>(), TC_TMEM_COLS = 2 * BN;
     constexpr int TC_BN = BN;
+    constexpr uint16_t PAIR = (uint16_t)((1u << CL) - 1u);  // both CTAs of the cluster
     extern __shared__ unsigned char smem_raw[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t raw = smem_u32(smem_raw);
@@ -284,16 +348,20 @@ __global__ void __launch_bounds__(192, 1) tc_rows_kernel(const __grid_constant__
     const uint32_t bars = sbase + TC_STAGES * TC_STAGE;
     const uint32_t full0 = bars, empty0 = bars + 8u * TC_STAGES;
     const uint32_t accf0 = bars + 16u * TC_STAGES, acce0 = accf0 + 16u;  // acc full / empty, 2 each
-    const uint32_t tmem_slot = acce0 + 16u;
+    const uint32_t tmem_slot = acce0 + 16u, done = tmem_slot + 8u;
+    const uint32_t rank = CL > 1 ? tc_cluster_rank() : 0u;
+    const int unit0 = CL > 1 ? (int)tc_cluster_id() : (int)blockIdx.x;
+    const int ustep = CL > 1 ? (int)tc_cluster_count() : (int)gridDim.x;
     if (threadIdx.x == 0) {
         for (int s = 0; s < TC_STAGES; ++s) {
             tc_mbar_init(full0 + 8u * s, 1);
-            tc_mbar_init(empty0 + 8u * s, 1);
+            tc_mbar_init(empty0 + 8u * s, CL);  // the MMA commits of every CTA of the cluster
         }
         for (int a = 0; a < 2; ++a) {
             tc_mbar_init(accf0 + 8u * a, 1);
             tc_mbar_init(acce0 + 8u * a, 4);  // the 4 epilogue warps
         }
+        tc_mbar_init(done, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
@@ -302,20 +370,27 @@ __global__ void __launch_bounds__(192, 1) tc_rows_kernel(const __grid_constant__
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     tc_fence_before();
-    __syncthreads();
+    if constexpr (CL > 1) tc_cluster_sync();  // the peer's barriers exist before anything signals them
+    else __syncthreads();
     tc_fence_after();
     uint32_t tmem;
     asm volatile("ld.shared.b32 %0, [%1];" : "=r"(tmem) : "r"(tmem_slot) : "memory");
+    // output tile of unit u of problem q for this CTA
+    auto tile_of = [&](const TcProblem &q, int u, int &m0, int &n0) {
+        const int local = u - q.tile_begin;
+        m0 = ((local / q.tiles_n) * CL + (int)rank) * TC_BM;
+        n0 = (local % q.tiles_n) * TC_BN;
+    };
 
     if (warp == 0) {
         if (lane == 0) {
             // producer: operand tiles of every K block of every tile of this CTA
             int64_t g = 0;  // K blocks issued so far (stage g % STAGES)
             bool ok = true;
-            for (int t = blockIdx.x; t < total_tiles && ok; t += gridDim.x) {
-                const TcProblem &q = p.prob[tc_problem_of(p, t)];
-                const int local = t - q.tile_begin;
-                const int m0 = (local / q.tiles_n) * TC_BM, n0 = (local % q.tiles_n) * TC_BN;
+            for (int u = unit0; u < total_units && ok; u += ustep) {
+                const TcProblem &q = p.prob[tc_problem_of(p, u)];
+                int m0, n0;
+                tile_of(q, u, m0, n0);
                 for (int kb = 0; kb < q.kblocks; ++kb, ++g) {
                     const int s = (int)(g % TC_STAGES);
                     if (g >= TC_STAGES &&
@@ -324,20 +399,38 @@ __global__ void __launch_bounds__(192, 1) tc_rows_kernel(const __grid_constant__
                         break;
                     }
                     const uint32_t st = sbase + (uint32_t)s * TC_STAGE;
-                    tc_expect_tx(full0 + 8u * s, TC_STAGE);
+                    tc_expect_tx(full0 + 8u * s, TC_STAGE);  // A, and all of B (half of it from the peer)
                     tc_tma_2d(st, &q.a_map, kb * TC_BK, m0, full0 + 8u * s);
                     if (q.b_mn) {
-                        // B in place: BN / 64 copies of 64 columns x 64 K rows, 8 KB apart
-                        for (int jb = 0; jb < TC_BN / 64; ++jb)
-                            tc_tma_2d(st + TC_TILE_A + 8192u * jb, &q.b_map, n0 + 64 * jb, kb * TC_BK, full0 + 8u * s);
+                        // B in place: BN / 64 copies of 64 columns x 64 K rows, 8 KB apart; this CTA's share
+                        constexpr int PER = TC_BN / 64 / CL;
+                        for (int jb = (int)rank * PER; jb < ((int)rank + 1) * PER; ++jb) {
+                            const uint32_t dst = st + TC_TILE_A + 8192u * jb;
+                            if constexpr (CL > 1)
+                                tc_tma_2d_mc(dst, &q.b_map, n0 + 64 * jb, kb * TC_BK, full0 + 8u * s, PAIR);
+                            else
+                                tc_tma_2d(dst, &q.b_map, n0 + 64 * jb, kb * TC_BK, full0 + 8u * s);
+                        }
+                    } else if constexpr (CL > 1) {
+                        // rows [rank * BN / 2, ...) of the K-major B tile (the map's box is BN / 2 rows)
+                        tc_tma_2d_mc(st + TC_TILE_A + rank * (uint32_t)(TC_BN / 2) * 128u, &q.b_map, kb * TC_BK,
+                                     n0 + (int)rank * (TC_BN / 2), full0 + 8u * s, PAIR);
                     } else {
                         tc_tma_2d(st + TC_TILE_A, &q.b_map, kb * TC_BK, n0, full0 + 8u * s);
                     }
                 }
             }
             // before the CTA can finish, every copy issued has landed
-            for (int64_t k = g - TC_STAGES > 0 ? g - TC_STAGES : 0; k < g; ++k)
+            const int64_t tail = g - TC_STAGES > 0 ? g - TC_STAGES : 0;
+            for (int64_t k = tail; k < g; ++k)
                 tc_wait(full0 + 8u * (uint32_t)(k % TC_STAGES), (uint32_t)((k / TC_STAGES) & 1), p.status, 22);
+            if constexpr (CL > 1) {
+                // the peer's last commits have reached this CTA's empty barriers; then trade "done"
+                for (int64_t k = tail; k < g; ++k)
+                    tc_wait(empty0 + 8u * (uint32_t)(k % TC_STAGES), (uint32_t)((k / TC_STAGES) & 1), p.status, 26);
+                tc_remote_arrive(done, rank ^ 1u);
+                tc_wait_cluster(done, 0, p.status, 27);
+            }
         }
     } else if (warp == 1) {
         if (lane == 0) {
@@ -346,8 +439,8 @@ __global__ void __launch_bounds__(192, 1) tc_rows_kernel(const __grid_constant__
             int64_t g = 0;
             int j = 0;  // this CTA's tile count
             bool ok = true;
-            for (int t = blockIdx.x; t < total_tiles && ok; t += gridDim.x, ++j) {
-                const TcProblem &q = p.prob[tc_problem_of(p, t)];
+            for (int u = unit0; u < total_units && ok; u += ustep, ++j) {
+                const TcProblem &q = p.prob[tc_problem_of(p, u)];
                 const int a = j & 1;
                 if (j >= 2 && !tc_wait(acce0 + 8u * a, (uint32_t)(((j >> 1) - 1) & 1), p.status, 25)) break;
                 tc_fence_after();
@@ -373,7 +466,9 @@ __global__ void __launch_bounds__(192, 1) tc_rows_kernel(const __grid_constant__
                             tc_mma(dacc, tc_desc(st + 32u * k), tc_desc(st + TC_TILE_A + 32u * k), idesc,
                                    (kb | k) != 0);
                     }
-                    tc_commit(empty0 + 8u * s);  // the stage is free once these MMAs have read it
+                    // the stage is free once these MMAs (and the peer's) have read it
+                    if constexpr (CL > 1) tc_commit_mc(empty0 + 8u * s, PAIR);
+                    else tc_commit(empty0 + 8u * s);
                 }
                 tc_commit(accf0 + 8u * a);  // accumulator a holds tile j once these MMAs complete
             }
@@ -383,10 +478,10 @@ __global__ void __launch_bounds__(192, 1) tc_rows_kernel(const __grid_constant__
         const int quarter = warp & 3;
         int j = 0;
         bool ok = true;
-        for (int t = blockIdx.x; t < total_tiles; t += gridDim.x, ++j) {
-            const TcProblem &q = p.prob[tc_problem_of(p, t)];
-            const int local = t - q.tile_begin;
-            const int m0 = (local / q.tiles_n) * TC_BM, n0 = (local % q.tiles_n) * TC_BN;
+        for (int u = unit0; u < total_units; u += ustep, ++j) {
+            const TcProblem &q = p.prob[tc_problem_of(p, u)];
+            int m0, n0;
+            tile_of(q, u, m0, n0);
             const int a = j & 1;
             ok = ok && __all_sync(0xffffffffu, tc_wait(accf0 + 8u * a, (uint32_t)((j >> 1) & 1), p.status, 24));
             tc_fence_after();
@@ -484,7 +579,46 @@ int tc_map(CUtensorMap *map, const void *base, int64_t cols, int64_t rows, int64
     return SPREG_OK;
 }
 
+// Clusters of the tensor-core launches: 0 = automatic, 1 = single CTAs, 2 = CTA pairs sharing B.
+std::atomic<int> g_tc_cluster{0};
+
+template <int BN, int CL> cudaError_t tc_launch(const TcParams &p, int units, int sms, size_t smem, cudaStream_t stream) {
+    if constexpr (CL == 1) {
+        tc_rows_kernel<BN, 1><<<(unsigned)std::min(units, sms), 192, smem, stream>>>(p, units);
+        return cudaGetLastError();
+    } else {
+        cudaLaunchConfig_t cfg = {};
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = CL;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.blockDim = dim3(192);
+        cfg.dynamicSmemBytes = smem;
+        cfg.stream = stream;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        // as many clusters as fit at once (a GPC's SMs may not pair up), at most one per unit
+        static int max_clusters[64] = {};
+        int dev = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e != cudaSuccess) return e;
+        int mc = dev >= 0 && dev < 64 ? max_clusters[dev] : 0;
+        if (mc <= 0) {
+            cfg.gridDim = dim3((unsigned)(CL * (sms / CL)));
+            e = cudaOccupancyMaxActiveClusters(&mc, tc_rows_kernel<BN, CL>, &cfg);
+            if (e != cudaSuccess) return e;
+            if (mc <= 0) return cudaErrorInvalidConfiguration;
+            if (dev >= 0 && dev < 64) max_clusters[dev] = mc;
+        }
+        cfg.gridDim = dim3((unsigned)(CL * std::min(units, mc)));
+        return cudaLaunchKernelEx(&cfg, tc_rows_kernel<BN, CL>, p, units);
+    }
+}
+
 }  // namespace
+
+void tc_set_cluster(int mode) { g_tc_cluster.store(mode); }
 
 int dense_rows_batched_impl(const spreg_dense_rows_item *items, int32_t count, cudaStream_t stream) {
     SPREG_CHECK_ARG(count >= 0 && (count == 0 || items), "bad item list");
@@ -596,9 +730,13 @@ int dense_rows_batched_impl(const spreg_dense_rows_item *items, int32_t count, c
     int dev = 0;
     SPREG_CUDA(cudaGetDevice(&dev));
     if (dev >= 0 && dev < 64 && !configured[dev]) {
-        SPREG_CUDA(cudaFuncSetAttribute(tc_rows_kernel<128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        SPREG_CUDA(cudaFuncSetAttribute(tc_rows_kernel<128, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)tc_smem<128>()));
-        SPREG_CUDA(cudaFuncSetAttribute(tc_rows_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        SPREG_CUDA(cudaFuncSetAttribute(tc_rows_kernel<256, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)tc_smem<256>()));
+        SPREG_CUDA(cudaFuncSetAttribute(tc_rows_kernel<128, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)tc_smem<128>()));
+        SPREG_CUDA(cudaFuncSetAttribute(tc_rows_kernel<256, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)tc_smem<256>()));
         configured[dev] = true;
     }
@@ -652,6 +790,17 @@ int dense_rows_batched_impl(const spreg_dense_rows_item *items, int32_t count, c
                 if (!hint && (items[m].tile_n == 128 || items[m].tile_n == 256)) hint = items[m].tile_n;
         }
         const int bn = hint ? hint : (min_n > 128 ? 256 : 128);
+        // CTA pairs sharing B (cl = 2) when the launch has at least one full wave of pairs and the
+        // padding of odd row block counts costs at most 1/8 of its tiles
+        int64_t tiles1 = 0, pairs = 0;
+        for (size_t j = 0; j < cnt; ++j) {
+            const int64_t tm = (groups[first + j].first->rows + TC_BM - 1) / TC_BM;
+            const int64_t tn = (groups[first + j].n + bn - 1) / bn;
+            tiles1 += tm * tn;
+            pairs += (tm + 1) / 2 * tn;
+        }
+        const int mode = g_tc_cluster.load();
+        const int cl = mode == 1 ? 1 : mode == 2 ? 2 : (pairs >= sms / 2 && 8 * (2 * pairs - tiles1) <= tiles1 ? 2 : 1);
         int64_t tiles = 0;
         for (size_t j = 0; j < cnt; ++j) {
             const size_t gi = first + j;
@@ -675,22 +824,22 @@ int dense_rows_batched_impl(const spreg_dense_rows_item *items, int32_t count, c
                 q.seg_ldc = reinterpret_cast<const int64_t *>(scratch + tab_base + seg_ldc_off[gi]);
             }
             q.tiles_n = (int32_t)((g.n + bn - 1) / bn);
-            q.tile_begin = (int32_t)tiles;
-            tiles += ((it.rows + TC_BM - 1) / TC_BM) * q.tiles_n;
+            q.tile_begin = (int32_t)tiles;  // in units of cl row blocks x one column block
+            tiles += ((it.rows + TC_BM - 1) / TC_BM + cl - 1) / cl * q.tiles_n;
             q.b_mn = g.mn ? 1 : 0;
             if ((st = tc_map(&q.a_map, it.a_rows, it.k, it.rows, it.lda, TC_BM)) ||
                 (st = g.mn ? tc_map(&q.b_map, it.b, g.n, it.k, it.ldb, 64)
-                           : tc_map(&q.b_map, scratch + g.bt_off, it.k, g.n, K8, bn)))
+                           : tc_map(&q.b_map, scratch + g.bt_off, it.k, g.n, K8, bn / cl)))
                 return fail(st);
         }
         if (tiles > INT32_MAX) {
             fail(0);
             SPREG_FAIL(SPREG_ERR_UNSUPPORTED, "too many output tiles in one launch");
         }
-        const unsigned grid = (unsigned)std::min<int64_t>(tiles, sms);
-        if (bn == 256) tc_rows_kernel<256><<<grid, 192, tc_smem<256>(), stream>>>(p, (int)tiles);
-        else tc_rows_kernel<128><<<grid, 192, tc_smem<128>(), stream>>>(p, (int)tiles);
-        e = cudaGetLastError();
+        if (bn == 256) e = cl == 2 ? tc_launch<256, 2>(p, (int)tiles, sms, tc_smem<256>(), stream)
+                                   : tc_launch<256, 1>(p, (int)tiles, sms, tc_smem<256>(), stream);
+        else e = cl == 2 ? tc_launch<128, 2>(p, (int)tiles, sms, tc_smem<128>(), stream)
+                         : tc_launch<128, 1>(p, (int)tiles, sms, tc_smem<128>(), stream);
         if (e != cudaSuccess) {
             fail(0);
             SPREG_FAIL(SPREG_ERR_CUDA, "tensor-core launch: %s", cudaGetErrorString(e));

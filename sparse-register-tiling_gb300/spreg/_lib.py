@@ -107,6 +107,7 @@ PROTOTYPES = {
     "spreg_dense_rows_bf16": (C.c_int, [P, C.c_int64, C.c_int64, C.c_int64, P, P, C.c_int64, P, C.c_int64,
                                         C.c_int64, C.c_int32, C.c_int32, C.c_int32, P]),
     "spreg_dense_rows_bf16_batched": (C.c_int, [P, C.c_int32, P]),
+    "spreg_tc_set_cluster": (C.c_int, [C.c_int32]),
     "spreg_pack_from_arena": (C.c_int, [P, C.POINTER(ArenaGeom), P, C.c_int64, P, C.c_int64, P, C.c_int64,
                                         C.POINTER(P), P]),
     "spreg_tile_create": (C.c_int, [P, C.c_int64, C.c_int64, C.c_int64, C.POINTER(P)]),

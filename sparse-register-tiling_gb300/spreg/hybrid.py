@@ -24,6 +24,12 @@ from .mapping import Mapping
 from .packed import PackedMatrix
 
 
+def set_tc_cluster(mode: int) -> None:
+    """Clusters of the tensor-core launches that follow (process-wide): 0 automatic, 1 single CTAs,
+    2 CTA pairs sharing each B tile through TMA multicast (spreg_tc_set_cluster)."""
+    _lib.check(_lib.lib().spreg_tc_set_cluster(int(mode)))
+
+
 def dense_rows_bf16(a_rows, row_index, B, C, n: Optional[int] = None, load_c: bool = False,
                     epilogue: int = _lib.EPILOGUE_NONE, stream=None, check_rows: bool = True):
     """C[row_index[i], :n] (+)= a_rows[i, :K] . B[:, :n] with K = B's rows, on the tensor cores (CUDA

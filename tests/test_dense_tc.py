@@ -190,3 +190,89 @@ def test_tile_width_hint_gives_the_same_products(cuda):
     it[0]["tile_n"] = 64
     with pytest.raises(_lib.SpregError, match="tile_n"):
         _lib.check(_lib.lib().spreg_dense_rows_bf16_batched(it.ctypes.data, 1, _lib.stream_handle(None)))
+
+
+@pytest.fixture
+def tc_cluster_mode():
+    from spreg.hybrid import set_tc_cluster
+    yield set_tc_cluster
+    set_tc_cluster(0)
+
+
+def _cluster_run(mode, set_mode):
+    """Single products (odd and even row block counts, 128- and 256-wide tiles, B read in place), a
+    batched call of many shapes and a coalesced call over several B (transposed B), all under one
+    cluster mode; returns every output."""
+    import torch
+    from spreg.hybrid import dense_rows_bf16
+    from spreg.serving import TC_ITEM_DTYPE
+    set_mode(mode)
+    g = torch.Generator(device="cuda").manual_seed(21)
+    outs = []
+    for R, K, n, c_bf16, load_c, relu in [(1, 8, 1, False, False, False), (300, 100, 200, False, True, True),
+                                          (640, 520, 384, False, False, False), (129, 1000, 257, True, True, False),
+                                          (1024, 256, 128, False, False, True), (2048, 512, 512, False, True, False)]:
+        k8 = (K + 7) // 8 * 8
+        a = torch.zeros((R, k8), device="cuda", dtype=torch.bfloat16)
+        a[:, :K] = torch.randn((R, K), device="cuda", generator=g).to(torch.bfloat16)
+        B = torch.randn((K, n), device="cuda", generator=g).to(torch.bfloat16)
+        rows = torch.randperm(R + 9, device="cuda", generator=g)[:R].to(torch.int32)
+        dt = torch.bfloat16 if c_bf16 else torch.float32
+        C0 = torch.randn((R + 9, n), device="cuda", generator=g).to(dt)
+        C = C0.clone()
+        dense_rows_bf16(a, rows, B, C, load_c=load_c, epilogue=1 if relu else 0)
+        want = a[:, :K].float() @ B.float()
+        if load_c:
+            want = want + C0[rows.long()].float()
+        if relu:
+            want = torch.relu(want)
+        assert _rel(C[rows.long()].float(), want) <= (BF16_OUT_TOL if c_bf16 else FP32_ACC_TOL), (mode, R, K, n)
+        others = torch.ones(R + 9, dtype=torch.bool, device="cuda")
+        others[rows.long()] = False
+        assert torch.equal(C[others], C0[others])
+        outs.append(C)
+    # many shapes in one launch, and 12 products sharing one weight (coalesced, B transposed)
+    cases = [(128, 64, 128), (7, 300, 33), (700, 1000, 200), (256, 520, 129), (384, 64, 300)] * 8
+    a_sh = torch.randn((512, 320), device="cuda", generator=g).to(torch.bfloat16)
+    i_sh = torch.randperm(512, device="cuda", generator=g).to(torch.int32)
+    items = np.zeros(len(cases) + 12, dtype=TC_ITEM_DTYPE)
+    keep = []
+    for i, (R, K, n) in enumerate(cases):
+        k8 = (K + 7) // 8 * 8
+        a = torch.zeros((R, k8), device="cuda", dtype=torch.bfloat16)
+        a[:, :K] = torch.randn((R, K), device="cuda", generator=g).to(torch.bfloat16)
+        B = torch.randn((K, n), device="cuda", generator=g).to(torch.bfloat16)
+        idx = torch.arange(R, device="cuda", dtype=torch.int32)
+        C = torch.randn((R, n), device="cuda", generator=g)
+        items[i] = (a.data_ptr(), R, K, a.stride(0), idx.data_ptr(), B.data_ptr(), B.stride(0), C.data_ptr(),
+                    C.stride(0), n, _lib.F32, i % 2, (i // 2) % 2, 0)
+        keep += [a, B, idx]
+        outs.append(C)
+    for j in range(12):
+        n = [64, 130, 256, 33][j % 4]
+        B = torch.randn((320, n + 5), device="cuda", generator=g).to(torch.bfloat16)[:, :n]
+        C = torch.zeros((512, n), device="cuda")
+        items[len(cases) + j] = (a_sh.data_ptr(), 512, 320, 320, i_sh.data_ptr(), B.data_ptr(), B.stride(0),
+                                 C.data_ptr(), n, n, _lib.F32, 0, 0, 0)
+        keep.append(B)
+        outs.append(C)
+    _lib.check(_lib.lib().spreg_dense_rows_bf16_batched(items.ctypes.data, len(items),
+                                                       _lib.stream_handle(torch.cuda.current_stream())))
+    torch.cuda.synchronize()
+    from spreg.packed import device_status
+    assert device_status() == 0
+    return outs
+
+
+def test_cta_pairs_sharing_b_give_the_same_products(cuda, tc_cluster_mode):
+    """CTA pairs that share each B tile through TMA multicast (cluster mode 2) produce the outputs of
+    single CTAs (mode 1) bit for bit, and so does the automatic choice; a bad mode is refused."""
+    import torch
+    single = _cluster_run(1, tc_cluster_mode)
+    for mode in (2, 0):
+        got = _cluster_run(mode, tc_cluster_mode)
+        for x, y in zip(single, got):
+            assert torch.equal(x.view(torch.int16) if x.dtype == torch.bfloat16 else x.view(torch.int32),
+                               y.view(torch.int16) if y.dtype == torch.bfloat16 else y.view(torch.int32)), mode
+    with pytest.raises(_lib.SpregError, match="cluster mode"):
+        tc_cluster_mode(3)
