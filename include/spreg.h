@@ -24,7 +24,7 @@
  * own bounds check refuses, records a nonzero code in a per-device word instead (read and clear it
  * with spreg_device_status):
  *   2, 5-7   executor waits (batched and B-tile kernels);   20  CSR column index out of range;
- *   21-25    tensor-core kernel waits;                        30  spreg_selftest_wait_timeout.
+ *   21-27    tensor-core kernel waits (26-27: CTA pairs);      30  spreg_selftest_wait_timeout.
  */
 #ifndef SPREG_H
 #define SPREG_H
