@@ -599,17 +599,17 @@ template <int BN, int CL> cudaError_t tc_launch(const TcParams &p, int units, in
         cfg.attrs = attr;
         cfg.numAttrs = 1;
         // as many clusters as fit at once (a GPC's SMs may not pair up), at most one per unit
-        static int max_clusters[64] = {};
+        static std::atomic<int> max_clusters[64];  // per device, 0 until queried
         int dev = 0;
         cudaError_t e = cudaGetDevice(&dev);
         if (e != cudaSuccess) return e;
-        int mc = dev >= 0 && dev < 64 ? max_clusters[dev] : 0;
+        int mc = dev >= 0 && dev < 64 ? max_clusters[dev].load() : 0;
         if (mc <= 0) {
             cfg.gridDim = dim3((unsigned)(CL * (sms / CL)));
             e = cudaOccupancyMaxActiveClusters(&mc, tc_rows_kernel<BN, CL>, &cfg);
             if (e != cudaSuccess) return e;
             if (mc <= 0) return cudaErrorInvalidConfiguration;
-            if (dev >= 0 && dev < 64) max_clusters[dev] = mc;
+            if (dev >= 0 && dev < 64) max_clusters[dev].store(mc);
         }
         cfg.gridDim = dim3((unsigned)(CL * std::min(units, mc)));
         return cudaLaunchKernelEx(&cfg, tc_rows_kernel<BN, CL>, p, units);
@@ -726,10 +726,10 @@ int dense_rows_batched_impl(const spreg_dense_rows_item *items, int32_t count, c
     const int64_t tab_base = (bytes + 255) / 256 * 256;
     int *status = device_status_word(&st);
     if (st != SPREG_OK) return st;
-    static bool configured[64] = {};
+    static std::atomic<bool> configured[64];  // per device
     int dev = 0;
     SPREG_CUDA(cudaGetDevice(&dev));
-    if (dev >= 0 && dev < 64 && !configured[dev]) {
+    if (dev >= 0 && dev < 64 && !configured[dev].load()) {
         SPREG_CUDA(cudaFuncSetAttribute(tc_rows_kernel<128, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)tc_smem<128>()));
         SPREG_CUDA(cudaFuncSetAttribute(tc_rows_kernel<256, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -738,11 +738,15 @@ int dense_rows_batched_impl(const spreg_dense_rows_item *items, int32_t count, c
                                         (int)tc_smem<128>()));
         SPREG_CUDA(cudaFuncSetAttribute(tc_rows_kernel<256, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)tc_smem<256>()));
-        configured[dev] = true;
+        configured[dev].store(true);
     }
-    static int sms_of[64] = {};
-    if (dev >= 0 && dev < 64 && !sms_of[dev]) SPREG_CUDA(cudaDeviceGetAttribute(&sms_of[dev], cudaDevAttrMultiProcessorCount, dev));
-    const int sms = (dev >= 0 && dev < 64 && sms_of[dev] > 0) ? sms_of[dev] : 148;
+    static std::atomic<int> sms_of[64];  // per device, 0 until queried
+    if (dev >= 0 && dev < 64 && !sms_of[dev].load()) {
+        int v = 0;
+        SPREG_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev));
+        sms_of[dev].store(v);
+    }
+    const int sms = (dev >= 0 && dev < 64 && sms_of[dev].load() > 0) ? sms_of[dev].load() : 148;
     char *scratch = nullptr;
     SPREG_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&scratch), (size_t)(tab_base + (int64_t)tab.size() + 16),
                                stream));

@@ -12,6 +12,7 @@
 // indices -- the role the reference's generated nanokernels play.  Each output element is an
 // fmaf chain in packed-entry order, identical to the CPU executor's.
 #pragma once
+#include <atomic>
 
 #include <type_traits>
 
@@ -1144,15 +1145,15 @@ cudaError_t launch_exec_batch(const BatchParams &p, int nv, unsigned grid, int t
         using V = ComboTypes<COMBO>::V;                                                               \
         using B = ComboTypes<COMBO>::B;                                                               \
         using C = ComboTypes<COMBO>::C;                                                               \
-        static bool configured[64][5] = {};                                                           \
+        static std::atomic<bool> configured[64][5];                                                           \
         int dev = 0;                                                                                  \
         cudaGetDevice(&dev);                                                                          \
         auto run = [&](auto kern) -> cudaError_t {                                                    \
             if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;                                  \
-            if (!configured[dev][nv]) {                                                               \
+            if (!configured[dev][nv].load()) {                                                               \
                 cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem); \
                 if (e != cudaSuccess) return e;                                                       \
-                configured[dev][nv] = true;                                                           \
+                configured[dev][nv].store(true);                                                           \
             }                                                                                         \
             kern<<<grid, threads, smem, s>>>(p);                                                      \
             return cudaGetLastError();                                                                \

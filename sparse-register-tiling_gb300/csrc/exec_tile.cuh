@@ -27,6 +27,7 @@
 // Every wait is bounded; a wait that gives up records a code in the device status word and the
 // warp stops, the producer first waiting (bounded) for the copies it issued.
 #pragma once
+#include <atomic>
 #include <cuda.h>
 
 #include <cstddef>
@@ -380,15 +381,15 @@ cudaError_t launch_exec_tile(const TileParams &p, int nv, unsigned grid, int thr
         using V = ComboTypes<COMBO>::V;                                                               \
         using B = ComboTypes<COMBO>::B;                                                               \
         using C = ComboTypes<COMBO>::C;                                                               \
-        static bool configured[64][9] = {};                                                           \
+        static std::atomic<bool> configured[64][9];                                                           \
         int dev = 0;                                                                                  \
         cudaGetDevice(&dev);                                                                          \
         auto run = [&](auto kern) -> cudaError_t {                                                    \
             if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;                                  \
-            if (!configured[dev][nv]) {                                                               \
+            if (!configured[dev][nv].load()) {                                                               \
                 cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem); \
                 if (e != cudaSuccess) return e;                                                       \
-                configured[dev][nv] = true;                                                           \
+                configured[dev][nv].store(true);                                                           \
             }                                                                                         \
             kern<<<grid, threads, smem, s>>>(p);                                                      \
             return cudaGetLastError();                                                                \
