@@ -274,8 +274,10 @@ int spreg_dense_rows_bf16_batched(const spreg_dense_rows_item *items, int32_t nu
 /* Thread-block clusters of the dense-rows launches that follow (process-wide): 0 = automatic, 1 =
  * one CTA per output tile, 2 = CTA pairs on two row blocks of one column block, each loading half of
  * the shared B tile into both CTAs (TMA multicast).  Automatic takes pairs when a launch has at
- * least a full wave of them and odd row block counts pad at most 1/8 of its tiles.  Results are the
- * same either way.  Returns SPREG_ERR_ARG for another mode. */
+ * least a full wave of them and odd row block counts pad at most 1/8 of its tiles, and single CTAs
+ * when no 2-CTA cluster fits the device or context (where mode 2 makes the launches fail with
+ * SPREG_ERR_UNSUPPORTED).  Results are the same either way.  Returns SPREG_ERR_INVALID_ARG for
+ * another mode. */
 int spreg_tc_set_cluster(int32_t mode);
 
 /* Status word of the current device: nonzero once a kernel gave up a bounded wait (its results

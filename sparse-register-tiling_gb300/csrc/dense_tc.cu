@@ -582,37 +582,50 @@ int tc_map(CUtensorMap *map, const void *base, int64_t cols, int64_t rows, int64
 // Clusters of the tensor-core launches: 0 = automatic, 1 = single CTAs, 2 = CTA pairs sharing B.
 std::atomic<int> g_tc_cluster{0};
 
-template <int BN, int CL> cudaError_t tc_launch(const TcParams &p, int units, int sms, size_t smem, cudaStream_t stream) {
+cudaLaunchConfig_t tc_pair_config(cudaLaunchAttribute *attr, size_t smem, cudaStream_t stream) {
+    cudaLaunchConfig_t cfg = {};
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 2;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.blockDim = dim3(192);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cfg;
+}
+
+// CTA pairs of tc_rows_kernel<BN, 2> that fit on device `dev` at once (a GPC's SMs may not all pair
+// up; an SM-limited context may fit none): queried once per device, 0 when none fit.
+template <int BN> int tc_max_pairs(int dev, int sms) {
+    static std::atomic<int> max_pairs[64];  // per device: 0 = not queried, -1 = none fit
+    if (dev < 0 || dev >= 64) return 0;
+    int mc = max_pairs[dev].load();
+    if (mc == 0) {
+        cudaLaunchAttribute attr[1];
+        cudaLaunchConfig_t cfg = tc_pair_config(attr, tc_smem<BN>(), nullptr);
+        cfg.gridDim = dim3((unsigned)(2 * (sms / 2 > 0 ? sms / 2 : 1)));
+        if (cudaOccupancyMaxActiveClusters(&mc, tc_rows_kernel<BN, 2>, &cfg) != cudaSuccess || mc <= 0) {
+            cudaGetLastError();  // a refused query leaves no error behind
+            mc = -1;
+        }
+        max_pairs[dev].store(mc);
+    }
+    return mc > 0 ? mc : 0;
+}
+
+template <int BN, int CL>
+cudaError_t tc_launch(const TcParams &p, int units, int sms, int pairs_fit, size_t smem, cudaStream_t stream) {
     if constexpr (CL == 1) {
         tc_rows_kernel<BN, 1><<<(unsigned)std::min(units, sms), 192, smem, stream>>>(p, units);
         return cudaGetLastError();
     } else {
-        cudaLaunchConfig_t cfg = {};
+        // as many clusters as fit at once, at most one per unit
         cudaLaunchAttribute attr[1];
-        attr[0].id = cudaLaunchAttributeClusterDimension;
-        attr[0].val.clusterDim.x = CL;
-        attr[0].val.clusterDim.y = 1;
-        attr[0].val.clusterDim.z = 1;
-        cfg.blockDim = dim3(192);
-        cfg.dynamicSmemBytes = smem;
-        cfg.stream = stream;
-        cfg.attrs = attr;
-        cfg.numAttrs = 1;
-        // as many clusters as fit at once (a GPC's SMs may not pair up), at most one per unit
-        static std::atomic<int> max_clusters[64];  // per device, 0 until queried
-        int dev = 0;
-        cudaError_t e = cudaGetDevice(&dev);
-        if (e != cudaSuccess) return e;
-        int mc = dev >= 0 && dev < 64 ? max_clusters[dev].load() : 0;
-        if (mc <= 0) {
-            cfg.gridDim = dim3((unsigned)(CL * (sms / CL)));
-            e = cudaOccupancyMaxActiveClusters(&mc, tc_rows_kernel<BN, CL>, &cfg);
-            if (e != cudaSuccess) return e;
-            if (mc <= 0) return cudaErrorInvalidConfiguration;
-            if (dev >= 0 && dev < 64) max_clusters[dev].store(mc);
-        }
-        cfg.gridDim = dim3((unsigned)(CL * std::min(units, mc)));
-        return cudaLaunchKernelEx(&cfg, tc_rows_kernel<BN, CL>, p, units);
+        cudaLaunchConfig_t cfg = tc_pair_config(attr, smem, stream);
+        cfg.gridDim = dim3((unsigned)(2 * std::min(units, pairs_fit)));
+        return cudaLaunchKernelEx(&cfg, tc_rows_kernel<BN, 2>, p, units);
     }
 }
 
@@ -804,7 +817,14 @@ int dense_rows_batched_impl(const spreg_dense_rows_item *items, int32_t count, c
             pairs += (tm + 1) / 2 * tn;
         }
         const int mode = g_tc_cluster.load();
-        const int cl = mode == 1 ? 1 : mode == 2 ? 2 : (pairs >= sms / 2 && 8 * (2 * pairs - tiles1) <= tiles1 ? 2 : 1);
+        const int pairs_fit = mode == 1 ? 0 : bn == 256 ? tc_max_pairs<256>(dev, sms) : tc_max_pairs<128>(dev, sms);
+        if (mode == 2 && pairs_fit == 0) {
+            fail(0);
+            SPREG_FAIL(SPREG_ERR_UNSUPPORTED, "tensor-core CTA pairs: no 2-CTA cluster fits this device or context");
+        }
+        const int cl = mode == 1 || pairs_fit == 0 ? 1
+                       : mode == 2 ? 2
+                                   : (pairs >= sms / 2 && 8 * (2 * pairs - tiles1) <= tiles1 ? 2 : 1);
         int64_t tiles = 0;
         for (size_t j = 0; j < cnt; ++j) {
             const size_t gi = first + j;
@@ -840,10 +860,10 @@ int dense_rows_batched_impl(const spreg_dense_rows_item *items, int32_t count, c
             fail(0);
             SPREG_FAIL(SPREG_ERR_UNSUPPORTED, "too many output tiles in one launch");
         }
-        if (bn == 256) e = cl == 2 ? tc_launch<256, 2>(p, (int)tiles, sms, tc_smem<256>(), stream)
-                                   : tc_launch<256, 1>(p, (int)tiles, sms, tc_smem<256>(), stream);
-        else e = cl == 2 ? tc_launch<128, 2>(p, (int)tiles, sms, tc_smem<128>(), stream)
-                         : tc_launch<128, 1>(p, (int)tiles, sms, tc_smem<128>(), stream);
+        if (bn == 256) e = cl == 2 ? tc_launch<256, 2>(p, (int)tiles, sms, pairs_fit, tc_smem<256>(), stream)
+                                   : tc_launch<256, 1>(p, (int)tiles, sms, pairs_fit, tc_smem<256>(), stream);
+        else e = cl == 2 ? tc_launch<128, 2>(p, (int)tiles, sms, pairs_fit, tc_smem<128>(), stream)
+                         : tc_launch<128, 1>(p, (int)tiles, sms, pairs_fit, tc_smem<128>(), stream);
         if (e != cudaSuccess) {
             fail(0);
             SPREG_FAIL(SPREG_ERR_CUDA, "tensor-core launch: %s", cudaGetErrorString(e));
