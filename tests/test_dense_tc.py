@@ -231,6 +231,13 @@ def _cluster_run(mode, set_mode):
         others[rows.long()] = False
         assert torch.equal(C[others], C0[others])
         outs.append(C)
+    # B rows of 602 bytes cannot be read in place: transposed into a K-major buffer, 256-wide tiles
+    a = torch.randn((700, 264), device="cuda", generator=g).to(torch.bfloat16)
+    Bu = torch.randn((264, 301), device="cuda", generator=g).to(torch.bfloat16)[:, :300]
+    C = torch.zeros((700, 300), device="cuda")
+    dense_rows_bf16(a, torch.arange(700, device="cuda", dtype=torch.int32), Bu, C)
+    assert _rel(C, a.float() @ Bu.float()) <= FP32_ACC_TOL, mode
+    outs.append(C)
     # many shapes in one launch, and 12 products sharing one weight (coalesced, B transposed)
     cases = [(128, 64, 128), (7, 300, 33), (700, 1000, 200), (256, 520, 129), (384, 64, 300)] * 8
     a_sh = torch.randn((512, 320), device="cuda", generator=g).to(torch.bfloat16)
