@@ -563,6 +563,22 @@ def tensor_core_suite(dev, reps: int = 20) -> dict:
     ref = a[:256].float() @ b.float()
     err = float((c[:256] - ref).norm() / ref.norm())
     tflops = 2.0 * M * N * K / us / 1e6
+    # the same product on single CTAs (no B tiles shared by CTA pairs), for comparison
+    from spreg.hybrid import set_tc_cluster
+    c1 = torch.empty_like(c)
+    set_tc_cluster(1)
+    try:
+        for _ in range(3):
+            dense_rows_bf16(a, idx, b, c1, check_rows=False)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(reps):
+            dense_rows_bf16(a, idx, b, c1, check_rows=False)
+        e1.record()
+        torch.cuda.synchronize()
+    finally:
+        set_tc_cluster(0)
+    us1 = e0.elapsed_time(e1) / reps * 1e3
     peak = None
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -575,7 +591,9 @@ def tensor_core_suite(dev, reps: int = 20) -> dict:
         hyb[f"{m}x{k}_n{n}"] = tune_tc_fill(A, Mapping.identity(2), n, k_tile=kt)
     return {"dense_bf16_4096^3_us": us, "tflops": tflops, "peak_tflops": peak,
             "frac_of_measured_peak": (tflops / peak) if peak else None,
-            "rel_err_vs_fp32_of_bf16_inputs": err, "includes": "API call: tcgen05 kernel reading B in place (N-major operand), set-up and launch",
+            "single_cta_us": us1, "single_cta_tflops": 2.0 * M * N * K / us1 / 1e6,
+            "single_cta_equal": bool(torch.equal(c, c1)),
+            "rel_err_vs_fp32_of_bf16_inputs": err, "includes": "API call: tcgen05 kernel reading B in place (N-major operand), CTA pairs sharing B tiles (automatic cluster mode), set-up and launch",
             "hybrid_threshold_serving_layers": hyb}
 
 
