@@ -19,6 +19,9 @@
 //   * warps 2-5 each read one 32-lane quarter of the accumulator with tcgen05.ld (the tile's rows),
 //     apply load_c / ReLU, store through the row index (and the segment table of coalesced products)
 //     and release the accumulator ("acc empty"), so the next tile's MMAs overlap these stores.
+// Launches with at least a full wave of work run as clusters of 2 CTAs (spreg_tc_set_cluster): a pair
+// computes two row blocks of one column block and each CTA loads its A tile and half of the B tile,
+// multicast into both CTAs, so a B tile leaves L2 once per pair (tc_rows_kernel<BN, 2>).
 // Rows past R and columns past n are zero-filled by the tensor copies and never stored; K past the
 // end of A_rows / Bt reads as zero.  Every wait is bounded: a wait that gives up records a code in
 // the device status word; TMEM is released on every path.
