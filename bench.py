@@ -818,7 +818,8 @@ def main():
     launch_s = sec / (args.steps * launches_per_step)
     achieved = (step_bytes / launches_per_step) / launch_s / 1e9
     spmm_us = sec / (args.steps * len(packs)) * 1e6
-    kname = "exec_tile_kernel" if args.staging == 1 else "exec_batch_kernel"
+    kname = ("exec_kernel" if args.meta == 2 else
+             "exec_tile_kernel" if args.staging == 1 else "exec_batch_kernel")  # meta 2: register streams
     traffic_key = (f"{kname}/{args.dtype}/{args.m}x{args.k}/s{args.sparsity}/n{args.n}/kt{args.k_tile}/"
                    f"{'identity' if args.mapping == 'identity' else args.mapping}")
     traffic = load_traffic(traffic_key, len(packs) // launches_per_step)
