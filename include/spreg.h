@@ -24,7 +24,7 @@
  * own bounds check refuses, records a nonzero code in a per-device word instead (read and clear it
  * with spreg_device_status):
  *   2, 5-7   executor waits (batched and B-tile kernels);   20  CSR column index out of range;
- *   21-27    tensor-core kernel waits (26-27: CTA pairs);      30  spreg_selftest_wait_timeout.
+ *   21-25    tensor-core kernel waits;                         30  spreg_selftest_wait_timeout.
  */
 #ifndef SPREG_H
 #define SPREG_H
@@ -236,9 +236,12 @@ int spreg_execute_batched(const spreg_work_item *items_host, int32_t num_items, 
  * until exit.  A list that needs more than SPREG_NOALLOC_MAX_LAUNCHES launches (one launch per
  * group of up to 224 SpMMs of one M_r / strip width / dtype combination) is rejected.  The first
  * call on each device looks up the array's device address; make it before any stream capture.
- * Calls share the array and clear it at their start, so calls that overlap on the GPU race.
- * Runs only the batched execution-layout kernel (no meta_staging = 2, no oversized blocks).
- * It has no counterpart in the reference. */
+ * Calls share the array and clear its counters at their start, so calls that overlap on the GPU
+ * race.  Its status word (a bounded wait that gave up) is read and cleared by spreg_device_status,
+ * like the regular executors' word, and keeps its value until then.  It runs only the batched
+ * execution-layout kernel (no meta_staging = 2, no oversized blocks): where spreg_execute_batched's
+ * automatic B staging picks the shared-memory B-tile kernel (K-tiled packs), this entry point gives
+ * the same results from the batched kernel, more slowly.  It has no counterpart in the reference. */
 #define SPREG_NOALLOC_MAX_LAUNCHES 64
 int spreg_execute_batched_noalloc(const spreg_work_item *items_host, int32_t num_items, spreg_stream_t stream);
 
@@ -268,20 +271,63 @@ typedef struct {
 } spreg_dense_rows_item;
 
 /* Many dense-rows products (any shapes) in as few launches as possible: the output tiles of up to
- * 80 products share one launch.  Same arguments and results as spreg_dense_rows_bf16 per item. */
+ * 192 products share one launch.  Same arguments and results as spreg_dense_rows_bf16 per item. */
 int spreg_dense_rows_bf16_batched(const spreg_dense_rows_item *items, int32_t num_items, spreg_stream_t stream);
 
-/* Thread-block clusters of the dense-rows launches that follow (process-wide): 0 = automatic, 1 =
- * one CTA per output tile, 2 = CTA pairs on two row blocks of one column block, each loading half of
- * the shared B tile into both CTAs (TMA multicast).  Automatic takes pairs when a launch has at
- * least a full wave of them and odd row block counts pad at most 1/8 of its tiles, and single CTAs
- * when no 2-CTA cluster fits the device or context (where mode 2 makes the launches fail with
- * SPREG_ERR_UNSUPPORTED).  Results are the same either way.  Returns SPREG_ERR_INVALID_ARG for
- * another mode. */
-int spreg_tc_set_cluster(int32_t mode);
+/* FP32-accurate dense rows on the tensor cores.  The FP32 executor's accuracy at tensor-core rate: A
+ * (per row) and B (per column) are scaled by powers of two and split into FP16 halves, x = hi + lo,
+ * and each product runs as hi.hi + hi.lo + lo.hi FP16 MMAs with FP32 accumulation.  The terms left
+ * out are below 2^-22 of each product.  The tensor core's FP32 accumulation truncates, so its error
+ * grows with the 16-deep K steps of one accumulator: products with k > 1024 run as passes over K
+ * chunks of 1024, each adding into C, which keeps the result within the FP32 executor's tolerance
+ * (rel err <= 1e-5) at any K.  Not bit-identical to the register-tiled order.
+ * Values whose magnitude is more than 2^17 below their row's (A) or column's (B) largest keep an
+ * absolute error below 2^-25 of the scaled unit; scales are limited to 2^-126 .. 2^126.
+ *
+ * spreg_dense_rows_f32_split prepares the A side once (a pruned weight's dense panels): a_rows is
+ * rows x k FP32 (row stride lda); a_split receives 2 * rows rows of ld_split FP16 (16-byte aligned,
+ * ld_split >= k a multiple of 8): rows [0, rows) the high halves, [rows, 2 rows) the low halves;
+ * row_scale[i] receives 2^-s of row i's scale. */
+int spreg_dense_rows_f32_split(const float *a_rows, int64_t rows, int64_t k, int64_t lda, void *a_split,
+                               int64_t ld_split, float *row_scale, spreg_stream_t stream);
+
+/* One FP32-accurate product: C[row_index[i], 0:n] (+)= A_rows[i, 0:k] . B[0:k, 0:n] with A_rows given
+ * as its split pair; B is FP32 k x n (row stride ldb), C FP32 (row stride ldc). */
+typedef struct {
+    const void *a_split;     /* spreg_dense_rows_f32_split output: 2 * rows x ld_split FP16 */
+    int64_t rows, k, ld_split;
+    const float *row_scale;  /* rows */
+    const int32_t *row_index;
+    const float *b;
+    int64_t ldb;
+    float *c;
+    int64_t ldc, n;
+    int32_t load_c, epilogue;
+    int32_t tile_n;          /* output tile width: 0 = automatic, 128 or 256 */
+    int32_t reserved;        /* 0 */
+} spreg_dense_rows_f32_item;
+
+/* One product / many products in as few launches as possible (B of each product is split into its
+ * FP16 pair by one preparation launch, then the output tiles of up to 192 products share one
+ * tensor-core launch).  Products with the same A, row index, load_c and epilogue coalesce into one
+ * product over their side-by-side B. */
+int spreg_dense_rows_f32(const spreg_dense_rows_f32_item *item, spreg_stream_t stream);
+int spreg_dense_rows_f32_batched(const spreg_dense_rows_f32_item *items, int32_t num_items, spreg_stream_t stream);
+
+/* A reusable plan of spreg_dense_rows_f32_batched for a fixed item list (the same pointers every
+ * run): its scratch, tensor maps and device tables are made once (synchronising `stream`), so a run
+ * is two kernel launches and no host-side work, and can be captured in a CUDA graph.  The plan
+ * belongs to the device current at creation; runs of one plan must not overlap on the GPU (they
+ * share its scratch). */
+typedef struct spreg_dense_rows_plan spreg_dense_rows_plan;
+int spreg_dense_rows_f32_plan_create(const spreg_dense_rows_f32_item *items, int32_t num_items,
+                                     spreg_dense_rows_plan **out, spreg_stream_t stream);
+int spreg_dense_rows_plan_run(const spreg_dense_rows_plan *plan, spreg_stream_t stream);
+void spreg_dense_rows_plan_destroy(spreg_dense_rows_plan *plan);
 
 /* Status word of the current device: nonzero once a kernel gave up a bounded wait (its results
- * are then incomplete).  Synchronous; reset != 0 clears it. */
+ * are then incomplete) -- the regular kernels' word, or, when that is 0, the word of
+ * spreg_execute_batched_noalloc.  Synchronous; reset != 0 clears both. */
 int spreg_device_status(int32_t *status_host, int32_t reset);
 
 /* Self-test of the bounded waits every kernel uses: one CTA waits on an mbarrier that nothing

@@ -18,7 +18,11 @@ void clear_error() { g_last_error.clear(); }
 int dense_rows_bf16_impl(const void *, int64_t, int64_t, int64_t, const int32_t *, const void *, int64_t, void *,
                          int64_t, int64_t, int32_t, int32_t, int32_t, cudaStream_t);
 int dense_rows_batched_impl(const spreg_dense_rows_item *, int32_t, cudaStream_t);
-void tc_set_cluster(int mode);
+int dense_rows_f32_batched_impl(const spreg_dense_rows_f32_item *, int32_t, cudaStream_t);
+int split_rows_f32_impl(const float *, int64_t, int64_t, int64_t, void *, int64_t, float *, cudaStream_t);
+int tc_plan_create_f32_impl(const spreg_dense_rows_f32_item *, int32_t, void **, cudaStream_t);
+int tc_plan_run_impl(const void *, cudaStream_t);
+void tc_plan_destroy_impl(void *);
 int pack_from_arena_impl(const spreg_mapping *, const spreg_arena_geom *, const void *, int64_t,
                          const spreg_panel_desc *, int64_t, const float *, int64_t, spreg_packed **, cudaStream_t);
 int pack_dense_impl(const spreg_mapping *, const float *, int64_t, int64_t, int64_t, const spreg_pack_opts *,
@@ -109,7 +113,7 @@ extern "C" {
 
 const char *spreg_last_error(void) { return g_last_error.c_str(); }
 
-int spreg_version(void) { return 100; /* 0.1.0 */ }
+int spreg_version(void) { return 200; /* 0.2.0 */ }
 
 // ---------------------------------------------------------------------- mapping
 int spreg_mapping_create(int32_t mr, const int32_t *map_offsets, const int32_t *map_codes, const int32_t *nanokernels,
@@ -247,12 +251,35 @@ int spreg_dense_rows_bf16_batched(const spreg_dense_rows_item *items, int32_t nu
     return dense_rows_batched_impl(items, num_items, (cudaStream_t)stream);
 }
 
-int spreg_tc_set_cluster(int32_t mode) {
+int spreg_dense_rows_f32_split(const float *a_rows, int64_t rows, int64_t k, int64_t lda, void *a_split,
+                               int64_t ld_split, float *row_scale, spreg_stream_t stream) {
     clear_error();
-    SPREG_CHECK_ARG(mode == 0 || mode == 1 || mode == 2, "cluster mode must be 0, 1 or 2 (got %d)", (int)mode);
-    tc_set_cluster(mode);
-    return SPREG_OK;
+    return split_rows_f32_impl(a_rows, rows, k, lda, a_split, ld_split, row_scale, (cudaStream_t)stream);
 }
+
+int spreg_dense_rows_f32(const spreg_dense_rows_f32_item *item, spreg_stream_t stream) {
+    clear_error();
+    SPREG_CHECK_ARG(item, "null item");
+    return dense_rows_f32_batched_impl(item, 1, (cudaStream_t)stream);
+}
+
+int spreg_dense_rows_f32_batched(const spreg_dense_rows_f32_item *items, int32_t num_items, spreg_stream_t stream) {
+    clear_error();
+    return dense_rows_f32_batched_impl(items, num_items, (cudaStream_t)stream);
+}
+
+int spreg_dense_rows_f32_plan_create(const spreg_dense_rows_f32_item *items, int32_t num_items,
+                                     spreg_dense_rows_plan **out, spreg_stream_t stream) {
+    clear_error();
+    return tc_plan_create_f32_impl(items, num_items, reinterpret_cast<void **>(out), (cudaStream_t)stream);
+}
+
+int spreg_dense_rows_plan_run(const spreg_dense_rows_plan *plan, spreg_stream_t stream) {
+    clear_error();
+    return tc_plan_run_impl(plan, (cudaStream_t)stream);
+}
+
+void spreg_dense_rows_plan_destroy(spreg_dense_rows_plan *plan) { tc_plan_destroy_impl(plan); }
 
 void spreg_packed_destroy(spreg_packed *p) { packed_release(p); }
 

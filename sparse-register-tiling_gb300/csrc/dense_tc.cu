@@ -2,38 +2,50 @@
 // TMA).
 //
 // C[row_index[i], 0:n] (+)= A_rows[i, 0:K] . B[0:K, 0:n] for the rows of a pruned matrix whose panels
-// are dense enough that a BF16 tensor-core product beats the register-tiled executors.  BF16 operands,
-// FP32 accumulation in tensor memory (TMEM), FP32 or BF16 output with load_c and the ReLU epilogue.
+// are dense enough that a tensor-core product beats the register-tiled executors.  Two operand forms:
+//   * BF16 (spreg_dense_rows_bf16): BF16 A and B, FP32 accumulation in tensor memory (TMEM), FP32 or
+//     BF16 output;
+//   * FP32-accurate split (spreg_dense_rows_f32): FP32 A and B, each scaled by a power of two (A per
+//     row, B per column) and split into two FP16 halves, x = hi + lo with hi = fp16(x) and
+//     lo = fp16(x - hi).  Three FP16 MMAs per K step, hi.hi + hi.lo + lo.hi, accumulate in FP32;
+//     the dropped lo.lo term and the rounding of lo are below 2^-22 of each product, the level of
+//     FP32's own rounding.  The epilogue undoes the scales (exact powers of two).  The tensor core
+//     accumulates in FP32 with truncation, an error that grows with the 16-deep K steps of one
+//     accumulator, so K is cut into chunks of TC_SPLIT_CHUNK run by successive launches that add
+//     into C.
+// load_c and the ReLU epilogue apply to both.
 //
-// One launch runs up to 80 such products ("problems", a tensor map pair each in the kernel
-// parameters).  Its output tiles (128 rows x BN columns; BN 256 when every product of the launch has
+// One launch runs up to TC_MAX_PROBLEMS products ("problems"; their tensor maps sit in a device
+// table).  Its output tiles (128 rows x BN columns; BN 256 when every product of the launch has
 // more than 128 columns, else 128) are shared out over persistent CTAs of 6 warps, at most one per
 // SM, each finding a tile's problem by a binary search over the problems' first tiles:
 //   * warp 0 (one lane) loads 64-deep K blocks of A_rows (128 x 64, K-major) and of B into a ring of
-//     4 stages with 2-D tensor copies (TMA, 128-byte swizzle; "full" mbarriers with expected bytes).
-//     A single product's B is read in place as an N-major operand (BN / 64 copies of 64 columns x
-//     64 K rows); products coalesced over several B are first transposed into one K-major buffer;
-//   * warp 1 (one lane) issues four tcgen05.mma.kind::f16 (M 128, N BN, K 16) per K block into one
-//     of two TMEM accumulators, tcgen05.commit releasing the stage ("empty") and, per tile, the
-//     accumulator ("acc full");
+//     stages with 2-D tensor copies (TMA, 128-byte swizzle; "full" mbarriers with expected bytes).
+//     A single BF16 product's B, and every split product's B halves, are read as N-major operands
+//     (BN / 64 copies of 64 columns x 64 K rows); BF16 products coalesced over several B are first
+//     transposed into one K-major buffer;
+//   * warp 1 (one lane) issues tcgen05.mma.kind::f16 (M 128, N BN, K 16; four per K block, twelve for
+//     a split product) into one of two TMEM accumulators, tcgen05.commit releasing the stage
+//     ("empty") and, per tile, the accumulator ("acc full");
 //   * warps 2-5 each read one 32-lane quarter of the accumulator with tcgen05.ld (the tile's rows),
-//     apply load_c / ReLU, store through the row index (and the segment table of coalesced products)
-//     and release the accumulator ("acc empty"), so the next tile's MMAs overlap these stores.
-// Launches with at least a full wave of work run as clusters of 2 CTAs (spreg_tc_set_cluster): a pair
-// computes two row blocks of one column block and each CTA loads its A tile and half of the B tile,
-// multicast into both CTAs, so a B tile leaves L2 once per pair (tc_rows_kernel<BN, 2>).
-// Rows past R and columns past n are zero-filled by the tensor copies and never stored; K past the
-// end of A_rows / Bt reads as zero.  Every wait is bounded: a wait that gives up records a code in
-// the device status word; TMEM is released on every path.
+//     apply the scales, load_c and ReLU, store through the row index (and the segment table of
+//     coalesced products) and release the accumulator ("acc empty"), so the next tile's MMAs overlap
+//     these stores.
+// Columns past n are zero-filled by the tensor copies and never stored; K past the end of A reads
+// as zero; rows past R are never stored.  Every wait is bounded: a wait that gives up records a
+// code in the device status word; TMEM is released on every path.
 #include "spreg_common.cuh"
 
 #include <cuda.h>
 #include <cudaTypedefs.h>
+#include <cuda_fp16.h>
 
 #include <algorithm>
 #include <atomic>
 #include <cstring>
 #include <map>
+#include <memory>
+#include <string>
 #include <tuple>
 #include <vector>
 
@@ -43,22 +55,30 @@ int *device_status_word(int *st);  // exec.cu
 
 namespace {
 
-constexpr int TC_BM = 128, TC_BK = 64, TC_STAGES = 4;
+constexpr int TC_BM = 128, TC_BK = 64;
 constexpr uint32_t TC_TILE_A = TC_BM * TC_BK * 2;  // 16 KB
 // Output tile width BN (128 or 256): the MMA's N, the TMEM accumulator's columns, B tile rows.
+// A split product stages both halves of A and of B.
 template <int BN> constexpr uint32_t tc_tile_b() { return (uint32_t)BN * TC_BK * 2; }
-template <int BN> constexpr uint32_t tc_stage() { return TC_TILE_A + tc_tile_b<BN>(); }
-template <int BN> constexpr size_t tc_smem() {
-    return 1024 /* alignment slack */ + TC_STAGES * tc_stage<BN>() + 256 /* barriers, TMEM slot */;
+template <int BN, bool SPLIT> constexpr uint32_t tc_stage() {
+    return (SPLIT ? 2u : 1u) * (TC_TILE_A + tc_tile_b<BN>());
+}
+// Stages of the ring: about 190 KB of operands.
+template <int BN, bool SPLIT> constexpr int tc_stages() { return !SPLIT ? 4 : BN == 256 ? 2 : 3; }
+template <int BN, bool SPLIT> constexpr size_t tc_smem() {
+    return 1024 /* alignment slack */ + tc_stages<BN, SPLIT>() * tc_stage<BN, SPLIT>() + 256 /* barriers, TMEM slot */;
 }
 
-constexpr int TC_MAX_PROBLEMS = 80;  // problems per launch (two tensor maps each; parameters <= 32 KB)
+constexpr int TC_MAX_PROBLEMS = 192;  // problems per launch (kernel parameters <= 32 KB)
+// K per pass of a split product (a multiple of TC_BK): bounds the MMA steps of one accumulator.
+constexpr int64_t TC_SPLIT_CHUNK = 1024;
 
 struct TcProblem {
-    CUtensorMap a_map;           // A_rows: columns [0, K) x rows [0, R), box 64 x 128, 128-byte swizzle
-    CUtensorMap b_map;           // Bt: columns [0, K) x rows [0, n), box 64 x BN, 128-byte swizzle; or
-                                 // (b_mn) B itself: columns [0, n) x rows [0, K), box 64 x 64
-    const int32_t *row_index;    // output row of each A row
+    // Tensor maps in the launch's device table (64-byte aligned):
+    const CUtensorMap *a_map;  // A_rows: columns [0, K) x rows, box 64 x 128, 128-byte swizzle
+    const CUtensorMap *b_map;  // Bt: columns [0, K) x rows [0, n), box 64 x BN; or (b_mn) B itself:
+                               // columns [0, n) x rows, box 64 x 64
+    const int32_t *row_index;  // output row of each A row
     void *C;
     int64_t ldc;
     int32_t R, n, kblocks, c_dtype;
@@ -70,7 +90,15 @@ struct TcProblem {
     void *const *seg_c;
     const int64_t *seg_ldc;
     int32_t nseg;
-    int32_t b_mn;                // B read in place (N-major operand), no transpose
+    int32_t b_mn;              // B read as an N-major operand, no transpose
+    // Split products: A's low halves are rows [a_lo_row, a_lo_row + R) of the A map, B's rows
+    // [b_lo_row, 2 b_lo_row) of the B map; C = acc * row_scale[r] * col_scale[j].
+    int32_t a_lo_row, b_lo_row;
+    const float *row_scale, *col_scale;
+    // First K block of this problem: a long split product runs as K chunks, one per launch, each
+    // accumulating into C (the tensor core's FP32 accumulation truncates, so its error grows with
+    // the K steps of one accumulator; a chunk bounds them).
+    int32_t kb0, pad1;
 };
 
 struct TcParams {
@@ -103,54 +131,15 @@ __device__ __forceinline__ void mbar_arrive_tc(uint32_t bar) {
 __device__ __forceinline__ void tc_expect_tx(uint32_t bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
 }
+// Tensor maps live in global memory, written by a host copy before the launch: make them visible
+// to the tensor-map proxy before the first copy through them.
+__device__ __forceinline__ void tc_map_acquire(const CUtensorMap *map) {
+    asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(reinterpret_cast<uint64_t>(map))
+                 : "memory");
+}
 __device__ __forceinline__ void tc_tma_2d(uint32_t dst, const CUtensorMap *map, int x, int y, uint32_t bar) {
     asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
                  ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar) : "memory");
-}
-
-// The same copy delivered to every CTA of `mask` in the cluster: the data lands at offset dst of each
-// CTA's shared memory and each CTA's barrier at offset bar receives the completed bytes.
-__device__ __forceinline__ void tc_tma_2d_mc(uint32_t dst, const CUtensorMap *map, int x, int y, uint32_t bar,
-                                             uint16_t mask) {
-    asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes.multicast::cluster "
-                 "[%0], [%1, {%2, %3}], [%4], %5;"
-                 ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar), "h"(mask) : "memory");
-}
-__device__ __forceinline__ uint32_t tc_cluster_rank() {
-    uint32_t r;
-    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
-    return r;
-}
-__device__ __forceinline__ uint32_t tc_cluster_id() {
-    uint32_t r;
-    asm volatile("mov.u32 %0, %%clusterid.x;" : "=r"(r));
-    return r;
-}
-__device__ __forceinline__ uint32_t tc_cluster_count() {
-    uint32_t r;
-    asm volatile("mov.u32 %0, %%nclusterid.x;" : "=r"(r));
-    return r;
-}
-// All threads of all CTAs of the cluster (every thread reaches it once, right after the set-up).
-__device__ __forceinline__ void tc_cluster_sync() {
-    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
-}
-// Arrive on the barrier at offset bar of CTA `cta` of the cluster.
-__device__ __forceinline__ void tc_remote_arrive(uint32_t bar, uint32_t cta) {
-    uint32_t r;
-    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(bar), "r"(cta));
-    asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(r) : "memory");
-}
-__device__ __forceinline__ bool tc_wait_cluster(uint32_t bar, uint32_t phase, int *status, int code) {
-    for (uint32_t it = 0; it < (1u << 22); ++it) {
-        uint32_t ok;
-        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
-                     "selp.u32 %0, 1, 0, p;\n\t}"
-                     : "=r"(ok) : "r"(bar), "r"(phase) : "memory");
-        if (ok) return true;
-    }
-    if (status) atomicCAS(status, 0, code);
-    return false;
 }
 
 // Shared-memory matrix descriptor of a K-major operand tile stored with the 128-byte swizzle: rows of
@@ -178,9 +167,10 @@ __device__ __forceinline__ uint64_t tc_desc_mn(uint32_t saddr) {
     return d;
 }
 
-// Instruction descriptor of kind::f16: D FP32, A and B BF16, both K-major, M x N.
-__host__ __device__ constexpr uint32_t tc_idesc(int M, int N) {
-    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+// Instruction descriptor of kind::f16: D FP32, A and B BF16 (bf16) or FP16, both K-major, M x N.
+__host__ __device__ constexpr uint32_t tc_idesc(int M, int N, bool bf16 = true) {
+    return (1u << 4) | ((bf16 ? 1u : 0u) << 7) | ((bf16 ? 1u : 0u) << 10) | ((uint32_t)(N >> 3) << 17) |
+           ((uint32_t)(M >> 4) << 24);
 }
 
 __device__ __forceinline__ void tc_mma(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc) {
@@ -190,11 +180,6 @@ __device__ __forceinline__ void tc_mma(uint32_t tmem_d, uint64_t adesc, uint64_t
 }
 __device__ __forceinline__ void tc_commit(uint32_t bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
-}
-// The same arrival on the barrier at offset bar of every CTA of `mask` in the cluster.
-__device__ __forceinline__ void tc_commit_mc(uint32_t bar, uint16_t mask) {
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;"
-                 ::"r"(bar), "h"(mask) : "memory");
 }
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
@@ -226,13 +211,14 @@ __device__ __forceinline__ int tc_problem_of(const TcParams &p, int t) {
 // Epilogue of one output tile by one warp: TMEM lanes 32 * quarter .. + 31 (tile rows) of the
 // accumulator at TMEM address tacc (lane 0, its first column); load_c / ReLU; store through the
 // row index (and segments).
-template <int BN>
+template <int BN, bool SPLIT>
 __device__ __forceinline__ void tc_store_tile(const TcProblem &q, int m0, int n0, int quarter, int lane, uint32_t tacc,
                                               bool ok) {
     constexpr int TC_BN = BN;
     const int r = m0 + 32 * quarter + lane;
     const bool row_ok = ok && r < q.R;
     const int64_t orow = row_ok ? q.row_index[r] : 0;
+    const float rs = (SPLIT && row_ok) ? q.row_scale[r] : 1.0f;
     const uint32_t tmem = tacc;
     const int warp = quarter;
     // vector stores need 16-byte (F32) / 8-byte (BF16) aligned row starts of C
@@ -253,6 +239,14 @@ __device__ __forceinline__ void tc_store_tile(const TcProblem &q, int m0, int n0
             float v[16];
             tc_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c, v);  // every lane takes part
             if (!row_ok) continue;
+            if constexpr (SPLIT) {
+                // undo the scales: (acc * 2^-s_row) * 2^-s_col, each factor exact
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    const int col = n0 + c + j;
+                    v[j] = (v[j] * rs) * (col < q.n ? __ldg(q.col_scale + col) : 0.0f);
+                }
+            }
             if (q.nseg <= 1 && vec_ok && n0 + c + 16 <= q.n) {
                 // whole 16-column chunk of one output: 16-byte (F32) / 8-byte (BF16) stores
                 if (q.c_dtype == SPREG_F32) {
@@ -322,49 +316,38 @@ __device__ __forceinline__ void tc_store_tile(const TcProblem &q, int m0, int n0
     }
 }
 
-// Persistent.  The scheduling unit is CL output tiles stacked along the rows: (row block pair (CL = 2)
-// or row block, column block).  Cluster c (a single CTA when CL = 1) takes units c, c + clusters, ...;
-// CTA `rank` of the cluster computes row block CL * pair + rank of each unit.  Warp 0 (lane 0) loads
-// the operand tiles of every K block of those tiles into the stage ring; warp 1 (lane 0) issues the
-// MMAs of tile j into TMEM accumulator j % 2 (2 x BN columns) and commits "acc full"; warps 2..5 read
-// an accumulator (warp w reads TMEM lane quarter w % 4), store the tile and arrive on "acc empty", so
+// Persistent.  CTA b takes output tiles b, b + gridDim.x, ...  Warp 0 (lane 0) loads the operand
+// tiles of every K block of those tiles into the stage ring; warp 1 (lane 0) issues the MMAs of tile j
+// into TMEM accumulator j % 2 (2 x BN columns) and commits "acc full"; warps 2..5 read an
+// accumulator (warp w reads TMEM lane quarter w % 4), store the tile and arrive on "acc empty", so
 // the next tile's MMAs overlap this tile's stores.
 //
-// CL = 2: both CTAs of a unit need the same B tile.  Each producer loads its own A tile and one half
-// of B, multicast into both CTAs at the same shared-memory offset, so a B tile leaves L2 once per
-// pair (64 KB per K block and pair instead of 96 KB).  A stage is free for refilling once the MMAs
-// of both CTAs have read it: every MMA issuer commits to the "empty" barrier of both CTAs (2 arrivals
-// a phase).  Before a CTA exits, its producer waits until the peer's last commits have reached this
-// CTA, then both producers exchange an arrival on a "done" barrier, so that no CTA leaves while the
-// other still signals into its shared memory.  Rows past R (the second tile of a pair at an odd row
-// block count) are zero-filled and never stored.
-template <int BN, int CL>
-__global__ void __launch_bounds__(192, 1) tc_rows_kernel(const __grid_constant__ TcParams p, const int total_units) {
-    static_assert(CL == 1 || CL == 2, "clusters of 1 or 2 CTAs");
-    constexpr uint32_t TC_TILE_B = tc_tile_b<BN>(), TC_STAGE = tc_stage<BN>(), TC_TMEM_COLS = 2 * BN;
+// SPLIT: a stage holds [A hi | A lo | B hi | B lo]; per 16-deep K step the issuer runs
+// hi.hi, hi.lo and lo.hi into the same accumulator (FP16 operands).
+template <int BN, bool SPLIT>
+__global__ void __launch_bounds__(192, 1) tc_rows_kernel(const __grid_constant__ TcParams p, const int total_tiles) {
+    constexpr int STAGES = tc_stages<BN, SPLIT>();
+    constexpr uint32_t TC_STAGE = tc_stage<BN, SPLIT>(), TC_TMEM_COLS = 2 * BN;
+    constexpr uint32_t A_BYTES = (SPLIT ? 2u : 1u) * TC_TILE_A;  // B tiles start here
+    constexpr uint32_t B_HALF = tc_tile_b<BN>();                 // B hi -> B lo
     constexpr int TC_BN = BN;
-    constexpr uint16_t PAIR = (uint16_t)((1u << CL) - 1u);  // both CTAs of the cluster
     extern __shared__ unsigned char smem_raw[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t raw = smem_u32(smem_raw);
     const uint32_t sbase = (raw + 1023u) & ~1023u;  // the swizzle atoms need 1024-byte alignment
-    const uint32_t bars = sbase + TC_STAGES * TC_STAGE;
-    const uint32_t full0 = bars, empty0 = bars + 8u * TC_STAGES;
-    const uint32_t accf0 = bars + 16u * TC_STAGES, acce0 = accf0 + 16u;  // acc full / empty, 2 each
-    const uint32_t tmem_slot = acce0 + 16u, done = tmem_slot + 8u;
-    const uint32_t rank = CL > 1 ? tc_cluster_rank() : 0u;
-    const int unit0 = CL > 1 ? (int)tc_cluster_id() : (int)blockIdx.x;
-    const int ustep = CL > 1 ? (int)tc_cluster_count() : (int)gridDim.x;
+    const uint32_t bars = sbase + STAGES * TC_STAGE;
+    const uint32_t full0 = bars, empty0 = bars + 8u * STAGES;
+    const uint32_t accf0 = bars + 16u * STAGES, acce0 = accf0 + 16u;  // acc full / empty, 2 each
+    const uint32_t tmem_slot = acce0 + 16u;
     if (threadIdx.x == 0) {
-        for (int s = 0; s < TC_STAGES; ++s) {
+        for (int s = 0; s < STAGES; ++s) {
             tc_mbar_init(full0 + 8u * s, 1);
-            tc_mbar_init(empty0 + 8u * s, CL);  // the MMA commits of every CTA of the cluster
+            tc_mbar_init(empty0 + 8u * s, 1);
         }
         for (int a = 0; a < 2; ++a) {
             tc_mbar_init(accf0 + 8u * a, 1);
             tc_mbar_init(acce0 + 8u * a, 4);  // the 4 epilogue warps
         }
-        tc_mbar_init(done, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
@@ -373,15 +356,14 @@ __global__ void __launch_bounds__(192, 1) tc_rows_kernel(const __grid_constant__
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     tc_fence_before();
-    if constexpr (CL > 1) tc_cluster_sync();  // the peer's barriers exist before anything signals them
-    else __syncthreads();
+    __syncthreads();
     tc_fence_after();
     uint32_t tmem;
     asm volatile("ld.shared.b32 %0, [%1];" : "=r"(tmem) : "r"(tmem_slot) : "memory");
-    // output tile of unit u of problem q for this CTA
-    auto tile_of = [&](const TcProblem &q, int u, int &m0, int &n0) {
-        const int local = u - q.tile_begin;
-        m0 = ((local / q.tiles_n) * CL + (int)rank) * TC_BM;
+    // output tile t of problem q
+    auto tile_of = [&](const TcProblem &q, int t, int &m0, int &n0) {
+        const int local = t - q.tile_begin;
+        m0 = (local / q.tiles_n) * TC_BM;
         n0 = (local % q.tiles_n) * TC_BN;
     };
 
@@ -390,67 +372,63 @@ __global__ void __launch_bounds__(192, 1) tc_rows_kernel(const __grid_constant__
             // producer: operand tiles of every K block of every tile of this CTA
             int64_t g = 0;  // K blocks issued so far (stage g % STAGES)
             bool ok = true;
-            for (int u = unit0; u < total_units && ok; u += ustep) {
-                const TcProblem &q = p.prob[tc_problem_of(p, u)];
+            int last_q = -1;
+            for (int t = (int)blockIdx.x; t < total_tiles && ok; t += (int)gridDim.x) {
+                const int qi = tc_problem_of(p, t);
+                const TcProblem &q = p.prob[qi];
+                if (qi != last_q) {
+                    tc_map_acquire(q.a_map);
+                    tc_map_acquire(q.b_map);
+                    last_q = qi;
+                }
                 int m0, n0;
-                tile_of(q, u, m0, n0);
+                tile_of(q, t, m0, n0);
                 for (int kb = 0; kb < q.kblocks; ++kb, ++g) {
-                    const int s = (int)(g % TC_STAGES);
-                    if (g >= TC_STAGES &&
-                        !tc_wait(empty0 + 8u * s, (uint32_t)(((g / TC_STAGES) - 1) & 1), p.status, 21)) {
+                    const int s = (int)(g % STAGES);
+                    if (g >= STAGES && !tc_wait(empty0 + 8u * s, (uint32_t)(((g / STAGES) - 1) & 1), p.status, 21)) {
                         ok = false;
                         break;
                     }
                     const uint32_t st = sbase + (uint32_t)s * TC_STAGE;
-                    tc_expect_tx(full0 + 8u * s, TC_STAGE);  // A, and all of B (half of it from the peer)
-                    tc_tma_2d(st, &q.a_map, kb * TC_BK, m0, full0 + 8u * s);
+                    tc_expect_tx(full0 + 8u * s, TC_STAGE);
+                    const int kx = (q.kb0 + kb) * TC_BK;  // K offset of this block
+                    tc_tma_2d(st, q.a_map, kx, m0, full0 + 8u * s);
+                    if constexpr (SPLIT) tc_tma_2d(st + TC_TILE_A, q.a_map, kx, q.a_lo_row + m0, full0 + 8u * s);
                     if (q.b_mn) {
-                        // B in place: BN / 64 copies of 64 columns x 64 K rows, 8 KB apart; this CTA's share
-                        constexpr int PER = TC_BN / 64 / CL;
-                        for (int jb = (int)rank * PER; jb < ((int)rank + 1) * PER; ++jb) {
-                            const uint32_t dst = st + TC_TILE_A + 8192u * jb;
-                            if constexpr (CL > 1)
-                                tc_tma_2d_mc(dst, &q.b_map, n0 + 64 * jb, kb * TC_BK, full0 + 8u * s, PAIR);
-                            else
-                                tc_tma_2d(dst, &q.b_map, n0 + 64 * jb, kb * TC_BK, full0 + 8u * s);
+                        // N-major B: BN / 64 copies of 64 columns x 64 K rows, 8 KB apart
+#pragma unroll
+                        for (int jb = 0; jb < TC_BN / 64; ++jb) {
+                            tc_tma_2d(st + A_BYTES + 8192u * jb, q.b_map, n0 + 64 * jb, kx, full0 + 8u * s);
+                            if constexpr (SPLIT)
+                                tc_tma_2d(st + A_BYTES + B_HALF + 8192u * jb, q.b_map, n0 + 64 * jb, q.b_lo_row + kx,
+                                          full0 + 8u * s);
                         }
-                    } else if constexpr (CL > 1) {
-                        // rows [rank * BN / 2, ...) of the K-major B tile (the map's box is BN / 2 rows)
-                        tc_tma_2d_mc(st + TC_TILE_A + rank * (uint32_t)(TC_BN / 2) * 128u, &q.b_map, kb * TC_BK,
-                                     n0 + (int)rank * (TC_BN / 2), full0 + 8u * s, PAIR);
                     } else {
-                        tc_tma_2d(st + TC_TILE_A, &q.b_map, kb * TC_BK, n0, full0 + 8u * s);
+                        tc_tma_2d(st + A_BYTES, q.b_map, kx, n0, full0 + 8u * s);
                     }
                 }
             }
             // before the CTA can finish, every copy issued has landed
-            const int64_t tail = g - TC_STAGES > 0 ? g - TC_STAGES : 0;
+            const int64_t tail = g - STAGES > 0 ? g - STAGES : 0;
             for (int64_t k = tail; k < g; ++k)
-                tc_wait(full0 + 8u * (uint32_t)(k % TC_STAGES), (uint32_t)((k / TC_STAGES) & 1), p.status, 22);
-            if constexpr (CL > 1) {
-                // the peer's last commits have reached this CTA's empty barriers; then trade "done"
-                for (int64_t k = tail; k < g; ++k)
-                    tc_wait(empty0 + 8u * (uint32_t)(k % TC_STAGES), (uint32_t)((k / TC_STAGES) & 1), p.status, 26);
-                tc_remote_arrive(done, rank ^ 1u);
-                tc_wait_cluster(done, 0, p.status, 27);
-            }
+                tc_wait(full0 + 8u * (uint32_t)(k % STAGES), (uint32_t)((k / STAGES) & 1), p.status, 22);
         }
     } else if (warp == 1) {
         if (lane == 0) {
             // MMA issuer
-            constexpr uint32_t idesc = tc_idesc(TC_BM, TC_BN);
+            constexpr uint32_t idesc = tc_idesc(TC_BM, TC_BN, !SPLIT);
             int64_t g = 0;
             int j = 0;  // this CTA's tile count
             bool ok = true;
-            for (int u = unit0; u < total_units && ok; u += ustep, ++j) {
-                const TcProblem &q = p.prob[tc_problem_of(p, u)];
+            for (int t = (int)blockIdx.x; t < total_tiles && ok; t += (int)gridDim.x, ++j) {
+                const TcProblem &q = p.prob[tc_problem_of(p, t)];
                 const int a = j & 1;
                 if (j >= 2 && !tc_wait(acce0 + 8u * a, (uint32_t)(((j >> 1) - 1) & 1), p.status, 25)) break;
                 tc_fence_after();
                 const uint32_t dacc = tmem + (uint32_t)(a * TC_BN);
                 for (int kb = 0; kb < q.kblocks; ++kb, ++g) {
-                    const int s = (int)(g % TC_STAGES);
-                    if (!tc_wait(full0 + 8u * s, (uint32_t)((g / TC_STAGES) & 1), p.status, 23)) {
+                    const int s = (int)(g % STAGES);
+                    if (!tc_wait(full0 + 8u * s, (uint32_t)((g / STAGES) & 1), p.status, 23)) {
                         ok = false;
                         break;
                     }
@@ -460,18 +438,21 @@ __global__ void __launch_bounds__(192, 1) tc_rows_kernel(const __grid_constant__
                         // N-major B (transpose-B bit of the instruction descriptor); a 16-deep K step is
                         // 16 rows of 128 bytes
 #pragma unroll
-                        for (int k = 0; k < TC_BK / 16; ++k)
-                            tc_mma(dacc, tc_desc(st + 32u * k), tc_desc_mn(st + TC_TILE_A + 2048u * k),
-                                   idesc | (1u << 16), (kb | k) != 0);
+                        for (int k = 0; k < TC_BK / 16; ++k) {
+                            const uint64_t ah = tc_desc(st + 32u * k), bh = tc_desc_mn(st + A_BYTES + 2048u * k);
+                            tc_mma(dacc, ah, bh, idesc | (1u << 16), (kb | k) != 0);
+                            if constexpr (SPLIT) {
+                                tc_mma(dacc, ah, tc_desc_mn(st + A_BYTES + B_HALF + 2048u * k), idesc | (1u << 16), 1);
+                                tc_mma(dacc, tc_desc(st + TC_TILE_A + 32u * k), bh, idesc | (1u << 16), 1);
+                            }
+                        }
                     } else {
 #pragma unroll
                         for (int k = 0; k < TC_BK / 16; ++k)
-                            tc_mma(dacc, tc_desc(st + 32u * k), tc_desc(st + TC_TILE_A + 32u * k), idesc,
+                            tc_mma(dacc, tc_desc(st + 32u * k), tc_desc(st + A_BYTES + 32u * k), idesc,
                                    (kb | k) != 0);
                     }
-                    // the stage is free once these MMAs (and the peer's) have read it
-                    if constexpr (CL > 1) tc_commit_mc(empty0 + 8u * s, PAIR);
-                    else tc_commit(empty0 + 8u * s);
+                    tc_commit(empty0 + 8u * s);  // the stage is free once these MMAs have read it
                 }
                 tc_commit(accf0 + 8u * a);  // accumulator a holds tile j once these MMAs complete
             }
@@ -481,15 +462,15 @@ __global__ void __launch_bounds__(192, 1) tc_rows_kernel(const __grid_constant__
         const int quarter = warp & 3;
         int j = 0;
         bool ok = true;
-        for (int u = unit0; u < total_units; u += ustep, ++j) {
-            const TcProblem &q = p.prob[tc_problem_of(p, u)];
+        for (int t = (int)blockIdx.x; t < total_tiles; t += (int)gridDim.x, ++j) {
+            const TcProblem &q = p.prob[tc_problem_of(p, t)];
             int m0, n0;
-            tile_of(q, u, m0, n0);
+            tile_of(q, t, m0, n0);
             const int a = j & 1;
             ok = ok && __all_sync(0xffffffffu, tc_wait(accf0 + 8u * a, (uint32_t)((j >> 1) & 1), p.status, 24));
             tc_fence_after();
             if (!ok) break;
-            tc_store_tile<BN>(q, m0, n0, quarter, lane, tmem + (uint32_t)(a * TC_BN), ok);  // adds the lane quarter
+            tc_store_tile<BN, SPLIT>(q, m0, n0, quarter, lane, tmem + (uint32_t)(a * TC_BN), ok);  // adds the lane quarter
             tc_fence_before();
             __syncwarp();
             if (lane == 0) mbar_arrive_tc(acce0 + 8u * a);
@@ -500,6 +481,126 @@ __global__ void __launch_bounds__(192, 1) tc_rows_kernel(const __grid_constant__
     if (warp == 0) {
         tc_fence_after();
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_TMEM_COLS) : "memory");
+    }
+}
+
+// FP32 -> (hi, lo) FP16 split with a power-of-two scale.  Exponent s with max * 2^s in [2^14, 2^15)
+// (0 for a zero or non-finite max), clamped to [-126, 126] so that 2^s and 2^-s are normal floats.
+__device__ __forceinline__ int split_exponent(float maxabs) {
+    const uint32_t bits = __float_as_uint(maxabs);
+    const int e = (int)((bits >> 23) & 0xFFu);
+    if (maxabs == 0.0f || e == 0xFF) return 0;
+    const int s = 14 - (e == 0 ? -126 : e - 127);  // max in [2^E, 2^(E+1)) for a normal max
+    return s < -126 ? -126 : s > 126 ? 126 : s;
+}
+__device__ __forceinline__ float pow2f(int s) { return __uint_as_float((uint32_t)(s + 127) << 23); }
+__device__ __forceinline__ void split_half(float x, __half &hi, __half &lo) {
+    hi = __float2half_rn(x);
+    lo = __float2half_rn(x - __half2float(hi));  // x - hi is exact in FP32
+}
+
+// A rows of a split product: row i of a (FP32, lda) -> out row i (high halves) and out row rows + i
+// (low halves), FP16, columns [k, ld_out) zero; inv_scale[i] = 2^-s of the row's scale.  One CTA per row.
+__global__ void __launch_bounds__(256) split_rows_kernel(const float *__restrict__ a, int64_t lda, int64_t rows,
+                                                          int64_t k, __half *__restrict__ out, int64_t ld_out,
+                                                          float *__restrict__ inv_scale) {
+    const int64_t i = blockIdx.x;
+    const float *ar = a + i * lda;
+    float m = 0.0f;
+    for (int64_t c = threadIdx.x; c < k; c += 256) m = fmaxf(m, fabsf(ar[c]));
+    __shared__ float red[8];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    __syncthreads();
+    m = red[0];
+#pragma unroll
+    for (int w = 1; w < 8; ++w) m = fmaxf(m, red[w]);
+    const int s = split_exponent(m);
+    const float sc = pow2f(s);
+    if (threadIdx.x == 0) inv_scale[i] = pow2f(-s);
+    __half *hi = out + i * ld_out, *lo = out + (rows + i) * ld_out;
+    for (int64_t c = threadIdx.x; c < ld_out; c += 256) {
+        __half h = __float2half_rn(0.0f), l = h;
+        if (c < k) split_half(ar[c] * sc, h, l);
+        hi[c] = h;
+        lo[c] = l;
+    }
+}
+
+// B of one split product (or one segment of coalesced products): FP32 k x n (row stride ldb) ->
+// FP16 high halves at hi[r * ld + j] for r < k64 and low halves at hi[lo_off + r * ld + j], rows
+// [k, k64) zero; inv_scale[j] = 2^-s of column j's scale.
+struct SplitBItem {
+    const float *b;
+    int64_t ldb;
+    __half *hi;
+    int64_t ld, lo_off;
+    float *inv_scale;
+    int32_t k, n, k64, pad;
+};
+
+// One CTA per (64-column chunk, item): lane l of each warp takes columns 2l and 2l + 1 of the chunk,
+// the 8 warps interleave the rows; a column's maximum over k, then the split.
+__global__ void __launch_bounds__(256) split_cols_kernel(const SplitBItem *__restrict__ items) {
+    const SplitBItem it = items[blockIdx.y];
+    const int j0 = blockIdx.x * 64;
+    if (j0 >= it.n) return;  // uniform per block
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int j = j0 + 2 * lane;
+    const bool c0 = j < it.n, c1 = j + 1 < it.n;
+    const bool vec = ((reinterpret_cast<uintptr_t>(it.b) | (uintptr_t)(it.ldb * 4)) % 8) == 0;
+    auto load2 = [&](int r, float &x0, float &x1) {
+        const float *row = it.b + (int64_t)r * it.ldb;
+        if (vec && c1) {
+            const float2 v = *reinterpret_cast<const float2 *>(row + j);
+            x0 = v.x;
+            x1 = v.y;
+        } else {
+            x0 = c0 ? row[j] : 0.0f;
+            x1 = c1 ? row[j + 1] : 0.0f;
+        }
+    };
+    float m0 = 0.0f, m1 = 0.0f;
+    for (int r = w; r < it.k; r += 8) {
+        float x0, x1;
+        load2(r, x0, x1);
+        m0 = fmaxf(m0, fabsf(x0));
+        m1 = fmaxf(m1, fabsf(x1));
+    }
+    __shared__ float red[8][64];
+    red[w][2 * lane] = m0;
+    red[w][2 * lane + 1] = m1;
+    __syncthreads();
+    m0 = red[0][2 * lane];
+    m1 = red[0][2 * lane + 1];
+#pragma unroll
+    for (int v = 1; v < 8; ++v) {
+        m0 = fmaxf(m0, red[v][2 * lane]);
+        m1 = fmaxf(m1, red[v][2 * lane + 1]);
+    }
+    // (every warp reduces the same values; red is not written again)
+    const int s0 = split_exponent(m0), s1 = split_exponent(m1);
+    const float sc0 = pow2f(s0), sc1 = pow2f(s1);
+    if (w == 0) {
+        if (c0) it.inv_scale[j] = pow2f(-s0);
+        if (c1) it.inv_scale[j + 1] = pow2f(-s1);
+    }
+    const bool vec_out = ((reinterpret_cast<uintptr_t>(it.hi + j0) | (uintptr_t)(it.ld * 2)) % 4) == 0;
+    for (int r = w; r < it.k64; r += 8) {
+        float x0 = 0.0f, x1 = 0.0f;
+        if (r < it.k) load2(r, x0, x1);
+        __half h0, l0, h1, l1;
+        split_half(x0 * sc0, h0, l0);
+        split_half(x1 * sc1, h1, l1);
+        __half *hp = it.hi + (int64_t)r * it.ld + j, *lp = hp + it.lo_off;
+        if (vec_out && c1) {
+            *reinterpret_cast<__half2 *>(hp) = __halves2half2(h0, h1);
+            *reinterpret_cast<__half2 *>(lp) = __halves2half2(l0, l1);
+        } else {
+            if (c0) { hp[0] = h0; lp[0] = l0; }
+            if (c1) { hp[1] = h1; lp[1] = l1; }
+        }
     }
 }
 
@@ -566,237 +667,282 @@ PFN_cuTensorMapEncodeTiled_v12000 tc_encoder() {
     return fn;
 }
 
-// BF16 matrix of `rows` x `cols` (row stride ld elements) as 64 x box_rows boxes with the 128-byte swizzle.
-int tc_map(CUtensorMap *map, const void *base, int64_t cols, int64_t rows, int64_t ld, int box_rows) {
+// 16-bit matrix of `rows` x `cols` (row stride ld elements) as 64 x box_rows boxes with the 128-byte swizzle.
+int tc_map(CUtensorMap *map, const void *base, int64_t cols, int64_t rows, int64_t ld, int box_rows, bool f16) {
     auto enc = tc_encoder();
     SPREG_CHECK_ARG(enc, "cuTensorMapEncodeTiled is not available from the driver");
     const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
     const cuuint64_t strides[1] = {(cuuint64_t)(ld * 2)};
     const cuuint32_t box[2] = {(cuuint32_t)TC_BK, (cuuint32_t)box_rows};
     const cuuint32_t es[2] = {1, 1};
-    CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), dims, strides, box, es,
-                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    SPREG_CHECK_ARG(r == CUDA_SUCCESS, "cuTensorMapEncodeTiled failed (%d) for a %lld x %lld BF16 operand", (int)r,
+    CUresult r = enc(map, f16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
+                     const_cast<void *>(base), dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                     CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    SPREG_CHECK_ARG(r == CUDA_SUCCESS, "cuTensorMapEncodeTiled failed (%d) for a %lld x %lld 16-bit operand", (int)r,
                     (long long)rows, (long long)cols);
     return SPREG_OK;
 }
 
-// Clusters of the tensor-core launches: 0 = automatic, 1 = single CTAs, 2 = CTA pairs sharing B.
-std::atomic<int> g_tc_cluster{0};
+// One product of either form, as the plan builder sees it.
+struct TcItem {
+    const void *a;         // BF16 rows (rows x lda), or the split pair (2 rows x lda, FP16)
+    int64_t rows, k, lda;
+    const int32_t *row_index;
+    const float *row_scale;  // split: 2^-s per row
+    const void *b;           // BF16 or (split) FP32, k x ldb
+    int64_t ldb;
+    void *c;
+    int64_t ldc, n;
+    int32_t c_dtype, load_c, epilogue, tile_n;
+};
 
-cudaLaunchConfig_t tc_pair_config(cudaLaunchAttribute *attr, size_t smem, cudaStream_t stream) {
-    cudaLaunchConfig_t cfg = {};
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = 2;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.blockDim = dim3(192);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = stream;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    return cfg;
+struct TcGroup {
+    int32_t first;
+    std::vector<int32_t> members;
+    int64_t n = 0;
+    int64_t buf_off = 0;     // Bt (transposed BF16) or the split B pair, in the scratch buffer
+    int64_t scale_off = 0;   // split: column scales
+    int64_t ldn = 0, k64 = 0;  // split: row stride of the B pair, K rounded up to 64
+    int64_t seg_off = 0, seg_c_off = 0, seg_ldc_off = 0;  // segment tables (in the table)
+    bool mn = false;         // B read as an N-major operand
+};
+
+struct TcLaunch {
+    std::unique_ptr<TcParams> p;
+    int bn = 128, tiles = 0;
+};
+
+// Everything one call (or one reusable plan) launches: the B preparation (transpose or split) and
+// the tensor-core launches, with their device table.  Built in two phases: sizes, then -- once the
+// scratch buffer exists -- pointers and tensor maps.
+struct TcPlan {
+    bool split = false;
+    std::vector<TcItem> items;
+    std::vector<TcGroup> groups;
+    int64_t buf_bytes = 0, tab_base = 0, scratch_bytes = 0;
+    std::vector<unsigned char> tab;
+    int64_t prep_off = 0;                 // transpose / split items in the table
+    int32_t nprep = 0;
+    int64_t max_kt = 1, max_nt = 1;       // transpose grid
+    int64_t max_ct = 1;                   // split grid: 64-column chunks
+    int64_t maps_off = 0;                 // 2 tensor maps per group
+    std::vector<TcLaunch> launches;
+    char *scratch = nullptr;
+    int sms = 148;
+};
+
+int64_t tab_put(std::vector<unsigned char> &tab, const void *src, size_t len, size_t align = 8) {
+    const size_t at = (tab.size() + align - 1) / align * align;
+    tab.resize(at + (len + 7) / 8 * 8);
+    if (src) memcpy(tab.data() + at, src, len);
+    return (int64_t)at;
 }
 
-// CTA pairs of tc_rows_kernel<BN, 2> that fit on device `dev` at once (a GPC's SMs may not all pair
-// up; an SM-limited context may fit none): queried once per device, 0 when none fit.
-template <int BN> int tc_max_pairs(int dev, int sms) {
-    static std::atomic<int> max_pairs[64];  // per device: 0 = not queried, -1 = none fit
-    if (dev < 0 || dev >= 64) return 0;
-    int mc = max_pairs[dev].load();
-    if (mc == 0) {
-        cudaLaunchAttribute attr[1];
-        cudaLaunchConfig_t cfg = tc_pair_config(attr, tc_smem<BN>(), nullptr);
-        cfg.gridDim = dim3((unsigned)(2 * (sms / 2 > 0 ? sms / 2 : 1)));
-        if (cudaOccupancyMaxActiveClusters(&mc, tc_rows_kernel<BN, 2>, &cfg) != cudaSuccess || mc <= 0) {
-            cudaGetLastError();  // a refused query leaves no error behind
-            mc = -1;
-        }
-        max_pairs[dev].store(mc);
+int tc_device_setup(int *sms_out) {
+    static std::atomic<bool> configured[64];  // per device
+    static std::atomic<int> sms_of[64];       // per device, 0 until queried
+    int dev = 0;
+    SPREG_CUDA(cudaGetDevice(&dev));
+    if (dev >= 0 && dev < 64 && !configured[dev].load()) {
+        SPREG_CUDA(cudaFuncSetAttribute(tc_rows_kernel<128, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)tc_smem<128, false>()));
+        SPREG_CUDA(cudaFuncSetAttribute(tc_rows_kernel<256, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)tc_smem<256, false>()));
+        SPREG_CUDA(cudaFuncSetAttribute(tc_rows_kernel<128, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)tc_smem<128, true>()));
+        SPREG_CUDA(cudaFuncSetAttribute(tc_rows_kernel<256, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)tc_smem<256, true>()));
+        configured[dev].store(true);
     }
-    return mc > 0 ? mc : 0;
-}
-
-template <int BN, int CL>
-cudaError_t tc_launch(const TcParams &p, int units, int sms, int pairs_fit, size_t smem, cudaStream_t stream) {
-    if constexpr (CL == 1) {
-        tc_rows_kernel<BN, 1><<<(unsigned)std::min(units, sms), 192, smem, stream>>>(p, units);
-        return cudaGetLastError();
-    } else {
-        // as many clusters as fit at once, at most one per unit
-        cudaLaunchAttribute attr[1];
-        cudaLaunchConfig_t cfg = tc_pair_config(attr, smem, stream);
-        cfg.gridDim = dim3((unsigned)(2 * std::min(units, pairs_fit)));
-        return cudaLaunchKernelEx(&cfg, tc_rows_kernel<BN, 2>, p, units);
+    if (dev >= 0 && dev < 64 && !sms_of[dev].load()) {
+        int v = 0;
+        SPREG_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev));
+        sms_of[dev].store(v);
     }
+    *sms_out = (dev >= 0 && dev < 64 && sms_of[dev].load() > 0) ? sms_of[dev].load() : 148;
+    return SPREG_OK;
 }
 
-}  // namespace
-
-void tc_set_cluster(int mode) { g_tc_cluster.store(mode); }
-
-int dense_rows_batched_impl(const spreg_dense_rows_item *items, int32_t count, cudaStream_t stream) {
-    SPREG_CHECK_ARG(count >= 0 && (count == 0 || items), "bad item list");
-    int st = SPREG_OK;
-    // checks; products with the same A, row index, output type and epilogue become one problem
-    struct Group {
-        const spreg_dense_rows_item *first;
-        std::vector<int32_t> members;
-        int64_t n = 0, bt_off = 0, tab_off = 0;
-        bool mn = false;  // one product whose B is read in place (16-byte aligned rows): no transpose
-    };
-    std::vector<Group> groups;
+// Phase 1: checks, groups of coalesced products, scratch and table sizes.
+int tc_plan_build(TcPlan &pl) {
+    const bool split = pl.split;
     std::map<std::tuple<const void *, int64_t, int64_t, int64_t, const void *, int32_t, int32_t, int32_t>, size_t> key;
-    for (int32_t i = 0; i < count; ++i) {
-        const spreg_dense_rows_item &it = items[i];
+    for (int32_t i = 0; i < (int32_t)pl.items.size(); ++i) {
+        const TcItem &it = pl.items[i];
         SPREG_CHECK_ARG(it.rows >= 0 && it.k >= 0 && it.n >= 0, "item %d: negative size", i);
         if (it.rows == 0 || it.n == 0) continue;
-        SPREG_CHECK_ARG(it.a_rows && it.row_index && it.c && it.b, "item %d: null pointer", i);
-        SPREG_CHECK_ARG(it.rows <= INT32_MAX && it.k <= INT32_MAX && it.n <= INT32_MAX, "item %d: size out of range", i);
-        SPREG_CHECK_ARG(it.c_dtype == SPREG_F32 || it.c_dtype == SPREG_BF16, "item %d: C must be F32 or BF16", i);
+        SPREG_CHECK_ARG(it.a && it.row_index && it.c && it.b && (!split || it.row_scale), "item %d: null pointer", i);
+        SPREG_CHECK_ARG(it.rows <= INT32_MAX / 2 && it.k <= INT32_MAX / 2 && it.n <= INT32_MAX, "item %d: size out of range",
+                        i);
+        SPREG_CHECK_ARG(it.c_dtype == SPREG_F32 || (!split && it.c_dtype == SPREG_BF16),
+                        split ? "item %d: C must be F32" : "item %d: C must be F32 or BF16", i);
         SPREG_CHECK_ARG(it.epilogue == SPREG_EPILOGUE_NONE || it.epilogue == SPREG_EPILOGUE_RELU, "item %d: bad epilogue",
                         i);
-        SPREG_CHECK_ARG(it.lda >= it.k && (it.lda * 2) % 16 == 0 && reinterpret_cast<uintptr_t>(it.a_rows) % 16 == 0,
+        SPREG_CHECK_ARG(it.lda >= it.k && (it.lda * 2) % 16 == 0 && reinterpret_cast<uintptr_t>(it.a) % 16 == 0,
                         "A rows must be 16-byte aligned with a row stride of a multiple of 8 elements (item %d, lda "
                         "%lld)", i, (long long)it.lda);
         SPREG_CHECK_ARG(it.ldb >= it.n && it.ldc >= it.n, "item %d: ldb / ldc smaller than n", i);
         SPREG_CHECK_ARG(it.k > 0, "item %d: K must be positive", i);
         SPREG_CHECK_ARG(it.tile_n == 0 || it.tile_n == 128 || it.tile_n == 256, "item %d: tile_n must be 0, 128 or 256",
                         i);
-        auto kk = std::make_tuple(it.a_rows, it.rows, it.k, it.lda, (const void *)it.row_index, it.c_dtype,
+        auto kk = std::make_tuple(it.a, it.rows, it.k, it.lda, (const void *)it.row_index, it.c_dtype,
                                   it.load_c ? 1 : 0, it.epilogue);
         auto f = key.find(kk);
         if (f == key.end()) {
-            key.emplace(kk, groups.size());
-            groups.push_back(Group{&it, {i}, it.n});
+            key.emplace(kk, pl.groups.size());
+            TcGroup g;
+            g.first = i;
+            g.members.push_back(i);
+            g.n = it.n;
+            pl.groups.push_back(std::move(g));
         } else {
-            Group &g = groups[f->second];
+            TcGroup &g = pl.groups[f->second];
             g.members.push_back(i);
             g.n += it.n;
         }
     }
-    if (groups.empty()) return SPREG_OK;
-    // scratch: each transposed problem's Bt (n x K8, 256-byte aligned), then the segment tables
+    // scratch: each group's Bt (n x K8) or split B pair (2 x K64 x ldn FP16) + column scales
     int64_t bytes = 0;
-    for (Group &g : groups) {
+    for (TcGroup &g : pl.groups) {
         SPREG_CHECK_ARG(g.n <= INT32_MAX, "coalesced products wider than 2^31 columns");
-        const spreg_dense_rows_item &f = *g.first;
+        const TcItem &f = pl.items[g.first];
+        if (split) {
+            g.mn = true;
+            g.k64 = (f.k + TC_BK - 1) / TC_BK * TC_BK;
+            g.ldn = (g.n + 7) / 8 * 8;
+            g.buf_off = bytes;
+            bytes += (2 * g.k64 * g.ldn * 2 + 255) / 256 * 256;
+            g.scale_off = bytes;
+            bytes += (g.n * 4 + 255) / 256 * 256;
+            continue;
+        }
         g.mn = g.members.size() == 1 && reinterpret_cast<uintptr_t>(f.b) % 16 == 0 && (f.ldb * 2) % 16 == 0;
         if (g.mn) continue;
         const int64_t K8 = (f.k + 7) / 8 * 8;
-        g.bt_off = bytes;
+        g.buf_off = bytes;
         bytes += (g.n * K8 * 2 + 255) / 256 * 256;
     }
-    std::vector<unsigned char> tab;
-    auto put = [&](const void *src, size_t len) {
-        const size_t at = tab.size();
-        tab.resize(at + (len + 7) / 8 * 8);
-        memcpy(tab.data() + at, src, len);
-        return (int64_t)at;
-    };
-    std::vector<int64_t> seg_c_off(groups.size(), 0), seg_ldc_off(groups.size(), 0);
-    for (size_t gi = 0; gi < groups.size(); ++gi) {
-        Group &g = groups[gi];
+    pl.buf_bytes = bytes;
+    // table: tensor maps, segment tables, preparation items (pointers filled in phase 2)
+    pl.tab.clear();
+    pl.maps_off = tab_put(pl.tab, nullptr, 2 * sizeof(CUtensorMap) * pl.groups.size(), 128);
+    for (TcGroup &g : pl.groups) {
         if (g.members.size() < 2) continue;
         std::vector<int32_t> starts;
-        std::vector<uint64_t> cs;
-        std::vector<int64_t> lds;
         int32_t o = 0;
         for (int32_t m : g.members) {
             starts.push_back(o);
-            o += (int32_t)items[m].n;
-            cs.push_back(reinterpret_cast<uint64_t>(items[m].c));
-            lds.push_back(items[m].ldc);
+            o += (int32_t)pl.items[m].n;
         }
         starts.push_back(o);
-        g.tab_off = put(starts.data(), starts.size() * 4);
-        seg_c_off[gi] = put(cs.data(), cs.size() * 8);
-        seg_ldc_off[gi] = put(lds.data(), lds.size() * 8);
+        g.seg_off = tab_put(pl.tab, starts.data(), starts.size() * 4);
+        g.seg_c_off = tab_put(pl.tab, nullptr, g.members.size() * 8);
+        g.seg_ldc_off = tab_put(pl.tab, nullptr, g.members.size() * 8);
     }
-    // transpose items (every member of every group), after the segment tables
-    std::vector<TransposeItem> titems;
-    int64_t max_kt = 1, max_nt = 1;
-    for (Group &g : groups) {
-        if (g.mn) continue;
-        const int64_t K8 = (g.first->k + 7) / 8 * 8;
-        int64_t o = 0;
+    pl.nprep = 0;
+    for (const TcGroup &g : pl.groups) {
+        if (g.mn && !split) continue;
         for (int32_t m : g.members) {
-            const spreg_dense_rows_item &it = items[m];
-            TransposeItem ti;
-            ti.b = static_cast<const __nv_bfloat16 *>(it.b);
-            ti.dst = nullptr;  // set once the scratch base is known
-            ti.ldb = it.ldb;
-            ti.k = (int32_t)it.k;
-            ti.n = (int32_t)it.n;
-            ti.K8 = (int32_t)K8;
-            ti.pad = 0;
-            titems.push_back(ti);
-            max_kt = std::max<int64_t>(max_kt, (K8 + 63) / 64);
-            max_nt = std::max<int64_t>(max_nt, (it.n + 63) / 64);
-            o += it.n;
-        }
-    }
-    SPREG_CHECK_ARG(titems.size() <= 65535 && max_nt <= 65535, "too many products in one call");
-    const int64_t titem_off = put(titems.data(), titems.size() * sizeof(TransposeItem));  // dst filled in below
-    const int64_t tab_base = (bytes + 255) / 256 * 256;
-    int *status = device_status_word(&st);
-    if (st != SPREG_OK) return st;
-    static std::atomic<bool> configured[64];  // per device
-    int dev = 0;
-    SPREG_CUDA(cudaGetDevice(&dev));
-    if (dev >= 0 && dev < 64 && !configured[dev].load()) {
-        SPREG_CUDA(cudaFuncSetAttribute(tc_rows_kernel<128, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)tc_smem<128>()));
-        SPREG_CUDA(cudaFuncSetAttribute(tc_rows_kernel<256, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)tc_smem<256>()));
-        SPREG_CUDA(cudaFuncSetAttribute(tc_rows_kernel<128, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)tc_smem<128>()));
-        SPREG_CUDA(cudaFuncSetAttribute(tc_rows_kernel<256, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)tc_smem<256>()));
-        configured[dev].store(true);
-    }
-    static std::atomic<int> sms_of[64];  // per device, 0 until queried
-    if (dev >= 0 && dev < 64 && !sms_of[dev].load()) {
-        int v = 0;
-        SPREG_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev));
-        sms_of[dev].store(v);
-    }
-    const int sms = (dev >= 0 && dev < 64 && sms_of[dev].load() > 0) ? sms_of[dev].load() : 148;
-    char *scratch = nullptr;
-    SPREG_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&scratch), (size_t)(tab_base + (int64_t)tab.size() + 16),
-                               stream));
-    auto fail = [&](int code) {
-        cudaFreeAsync(scratch, stream);
-        return code;
-    };
-    // B of every product, transposed into its problem's Bt at its segment's row offset: one launch
-    {
-        size_t t = 0;
-        for (Group &g : groups) {
-            if (g.mn) continue;
-            const int64_t K8 = (g.first->k + 7) / 8 * 8;
-            int64_t o = 0;
-            for (int32_t m : g.members) {
-                titems[t++].dst = reinterpret_cast<__nv_bfloat16 *>(scratch + g.bt_off) + o * K8;
-                o += items[m].n;
+            ++pl.nprep;
+            const TcItem &it = pl.items[m];
+            if (split) {
+                pl.max_ct = std::max<int64_t>(pl.max_ct, (it.n + 63) / 64);
+            } else {
+                pl.max_kt = std::max<int64_t>(pl.max_kt, ((it.k + 7) / 8 * 8 + 63) / 64);
+                pl.max_nt = std::max<int64_t>(pl.max_nt, (it.n + 63) / 64);
             }
         }
     }
-    memcpy(tab.data() + titem_off, titems.data(), titems.size() * sizeof(TransposeItem));
-    cudaError_t e = cudaMemcpyAsync(scratch + tab_base, tab.data(), tab.size(), cudaMemcpyHostToDevice, stream);
-    if (e == cudaSuccess && !titems.empty()) {
-        transpose_items_kernel<<<dim3((unsigned)max_kt, (unsigned)max_nt, (unsigned)titems.size()), 256, 0,
-                                 stream>>>(reinterpret_cast<const TransposeItem *>(scratch + tab_base + titem_off));
-        e = cudaGetLastError();
+    SPREG_CHECK_ARG(pl.nprep <= 65535 && pl.max_nt <= 65535 && pl.max_ct <= INT32_MAX, "too many products in one call");
+    pl.prep_off = tab_put(pl.tab, nullptr, (size_t)pl.nprep * (split ? sizeof(SplitBItem) : sizeof(TransposeItem)));
+    pl.tab_base = (pl.buf_bytes + 255) / 256 * 256;
+    pl.scratch_bytes = pl.tab_base + (int64_t)pl.tab.size() + 16;
+    return SPREG_OK;
+}
+
+// Phase 2 (scratch allocated): preparation items, segment tables, tensor maps, launch parameters.
+int tc_plan_fill(TcPlan &pl, int *status) {
+    const bool split = pl.split;
+    char *const scratch = pl.scratch;
+    char *const tabd = scratch + pl.tab_base;
+    int st = SPREG_OK;
+    // preparation items and segment tables
+    {
+        int32_t t = 0;
+        for (TcGroup &g : pl.groups) {
+            if (g.members.size() > 1) {
+                std::vector<uint64_t> cs;
+                std::vector<int64_t> lds;
+                for (int32_t m : g.members) {
+                    cs.push_back(reinterpret_cast<uint64_t>(pl.items[m].c));
+                    lds.push_back(pl.items[m].ldc);
+                }
+                memcpy(pl.tab.data() + g.seg_c_off, cs.data(), cs.size() * 8);
+                memcpy(pl.tab.data() + g.seg_ldc_off, lds.data(), lds.size() * 8);
+            }
+            if (g.mn && !split) continue;
+            int64_t o = 0;  // column offset of the member in its group
+            for (int32_t m : g.members) {
+                const TcItem &it = pl.items[m];
+                if (split) {
+                    SplitBItem si;
+                    si.b = static_cast<const float *>(it.b);
+                    si.ldb = it.ldb;
+                    si.hi = reinterpret_cast<__half *>(scratch + g.buf_off) + o;
+                    si.ld = g.ldn;
+                    si.lo_off = g.k64 * g.ldn;
+                    si.inv_scale = reinterpret_cast<float *>(scratch + g.scale_off) + o;
+                    si.k = (int32_t)it.k;
+                    si.n = (int32_t)it.n;
+                    si.k64 = (int32_t)g.k64;
+                    si.pad = 0;
+                    memcpy(pl.tab.data() + pl.prep_off + sizeof(SplitBItem) * t, &si, sizeof si);
+                } else {
+                    const int64_t K8 = (pl.items[g.first].k + 7) / 8 * 8;
+                    TransposeItem ti;
+                    ti.b = static_cast<const __nv_bfloat16 *>(it.b);
+                    ti.dst = reinterpret_cast<__nv_bfloat16 *>(scratch + g.buf_off) + o * K8;
+                    ti.ldb = it.ldb;
+                    ti.k = (int32_t)it.k;
+                    ti.n = (int32_t)it.n;
+                    ti.K8 = (int32_t)K8;
+                    ti.pad = 0;
+                    memcpy(pl.tab.data() + pl.prep_off + sizeof(TransposeItem) * t, &ti, sizeof ti);
+                }
+                ++t;
+                o += it.n;
+            }
+        }
     }
-    if (e != cudaSuccess) {
-        fail(0);
-        SPREG_FAIL(SPREG_ERR_CUDA, "tensor-core set-up: %s", cudaGetErrorString(e));
+    // tensor maps (device table) and launches of up to TC_MAX_PROBLEMS problems
+    CUtensorMap *maps_h = reinterpret_cast<CUtensorMap *>(pl.tab.data() + pl.maps_off);
+    const CUtensorMap *maps_d = reinterpret_cast<const CUtensorMap *>(tabd + pl.maps_off);
+    pl.launches.clear();
+    // (group, pass) problems: a split product of K > TC_SPLIT_CHUNK runs as passes over K chunks, pass
+    // p in the launches after those of pass p - 1 (each pass adds into C); every other product is one
+    // pass.  The maps of a group serve all its passes.
+    std::vector<std::pair<int, int>> specs;
+    int passes = 1;
+    for (const TcGroup &g : pl.groups)
+        passes = std::max<int>(passes, split ? (int)((pl.items[g.first].k + TC_SPLIT_CHUNK - 1) / TC_SPLIT_CHUNK) : 1);
+    std::vector<size_t> pass_begin;
+    for (int ps = 0; ps < passes; ++ps) {
+        pass_begin.push_back(specs.size());
+        for (size_t gi = 0; gi < pl.groups.size(); ++gi) {
+            const int64_t k = pl.items[pl.groups[gi].first].k;
+            if ((int64_t)ps * (split ? TC_SPLIT_CHUNK : k) < k) specs.emplace_back((int)gi, ps);
+        }
     }
-    static thread_local TcParams p;  // ~31 KB: kept off the stack
-    for (size_t first = 0; first < groups.size(); first += TC_MAX_PROBLEMS) {
-        const size_t cnt = std::min<size_t>(TC_MAX_PROBLEMS, groups.size() - first);
+    pass_begin.push_back(specs.size());
+    std::vector<std::pair<size_t, size_t>> chunks;  // [first, first + cnt) of specs, within one pass
+    for (int ps = 0; ps < passes; ++ps)
+        for (size_t f = pass_begin[ps]; f < pass_begin[ps + 1]; f += TC_MAX_PROBLEMS)
+            chunks.emplace_back(f, std::min<size_t>(TC_MAX_PROBLEMS, pass_begin[ps + 1] - f));
+    for (const auto &ch : chunks) {
+        const size_t first = ch.first, cnt = ch.second;
+        TcLaunch L;
+        L.p.reset(new TcParams);
+        TcParams &p = *L.p;
         memset(&p, 0, sizeof p);
         p.status = status;
         p.nprob = (int32_t)cnt;
@@ -805,75 +951,176 @@ int dense_rows_batched_impl(const spreg_dense_rows_item *items, int32_t count, c
         int64_t min_n = INT64_MAX;
         int hint = 0;
         for (size_t j = 0; j < cnt; ++j) {
-            min_n = std::min<int64_t>(min_n, groups[first + j].n);
-            for (int32_t m : groups[first + j].members)
-                if (!hint && (items[m].tile_n == 128 || items[m].tile_n == 256)) hint = items[m].tile_n;
+            const TcGroup &g = pl.groups[specs[first + j].first];
+            min_n = std::min<int64_t>(min_n, g.n);
+            for (int32_t m : g.members)
+                if (!hint && (pl.items[m].tile_n == 128 || pl.items[m].tile_n == 256)) hint = pl.items[m].tile_n;
         }
         const int bn = hint ? hint : (min_n > 128 ? 256 : 128);
-        // CTA pairs sharing B (cl = 2) when the launch has at least one full wave of pairs and the
-        // padding of odd row block counts costs at most 1/8 of its tiles
-        int64_t tiles1 = 0, pairs = 0;
-        for (size_t j = 0; j < cnt; ++j) {
-            const int64_t tm = (groups[first + j].first->rows + TC_BM - 1) / TC_BM;
-            const int64_t tn = (groups[first + j].n + bn - 1) / bn;
-            tiles1 += tm * tn;
-            pairs += (tm + 1) / 2 * tn;
-        }
-        const int mode = g_tc_cluster.load();
-        const int pairs_fit = mode == 1 ? 0 : bn == 256 ? tc_max_pairs<256>(dev, sms) : tc_max_pairs<128>(dev, sms);
-        if (mode == 2 && pairs_fit == 0) {
-            fail(0);
-            SPREG_FAIL(SPREG_ERR_UNSUPPORTED, "tensor-core CTA pairs: no 2-CTA cluster fits this device or context");
-        }
-        const int cl = mode == 1 || pairs_fit == 0 ? 1
-                       : mode == 2 ? 2
-                                   : (pairs >= sms / 2 && 8 * (2 * pairs - tiles1) <= tiles1 ? 2 : 1);
         int64_t tiles = 0;
         for (size_t j = 0; j < cnt; ++j) {
-            const size_t gi = first + j;
-            const Group &g = groups[gi];
-            const spreg_dense_rows_item &it = *g.first;
+            const size_t gi = (size_t)specs[first + j].first;
+            const int ps = specs[first + j].second;
+            const TcGroup &g = pl.groups[gi];
+            const TcItem &it = pl.items[g.first];
             TcProblem &q = p.prob[j];
-            const int64_t K8 = (it.k + 7) / 8 * 8;
+            q.a_map = maps_d + 2 * gi;
+            q.b_map = maps_d + 2 * gi + 1;
             q.row_index = it.row_index;
             q.C = it.c;
             q.ldc = it.ldc;
             q.R = (int32_t)it.rows;
             q.n = (int32_t)g.n;
-            q.kblocks = (int32_t)((it.k + TC_BK - 1) / TC_BK);
+            const int64_t k0 = split ? (int64_t)ps * TC_SPLIT_CHUNK : 0;
+            const int64_t kc = split ? std::min<int64_t>(TC_SPLIT_CHUNK, it.k - k0) : it.k;
+            const bool last = k0 + kc >= it.k;
+            q.kb0 = (int32_t)(k0 / TC_BK);
+            q.kblocks = (int32_t)((kc + TC_BK - 1) / TC_BK);
             q.c_dtype = it.c_dtype;
-            q.load_c = it.load_c ? 1 : 0;
-            q.epilogue = it.epilogue;
+            q.load_c = (it.load_c || ps > 0) ? 1 : 0;
+            q.epilogue = last ? it.epilogue : SPREG_EPILOGUE_NONE;
             q.nseg = (int32_t)g.members.size();
             if (q.nseg > 1) {
-                q.seg_start = reinterpret_cast<const int32_t *>(scratch + tab_base + g.tab_off);
-                q.seg_c = reinterpret_cast<void *const *>(scratch + tab_base + seg_c_off[gi]);
-                q.seg_ldc = reinterpret_cast<const int64_t *>(scratch + tab_base + seg_ldc_off[gi]);
+                q.seg_start = reinterpret_cast<const int32_t *>(tabd + g.seg_off);
+                q.seg_c = reinterpret_cast<void *const *>(tabd + g.seg_c_off);
+                q.seg_ldc = reinterpret_cast<const int64_t *>(tabd + g.seg_ldc_off);
             }
             q.tiles_n = (int32_t)((g.n + bn - 1) / bn);
-            q.tile_begin = (int32_t)tiles;  // in units of cl row blocks x one column block
-            tiles += ((it.rows + TC_BM - 1) / TC_BM + cl - 1) / cl * q.tiles_n;
+            q.tile_begin = (int32_t)tiles;
+            tiles += (it.rows + TC_BM - 1) / TC_BM * q.tiles_n;
             q.b_mn = g.mn ? 1 : 0;
-            if ((st = tc_map(&q.a_map, it.a_rows, it.k, it.rows, it.lda, TC_BM)) ||
-                (st = g.mn ? tc_map(&q.b_map, it.b, g.n, it.k, it.ldb, 64)
-                           : tc_map(&q.b_map, scratch + g.bt_off, it.k, g.n, K8, bn / cl)))
-                return fail(st);
+            if (ps > 0) {  // later pass of a split product: the maps exist
+                q.a_lo_row = (int32_t)it.rows;
+                q.b_lo_row = (int32_t)g.k64;
+                q.row_scale = it.row_scale;
+                q.col_scale = reinterpret_cast<const float *>(scratch + g.scale_off);
+            } else if (split) {
+                q.a_lo_row = (int32_t)it.rows;
+                q.b_lo_row = (int32_t)g.k64;
+                q.row_scale = it.row_scale;
+                q.col_scale = reinterpret_cast<const float *>(scratch + g.scale_off);
+                if ((st = tc_map(&maps_h[2 * gi], it.a, it.k, 2 * it.rows, it.lda, TC_BM, true)) ||
+                    (st = tc_map(&maps_h[2 * gi + 1], scratch + g.buf_off, g.n, 2 * g.k64, g.ldn, 64, true)))
+                    return st;
+            } else {
+                const int64_t K8 = (it.k + 7) / 8 * 8;
+                if ((st = tc_map(&maps_h[2 * gi], it.a, it.k, it.rows, it.lda, TC_BM, false)) ||
+                    (st = g.mn ? tc_map(&maps_h[2 * gi + 1], it.b, g.n, it.k, it.ldb, 64, false)
+                               : tc_map(&maps_h[2 * gi + 1], scratch + g.buf_off, it.k, g.n, K8, bn, false)))
+                    return st;
+            }
         }
-        if (tiles > INT32_MAX) {
-            fail(0);
-            SPREG_FAIL(SPREG_ERR_UNSUPPORTED, "too many output tiles in one launch");
-        }
-        if (bn == 256) e = cl == 2 ? tc_launch<256, 2>(p, (int)tiles, sms, pairs_fit, tc_smem<256>(), stream)
-                                   : tc_launch<256, 1>(p, (int)tiles, sms, pairs_fit, tc_smem<256>(), stream);
-        else e = cl == 2 ? tc_launch<128, 2>(p, (int)tiles, sms, pairs_fit, tc_smem<128>(), stream)
-                         : tc_launch<128, 1>(p, (int)tiles, sms, pairs_fit, tc_smem<128>(), stream);
-        if (e != cudaSuccess) {
-            fail(0);
-            SPREG_FAIL(SPREG_ERR_CUDA, "tensor-core launch: %s", cudaGetErrorString(e));
-        }
+        SPREG_CHECK_ARG(tiles <= INT32_MAX, "too many output tiles in one launch");
+        L.bn = bn;
+        L.tiles = (int)tiles;
+        pl.launches.push_back(std::move(L));
     }
-    cudaFreeAsync(scratch, stream);
     return SPREG_OK;
+}
+
+// Device table upload (stream-ordered copy of the host image).
+int tc_plan_upload(const TcPlan &pl, cudaStream_t stream) {
+    cudaError_t e = cudaMemcpyAsync(pl.scratch + pl.tab_base, pl.tab.data(), pl.tab.size(), cudaMemcpyHostToDevice, stream);
+    if (e != cudaSuccess) SPREG_FAIL(SPREG_ERR_CUDA, "tensor-core set-up: %s", cudaGetErrorString(e));
+    return SPREG_OK;
+}
+
+template <int BN, bool SPLIT>
+cudaError_t tc_launch(const TcParams &p, int tiles, int sms, cudaStream_t stream) {
+    tc_rows_kernel<BN, SPLIT><<<(unsigned)std::min(tiles, sms), 192, tc_smem<BN, SPLIT>(), stream>>>(p, tiles);
+    return cudaGetLastError();
+}
+
+// The B preparation, then every tensor-core launch.
+int tc_plan_launch(const TcPlan &pl, cudaStream_t stream) {
+    cudaError_t e = cudaSuccess;
+    const char *tabd = pl.scratch + pl.tab_base;
+    if (pl.nprep > 0) {
+        if (pl.split)
+            split_cols_kernel<<<dim3((unsigned)pl.max_ct, (unsigned)pl.nprep), 256, 0, stream>>>(
+                reinterpret_cast<const SplitBItem *>(tabd + pl.prep_off));
+        else
+            transpose_items_kernel<<<dim3((unsigned)pl.max_kt, (unsigned)pl.max_nt, (unsigned)pl.nprep), 256, 0,
+                                     stream>>>(reinterpret_cast<const TransposeItem *>(tabd + pl.prep_off));
+        e = cudaGetLastError();
+    }
+    for (size_t i = 0; i < pl.launches.size() && e == cudaSuccess; ++i) {
+        const TcLaunch &L = pl.launches[i];
+        if (L.tiles == 0) continue;
+        if (pl.split)
+            e = L.bn == 256 ? tc_launch<256, true>(*L.p, L.tiles, pl.sms, stream)
+                            : tc_launch<128, true>(*L.p, L.tiles, pl.sms, stream);
+        else
+            e = L.bn == 256 ? tc_launch<256, false>(*L.p, L.tiles, pl.sms, stream)
+                            : tc_launch<128, false>(*L.p, L.tiles, pl.sms, stream);
+    }
+    if (e != cudaSuccess) SPREG_FAIL(SPREG_ERR_CUDA, "tensor-core launch: %s", cudaGetErrorString(e));
+    return SPREG_OK;
+}
+
+// One call: plan, stream-ordered scratch, upload, launch, stream-ordered free.
+int tc_run_once(TcPlan &pl, cudaStream_t stream) {
+    int st = tc_plan_build(pl);
+    if (st) return st;
+    if (pl.groups.empty()) return SPREG_OK;
+    int *status = device_status_word(&st);
+    if (st) return st;
+    if ((st = tc_device_setup(&pl.sms))) return st;
+    SPREG_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&pl.scratch), (size_t)pl.scratch_bytes, stream));
+    if (!(st = tc_plan_fill(pl, status)) && !(st = tc_plan_upload(pl, stream))) st = tc_plan_launch(pl, stream);
+    cudaFreeAsync(pl.scratch, stream);
+    pl.scratch = nullptr;
+    return st;
+}
+
+TcItem from_bf16(const spreg_dense_rows_item &it) {
+    TcItem t;
+    t.a = it.a_rows;
+    t.rows = it.rows;
+    t.k = it.k;
+    t.lda = it.lda;
+    t.row_index = it.row_index;
+    t.row_scale = nullptr;
+    t.b = it.b;
+    t.ldb = it.ldb;
+    t.c = it.c;
+    t.ldc = it.ldc;
+    t.n = it.n;
+    t.c_dtype = it.c_dtype;
+    t.load_c = it.load_c;
+    t.epilogue = it.epilogue;
+    t.tile_n = it.tile_n;
+    return t;
+}
+
+TcItem from_f32(const spreg_dense_rows_f32_item &it) {
+    TcItem t;
+    t.a = it.a_split;
+    t.rows = it.rows;
+    t.k = it.k;
+    t.lda = it.ld_split;
+    t.row_index = it.row_index;
+    t.row_scale = it.row_scale;
+    t.b = it.b;
+    t.ldb = it.ldb;
+    t.c = it.c;
+    t.ldc = it.ldc;
+    t.n = it.n;
+    t.c_dtype = SPREG_F32;
+    t.load_c = it.load_c;
+    t.epilogue = it.epilogue;
+    t.tile_n = it.tile_n;
+    return t;
+}
+
+}  // namespace
+
+int dense_rows_batched_impl(const spreg_dense_rows_item *items, int32_t count, cudaStream_t stream) {
+    SPREG_CHECK_ARG(count >= 0 && (count == 0 || items), "bad item list");
+    TcPlan pl;
+    pl.split = false;
+    for (int32_t i = 0; i < count; ++i) pl.items.push_back(from_bf16(items[i]));
+    return tc_run_once(pl, stream);
 }
 
 int dense_rows_bf16_impl(const void *a_rows, int64_t R, int64_t K, int64_t lda, const int32_t *row_index,
@@ -881,6 +1128,90 @@ int dense_rows_bf16_impl(const void *a_rows, int64_t R, int64_t K, int64_t lda, 
                          int32_t epilogue, cudaStream_t stream) {
     const spreg_dense_rows_item it = {a_rows, R, K, lda, row_index, b, ldb, c, ldc, n, c_dtype, load_c, epilogue, 0};
     return dense_rows_batched_impl(&it, 1, stream);
+}
+
+int dense_rows_f32_batched_impl(const spreg_dense_rows_f32_item *items, int32_t count, cudaStream_t stream) {
+    SPREG_CHECK_ARG(count >= 0 && (count == 0 || items), "bad item list");
+    TcPlan pl;
+    pl.split = true;
+    for (int32_t i = 0; i < count; ++i) pl.items.push_back(from_f32(items[i]));
+    return tc_run_once(pl, stream);
+}
+
+int split_rows_f32_impl(const float *a_rows, int64_t rows, int64_t k, int64_t lda, void *a_split, int64_t ld_split,
+                        float *row_scale, cudaStream_t stream) {
+    SPREG_CHECK_ARG(rows >= 0 && k >= 0, "negative size");
+    if (rows == 0) return SPREG_OK;
+    SPREG_CHECK_ARG(a_rows && a_split && row_scale, "null pointer");
+    SPREG_CHECK_ARG(lda >= k && ld_split >= k && ld_split % 8 == 0 && reinterpret_cast<uintptr_t>(a_split) % 16 == 0,
+                    "the split pair needs a 16-byte aligned base and a row stride of a multiple of 8 elements >= k "
+                    "(ld_split %lld, k %lld)", (long long)ld_split, (long long)k);
+    SPREG_CHECK_ARG(rows <= INT32_MAX / 2, "too many rows");
+    split_rows_kernel<<<(unsigned)rows, 256, 0, stream>>>(a_rows, lda, rows, k, static_cast<__half *>(a_split),
+                                                         ld_split, row_scale);
+    SPREG_CUDA(cudaGetLastError());
+    return SPREG_OK;
+}
+
+// Reusable plan of FP32-accurate products: everything but the launches is done once (scratch, tensor
+// maps, device table), so a run is two kernel launches with no host-side preparation.
+struct TcPlanHandle {
+    TcPlan pl;
+    int device = -1;
+};
+
+int tc_plan_create_f32_impl(const spreg_dense_rows_f32_item *items, int32_t count, void **out, cudaStream_t stream) {
+    SPREG_CHECK_ARG(out && count >= 0 && (count == 0 || items), "bad arguments");
+    *out = nullptr;
+    auto *h = new TcPlanHandle;
+    TcPlan &pl = h->pl;
+    pl.split = true;
+    for (int32_t i = 0; i < count; ++i) pl.items.push_back(from_f32(items[i]));
+    int st = tc_plan_build(pl);
+    int *status = nullptr;
+    if (!st && !pl.groups.empty()) status = device_status_word(&st);
+    if (!st) st = tc_device_setup(&pl.sms);
+    if (!st) {
+        cudaError_t e = cudaGetDevice(&h->device);
+        if (e == cudaSuccess && !pl.groups.empty()) e = cudaMalloc(reinterpret_cast<void **>(&pl.scratch), (size_t)pl.scratch_bytes);
+        if (e != cudaSuccess) {
+            set_error(std::string("tensor-core plan: ") + cudaGetErrorString(e));
+            st = e == cudaErrorMemoryAllocation ? SPREG_ERR_NOMEM : SPREG_ERR_CUDA;
+        }
+    }
+    if (!st && !pl.groups.empty()) st = tc_plan_fill(pl, status);
+    if (!st && !pl.groups.empty()) st = tc_plan_upload(pl, stream);
+    if (!st && !pl.groups.empty()) {
+        cudaError_t e = cudaStreamSynchronize(stream);  // the host image may change with the next build
+        if (e != cudaSuccess) {
+            set_error(std::string("tensor-core plan: ") + cudaGetErrorString(e));
+            st = SPREG_ERR_CUDA;
+        }
+    }
+    if (st) {
+        if (pl.scratch) cudaFree(pl.scratch);
+        delete h;
+        return st;
+    }
+    *out = h;
+    return SPREG_OK;
+}
+
+int tc_plan_run_impl(const void *plan, cudaStream_t stream) {
+    SPREG_CHECK_ARG(plan, "null plan");
+    const TcPlanHandle *h = static_cast<const TcPlanHandle *>(plan);
+    if (h->pl.groups.empty()) return SPREG_OK;
+    int dev = -1;
+    SPREG_CUDA(cudaGetDevice(&dev));
+    SPREG_CHECK_ARG(dev == h->device, "the plan was made on device %d, the current device is %d", h->device, dev);
+    return tc_plan_launch(h->pl, stream);
+}
+
+void tc_plan_destroy_impl(void *plan) {
+    if (!plan) return;
+    auto *h = static_cast<TcPlanHandle *>(plan);
+    if (h->pl.scratch) cudaFree(h->pl.scratch);
+    delete h;
 }
 
 }  // namespace spreg

@@ -79,6 +79,13 @@ class WorkItem(C.Structure):
     _fields_ = [("a", C.c_void_p), ("args", ExecArgs)]
 
 
+class DenseRowsF32Item(C.Structure):
+    _fields_ = [("a_split", C.c_void_p), ("rows", C.c_int64), ("k", C.c_int64), ("ld_split", C.c_int64),
+                ("row_scale", C.c_void_p), ("row_index", C.c_void_p), ("b", C.c_void_p), ("ldb", C.c_int64),
+                ("c", C.c_void_p), ("ldc", C.c_int64), ("n", C.c_int64), ("load_c", C.c_int32),
+                ("epilogue", C.c_int32), ("tile_n", C.c_int32), ("reserved", C.c_int32)]
+
+
 class TileConfig(C.Structure):
     _fields_ = [("m_tile", C.c_int32), ("k_tile", C.c_int32), ("n_tile", C.c_int32), ("nr", C.c_int32),
                 ("outer_schedule", C.c_int32), ("value_dtype", C.c_int32), ("sparse_a", C.c_int32),
@@ -107,7 +114,12 @@ PROTOTYPES = {
     "spreg_dense_rows_bf16": (C.c_int, [P, C.c_int64, C.c_int64, C.c_int64, P, P, C.c_int64, P, C.c_int64,
                                         C.c_int64, C.c_int32, C.c_int32, C.c_int32, P]),
     "spreg_dense_rows_bf16_batched": (C.c_int, [P, C.c_int32, P]),
-    "spreg_tc_set_cluster": (C.c_int, [C.c_int32]),
+    "spreg_dense_rows_f32_split": (C.c_int, [P, C.c_int64, C.c_int64, C.c_int64, P, C.c_int64, P, P]),
+    "spreg_dense_rows_f32": (C.c_int, [C.POINTER(DenseRowsF32Item), P]),
+    "spreg_dense_rows_f32_batched": (C.c_int, [P, C.c_int32, P]),
+    "spreg_dense_rows_f32_plan_create": (C.c_int, [P, C.c_int32, C.POINTER(P), P]),
+    "spreg_dense_rows_plan_run": (C.c_int, [P, P]),
+    "spreg_dense_rows_plan_destroy": (None, [P]),
     "spreg_pack_from_arena": (C.c_int, [P, C.POINTER(ArenaGeom), P, C.c_int64, P, C.c_int64, P, C.c_int64,
                                         C.POINTER(P), P]),
     "spreg_tile_create": (C.c_int, [P, C.c_int64, C.c_int64, C.c_int64, C.POINTER(P)]),

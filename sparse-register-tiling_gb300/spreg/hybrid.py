@@ -1,17 +1,21 @@
 """Dense panels on the tensor cores, the rest register-tiled.
 
 A row panel (M_r rows) whose fill -- nonzeros / (M_r x K) -- reaches `tc_fill` runs as part of a
-dense BF16 product on the tensor cores (``spreg_dense_rows_bf16``: tcgen05 MMA, FP32 accumulation
-in tensor memory); the other panels are packed and executed as usual.  The threshold is a tuning
-parameter (`tune_tc_fill` measures it); 1.0 disables the tensor-core part, 0.0 runs every panel on
-it.
+dense product on the tensor cores; the other panels are packed and executed as usual.  The threshold
+is a tuning parameter (`tune_tc_fill` measures it); above 1.0 disables the tensor-core part, 0.0 runs
+every panel on it.  Two storage forms:
+  * BF16 (``spreg_dense_rows_bf16``): BF16 values and B, FP32 accumulation in tensor memory; the error
+    bound is that of an FP32-accumulated BF16 product;
+  * FP32 (``spreg_dense_rows_f32``): the FP32 executor's accuracy at tensor-core rate.  The dense rows
+    and B are split into scaled FP16 pairs and multiplied as hi.hi + hi.lo + lo.hi; the result carries
+    the error of an FP32 dot product in the tensor core's summation order (the register-tiled rows stay
+    bit-identical to the oracle).
 
 Order of the two parts, so that load_c and the ReLU epilogue apply once to every row: without
 load_c the register-tiled part runs first (its empty dense panels store zeros), then the tensor-core
 part writes those rows; with load_c the tensor-core part runs first (C_in + A.B, epilogue), then
 the register-tiled part adds nothing to those rows (ReLU of a ReLU result is the same value).
-Results of the tensor-core rows are not bit-identical to the register-tiled order; the error bound
-is that of an FP32-accumulated BF16 product.
+The reference runs every panel register-tiled (cpp_testbed/src/spmm/nano/SpMM_SOP.h:174-178).
 """
 from __future__ import annotations
 
@@ -22,12 +26,6 @@ import numpy as np
 from . import _lib
 from .mapping import Mapping
 from .packed import PackedMatrix
-
-
-def set_tc_cluster(mode: int) -> None:
-    """Clusters of the tensor-core launches that follow (process-wide): 0 automatic, 1 single CTAs,
-    2 CTA pairs sharing each B tile through TMA multicast (spreg_tc_set_cluster)."""
-    _lib.check(_lib.lib().spreg_tc_set_cluster(int(mode)))
 
 
 def dense_rows_bf16(a_rows, row_index, B, C, n: Optional[int] = None, load_c: bool = False,
@@ -74,23 +72,100 @@ def panel_fill(A, mr: int):
     return nz.view(P, mr).sum(dim=1) / float(mr * max(k, 1))
 
 
+def split_rows_f32(a_rows, stream=None):
+    """The FP16 split pair of FP32 rows (spreg_dense_rows_f32_split): returns (a_split, row_scale) with
+    a_split 2R x K8 float16 (rows [0, R) high halves, [R, 2R) low halves) and row_scale float32 R."""
+    import torch
+    if not a_rows.is_cuda or a_rows.dtype != torch.float32 or a_rows.dim() != 2 or a_rows.stride(1) != 1:
+        raise ValueError("a_rows must be a 2-D float32 CUDA tensor with unit column stride")
+    R, k = a_rows.shape
+    k8 = max(8, (k + 7) // 8 * 8)
+    a_split = torch.empty((2 * R, k8), dtype=torch.float16, device=a_rows.device)
+    scale = torch.empty(R, dtype=torch.float32, device=a_rows.device)
+    _lib.check(_lib.lib().spreg_dense_rows_f32_split(a_rows.data_ptr(), R, k, a_rows.stride(0), a_split.data_ptr(),
+                                                     k8, scale.data_ptr(), _lib.stream_handle(stream)))
+    return a_split, scale
+
+
+def f32_item(a_split, row_scale, row_index, B, C, n: Optional[int] = None, k: Optional[int] = None,
+             load_c: bool = False, epilogue: int = _lib.EPILOGUE_NONE, tile_n: int = 0) -> "_lib.DenseRowsF32Item":
+    """spreg_dense_rows_f32_item of one FP32-accurate product (CUDA tensors: the split pair, FP32 B and C)."""
+    import torch
+    n = B.shape[1] if n is None else int(n)
+    k = B.shape[0] if k is None else int(k)
+    R = a_split.shape[0] // 2
+    if B.dtype != torch.float32 or C.dtype != torch.float32 or a_split.dtype != torch.float16:
+        raise ValueError("B and C must be float32, the split pair float16")
+    if B.stride(1) != 1 or C.stride(1) != 1 or a_split.shape[1] < k or B.shape[0] < k:
+        raise ValueError("operands need unit column stride and K columns / rows")
+    if n > B.shape[1] or n > C.shape[1] or row_index.numel() != R or row_scale.numel() != R:
+        raise ValueError("n exceeds B or C, or the row index / scales do not match the split pair")
+    return _lib.DenseRowsF32Item(a_split.data_ptr(), R, k, a_split.stride(0), row_scale.data_ptr(),
+                                 row_index.data_ptr(), B.data_ptr(), B.stride(0), C.data_ptr(), C.stride(0), n,
+                                 int(bool(load_c)), int(epilogue), int(tile_n), 0)
+
+
+def dense_rows_f32(a_split, row_scale, row_index, B, C, n: Optional[int] = None, load_c: bool = False,
+                   epilogue: int = _lib.EPILOGUE_NONE, stream=None):
+    """C[row_index[i], :n] (+)= A_rows[i, :K] . B[:, :n] with FP32 accuracy on the tensor cores (A_rows
+    given as its split pair from `split_rows_f32`; B, C float32 CUDA tensors)."""
+    import ctypes
+    it = f32_item(a_split, row_scale, row_index, B, C, n=n, load_c=load_c, epilogue=epilogue)
+    _lib.check(_lib.lib().spreg_dense_rows_f32(ctypes.byref(it), _lib.stream_handle(stream)))
+    return C
+
+
+class DenseRowsPlan:
+    """A reusable plan of FP32-accurate products over fixed tensors (spreg_dense_rows_f32_plan_create):
+    a run is the B split and the tensor-core launch, with no host-side preparation (capturable)."""
+
+    def __init__(self, items, stream=None):
+        import ctypes
+        arr = (_lib.DenseRowsF32Item * max(1, len(items)))(*items)
+        h = ctypes.c_void_p()
+        _lib.check(_lib.lib().spreg_dense_rows_f32_plan_create(arr, len(items), ctypes.byref(h),
+                                                               _lib.stream_handle(stream)))
+        self._h = h
+
+    def run(self, stream=None) -> None:
+        _lib.check(_lib.lib().spreg_dense_rows_plan_run(self._h, _lib.stream_handle(stream)))
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            _lib.lib().spreg_dense_rows_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class HybridMatrix:
     """A pruned matrix split into tensor-core panels (fill >= tc_fill) and register-tiled panels.
 
-    BF16 storage (values and B), FP32 or BF16 output -- the tensor cores take BF16 operands."""
+    value_dtype BF16: BF16 values and B, FP32 or BF16 output.  value_dtype F32: FP32 values, B and C;
+    the tensor-core rows run as FP32-accurate split products."""
 
-    def __init__(self, packed: PackedMatrix, a_rows, row_index, rows: int, cols: int, tc_fill: float):
+    def __init__(self, packed: PackedMatrix, a_rows, row_index, rows: int, cols: int, tc_fill: float,
+                 value_dtype: int = _lib.BF16, row_scale=None):
         self.packed = packed
-        self.a_rows = a_rows
+        self.a_rows = a_rows          # BF16 rows, or (F32) the FP16 split pair (2 x tc_rows rows)
+        self.row_scale = row_scale    # F32 only
         self.row_index = row_index
         self.rows, self.cols = rows, cols
         self.tc_fill = tc_fill
+        self.value_dtype = value_dtype
 
     @classmethod
-    def from_dense(cls, A, mapping: Mapping, tc_fill: float, k_tile: int = 0, m_tile: int = 0) -> "HybridMatrix":
+    def from_dense(cls, A, mapping: Mapping, tc_fill: float, k_tile: int = 0, m_tile: int = 0,
+                   value_dtype: int = _lib.BF16) -> "HybridMatrix":
         import torch
         if not A.is_cuda or A.dtype != torch.float32 or A.dim() != 2:
             raise ValueError("A must be a 2-D float32 CUDA tensor")
+        if value_dtype not in (_lib.BF16, _lib.F32):
+            raise ValueError("the hybrid stores BF16 or FP32 values")
         mr = mapping.mr
         m, k = A.shape
         fill = panel_fill(A, mr)
@@ -100,16 +175,32 @@ class HybridMatrix:
         rows = rows[rows < m]
         A_sp = A.clone()
         k8 = max(8, (k + 7) // 8 * 8)
-        a_rows = torch.zeros((rows.numel(), k8), dtype=torch.bfloat16, device=A.device)
+        scale = None
+        if value_dtype == _lib.F32:
+            a_rows, scale = split_rows_f32(A[rows].contiguous()) if rows.numel() else (
+                torch.zeros((0, k8), dtype=torch.float16, device=A.device),
+                torch.zeros(0, dtype=torch.float32, device=A.device))
+        else:
+            a_rows = torch.zeros((rows.numel(), k8), dtype=torch.bfloat16, device=A.device)
+            if rows.numel():
+                a_rows[:, :k] = A[rows].to(torch.bfloat16)
         if rows.numel():
-            a_rows[:, :k] = A[rows].to(torch.bfloat16)
             A_sp[rows] = 0.0
-        packed = PackedMatrix.from_dense(A_sp, mapping, m_tile=m_tile, k_tile=k_tile, value_dtype=_lib.BF16)
-        return cls(packed, a_rows, rows.to(torch.int32).contiguous(), m, k, tc_fill)
+        packed = PackedMatrix.from_dense(A_sp, mapping, m_tile=m_tile, k_tile=k_tile, value_dtype=value_dtype)
+        return cls(packed, a_rows, rows.to(torch.int32).contiguous(), m, k, tc_fill, value_dtype, scale)
 
     @property
     def tc_rows(self) -> int:
         return int(self.row_index.numel())
+
+    @property
+    def all_tc(self) -> bool:
+        return self.tc_rows == self.rows and self.cols > 0
+
+    def tc_item(self, B, C, n: Optional[int] = None, load_c: bool = False, epilogue: int = _lib.EPILOGUE_NONE):
+        """spreg_dense_rows_f32_item of the tensor-core part (F32 storage)."""
+        return f32_item(self.a_rows, self.row_scale, self.row_index, B, C, n=n, k=self.cols, load_c=load_c,
+                        epilogue=epilogue)
 
     def execute(self, B, C=None, n: Optional[int] = None, load_c: bool = False, epilogue: int = _lib.EPILOGUE_NONE,
                 nr: int = 0, stream=None):
@@ -121,7 +212,7 @@ class HybridMatrix:
         if B.shape[0] < self.cols or C.shape[0] != self.rows or (n or B.shape[1]) > min(B.shape[1], C.shape[1]):
             raise ValueError(f"B needs {self.cols} rows, C {self.rows} rows, both at least n columns")
         kw = dict(n=n, load_c=load_c, epilogue=epilogue, nr=nr, stream=stream)
-        if self.tc_rows == self.rows and self.cols > 0:
+        if self.all_tc:
             self._tc(B, C, n, load_c, epilogue, stream)  # every row is a tensor-core row
         elif self.tc_rows and self.cols > 0:
             if load_c:
@@ -137,6 +228,11 @@ class HybridMatrix:
     def _tc(self, B, C, n, load_c, epilogue, stream):
         n = B.shape[1] if n is None else int(n)
         import torch
+        if self.value_dtype == _lib.F32:
+            import ctypes
+            it = self.tc_item(B, C, n=n, load_c=load_c, epilogue=epilogue)
+            _lib.check(_lib.lib().spreg_dense_rows_f32(ctypes.byref(it), _lib.stream_handle(stream)))
+            return
         cd = _lib.F32 if C.dtype == torch.float32 else _lib.BF16
         _lib.check(_lib.lib().spreg_dense_rows_bf16(
             self.a_rows.data_ptr(), self.a_rows.shape[0], self.cols, self.a_rows.stride(0), self.row_index.data_ptr(),
@@ -144,16 +240,43 @@ class HybridMatrix:
             _lib.stream_handle(stream)))
 
 
+class HybridBatch:
+    """Many FP32 hybrid SpMMs C_i = A_i . B_i over fixed tensors in as few launches as possible: the
+    register-tiled parts in one batched executor call, the tensor-core parts as one reusable plan
+    (B split + tensor-core launch).  Without load_c the register-tiled part runs first, as in
+    HybridMatrix.execute."""
+
+    def __init__(self, triples, stream=None):
+        from .packed import work_items
+        self.triples = list(triples)
+        for h, _, _ in self.triples:
+            if h.value_dtype != _lib.F32:
+                raise ValueError("HybridBatch runs FP32 hybrids")
+        tc = [h.tc_item(B, C) for h, B, C in self.triples if h.tc_rows and h.cols > 0]
+        self.plan = DenseRowsPlan(tc, stream=stream) if tc else None
+        sp = [(h.packed, B, C) for h, B, C in self.triples if not h.all_tc]
+        self.items = work_items(sp) if sp else None
+        self.n_sparse = len(sp)
+
+    def run(self, stream=None) -> None:
+        if self.items is not None:
+            _lib.check(_lib.lib().spreg_execute_batched(self.items, self.n_sparse, _lib.stream_handle(stream)))
+        if self.plan is not None:
+            self.plan.run(stream)
+
+
 def tune_tc_fill(A, mapping: Mapping, n: int, fills=(1.01, 0.5, 0.3, 0.2, 0.1, 0.05, 0.0), k_tile: int = 0,
-                 reps: int = 20) -> dict:
-    """Time the hybrid at each threshold on the device (BF16, n columns); returns {fill: us} and the
-    fastest threshold."""
+                 reps: int = 20, value_dtype: int = _lib.BF16) -> dict:
+    """Time the hybrid at each threshold on the device (BF16 or FP32 storage, n columns); returns
+    {fill: us} and the fastest threshold."""
     import torch
-    B = torch.randn((A.shape[1], n), device=A.device).to(torch.bfloat16)
+    B = torch.randn((A.shape[1], n), device=A.device)
+    if value_dtype == _lib.BF16:
+        B = B.to(torch.bfloat16)
     C = torch.empty((A.shape[0], n), device=A.device)
     out = {}
     for f in fills:
-        h = HybridMatrix.from_dense(A, mapping, f, k_tile=k_tile)
+        h = HybridMatrix.from_dense(A, mapping, f, k_tile=k_tile, value_dtype=value_dtype)
         for _ in range(3):  # warm-up: lazy set-up and clock ramp stay out of the timed calls
             h.execute(B, C)
         torch.cuda.synchronize()

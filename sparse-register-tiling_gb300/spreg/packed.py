@@ -200,3 +200,13 @@ def execute_batched(items, stream=None) -> None:
         arr[i].a = pm.handle
         arr[i].args = pm.exec_args(B, Cm, **kw)
     _lib.check(_lib.lib().spreg_execute_batched(arr, len(items), _lib.stream_handle(stream)))
+
+
+def work_items(triples):
+    """spreg_work_item array of [(PackedMatrix, B, C), ...] (C = A . B over all of B's columns)."""
+    arr = (_lib.WorkItem * max(len(triples), 1))()
+    for i, (pm, B, Cm) in enumerate(triples):
+        pm._check_operands(B, Cm)
+        arr[i].a = pm.handle
+        arr[i].args = pm.exec_args(B, Cm)
+    return arr

@@ -43,8 +43,6 @@ int cpu_checks() {
     if (spreg_mapping_create(3, offs.data(), offs.data(), nullptr, 0, &bad) != SPREG_ERR_INVALID_ARG || bad ||
         std::strlen(spreg_last_error()) == 0)
         return failed("M_r = 3 refused with a message");
-    if (spreg_tc_set_cluster(7) != SPREG_ERR_INVALID_ARG) return failed("cluster mode 7 refused");
-    if (spreg_tc_set_cluster(0) != SPREG_OK) return failed("cluster mode 0");
     spreg_mapping_destroy(m);
     std::printf("ok cpu\n");
     return 0;

@@ -71,19 +71,6 @@ def test_mapping_argument_errors():
     assert e.value.status == _lib.SPREG_ERR_INVALID_ARG
 
 
-def test_tensor_core_cluster_mode_setter():
-    """spreg_tc_set_cluster takes 0 (automatic), 1 and 2 and refuses anything else (no GPU needed)."""
-    from spreg.hybrid import set_tc_cluster
-    try:
-        for mode in (1, 2, 0):
-            set_tc_cluster(mode)
-        for bad in (-1, 3, 4):
-            st = _lib.lib().spreg_tc_set_cluster(bad)
-            assert st == _lib.SPREG_ERR_INVALID_ARG and "cluster mode" in _lib.last_error()
-    finally:
-        set_tc_cluster(0)
-
-
 def test_make_sop_module_without_gpu():
     m = Mapping.load("400fa")
     mod = make_sop_module(Acc(8, 2), m.nanokernels, m)

@@ -192,21 +192,14 @@ def test_tile_width_hint_gives_the_same_products(cuda):
         _lib.check(_lib.lib().spreg_dense_rows_bf16_batched(it.ctypes.data, 1, _lib.stream_handle(None)))
 
 
-@pytest.fixture
-def tc_cluster_mode():
-    from spreg.hybrid import set_tc_cluster
-    yield set_tc_cluster
-    set_tc_cluster(0)
-
-
-def _cluster_run(mode, set_mode):
+def _shapes_run():
     """Single products (odd and even row block counts, 128- and 256-wide tiles, B read in place), a
-    batched call of many shapes and a coalesced call over several B (transposed B), all under one
-    cluster mode; returns every output."""
+    batched call of many shapes and a coalesced call over several B (transposed B); returns every
+    output."""
     import torch
     from spreg.hybrid import dense_rows_bf16
     from spreg.serving import TC_ITEM_DTYPE
-    set_mode(mode)
+    mode = "single CTAs"
     g = torch.Generator(device="cuda").manual_seed(21)
     outs = []
     for R, K, n, c_bf16, load_c, relu in [(1, 8, 1, False, False, False), (300, 100, 200, False, True, True),
@@ -271,15 +264,12 @@ def _cluster_run(mode, set_mode):
     return outs
 
 
-def test_cta_pairs_sharing_b_give_the_same_products(cuda, tc_cluster_mode):
-    """CTA pairs that share each B tile through TMA multicast (cluster mode 2) produce the outputs of
-    single CTAs (mode 1) bit for bit, and so does the automatic choice; a bad mode is refused."""
+def test_products_of_many_shapes_alone_batched_and_coalesced_are_repeatable(cuda):
+    """Every shape family (single products, one launch of many shapes, coalesced products over
+    several B) meets its tolerance, and a second run gives the same bits."""
     import torch
-    single = _cluster_run(1, tc_cluster_mode)
-    for mode in (2, 0):
-        got = _cluster_run(mode, tc_cluster_mode)
-        for x, y in zip(single, got):
-            assert torch.equal(x.view(torch.int16) if x.dtype == torch.bfloat16 else x.view(torch.int32),
-                               y.view(torch.int16) if y.dtype == torch.bfloat16 else y.view(torch.int32)), mode
-    with pytest.raises(_lib.SpregError, match="cluster mode"):
-        tc_cluster_mode(3)
+    first = _shapes_run()
+    again = _shapes_run()
+    for x, y in zip(first, again):
+        assert torch.equal(x.view(torch.int16) if x.dtype == torch.bfloat16 else x.view(torch.int32),
+                           y.view(torch.int16) if y.dtype == torch.bfloat16 else y.view(torch.int32))
