@@ -111,9 +111,14 @@ struct DevFacts {
 };
 constexpr int kCounters = 4096;
 
+namespace {
+DevFacts g_facts[64];
+std::mutex g_facts_mu;
+}  // namespace
+
 int dev_facts(DevFacts **out) {
-    static DevFacts facts[64];
-    static std::mutex mu;
+    DevFacts *const facts = g_facts;
+    std::mutex &mu = g_facts_mu;
     int dev = 0;
     SPREG_CUDA(cudaGetDevice(&dev));
     SPREG_CHECK_ARG(dev >= 0 && dev < 64, "device ordinal %d out of range", dev);
@@ -183,14 +188,35 @@ int selftest_wait_impl(uint32_t limit, int32_t *status_out, uint32_t *polled_out
     return SPREG_OK;
 }
 
+int noalloc_status_word(int dev, int32_t *v, int reset, bool *have);  // noalloc.cu
+
+// The device's status word: the regular executors' word, or (when that is 0) the no-allocation
+// entry point's.  A caller that has only used the no-allocation entry point on this device gets its
+// word without the regular executors' per-device pool being created.
 int device_status_impl(int32_t *status, int reset) {
+    int dev = 0;
+    SPREG_CUDA(cudaGetDevice(&dev));
+    SPREG_CHECK_ARG(dev >= 0 && dev < 64, "device ordinal %d out of range", dev);
+    int32_t v_na = 0;
+    bool have_na = false;
+    int st = noalloc_status_word(dev, &v_na, reset, &have_na);
+    if (st) return st;
+    bool pool = false;
+    {
+        std::lock_guard<std::mutex> lk(g_facts_mu);
+        pool = g_facts[dev].status != nullptr;
+    }
+    if (have_na && !pool) {
+        if (status) *status = v_na;
+        return SPREG_OK;
+    }
     DevFacts *f;
-    int st = dev_facts(&f);
+    st = dev_facts(&f);
     if (st) return st;
     int v = 0;
     SPREG_CUDA(cudaMemcpy(&v, f->status, sizeof(int), cudaMemcpyDeviceToHost));
     if (reset) SPREG_CUDA(cudaMemset(f->status, 0, sizeof(int)));
-    if (status) *status = v;
+    if (status) *status = v ? v : v_na;
     return SPREG_OK;
 }
 

@@ -15,8 +15,10 @@
 // one configuration).  Larger calls are rejected.  Host code cannot use the array's name as a
 // device address (it is a host-side stand-in), so the first call on each device looks the address
 // up with cudaGetSymbolAddress while that device is current; make that first call before any
-// stream capture.  Every call shares the array and clears the slots it uses before its launches,
-// so calls whose work overlaps on the GPU (other streams, other threads) race on it.
+// stream capture.  Every call shares the array and clears the counters it uses before its
+// launches, so calls whose work overlaps on the GPU (other streams, other threads) race on it.  The
+// status word keeps its value until spreg_device_status reads and clears it (that call reports the
+// word of the regular executors and this one's).
 #include "exec_kernel.cuh"
 
 #include <algorithm>
@@ -105,6 +107,24 @@ struct NoAllocGroup {
 bool is_aligned(const void *p, size_t bytes) { return (reinterpret_cast<uintptr_t>(p) % bytes) == 0; }
 
 }  // namespace
+
+// Status word of the no-allocation entry point on device `dev` (*have = false if that entry point
+// was never set up there): read, and cleared when reset != 0.  For spreg_device_status.
+int noalloc_status_word(int dev, int32_t *v, int reset, bool *have) {
+    *have = false;
+    *v = 0;
+    if (dev < 0 || dev >= 64) return SPREG_OK;
+    int *w = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g_noalloc_mu);
+        w = g_noalloc_dev[dev].scratch;
+    }
+    if (!w) return SPREG_OK;
+    *have = true;
+    SPREG_CUDA(cudaMemcpy(v, w, sizeof(int), cudaMemcpyDeviceToHost));
+    if (reset) SPREG_CUDA(cudaMemset(w, 0, sizeof(int)));
+    return SPREG_OK;
+}
 
 }  // namespace spreg
 
@@ -196,9 +216,10 @@ extern "C" int spreg_execute_batched_noalloc(const spreg_work_item *items, int32
                     "(each launch runs up to %d SpMMs of one M_r / strip width / dtype combination)",
                     (long long)launches, kNoAllocLaunches, kMaxBatchProblems);
 
-    // Clear the status word and every counter this call uses, then launch.
+    // Clear every counter this call uses, then launch.  The status word keeps what earlier calls
+    // recorded until spreg_device_status reads and clears it.
     int *scratch = d->scratch;
-    SPREG_CUDA(cudaMemsetAsync(scratch, 0, sizeof(int) * (size_t)(1 + launches), s));
+    if (launches > 0) SPREG_CUDA(cudaMemsetAsync(scratch + 1, 0, sizeof(int) * (size_t)launches, s));
     int slot = 0;
     for (auto &kv : groups) {
         NoAllocGroup &g = kv.second;
