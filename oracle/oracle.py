@@ -21,7 +21,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
 REF_PATH = os.path.join(HERE, "_ref", "libref_naive.so")
-REFERENCE_ROOT = "/root/reference"
+# Checkout of the reference project, for building its spmm_naive (absent on machines without it).
+REFERENCE_ROOT = os.environ.get("SPREG_REFERENCE", os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference"))
 
 F32, BF16, F16 = 0, 1, 2
 ZERO = 0xFFFF
@@ -211,6 +212,26 @@ class Packed:
                           int(bool(load_c)), int(epilogue), int(threads))
         return out
 
+    def execute_fast(self, B: np.ndarray, out: np.ndarray | None = None, load_c=False, epilogue=0,
+                     threads=0) -> np.ndarray:
+        """The SIMD CPU executor (spreg_cpu_fast.c: per-pattern FMA blocks on vector registers; the timed
+        CPU baseline), bit-identical to `execute` for FP32; N a multiple of 16."""
+        if self.value_dtype != F32:
+            raise ValueError("the SIMD CPU executor runs FP32 values")
+        B = np.ascontiguousarray(B, dtype=np.float32)
+        if out is None:
+            out = np.zeros((self.M, B.shape[1]), dtype=np.float32)
+        arena = self.arena if self.arena.size else np.zeros(1, np.uint8)
+        descs = self.descs if self.descs.size else np.zeros(1, DESC_DTYPE)
+        rc = lib().orc_execute_fast(self.t.mr, self.t.num_nkern, _p(self.t.id_to_pattern), _p(arena), _p(descs),
+                                    C_int64(self.M), C_int64(self.num_panels), C_int64(self.sizes["panels_per_tile"]),
+                                    C_int64(self.sizes["num_k_tiles"]), _p(B), C_int64(B.shape[1]), _p(out),
+                                    C_int64(out.shape[1]), C_int64(B.shape[1]), int(bool(load_c)), int(epilogue),
+                                    int(threads))
+        if rc:
+            raise ValueError("the SIMD CPU executor needs N a multiple of 16 and M_r <= 8")
+        return out
+
 
 def C_int64(v):
     return C.c_int64(int(v))
@@ -227,6 +248,22 @@ def csr_spmm(row_ptrs, col_inds, values, B: np.ndarray, threads=0) -> np.ndarray
     lib().orc_csr_spmm(C_int64(M), C_int64(B.shape[1]), _p(rp), _p(ci if ci.size else np.zeros(1, np.int32)),
                        _p(v if v.size else np.zeros(1, np.float32)), _p(B), C_int64(B.shape[1]), _p(out),
                        C_int64(B.shape[1]), int(threads))
+    return out
+
+
+def csr_spmm_fast(row_ptrs, col_inds, values, B: np.ndarray, threads=0) -> np.ndarray:
+    """The CSR baseline as SIMD code (spreg_cpu_fast.c), bit-identical to `csr_spmm`; N a multiple of 64."""
+    rp = np.ascontiguousarray(row_ptrs, dtype=np.int32)
+    ci = np.ascontiguousarray(col_inds, dtype=np.int32)
+    v = np.ascontiguousarray(values, dtype=np.float32)
+    B = np.ascontiguousarray(B, dtype=np.float32)
+    M = rp.size - 1
+    out = np.zeros((M, B.shape[1]), dtype=np.float32)
+    rc = lib().orc_csr_spmm_fast(C_int64(M), C_int64(B.shape[1]), _p(rp), _p(ci if ci.size else np.zeros(1, np.int32)),
+                                 _p(v if v.size else np.zeros(1, np.float32)), _p(B), C_int64(B.shape[1]), _p(out),
+                                 C_int64(B.shape[1]), int(threads))
+    if rc:
+        raise ValueError("the SIMD CSR baseline needs N a multiple of 64")
     return out
 
 
