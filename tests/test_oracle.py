@@ -218,3 +218,28 @@ def test_edge_shapes(shape):
 
 def test_popcount_helper():
     assert [popcount(x) for x in (0, 1, 255, 0b1010)] == [0, 1, 8, 2]
+
+
+@pytest.mark.parametrize("mapping_id,mr", [("61fee", 4), ("400fa", 8), (None, 2), (None, 6)])
+@pytest.mark.parametrize("k_tile,load_c,relu", [(0, False, False), (128, True, True), (64, False, True)])
+def test_simd_cpu_executor_is_bit_identical_to_the_checker(mapping_id, mr, k_tile, load_c, relu):
+    """The timed CPU baseline (SIMD, per-pattern FMA blocks) gives the checker's bits."""
+    from spreg import synth
+    from spreg.mapping import Mapping
+    m = Mapping.load(mapping_id) if mapping_id else Mapping.identity(mr)
+    A = synth.row_skew(130, 300, 0.85, seed=3, std=0.5)
+    B = synth.dense(300, 48, seed=4)
+    C0 = synth.dense(130, 48, seed=5)
+    pk = O.Packed(O.Tables.of(m), A, k_tile=k_tile)
+    want = pk.execute(B, C0.copy() if load_c else None, load_c=load_c, epilogue=int(relu))
+    got = pk.execute_fast(B, C0.copy() if load_c else None, load_c=load_c, epilogue=int(relu), threads=3)
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
+def test_simd_csr_baseline_is_bit_identical():
+    from spreg import synth
+    A = synth.row_skew(200, 256, 0.9, seed=8, std=1.0)
+    rp, ci, v = synth.to_csr(A)
+    B = synth.dense(256, 128, seed=9)
+    assert np.array_equal(O.csr_spmm_fast(rp, ci, v, B, threads=3).view(np.uint32),
+                          O.csr_spmm(rp, ci, v, B).view(np.uint32))
