@@ -59,6 +59,12 @@ def parse():
     ap.add_argument("--meta", type=int, default=0, help="0 auto, 1 execution-layout kernel, 2 register streams")
     ap.add_argument("--dtype", choices=["f32", "bf16"], default="f32",
                     help="storage of A values and B (FP32 accumulation and FP32 C either way)")
+    ap.add_argument("--path", choices=["hybrid", "register"], default="hybrid",
+                    help="headline path: hybrid = FP32-accurate tensor-core panels (split FP16 products) beside "
+                         "register-tiled panels by the tuned fill threshold; register = the bit-exact register-tiled "
+                         "executor alone (it is timed either way)")
+    ap.add_argument("--tc-fill", type=float, default=-1.0,
+                    help="panel fill threshold of the hybrid; < 0: tuned on replica 0")
     ap.add_argument("--no-graph", action="store_true")
     ap.add_argument("--batched", type=int, default=1, help="1: one batched launch per step; 0: one launch per SpMM")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline budget; 0 skips it")
@@ -248,7 +254,13 @@ def serving_bench(args, dev) -> dict:
     configs, tuned = tune_mlp(w, "bf16", n=96, batch=32, device=dev)
     t_tune = time.perf_counter() - t_tune
     bf = SparseMLP(w, "bf16", device=dev, configs=configs)
-    fp = SparseMLP(w, "f32", device=dev)  # the plain path: M_r = 4 identity, untiled, auto N_r
+    # the plain FP32 path at its best single-request packing: the autotuner's choice for one request
+    # of the median token count (candidates include the headline's K_c = 128 B-tile packing with the
+    # histogram nanokernel set)
+    t_fp = time.perf_counter()
+    fp_configs, fp_tuned = tune_mlp(w, "f32", n=64, batch=1, device=dev)
+    t_fp = time.perf_counter() - t_fp
+    fp = SparseMLP(w, "f32", device=dev, configs=fp_configs)
     R = args.serve_requests
     ns = synth.token_counts(R, median=64, sigma=1.0, lo=1, hi=2048, seed=5)
     g = synth.rng(6)
@@ -268,7 +280,7 @@ def serving_bench(args, dev) -> dict:
     # capacity: every request queued at t = 0
     rb = reqs_for(bf, R, float("inf"), 2)
     cap_b = server.run(rb)
-    n_plain = max(32, R // 3)
+    n_plain = R  # the same requests as the server
     rp = reqs_for(fp, n_plain, float("inf"), 2)
     cap_p = serve_per_request(fp, rp)
 
@@ -305,7 +317,9 @@ def serving_bench(args, dev) -> dict:
             "batched_bf16": _stat(cap_b) | {"max_batch": cap_b.max_batch, "iterations": cap_b.iterations,
                                            "peak_activation_mib": cap_b.peak_activation_bytes / 2 ** 20,
                                            "slots": args.serve_slots, "budget_mib": args.serve_budget_mb},
-            "per_request_fp32": _stat(cap_p) | {"packing": "M_r=4 identity, untiled, N_r auto"},
+            "per_request_fp32": _stat(cap_p) | {"packing": {"up": fp_tuned[0].best.name(), "down": fp_tuned[1].best.name(),
+                                                            "tuned_for": "one request of 64 tokens",
+                                                            "tune_seconds": t_fp}},
             "autotuned_packing": {"up": tuned[0].best.name(), "down": tuned[1].best.name(),
                                   "tune_seconds": t_tune,
                                   "measured_ns_per_spmm": {"up": tuned[0].measured_ns, "down": tuned[1].measured_ns}},
@@ -322,12 +336,13 @@ def serving_bench(args, dev) -> dict:
 def precision_suite(dev) -> list:
     """1x1-conv-shaped SpMMs (B = K x 3136: batch 1, 56 x 56 spatial) at sparsity 0.8-0.95 with
     log-normal row skew: rel err against FP64 of FP32, BF16 and FP16 (per-panel scaled) storage,
-    FP32 accumulation, and the kernel time of each layer in each storage (one SpMM per launch,
-    the reference's timing protocol)."""
+    FP32 accumulation, and the kernel time of each layer in each storage through the product's best
+    path: the autotuner's packing (M_r, nanokernel set, K tile, N_r) for that storage, one SpMM per
+    launch timed with the reference's protocol (median of 150 x num_runs runs)."""
     import torch
     from oracle import oracle as O
-    from spreg import BF16, F16, F32, Mapping, PackedMatrix, synth
-    m = Mapping.identity(4)
+    from spreg import BF16, F16, F32, PackedMatrix, synth
+    from spreg.autotune import mapping_of, tune
     rows = []
     for i, (M, K) in enumerate(((64, 256), (128, 512), (256, 1024), (512, 2048), (2048, 512))):
         sp = (0.8, 0.85, 0.9, 0.95, 0.9)[i]
@@ -336,20 +351,28 @@ def precision_suite(dev) -> list:
         ref = O.dense_fp64(A, B)
         At = torch.from_numpy(A).to(dev)
         row = {"shape": [M, K], "sparsity": sp, "n": 3136}
+        tuned = {}
         for name, vd, tdt in (("fp32", F32, torch.float32), ("bf16", BF16, torch.bfloat16), ("fp16", F16, torch.float16)):
-            pm = PackedMatrix.from_dense(At, m, value_dtype=vd)
+            tkey = "f32" if vd == F32 else "bf16"  # FP16 runs the 16-bit executor paths that BF16 tunes
+            if tkey not in tuned:
+                tuned[tkey] = tune(A, 3136, tkey, top=4, device=dev).best
+            c = tuned[tkey]
+            pm = PackedMatrix.from_dense(At, mapping_of(c.mr, c.mapping), k_tile=c.k_tile, value_dtype=vd)
             Bt = torch.from_numpy(B).to(dev).to(tdt)
-            C = pm.execute(Bt)
+            C = pm.execute(Bt, nr=c.nr)
             row[f"rel_err_{name}"] = float(O.rel_err(C.cpu().numpy(), ref))
             Cf = torch.empty((M, 3136), device=dev)
-            t = pm.execute_timed(Bt, Cf, num_runs=1)
+            t = pm.execute_timed(Bt, Cf, num_runs=2, nr=c.nr)
             row[f"{name}_us"] = t / 1e3
             row[f"{name}_gflops"] = 2 * int(pm.info["nnz"]) * 3136 / t
+            row[f"{name}_gbs"] = pm.algorithmic_bytes(3136, b_bytes=4 if vd == F32 else 2) / t
+            row[f"{name}_config"] = c.name()
             if name != "fp32":
                 # the same storage with its own inputs rounded: the error the kernel adds
                 Bq = Bt.float().cpu().numpy()
                 row[f"rel_err_{name}_vs_rounded_inputs"] = float(O.rel_err(
                     C.cpu().numpy(), O.dense_fp64(_rounded(A, vd, pm), Bq)))
+        row["bf16_speedup_vs_fp32"] = row["fp32_us"] / row["bf16_us"]
         rows.append(row)
     return rows
 
@@ -381,66 +404,144 @@ def csr_baseline_leg(A, B_dev, pack, args, batched_spmm_us: float) -> dict:
             "note": "replica 0; one SpMM per launch (median of 150 x 10 runs), except sop_batched_us (96 per launch)"}
 
 
-def ffn_sweep(dev, replicas: int = 32, steps: int = 20) -> list:
+def config1_leg(dev) -> dict:
+    """The minimum slice as the workload states it: A 512 x 512 at 80 % Bernoulli sparsity, N(0, 1)
+    values, B 512 x 256 N(0, 1), M_r = 4, identity mapping 61fee, N_r = 64.  GPU: one SpMM per launch
+    (median of 150 x 10 runs, the reference's execute_tile protocol); CPU: the SIMD restatement of the
+    reference executor on 1 thread and on all host threads (median of 7); both checked bit for bit
+    against the oracle and against FP64."""
+    import torch
+    from oracle import oracle as O
+    from spreg import Mapping, PackedMatrix, synth
+    A = synth.bernoulli(512, 512, 0.8, seed=0, std=1.0)
+    B = synth.dense(512, 256, seed=1, std=1.0)
+    m = Mapping.identity(4)
+    pm = PackedMatrix.from_dense(torch.from_numpy(A).to(dev), m)
+    Bd = torch.from_numpy(B).to(dev)
+    C = pm.execute(Bd, nr=64).cpu().numpy()
+    ref = O.Packed(O.Tables.of(m), A)
+    want = ref.execute(B)
+    arena, descs, _ = pm.to_host()
+    Cd = torch.empty((512, 256), device=dev)
+    gpu_ns = pm.execute_timed(Bd, Cd, num_runs=10, nr=64)
+    nbytes = pm.algorithmic_bytes(256)
+    flops = pm.flops(256)
+    out = {"workload": "A 512x512 @80% Bernoulli, N(0,1) values; B 512x256 N(0,1); M_r=4, N_r=64, mapping 61fee",
+           "pack_bit_exact_vs_oracle": bool(np.array_equal(arena, ref.arena) and np.array_equal(descs, ref.descs)),
+           "execute_bit_exact_vs_oracle": bool(np.array_equal(C.view(np.uint32), want.view(np.uint32))),
+           "rel_err_vs_fp64": float(O.rel_err(C, O.dense_fp64(A, B))),
+           "gpu_us": gpu_ns / 1e3, "gpu_gbs": nbytes / gpu_ns, "gpu_gflops": flops / gpu_ns,
+           "algorithmic_bytes": nbytes, "flops": flops,
+           "note": "one SpMM of 1.4 MB per launch: latency, not bandwidth, bounds the GPU time"}
+    for th in (1, O.max_threads()):
+        ref.execute_fast(B, threads=th)
+        ts = []
+        for _ in range(7):
+            t0 = time.perf_counter()
+            got = ref.execute_fast(B, threads=th)
+            ts.append(time.perf_counter() - t0)
+        med = statistics.median(ts)
+        out[f"cpu_simd_{th}t_us"] = med * 1e6
+        out[f"cpu_simd_{th}t_gbs"] = nbytes / med / 1e9
+        out[f"cpu_simd_{th}t_bit_exact"] = bool(np.array_equal(got.view(np.uint32), want.view(np.uint32)))
+    out["gpu_vs_cpu_all_threads"] = out[f"cpu_simd_{O.max_threads()}t_us"] / out["gpu_us"]
+    return out
+
+
+def ffn_sweep(dev, min_replicas: int = 96, steps: int = 20) -> list:
     """The FFN-shaped workload across its sparsities and storage types: A 2048 x 512 and 512 x 2048
     at 0.7, 0.8, 0.9, 0.95 and 0.98 (log-normal row skew, sigma 0.5, values N(0, 0.02)), B K x 512
     N(0, 1); FP32, BF16 and FP16 (per-panel scaled) storage of A values and B, FP32 accumulation
     and FP32 C.
 
-    Each point runs `replicas` distinct replicas (working set larger than L2) in one launch of the
-    default packing (M_r = 4, K_c = 128, nanokernel set from replica 0's histogram), replayed from
-    a CUDA graph. It reports algorithmic GB/s (2-byte values and B for the 16-bit forms) and
-    GFLOP/s (2 nnz N), and checks replica 0 bit for bit against the oracle and against FP64.
+    Each point runs enough distinct replicas that their algorithmic bytes reach 4 x L2 (at least
+    `min_replicas`) in one batched launch of the autotuner's register-tiled packing for that point
+    and storage (M_r, nanokernel set, N_r, K tile, CTA tiling; tuned on replica 0 as a batch of 8),
+    replayed from a CUDA graph.  It reports algorithmic GB/s (2-byte values and B for the 16-bit
+    forms) and GFLOP/s (2 nnz N), and checks replica 0 bit for bit against the oracle and against
+    FP64.  Beside it, the FP32-accurate tensor-core hybrid with every panel on the tensor cores
+    (split FP16 products), timed the same way.
     """
     import torch
     from oracle import oracle as O
     from spreg import BF16, F16, F32, PackedMatrix, execute_batched, synth
-    from spreg.kernel_sets import executor_penalty, greedy_kernel_set, pattern_histogram
+    from spreg.autotune import mapping_of, tune
+    from spreg.hybrid import HybridBatch, HybridMatrix
     peak, _ = measured_peaks()
     forms = (("fp32", F32, torch.float32), ("bf16", BF16, torch.bfloat16), ("fp16", F16, torch.float16))
+
+    def timed(run):
+        run()
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            run()
+        for _ in range(3):
+            g.replay()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(steps):
+            g.replay()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / 1e3 / steps
+
     rows = []
     for M, K in ((2048, 512), (512, 2048)):
         for sp in (0.7, 0.8, 0.9, 0.95, 0.98):
-            As = [synth.row_skew(M, K, sp, seed=7000 + 10 * r + int(sp * 100), sigma=0.5, std=0.02)
-                  for r in range(replicas)]
+            A0 = synth.row_skew(M, K, sp, seed=7000 + int(sp * 100), sigma=0.5, std=0.02)
             B0 = torch.from_numpy(synth.dense(K, 512, seed=7500 + K)).to(dev)
-            m = greedy_kernel_set(pattern_histogram(As[0], 4), 4, 15, ((M + 3) // 4) * (-(-K // 128)),
-                                  penalty=executor_penalty(4, tile=True))
-            exact = O.dense_fp64(As[0], B0.cpu().numpy())
-            row = {"shape": [M, K], "sparsity": sp, "n": 512, "replicas": replicas, "nanokernels": m.nanokernels}
+            exact = O.dense_fp64(A0, B0.cpu().numpy())
+            row = {"shape": [M, K], "sparsity": sp, "n": 512}
+            tuned = {}
+            As = None
             for name, vd, tdt in forms:
-                packs = [PackedMatrix.from_dense(torch.from_numpy(A).to(dev), m, k_tile=128, value_dtype=vd)
-                         for A in As]
+                tkey = "f32" if vd == F32 else "bf16"
+                if tkey not in tuned:
+                    tuned[tkey] = tune(A0, 512, tkey, top=4, batch=8, device=dev, tc=False).best
+                c = tuned[tkey]
+                m = mapping_of(c.mr, c.mapping)
+                p0 = PackedMatrix.from_dense(torch.from_numpy(A0).to(dev), m, k_tile=c.k_tile, value_dtype=vd)
+                per = p0.algorithmic_bytes(512, b_bytes=4 if vd == F32 else 2)
+                replicas = max(min_replicas, -(-4 * L2_BYTES // per))
+                if As is None or len(As) < replicas:
+                    As = [A0] + [synth.row_skew(M, K, sp, seed=7000 + 10 * r + int(sp * 100) + 1, sigma=0.5, std=0.02)
+                                 for r in range(1, replicas)]
+                packs = [p0] + [PackedMatrix.from_dense(torch.from_numpy(A).to(dev), m, k_tile=c.k_tile, value_dtype=vd)
+                                for A in As[1:replicas]]
                 Bd = [B0.roll(r, 0).to(tdt) for r in range(replicas)]  # a distinct B per replica
                 Cd = [torch.empty((M, 512), device=dev) for _ in range(replicas)]
-                work = [(p, b, c, {}) for p, b, c in zip(packs, Bd, Cd)]
-                execute_batched(work)
-                torch.cuda.synchronize()
-                g = torch.cuda.CUDAGraph()
-                with torch.cuda.graph(g):
-                    execute_batched(work)
-                for _ in range(3):
-                    g.replay()
-                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                torch.cuda.synchronize()
-                e0.record()
-                for _ in range(steps):
-                    g.replay()
-                e1.record()
-                torch.cuda.synchronize()
-                sec = e0.elapsed_time(e1) / 1e3 / steps
+                work = [(p, b, cc, dict(nr=c.nr, warps=c.warps)) for p, b, cc in zip(packs, Bd, Cd)]
+                sec = timed(lambda: execute_batched(work))
                 bsz = 4 if vd == F32 else 2
                 nbytes = sum(p.algorithmic_bytes(512, b_bytes=bsz) for p in packs)
                 flops = sum(p.flops(512) for p in packs)
                 got = Cd[0].cpu().numpy()
                 Bq = Bd[0].cpu()
                 Bref = Bq.numpy() if vd == F32 else Bq.view(torch.int16).numpy().view(np.uint16)
-                want = O.Packed(O.Tables.of(m), As[0], k_tile=128, value_dtype=vd).execute(Bref)
+                want = O.Packed(O.Tables.of(m), A0, k_tile=c.k_tile, value_dtype=vd).execute(Bref)
                 row[name] = {"spmm_us": sec / replicas * 1e6, "gbs": nbytes / sec / 1e9,
                              "frac_of_measured_hbm": nbytes / sec / 1e9 / peak, "gflops": flops / sec / 1e9,
+                             "config": c.name(), "replicas": replicas,
+                             "working_set_mib": (nbytes + (0 if vd == F32 else 0)) / 2 ** 20,
                              "bit_exact_vs_oracle": bool(np.array_equal(got.view(np.uint32), want.view(np.uint32))),
                              "rel_err_vs_fp64": float(O.rel_err(got, exact))}
-                del packs, Bd, Cd, work, g
+                if name == "fp32":
+                    # the FP32-accurate hybrid with every panel on the tensor cores, same replicas
+                    hs = [HybridMatrix.from_dense(torch.from_numpy(A).to(dev), m, 0.0, k_tile=c.k_tile, value_dtype=F32)
+                          for A in As[:replicas]]
+                    Ch = [torch.empty((M, 512), device=dev) for _ in range(replicas)]
+                    hb = HybridBatch(list(zip(hs, Bd, Ch)))
+                    sec_h = timed(hb.run)
+                    gh = Ch[0].cpu().numpy()
+                    row["fp32_tensor_cores"] = {
+                        "spmm_us": sec_h / replicas * 1e6, "gbs": nbytes / sec_h / 1e9,
+                        "frac_of_measured_hbm": nbytes / sec_h / 1e9 / peak, "gflops": flops / sec_h / 1e9,
+                        "rel_err_vs_oracle": float(O.rel_err(gh, want)), "rel_err_vs_fp64": float(O.rel_err(gh, exact)),
+                        "path": "every panel as a split-FP16 tcgen05 product (hi.hi + hi.lo + lo.hi)"}
+                    del hs, Ch, hb
+                del packs, Bd, Cd, work
             rows.append(row)
     return rows
 
@@ -465,10 +566,13 @@ def layers_suite(dev, steps: int = 50) -> dict:
     """The 36 sparse linear layers of a 6-layer transformer (Q/K/V/O 512x512, FFN 2048x512 and
     512x2048) at 90 % row-skew sparsity, BF16 values and B, FP32 output, N per instance uniform in
     16..1024: the fixed-tile plain path (one launch per SpMM: M_r = 4, N_r = 64, untiled) against
-    one batched launch per step of autotuned packings, replayed from a CUDA graph."""
+    one step of autotuned layers -- M_r, nanokernel set, N_r, K tile, CTA tiling and tensor-core
+    threshold per layer -- with every register-tiled part in one batched launch and every
+    tensor-core part in one tcgen05 plan, replayed from a CUDA graph."""
     import torch
     from spreg import BF16, Mapping, PackedMatrix, execute_batched, synth
     from spreg.autotune import mapping_of, tune
+    from spreg.hybrid import DenseRowsPlan, HybridMatrix, bf16_items
     g = synth.rng(900)
     shapes = []
     for _ in range(6):
@@ -488,21 +592,37 @@ def layers_suite(dev, steps: int = 50) -> dict:
     for A, n, (M, K) in zip(As, ns, shapes):
         key = (M, K, min(1024, 1 << max(4, int(n - 1).bit_length())))  # tune once per shape and N octave
         if key not in cache:
-            cache[key] = tune(A, n, "bf16", top=6, device=dev).best
+            cache[key] = tune(A, n, "bf16", top=6, batch=4, device=dev).best
         c = cache[key]
         cfg.append(c)
-        tuned.append(PackedMatrix.from_dense(torch.from_numpy(A).to(dev), mapping_of(c.mr, c.mapping),
-                                             k_tile=c.k_tile, value_dtype=BF16))
+        At = torch.from_numpy(A).to(dev)
+        if c.tc_fill <= 1.0:
+            tuned.append(HybridMatrix.from_dense(At, mapping_of(c.mr, c.mapping), c.tc_fill, k_tile=c.k_tile,
+                                                 value_dtype=BF16))
+        else:
+            tuned.append(PackedMatrix.from_dense(At, mapping_of(c.mr, c.mapping), k_tile=c.k_tile, value_dtype=BF16))
     t_tune = time.perf_counter() - t0
 
     def plain_step():
         for p, B, C in zip(plain, Bs, Cp):
             p.execute(B, C, nr=64)
 
-    work = [(p, B, C, dict(nr=c.nr)) for p, B, C, c in zip(tuned, Bs, Cb, cfg)]
+    work, tc_rows = [], []
+    for t, B, C, c in zip(tuned, Bs, Cb, cfg):
+        if isinstance(t, HybridMatrix):
+            if t.tc_rows:
+                tc_rows.append((t.a_rows, t.row_index, B, C, B.shape[1], t.cols, False, 0))
+            if not t.all_tc:
+                work.append((t.packed, B, C, dict(nr=c.nr, warps=c.warps)))
+        else:
+            work.append((t, B, C, dict(nr=c.nr, warps=c.warps)))
+    plan = DenseRowsPlan(bf16_items(tc_rows)) if tc_rows else None
 
     def batched_step():
-        execute_batched(work)
+        if work:
+            execute_batched(work)  # register-tiled parts first: no load_c, the tensor-core rows follow
+        if plan is not None:
+            plan.run()
 
     def time_it(fn):
         for _ in range(3):
@@ -527,13 +647,20 @@ def layers_suite(dev, steps: int = 50) -> dict:
         batched_step()
     t_batched = time_it(graph.replay)
     err = max(float((a - b).norm() / max(b.norm(), 1e-30)) for a, b in zip(Cb, Cp))
+    # accuracy of every tuned layer against FP64 of its BF16 operands
+    err64 = 0.0
+    for A, B, C in zip(As, Bs, Cb):
+        Aq = torch.from_numpy(A).to(torch.bfloat16).double().to(dev)
+        ref = Aq @ B.double()
+        err64 = max(err64, float((C.double() - ref).norm() / ref.norm()))
     return {"workload": "36 layers (6 x Q/K/V/O 512x512, FFN 2048x512, 512x2048) @90% row-skew, BF16 values and B, "
                         "FP32 out, N uniform 16..1024 per layer",
             "plain_fixed_tile_us": t_plain, "batched_autotuned_graph_us": t_batched, "speedup": t_plain / t_batched,
             "plain_tflops": flops / t_plain / 1e6, "batched_tflops": flops / t_batched / 1e6,
             "plain_launches_per_step": len(plain), "tune_seconds": t_tune,
-            "configs": sorted({c.name() for c in cfg}),
-            "max_rel_diff_batched_vs_plain": err}
+            "layers_on_tensor_cores": sum(1 for c in cfg if c.tc_fill <= 1.0),
+            "per_layer_config": [{"shape": list(sh), "n": n, "config": c.name()} for sh, n, c in zip(shapes, ns, cfg)],
+            "max_rel_diff_batched_vs_plain": err, "max_rel_err_vs_fp64_of_bf16_operands": err64}
 
 
 def tensor_core_suite(dev, reps: int = 20) -> dict:
@@ -563,22 +690,6 @@ def tensor_core_suite(dev, reps: int = 20) -> dict:
     ref = a[:256].float() @ b.float()
     err = float((c[:256] - ref).norm() / ref.norm())
     tflops = 2.0 * M * N * K / us / 1e6
-    # the same product on single CTAs (no B tiles shared by CTA pairs), for comparison
-    from spreg.hybrid import set_tc_cluster
-    c1 = torch.empty_like(c)
-    set_tc_cluster(1)
-    try:
-        for _ in range(3):
-            dense_rows_bf16(a, idx, b, c1, check_rows=False)
-        torch.cuda.synchronize()
-        e0.record()
-        for _ in range(reps):
-            dense_rows_bf16(a, idx, b, c1, check_rows=False)
-        e1.record()
-        torch.cuda.synchronize()
-    finally:
-        set_tc_cluster(0)
-    us1 = e0.elapsed_time(e1) / reps * 1e3
     peak = None
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -591,9 +702,7 @@ def tensor_core_suite(dev, reps: int = 20) -> dict:
         hyb[f"{m}x{k}_n{n}"] = tune_tc_fill(A, Mapping.identity(2), n, k_tile=kt)
     return {"dense_bf16_4096^3_us": us, "tflops": tflops, "peak_tflops": peak,
             "frac_of_measured_peak": (tflops / peak) if peak else None,
-            "single_cta_us": us1, "single_cta_tflops": 2.0 * M * N * K / us1 / 1e6,
-            "single_cta_equal": bool(torch.equal(c, c1)),
-            "rel_err_vs_fp32_of_bf16_inputs": err, "includes": "API call: tcgen05 kernel reading B in place (N-major operand), CTA pairs sharing B tiles (automatic cluster mode), set-up and launch",
+            "rel_err_vs_fp32_of_bf16_inputs": err, "includes": "API call: tcgen05 kernel reading B in place (N-major operand), one CTA per SM, set-up and launch",
             "hybrid_threshold_serving_layers": hyb}
 
 
@@ -617,7 +726,7 @@ def cpu_baseline(As, Bs, args, seconds: float, threads: int = 0, mapping=None):
             packs[r] = O.Packed(t, As[r], k_tile=args.k_tile)
         pk = packs[r]
         s = time.perf_counter()
-        pk.execute(Bs[r], threads=threads)
+        pk.execute_fast(Bs[r], threads=threads)
         elapsed_run = time.perf_counter() - s
         done_bytes += algorithmic_bytes_oracle(pk, args.n)
         done_flops += 2 * pk.sizes["nnz"] * args.n
@@ -629,7 +738,9 @@ def cpu_baseline(As, Bs, args, seconds: float, threads: int = 0, mapping=None):
     return {"value": done_bytes / elapsed / 1e9, "unit": UNIT, "gflops": done_flops / elapsed / 1e9,
             "cores": threads if threads > 0 else O.max_threads(), "kind": "port",
             "sample": f"{runs} SpMMs of the workload ({len(packs)} distinct replicas), {elapsed:.1f} s of "
-                      "executor time, restated reference executor (oracle/spreg_oracle.c) with OpenMP over panels"}
+                      "executor time, the reference's register-tiled executor restated as SIMD code "
+                      "(oracle/spreg_cpu_fast.c: M_r x 16 accumulators in vector registers, one FMA block per "
+                      "nanokernel pattern, bit-identical to the checker) with OpenMP over panels"}
 
 
 def host_cpu() -> dict:
@@ -663,9 +774,15 @@ def cpu_baselines(As, Bs, args, mapping, seconds: float = 2.0) -> dict:
     nbytes = algorithmic_bytes_oracle(pk, args.n)
     flops = 2 * pk.sizes["nnz"] * args.n
     csr_bytes = v.size * 8 + rp.size * 4 + args.k * args.n * 4 + args.m * args.n * 4
-    out = {"host": host_cpu(), "sample": "replica 0 of the headline workload, median of 7 runs after 1 warm-up"}
-    legs = [("sop_executor", lambda th: pk.execute(Bs[0], threads=th), nbytes, (1, O.max_threads())),
-            ("csr_baseline", lambda th: O.csr_spmm(rp, ci, v, Bs[0], threads=th), csr_bytes, (1, O.max_threads()))]
+    out = {"host": host_cpu(), "sample": "replica 0 of the headline workload, median of 7 runs after 1 warm-up",
+           "legs": "simd: vector-register accumulators, FMAs contracted (-ffp-contract=fast), bit-identical to the "
+                   "scalar checker (explicit fmaf chain, -ffp-contract=off) that the parity tests use"}
+    legs = [("sop_executor_simd", lambda th: pk.execute_fast(Bs[0], threads=th), nbytes, (1, O.max_threads())),
+            ("csr_baseline_simd", lambda th: O.csr_spmm_fast(rp, ci, v, Bs[0], threads=th), csr_bytes,
+             (1, O.max_threads())),
+            ("sop_executor_scalar_checker", lambda th: pk.execute(Bs[0], threads=th), nbytes, (1, O.max_threads())),
+            ("csr_baseline_scalar", lambda th: O.csr_spmm(rp, ci, v, Bs[0], threads=th), csr_bytes,
+             (1, O.max_threads()))]
     if O.has_ref():  # the reference's own scalar CSR SpMM, compiled from its source where that exists
         legs.append(("spmm_naive", lambda th: O.ref_naive(rp, ci, v, Bs[0]), csr_bytes, (1,)))
     else:
@@ -685,6 +802,16 @@ def cpu_baselines(As, Bs, args, mapping, seconds: float = 2.0) -> dict:
     return out
 
 
+def workload_config(args, m, working_set: int) -> dict:
+    """`config` of the JSON line: the workload and its packing, the same in both arms."""
+    return {"workload": f"spmm_f32_{args.m}x{args.k}_s{args.sparsity}_n{args.n}_x{args.replicas}",
+            "replicas": args.replicas, "m": args.m, "k": args.k, "n": args.n, "sparsity": args.sparsity,
+            "mr": args.mr, "mapping": m.mapping_id,
+            "nanokernels": m.nanokernels if args.mapping != "identity" else "all", "k_tile": args.k_tile,
+            "l2": (f"inputs {'larger' if working_set > L2_BYTES else 'SMALLER'} than L2: working set "
+                   f"{working_set / 2**20:.0f} MiB per step vs {L2_BYTES / 2**20:.0f} MiB L2")}
+
+
 def run_reference(args):
     """--impl reference: the reference's CPU algorithm (restated; its own executor source is absent)."""
     ws, rank, _ = dist_env()
@@ -693,16 +820,17 @@ def run_reference(args):
     from oracle import oracle as O
     O.build(with_reference=False) if not os.path.exists(O.LIB_PATH) else None
     As, Bs = make_inputs(args, 0)
-    t = O.Tables.of(bench_mapping(args, As[0]))
+    m = bench_mapping(args, As[0])
+    t = O.Tables.of(m)
     packs = [O.Packed(t, A, k_tile=args.k_tile) for A in As]
     per_step = sum(algorithmic_bytes_oracle(p, args.n) for p in packs)
     for _ in range(args.warmup):
         for p, B in zip(packs, Bs):
-            p.execute(B)
+            p.execute_fast(B)
     t0 = time.perf_counter()
     for _ in range(args.steps):
         for p, B in zip(packs, Bs):
-            p.execute(B)
+            p.execute_fast(B)
     dt = time.perf_counter() - t0
     v = per_step * args.steps / dt / 1e9
     cores = O.max_threads()
@@ -710,14 +838,95 @@ def run_reference(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded row-skew sparse A, N(0,1) B)",
-            "config": {"workload": f"spmm_fp32_{args.m}x{args.k}_s{args.sparsity}_n{args.n}_x{args.replicas}",
-                       "replicas": args.replicas, "m": args.m, "k": args.k, "n": args.n, "sparsity": args.sparsity,
-                       "mr": args.mr, "mapping": args.mapping, "k_tile": args.k_tile},
+            "config": workload_config(args, m, per_step),
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": f"the full workload ({args.replicas} replicas) per step, restated reference "
-                                       "executor (oracle/spreg_oracle.c), OpenMP over all host threads"},
+                             "sample": f"the full workload ({args.replicas} replicas) per step, the reference's "
+                                       "register-tiled executor restated as SIMD code (oracle/spreg_cpu_fast.c, "
+                                       "bit-identical to the checker), OpenMP over all host threads",
+                             "host": host_cpu()},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
+
+
+def hybrid_leg(args, As, Bs, m, dev, step_bytes: int, step_flops: int, clk, peak: float, peak_kind: str) -> dict:
+    """The FP32-accurate hybrid on the headline workload: panels whose fill reaches the tuned threshold
+    run as split-FP16 tensor-core products (spreg_dense_rows_f32: hi.hi + hi.lo + lo.hi, FP32
+    accumulation), the others register-tiled; all replicas per step as one HybridBatch (register-tiled
+    parts in one batched launch, tensor-core parts as one reusable plan: B split + one tcgen05
+    launch), replayed from a CUDA graph.  Parity: rel err against the oracle's FP32 executor and
+    FP64 for replicas 0..3 (tolerance 1e-5)."""
+    import torch
+    from oracle import oracle as O
+    from spreg import F32
+    from spreg.hybrid import HybridBatch, HybridMatrix, tune_tc_fill
+    t0 = time.perf_counter()
+    tuned = tune_tc_fill(torch.from_numpy(As[0]).to(dev), m, args.n, fills=(1.01, 0.3, 0.2, 0.15, 0.1, 0.05, 0.0),
+                         k_tile=args.k_tile, value_dtype=F32, batch=16)
+    t_tune = time.perf_counter() - t0
+    fill = tuned["best_fill"] if args.tc_fill < 0 else args.tc_fill
+    hs = [HybridMatrix.from_dense(torch.from_numpy(A).to(dev), m, fill, k_tile=args.k_tile, value_dtype=F32)
+          for A in As]
+    Bd = [torch.from_numpy(B).to(dev) for B in Bs]
+    Cd = [torch.empty((args.m, args.n), device=dev) for _ in As]
+    batch = HybridBatch(list(zip(hs, Bd, Cd)))
+    batch.run()
+    torch.cuda.synchronize()
+    errs_ref, errs_64 = [], []
+    for r in range(min(4, len(As))):
+        got = Cd[r].cpu().numpy()
+        want = O.Packed(O.Tables.of(m), As[r], k_tile=args.k_tile).execute(Bs[r])
+        errs_ref.append(O.rel_err(got, want))
+        errs_64.append(O.rel_err(got, O.dense_fp64(As[r], Bs[r])))
+    stream = torch.cuda.current_stream()
+    graph = None
+    if not args.no_graph:
+        s2 = torch.cuda.Stream()
+        s2.wait_stream(stream)
+        with torch.cuda.stream(s2):
+            batch.run()
+        stream.wait_stream(s2)
+        torch.cuda.synchronize()
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph):
+            batch.run()
+        torch.cuda.synchronize()
+    run = graph.replay if graph is not None else batch.run
+    for _ in range(max(args.warmup, 3)):
+        run()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    lead = args.path == "hybrid"
+    if lead:
+        clk.mark_start()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        run()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    if lead:
+        clk.mark_end()
+    ms = ev0.elapsed_time(ev1)
+    step_s = ms / 1e3 / args.steps
+    tc_rows = sum(h.tc_rows for h in hs)
+    sparse_launch = any(not h.all_tc for h in hs)
+    kernels = ["split_cols_kernel", "tc_rows_kernel<256,true>"] + (["exec_tile_kernel"] if sparse_launch else [])
+    achieved = step_bytes / step_s / 1e9
+    # bytes the split path moves per SpMM (dense split A of the tensor-core rows, B read and its split
+    # pair written and read, C written), for comparison with the algorithmic bytes
+    moved = (tc_rows / len(hs)) * args.k * 4 + args.k * args.n * (4 + 4 + 4) + args.m * args.n * 4
+    return {"value": achieved, "ms": ms, "step_s": step_s, "spmm_us": step_s / len(hs) * 1e6,
+            "gflops": step_flops / step_s / 1e9, "tc_fill": fill, "tc_rows_per_spmm": tc_rows / len(hs),
+            "tuning": {"us_per_spmm_by_fill": tuned["us"], "best_fill": tuned["best_fill"], "seconds": t_tune,
+                       "timed_as": f"{tuned['batch']} SpMMs of replica 0 per HybridBatch run"},
+            "rel_err_vs_oracle_fp32_executor": max(errs_ref), "rel_err_vs_fp64": max(errs_64),
+            "tolerance": 1e-5, "within_tolerance": max(errs_ref) <= 1e-5 and max(errs_64) <= 1e-5,
+            "cuda_graph": graph is not None, "launches_per_step": len(kernels),
+            "kernels": kernels, "split_path_bytes_per_spmm": moved,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "peak_source": f"{peak_kind} hbm_gbs", "kernel": "spreg::tc_rows_kernel<256,true>",
+                         "timing": "per step (B split launch + tensor-core launch); the tensor-core kernel's share "
+                                   "of the step is in the ncu launch list summary",
+                         "algorithmic_bytes_per_step": step_bytes, "launch_us": step_s * 1e6}}
 
 
 def main():
@@ -798,23 +1007,33 @@ def main():
             torch.distributed.barrier()
         ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()
-        clk.mark_start()
+        if args.path == "register":
+            clk.mark_start()
         ev0.record(stream)
         for _ in range(args.steps):
             run()
         ev1.record(stream)
         torch.cuda.synchronize()
-        clk.mark_end()
-    ms = max_over_ranks(ev0.elapsed_time(ev1), dev)  # replicas: the job takes as long as its slowest rank
+        if args.path == "register":
+            clk.mark_end()
+        peak, peak_kind = measured_peaks()
+        hyb = None
+        if args.path == "hybrid":
+            if ws > 1:
+                torch.distributed.barrier()
+            hyb = hybrid_leg(args, As, Bs, m, dev, step_bytes, step_flops, clk, peak, peak_kind)
+    ms_reg = max_over_ranks(ev0.elapsed_time(ev1), dev)  # replicas: the job takes as long as its slowest rank
+    ms = max_over_ranks(hyb["ms"], dev) if hyb is not None else ms_reg
     if ws > 1:
         torch.distributed.barrier()
-    sec = ms / 1e3
+    sec = ms_reg / 1e3
     value = whole_job_rate(step_bytes, args.steps, ws, ms) / 1e9
     gflops = whole_job_rate(step_flops, args.steps, ws, ms) / 1e9
     ms_per_step = ms / args.steps
+    value_reg = whole_job_rate(step_bytes, args.steps, ws, ms_reg) / 1e9
+    gflops_reg = whole_job_rate(step_flops, args.steps, ws, ms_reg) / 1e9
 
     # roofline of the executor kernel (one launch per replica per step)
-    peak, peak_kind = measured_peaks()
     launch_s = sec / (args.steps * launches_per_step)
     achieved = (step_bytes / launches_per_step) / launch_s / 1e9
     spmm_us = sec / (args.steps * len(packs)) * 1e6
@@ -829,7 +1048,7 @@ def main():
                                                     "bf16,bf16,float"),
                 "spmm_us": spmm_us, "launches_per_step": launches_per_step,
                 "algorithmic_bytes_per_launch": step_bytes / launches_per_step,
-                "flops_per_launch": step_flops / launches_per_step, "gflops": gflops,
+                "flops_per_launch": step_flops / launches_per_step, "gflops": gflops_reg,
                 "launch_us": launch_s * 1e6}
 
     # e2e through the host-buffer C ABI (MatMulSpecialized operator()(C, B))
@@ -884,6 +1103,7 @@ def main():
     # the secondary legs describe one GPU: rank 0 alone runs them, the other ranks are done
     lead = rank == 0
     csr_leg = csr_baseline_leg(As[0], Bd[0], packs[0], args, spmm_us) if (lead and args.dtype == "f32") else None
+    cfg1 = config1_leg(dev) if lead else None
     serving = serving_bench(args, dev) if (lead and args.serving) else None
     precision = precision_suite(dev) if (lead and args.precision) else None
     tensor_cores = tensor_core_suite(dev) if (lead and args.tensor_cores) else None
@@ -899,24 +1119,35 @@ def main():
     if args.staging == 1:
         roofline["smem"] = smem_roofline(packs, args.n, bsz, args.k_tile, spmm_us / 1e6, clocks.get("sm_mhz"))
     if rank == 0:
+        reg = {"value": value_reg, "unit": UNIT, "gflops": gflops_reg, "ms_per_step": ms_reg / args.steps,
+               "roofline": roofline, "parity_bit_exact_vs_oracle": parity_ok,
+               "nr": args.nr or "auto", "b_staging": {0: "auto", 1: "shared-memory B tiles", 2: "L1/L2"}[args.staging],
+               "cuda_graph": graph is not None, "batched_launch": bool(args.batched),
+               "launches_per_step": launches_per_step}
+        cfg = workload_config(args, m, working_set) | {"parallelism": f"replicas x{ws}"}
+        if hyb is not None:
+            path = ("FP32-accurate hybrid: panels with fill >= %g as split-FP16 tcgen05 products (hi.hi + hi.lo + "
+                    "lo.hi, FP32 accumulation; rel err <= 1e-5 vs the reference executor and FP64), the rest "
+                    "register-tiled" % hyb["tc_fill"])
+            launches = hyb["launches_per_step"] * args.steps
+            head_roof = hyb.pop("roofline")
+            head_roof["traffic"] = load_traffic(f"tc_rows_kernel_split/f32/{args.m}x{args.k}/n{args.n}", len(packs))
+            parity = hyb["within_tolerance"]
+        else:
+            path = "register-tiled executor (bit-exact with the reference executor's FMA order)"
+            launches = launches_per_step * args.steps
+            head_roof = roofline
+            parity = parity_ok
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": args.dtype, "data": "synthetic (seeded row-skew sparse A, N(0,1) B)",
-                "config": {"workload": f"spmm_{args.dtype}_{args.m}x{args.k}_s{args.sparsity}_n{args.n}_x{args.replicas}",
-                           "replicas": args.replicas, "m": args.m, "k": args.k, "n": args.n,
-                           "sparsity": args.sparsity, "mr": args.mr, "mapping": m.mapping_id,
-                           "nanokernels": m.nanokernels if args.mapping != "identity" else "all", "nr": args.nr or "auto",
-                           "b_staging": {0: "auto", 1: "shared-memory B tiles", 2: "L1/L2"}[args.staging],
-                           "k_tile": args.k_tile,
-                           "cuda_graph": graph is not None, "batched_launch": bool(args.batched),
-                           "l2": f"inputs larger than L2: working set {working_set / 2**20:.0f} MiB per step "
-                                 f"vs {L2_BYTES / 2**20:.0f} MiB L2",
-                           "parallelism": f"replicas x{ws}"},
-                "gflops": gflops, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "serving": serving,
+                "config": cfg, "path": path,
+                "gflops": gflops, "roofline": head_roof, "hybrid": hyb, "bit_exact_register_tiled": reg,
+                "cpu_baseline": cpu, "e2e": e2e, "serving": serving,
                 "precision": precision, "batched_layers": layers, "tensor_cores": tensor_cores,
-                "ffn_sparsity_sweep": sweep, "gpu_csr_baseline": csr_leg,
-                "clocks": clocks, "gpu_launches": launches_per_step * args.steps,
-                "parity_bit_exact_vs_oracle": parity_ok}
+                "ffn_sparsity_sweep": sweep, "gpu_csr_baseline": csr_leg, "config1_minimum_slice": cfg1,
+                "clocks": clocks, "gpu_launches": launches,
+                "parity": parity}
         print(json.dumps(line))
     if ws > 1:
         torch.distributed.destroy_process_group()

@@ -211,7 +211,9 @@ typedef struct {
     int32_t load_c;      /* 1: C += A.B (template:290-297 load_c) ; 0: C = A.B */
     int32_t epilogue;    /* SPREG_EPILOGUE_* applied to the stored result */
     int32_t nr;          /* columns per warp strip: 32, 64, 128 or 256; 0 = automatic */
-    int32_t warps_per_cta; /* 1..8 for the L1/L2 kernel; 0 = automatic */
+    int32_t warps_per_cta; /* CTA tiling, 1..8; 0 = automatic: warps per CTA of the batched and
+                              register-stream kernels (8 and 4 by default), consumer warps (row panels
+                              per job) of the B-tile kernel (15 by default) */
     int32_t b_staging;   /* 0 automatic, 1 stage B strips in shared memory (bulk copies), 2 read B via L1/L2 */
     int32_t meta_staging; /* 0 automatic, 1 stage each panel's execution block in shared memory, 2 stream
                              the packed arena through registers */
@@ -314,14 +316,16 @@ typedef struct {
 int spreg_dense_rows_f32(const spreg_dense_rows_f32_item *item, spreg_stream_t stream);
 int spreg_dense_rows_f32_batched(const spreg_dense_rows_f32_item *items, int32_t num_items, spreg_stream_t stream);
 
-/* A reusable plan of spreg_dense_rows_f32_batched for a fixed item list (the same pointers every
- * run): its scratch, tensor maps and device tables are made once (synchronising `stream`), so a run
- * is two kernel launches and no host-side work, and can be captured in a CUDA graph.  The plan
- * belongs to the device current at creation; runs of one plan must not overlap on the GPU (they
- * share its scratch). */
+/* A reusable plan of spreg_dense_rows_f32_batched / spreg_dense_rows_bf16_batched for a fixed item
+ * list (the same pointers every run): its scratch, tensor maps and device tables are made once
+ * (synchronising `stream`), so a run is its kernel launches (B preparation, tensor-core launches)
+ * and no host-side work, and can be captured in a CUDA graph.  The plan belongs to the device
+ * current at creation; runs of one plan must not overlap on the GPU (they share its scratch). */
 typedef struct spreg_dense_rows_plan spreg_dense_rows_plan;
 int spreg_dense_rows_f32_plan_create(const spreg_dense_rows_f32_item *items, int32_t num_items,
                                      spreg_dense_rows_plan **out, spreg_stream_t stream);
+int spreg_dense_rows_bf16_plan_create(const spreg_dense_rows_item *items, int32_t num_items,
+                                      spreg_dense_rows_plan **out, spreg_stream_t stream);
 int spreg_dense_rows_plan_run(const spreg_dense_rows_plan *plan, spreg_stream_t stream);
 void spreg_dense_rows_plan_destroy(spreg_dense_rows_plan *plan);
 

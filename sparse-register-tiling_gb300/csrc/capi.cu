@@ -21,6 +21,7 @@ int dense_rows_batched_impl(const spreg_dense_rows_item *, int32_t, cudaStream_t
 int dense_rows_f32_batched_impl(const spreg_dense_rows_f32_item *, int32_t, cudaStream_t);
 int split_rows_f32_impl(const float *, int64_t, int64_t, int64_t, void *, int64_t, float *, cudaStream_t);
 int tc_plan_create_f32_impl(const spreg_dense_rows_f32_item *, int32_t, void **, cudaStream_t);
+int tc_plan_create_bf16_impl(const spreg_dense_rows_item *, int32_t, void **, cudaStream_t);
 int tc_plan_run_impl(const void *, cudaStream_t);
 void tc_plan_destroy_impl(void *);
 int pack_from_arena_impl(const spreg_mapping *, const spreg_arena_geom *, const void *, int64_t,
@@ -272,6 +273,12 @@ int spreg_dense_rows_f32_plan_create(const spreg_dense_rows_f32_item *items, int
                                      spreg_dense_rows_plan **out, spreg_stream_t stream) {
     clear_error();
     return tc_plan_create_f32_impl(items, num_items, reinterpret_cast<void **>(out), (cudaStream_t)stream);
+}
+
+int spreg_dense_rows_bf16_plan_create(const spreg_dense_rows_item *items, int32_t num_items,
+                                      spreg_dense_rows_plan **out, spreg_stream_t stream) {
+    clear_error();
+    return tc_plan_create_bf16_impl(items, num_items, reinterpret_cast<void **>(out), (cudaStream_t)stream);
 }
 
 int spreg_dense_rows_plan_run(const spreg_dense_rows_plan *plan, spreg_stream_t stream) {

@@ -1160,13 +1160,10 @@ struct TcPlanHandle {
     int device = -1;
 };
 
-int tc_plan_create_f32_impl(const spreg_dense_rows_f32_item *items, int32_t count, void **out, cudaStream_t stream) {
-    SPREG_CHECK_ARG(out && count >= 0 && (count == 0 || items), "bad arguments");
-    *out = nullptr;
-    auto *h = new TcPlanHandle;
+namespace {
+
+int tc_plan_create(TcPlanHandle *h, void **out, cudaStream_t stream) {
     TcPlan &pl = h->pl;
-    pl.split = true;
-    for (int32_t i = 0; i < count; ++i) pl.items.push_back(from_f32(items[i]));
     int st = tc_plan_build(pl);
     int *status = nullptr;
     if (!st && !pl.groups.empty()) status = device_status_word(&st);
@@ -1195,6 +1192,26 @@ int tc_plan_create_f32_impl(const spreg_dense_rows_f32_item *items, int32_t coun
     }
     *out = h;
     return SPREG_OK;
+}
+
+}  // namespace
+
+int tc_plan_create_f32_impl(const spreg_dense_rows_f32_item *items, int32_t count, void **out, cudaStream_t stream) {
+    SPREG_CHECK_ARG(out && count >= 0 && (count == 0 || items), "bad arguments");
+    *out = nullptr;
+    auto *h = new TcPlanHandle;
+    h->pl.split = true;
+    for (int32_t i = 0; i < count; ++i) h->pl.items.push_back(from_f32(items[i]));
+    return tc_plan_create(h, out, stream);
+}
+
+int tc_plan_create_bf16_impl(const spreg_dense_rows_item *items, int32_t count, void **out, cudaStream_t stream) {
+    SPREG_CHECK_ARG(out && count >= 0 && (count == 0 || items), "bad arguments");
+    *out = nullptr;
+    auto *h = new TcPlanHandle;
+    h->pl.split = false;
+    for (int32_t i = 0; i < count; ++i) h->pl.items.push_back(from_bf16(items[i]));
+    return tc_plan_create(h, out, stream);
 }
 
 int tc_plan_run_impl(const void *plan, cudaStream_t stream) {

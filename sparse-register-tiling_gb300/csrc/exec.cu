@@ -284,6 +284,7 @@ struct CallPlan {
     int64_t xbuf;            // per-warp buffer for this pack
     ExecParams sp;           // parameters of the register-stream kernel
     int warps;
+    int warps_req;           // warps_per_cta as asked (0: each kernel's own choice) -- the CTA tiling
 };
 
 int plan_call(const spreg_packed *a, const spreg_exec_args *args, CallPlan *cp, int64_t others1) {
@@ -322,6 +323,7 @@ int plan_call(const spreg_packed *a, const spreg_exec_args *args, CallPlan *cp, 
     cp->mr = in.mr;
     cp->combo = combo;
     cp->warps = args->warps_per_cta > 0 ? args->warps_per_cta : 4;
+    cp->warps_req = args->warps_per_cta > 0 ? args->warps_per_cta : 0;
     SPREG_CHECK_ARG(cp->warps >= 1 && cp->warps <= 8, "warps_per_cta must be in [1, 8]");
     cp->xbuf = (a->max_exec_bytes + 127) / 128 * 128;
     const bool x_fits = a->exec && 1024 + 2 * cp->xbuf <= f->smem_optin;
@@ -497,6 +499,7 @@ int launch_stream(const CallPlan &cp, cudaStream_t stream) {
 // One batch-kernel launch per group of at most kMaxBatchProblems problems of one configuration.
 struct Group {
     int mr, combo, nv;
+    int warps_req = 0;  // warps per CTA asked by the first call that asked (0: 8)
     std::vector<XProblem> probs;
     int64_t xbuf = 0;
 };
@@ -523,8 +526,8 @@ int launch_groups(std::map<std::tuple<int, int, int>, Group> &groups, cudaStream
             bp.xbuf = (int32_t)g.xbuf;
             bp.status = f->status;
             bp.counter = next_counter(f);
-            // warps per CTA: 8, fewer if the buffers do not fit
-            int nw = 8;
+            // warps per CTA: as asked, else 8; fewer if the buffers do not fit
+            int nw = g.warps_req > 0 ? g.warps_req : 8;
             while (nw > 1 && 1024 + 2 * g.xbuf * nw > f->smem_optin) nw >>= 1;
             const size_t smem = (size_t)(1024 + 2 * g.xbuf * nw);
             const int threads = 32 * nw;
@@ -541,6 +544,7 @@ int launch_groups(std::map<std::tuple<int, int, int>, Group> &groups, cudaStream
 // One tile-kernel launch per group of at most kMaxBatchProblems problems of one configuration.
 struct TileGroup {
     int mr, combo, nv;
+    int warps_req = 0;  // consumer warps (panels per job) asked by the first call that asked (0: 16)
     std::vector<TProblem> probs;
     int64_t xbuf = 0, stage_b = 0;
 };
@@ -551,8 +555,8 @@ int launch_tile_groups(std::map<std::tuple<int, int, int>, TileGroup> &groups, c
     if (st) return st;
     for (auto &kv : groups) {
         TileGroup &g = kv.second;
-        // consumer warps: 16, fewer if the stages do not fit
-        int W = kTileMaxWarps;
+        // consumer warps: as asked, else 16; fewer if the stages do not fit
+        int W = g.warps_req > 0 ? std::min(g.warps_req, kTileMaxWarps) : kTileMaxWarps;
         auto smem_for = [&](int w) { return (int64_t)1024 + kTileStages * (g.stage_b + (int64_t)w * g.xbuf); };
         while (W > 1 && smem_for(W) > f->smem_optin) W >>= 1;
         SPREG_CHECK_ARG(smem_for(W) <= f->smem_optin, "shared-memory B tiles: a stage does not fit (%lld bytes)",
@@ -594,6 +598,7 @@ void add_tile_call(std::map<std::tuple<int, int, int>, TileGroup> &groups, const
         g.mr = cp.mr;
         g.combo = cp.combo;
         g.nv = nv;
+        if (!g.warps_req) g.warps_req = cp.warps_req;
         g.probs.push_back(pr);
         g.xbuf = std::max(g.xbuf, cp.xbuf);
         g.stage_b = std::max(g.stage_b, stage_b);
@@ -608,6 +613,7 @@ void add_call(std::map<std::tuple<int, int, int>, Group> &groups, const CallPlan
         g.mr = cp.mr;
         g.combo = cp.combo;
         g.nv = nv;
+        if (!g.warps_req) g.warps_req = cp.warps_req;
         g.probs.push_back(pr);
         g.xbuf = std::max(g.xbuf, cp.xbuf);
     };

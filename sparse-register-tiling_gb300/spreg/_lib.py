@@ -118,6 +118,7 @@ PROTOTYPES = {
     "spreg_dense_rows_f32": (C.c_int, [C.POINTER(DenseRowsF32Item), P]),
     "spreg_dense_rows_f32_batched": (C.c_int, [P, C.c_int32, P]),
     "spreg_dense_rows_f32_plan_create": (C.c_int, [P, C.c_int32, C.POINTER(P), P]),
+    "spreg_dense_rows_bf16_plan_create": (C.c_int, [P, C.c_int32, C.POINTER(P), P]),
     "spreg_dense_rows_plan_run": (C.c_int, [P, P]),
     "spreg_dense_rows_plan_destroy": (None, [P]),
     "spreg_pack_from_arena": (C.c_int, [P, C.POINTER(ArenaGeom), P, C.c_int64, P, C.c_int64, P, C.c_int64,

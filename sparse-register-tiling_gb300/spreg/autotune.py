@@ -15,12 +15,19 @@ panel, stands for the critical path of one warp when there are too few items to 
 GPU.  One coefficient set per (M_r, NV, value/B type); `fit_costs` solves non-negative least
 squares over measured samples.
 
-For M_r = 8 the candidates also include a nanokernel set built for the matrix from its pattern
-histogram (`kernel_sets.greedy_kernel_set`, the reference's set-cover model in greedy form).
+For M_r = 8, and for K-tiled M_r = 4 packs, the candidates also include a nanokernel set built for
+the matrix from its pattern histogram (`kernel_sets.greedy_kernel_set`, the reference's set-cover
+model in greedy form; for K-tiled M_r = 4 with the B-tile executor's penalty for patterns without a
+loop of their own).
+
+Beyond the reference's M_r / N_r / mapping, a candidate carries the CTA tiling (`warps`: warps per
+CTA of the batched kernel, row panels per job of the B-tile kernel) and a tensor-core threshold
+(`tc_fill`: panels whose fill reaches it run as dense tcgen05 products, `spreg.hybrid`).
 
 `tune` ranks every candidate with the model, times the best few on the device with the reference's
-timing protocol (`execute_timed`: median of repeated runs), and returns the fastest, so a poor
-model costs tuning time, not speed.
+timing protocol (`execute_timed`: median of repeated runs) or as a batch, then times the CTA tiling
+of the best and the tensor-core thresholds (all panels; the densest tenth), and returns the
+fastest, so a poor model costs tuning time, not speed.
 """
 from __future__ import annotations
 
@@ -48,6 +55,8 @@ class Candidate:
     mapping: str     # "identity" or a mapping id
     nr: int          # strip width: 32, 64, 128 or (16-bit B, K_c <= 128) 256 columns
     k_tile: int = 0  # K_c of the packing (0: one K tile)
+    warps: int = 0   # CTA tiling (spreg_exec_args.warps_per_cta; 0: the executor's choice)
+    tc_fill: float = 2.0  # panels with fill >= tc_fill on the tensor cores (> 1: none)
 
     @property
     def nv(self) -> int:
@@ -56,7 +65,8 @@ class Candidate:
     def name(self) -> str:
         """The reference's method grammar, M{Mr}N{nr}_{mapping} (tools/paper/configs.py:54-68), with
         the K tile appended as _K{K_c} when the packing is K-tiled."""
-        return f"M{self.mr}N{self.nr}_{self.mapping}" + (f"_K{self.k_tile}" if self.k_tile else "")
+        return (f"M{self.mr}N{self.nr}_{self.mapping}" + (f"_K{self.k_tile}" if self.k_tile else "") +
+                (f"_W{self.warps}" if self.warps else "") + (f"_TC{self.tc_fill:g}" if self.tc_fill <= 1.0 else ""))
 
 
 # Mappings built in this process (greedy sets from a matrix's histogram), by mapping id.
@@ -71,13 +81,13 @@ def mapping_of(mr: int, name: str) -> Mapping:
     return Mapping.load(name)
 
 
-def greedy_mapping(mask: np.ndarray, mr: int, budget: int = 19, k_c: int = 128) -> Mapping:
+def greedy_mapping(mask: np.ndarray, mr: int, budget: int = 19, k_c: int = 128, tile: bool = False) -> Mapping:
     """Nanokernel set for this matrix from its pattern histogram (`kernel_sets`), registered under
-    its mapping id so that `mapping_of` finds it."""
+    its mapping id so that `mapping_of` finds it.  `tile`: for the B-tile executor (K-tiled packs)."""
     from .kernel_sets import executor_penalty, greedy_kernel_set
     hist = np.bincount(panel_codes(mask, mr).ravel(), minlength=2 ** mr)
     units = ((mask.shape[0] + mr - 1) // mr) * max(1, math.ceil(mask.shape[1] / k_c))
-    m = greedy_kernel_set(hist, mr, budget, units, penalty=executor_penalty(mr))
+    m = greedy_kernel_set(hist, mr, budget, units, penalty=executor_penalty(mr, tile=tile))
     GENERATED[m.mapping_id] = m
     return m
 
@@ -277,6 +287,11 @@ def rank(mask: np.ndarray, n: int, dtype: str = "f32", costs: Optional[Costs] = 
     if greedy and 8 in tuple(mrs):
         gid = greedy_mapping(mask, 8).mapping_id
         cands += [Candidate(c.mr, gid, c.nr, c.k_tile) for c in cands if c.mr == 8 and c.mapping == "identity"]
+    if greedy and 4 in tuple(mrs):
+        gid4 = greedy_mapping(mask, 4, budget=15, tile=True).mapping_id
+        if gid4 != mapping_of(4, "identity").mapping_id:
+            cands += [Candidate(c.mr, gid4, c.nr, c.k_tile) for c in cands
+                      if c.mr == 4 and c.mapping == "identity" and c.k_tile]
     for c in cands:
         key = (c.mr, c.mapping)
         if key not in stats:
@@ -292,11 +307,11 @@ def rank(mask: np.ndarray, n: int, dtype: str = "f32", costs: Optional[Costs] = 
     return ranked, stats
 
 
-def _time_batched(pm, Bs, Cs, nr: int, reps: int = 5) -> float:
+def _time_batched(pm, Bs, Cs, nr: int, reps: int = 5, warps: int = 0) -> float:
     """ns per SpMM of len(Bs) SpMMs of one packed matrix in one batched call (CUDA events)."""
     import torch
     from .packed import execute_batched
-    work = [(pm, b, c, dict(nr=nr)) for b, c in zip(Bs, Cs)]
+    work = [(pm, b, c, dict(nr=nr, warps=warps)) for b, c in zip(Bs, Cs)]
     execute_batched(work)
     s = torch.cuda.current_stream()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -308,13 +323,55 @@ def _time_batched(pm, Bs, Cs, nr: int, reps: int = 5) -> float:
     return e0.elapsed_time(e1) * 1e6 / (reps * len(Bs))
 
 
+def _time_tc(At, mapping: Mapping, n: int, dtype: str, fill: float, k_tile: int, nb: int, reps: int = 5) -> float:
+    """ns per SpMM of the hybrid at threshold `fill`: nb SpMMs of A with distinct B as one HybridBatch
+    (one batched register-tiled launch, one tensor-core plan), CUDA events."""
+    import torch
+    from . import _lib
+    from .hybrid import HybridBatch, HybridMatrix
+    vd = _lib.BF16 if dtype == "bf16" else _lib.F32
+    h = HybridMatrix.from_dense(At, mapping, fill, k_tile=k_tile, value_dtype=vd)
+    tdt = torch.bfloat16 if dtype == "bf16" else torch.float32
+    Bs = [torch.randn((At.shape[1], n), device=At.device).to(tdt) for _ in range(nb)]
+    Cs = [torch.empty((At.shape[0], n), device=At.device) for _ in range(nb)]
+    hb = HybridBatch([(h, b, c) for b, c in zip(Bs, Cs)])
+    hb.run()
+    s = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(reps):
+        hb.run()
+    e1.record(s)
+    e1.synchronize()
+    return e0.elapsed_time(e1) * 1e6 / (reps * nb)
+
+
+def tc_predict_ns(mask: np.ndarray, n: int, dtype: str, fill: float, mr: int) -> Tuple[float, float]:
+    """(predicted ns of the tensor-core part, share of the nonzeros it takes) at threshold `fill`:
+    dense products of the panels at or above it at a sustained tensor-core rate (three FP16 passes
+    for the FP32-accurate split) plus set-up."""
+    m, k = mask.shape
+    P = (m + mr - 1) // mr
+    nz = np.zeros(P * mr)
+    nz[:m] = mask.sum(axis=1)
+    pf = nz.reshape(P, mr).sum(axis=1) / float(mr * max(k, 1))
+    sel = pf >= fill
+    rows = int(sel.sum()) * mr
+    passes = 3 if dtype == "f32" else 1
+    rate = 0.9e15  # FLOP/s, dense products of these sizes through the plan
+    share = float(nz.reshape(P, mr).sum(axis=1)[sel].sum() / max(nz.sum(), 1))
+    return 3000.0 + 2.0 * rows * k * n * passes / rate * 1e9, share
+
+
 def tune(A: np.ndarray, n: int, dtype: str = "f32", top: int = 4, costs: Optional[Costs] = None,
          mrs: Iterable[int] = (2, 4, 8), k_tiles: Iterable[int] = K_TILES, runs: int = 1, batch: int = 1,
-         device=None) -> TuneResult:
+         device=None, tc: bool = True, warps: bool = True) -> TuneResult:
     """Pick the fastest candidate for weight A (M x K, float32, zeros pruned) and n columns of B:
     rank by the cost model, then time the ``top`` best on the device -- one SpMM at a time with
     the reference's protocol (execute_timed) when ``batch`` is 1, else ``batch`` SpMMs of A with
-    distinct B in one batched launch, as a serving loop runs them."""
+    distinct B in one batched launch, as a serving loop runs them.  Then (``warps``) the CTA tiling
+    of the best register-tiled candidate, and (``tc``) the tensor-core thresholds: every panel, and
+    the densest tenth of the panels, each timed as a batch of SpMMs through `spreg.hybrid`."""
     import torch
     from . import _lib
     from .packed import PackedMatrix
@@ -328,17 +385,49 @@ def tune(A: np.ndarray, n: int, dtype: str = "f32", top: int = 4, costs: Optiona
     Cs = [torch.empty((A.shape[0], n), device=dev, dtype=tdt if nb > 1 else torch.float32) for _ in range(nb)]
     packs = {}
     measured = {}
-    for _, c in ranked[:max(1, top)]:
+    by_name = {c.name(): c for _, c in ranked}
+
+    def time_reg(c):
         key = (c.mr, c.mapping, c.k_tile)
         if key not in packs:
             packs[key] = PackedMatrix.from_dense(At, mapping_of(c.mr, c.mapping), k_tile=c.k_tile, value_dtype=vd)
         if nb == 1:
-            measured[c.name()] = packs[key].execute_timed(Bs[0], Cs[0], num_runs=runs, nr=c.nr)
-        else:
-            measured[c.name()] = _time_batched(packs[key], Bs, Cs, c.nr)
+            return packs[key].execute_timed(Bs[0], Cs[0], num_runs=runs, nr=c.nr, warps=c.warps)
+        return _time_batched(packs[key], Bs, Cs, c.nr, warps=c.warps)
+
+    for _, c in ranked[:max(1, top)]:
+        measured[c.name()] = time_reg(c)
+    best_reg = by_name[min(measured, key=measured.get)]
+    if warps:
+        # CTA tiling: fewer warps per CTA for the batched kernel (8 by default), fewer row panels per
+        # job for the B-tile kernel (15 by default)
+        for w in ((4,) if best_reg.k_tile == 0 else (8,)):
+            c = dataclasses.replace(best_reg, warps=w)
+            by_name[c.name()] = c
+            measured[c.name()] = time_reg(c)
+    best_reg = by_name[min(measured, key=measured.get)]
+    predicted = {c.name(): t for t, c in ranked}
+    if tc and n >= 16:
+        mask = A != 0
+        mr = best_reg.mr
+        P = (A.shape[0] + mr - 1) // mr
+        nz = np.zeros(P * mr)
+        nz[:A.shape[0]] = mask.sum(axis=1)
+        pf = nz.reshape(P, mr).sum(axis=1) / float(mr * max(A.shape[1], 1))
+        fills = sorted({0.0, float(np.quantile(pf, 0.9))}) if P > 1 else [0.0]
+        reg_mapping = mapping_of(best_reg.mr, best_reg.mapping)
+        reg_ns = measured[best_reg.name()]
+        for f in fills:
+            c = dataclasses.replace(best_reg, tc_fill=f)
+            t_tc, share = tc_predict_ns(mask, n, dtype, f, mr)
+            predicted[c.name()] = t_tc + (1.0 - share) * reg_ns  # the register-tiled rest at its measured rate
+            if predicted[c.name()] > 3.0 * reg_ns:
+                continue  # the model rules it out
+            by_name[c.name()] = c
+            measured[c.name()] = _time_tc(At, reg_mapping, n, dtype, f, best_reg.k_tile, max(nb, 4))
     best_name = min(measured, key=measured.get)
-    best = next(c for _, c in ranked if c.name() == best_name)
-    return TuneResult(best=best, predicted_ns={c.name(): t for t, c in ranked}, measured_ns=measured,
+    best = by_name[best_name]
+    return TuneResult(best=best, predicted_ns=predicted, measured_ns=measured,
                       stats={f"M{k[0]}_{k[1]}": {"P": s.P, "U": s.U, "V": s.V, "G": s.G, "padding": s.padding}
                              for k, s in stats.items()})
 

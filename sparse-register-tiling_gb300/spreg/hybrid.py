@@ -115,16 +115,33 @@ def dense_rows_f32(a_split, row_scale, row_index, B, C, n: Optional[int] = None,
     return C
 
 
+def bf16_items(rows) -> np.ndarray:
+    """spreg_dense_rows_item records (numpy) of BF16 products [(a_rows, row_index, B, C, n, k, load_c,
+    epilogue), ...] (CUDA tensors; C float32 or BF16)."""
+    import torch
+    from .serving import TC_ITEM_DTYPE
+    it = np.zeros(len(rows), dtype=TC_ITEM_DTYPE)
+    for i, (a, idx, B, C, n, k, load_c, epi) in enumerate(rows):
+        it[i] = (a.data_ptr(), a.shape[0], k, a.stride(0), idx.data_ptr(), B.data_ptr(), B.stride(0), C.data_ptr(),
+                 C.stride(0), n, _lib.F32 if C.dtype == torch.float32 else _lib.BF16, int(bool(load_c)), int(epi), 0)
+    return it
+
+
 class DenseRowsPlan:
-    """A reusable plan of FP32-accurate products over fixed tensors (spreg_dense_rows_f32_plan_create):
-    a run is the B split and the tensor-core launch, with no host-side preparation (capturable)."""
+    """A reusable plan of tensor-core products over fixed tensors (spreg_dense_rows_f32_plan_create for
+    FP32-accurate items, spreg_dense_rows_bf16_plan_create for a numpy array of BF16 items): a run is
+    the B preparation and the tensor-core launches, with no host-side work (capturable)."""
 
     def __init__(self, items, stream=None):
         import ctypes
-        arr = (_lib.DenseRowsF32Item * max(1, len(items)))(*items)
         h = ctypes.c_void_p()
-        _lib.check(_lib.lib().spreg_dense_rows_f32_plan_create(arr, len(items), ctypes.byref(h),
-                                                               _lib.stream_handle(stream)))
+        if isinstance(items, np.ndarray):
+            _lib.check(_lib.lib().spreg_dense_rows_bf16_plan_create(items.ctypes.data, len(items), ctypes.byref(h),
+                                                                    _lib.stream_handle(stream)))
+        else:
+            arr = (_lib.DenseRowsF32Item * max(1, len(items)))(*items)
+            _lib.check(_lib.lib().spreg_dense_rows_f32_plan_create(arr, len(items), ctypes.byref(h),
+                                                                   _lib.stream_handle(stream)))
         self._h = h
 
     def run(self, stream=None) -> None:
@@ -241,19 +258,26 @@ class HybridMatrix:
 
 
 class HybridBatch:
-    """Many FP32 hybrid SpMMs C_i = A_i . B_i over fixed tensors in as few launches as possible: the
+    """Many hybrid SpMMs C_i = A_i . B_i over fixed tensors in as few launches as possible: the
     register-tiled parts in one batched executor call, the tensor-core parts as one reusable plan
-    (B split + tensor-core launch).  Without load_c the register-tiled part runs first, as in
-    HybridMatrix.execute."""
+    (B preparation + tensor-core launches; BF16 products of one weight coalesce).  Without load_c
+    the register-tiled part runs first, as in HybridMatrix.execute.  All hybrids of one batch share
+    a storage type."""
 
     def __init__(self, triples, stream=None):
         from .packed import work_items
         self.triples = list(triples)
-        for h, _, _ in self.triples:
-            if h.value_dtype != _lib.F32:
-                raise ValueError("HybridBatch runs FP32 hybrids")
-        tc = [h.tc_item(B, C) for h, B, C in self.triples if h.tc_rows and h.cols > 0]
-        self.plan = DenseRowsPlan(tc, stream=stream) if tc else None
+        kinds = {h.value_dtype for h, _, _ in self.triples}
+        if len(kinds) > 1:
+            raise ValueError("one storage type per HybridBatch")
+        tc_t = [(h, B, C) for h, B, C in self.triples if h.tc_rows and h.cols > 0]
+        if not tc_t:
+            self.plan = None
+        elif kinds == {_lib.F32}:
+            self.plan = DenseRowsPlan([h.tc_item(B, C) for h, B, C in tc_t], stream=stream)
+        else:
+            self.plan = DenseRowsPlan(bf16_items([(h.a_rows, h.row_index, B, C, B.shape[1], h.cols, False, 0)
+                                                  for h, B, C in tc_t]), stream=stream)
         sp = [(h.packed, B, C) for h, B, C in self.triples if not h.all_tc]
         self.items = work_items(sp) if sp else None
         self.n_sparse = len(sp)
@@ -266,26 +290,30 @@ class HybridBatch:
 
 
 def tune_tc_fill(A, mapping: Mapping, n: int, fills=(1.01, 0.5, 0.3, 0.2, 0.1, 0.05, 0.0), k_tile: int = 0,
-                 reps: int = 20, value_dtype: int = _lib.BF16) -> dict:
-    """Time the hybrid at each threshold on the device (BF16 or FP32 storage, n columns); returns
-    {fill: us} and the fastest threshold."""
+                 reps: int = 20, value_dtype: int = _lib.BF16, batch: int = 8) -> dict:
+    """Time the hybrid at each threshold on the device (BF16 or FP32 storage, n columns): `batch`
+    SpMMs of A with distinct B as one HybridBatch (one batched register-tiled launch, one tensor-core
+    plan), so neither part pays per-call set-up; returns {fill: us per SpMM} and the fastest
+    threshold."""
     import torch
-    B = torch.randn((A.shape[1], n), device=A.device)
+    Bs = [torch.randn((A.shape[1], n), device=A.device) for _ in range(max(1, batch))]
     if value_dtype == _lib.BF16:
-        B = B.to(torch.bfloat16)
-    C = torch.empty((A.shape[0], n), device=A.device)
+        Bs = [b.to(torch.bfloat16) for b in Bs]
+    Cs = [torch.empty((A.shape[0], n), device=A.device) for _ in Bs]
     out = {}
     for f in fills:
         h = HybridMatrix.from_dense(A, mapping, f, k_tile=k_tile, value_dtype=value_dtype)
+        hb = HybridBatch([(h, b, c) for b, c in zip(Bs, Cs)])
         for _ in range(3):  # warm-up: lazy set-up and clock ramp stay out of the timed calls
-            h.execute(B, C)
+            hb.run()
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
         for _ in range(reps):
-            h.execute(B, C)
+            hb.run()
         e1.record()
         torch.cuda.synchronize()
-        out[float(f)] = e0.elapsed_time(e1) / reps * 1e3
+        out[float(f)] = e0.elapsed_time(e1) / reps * 1e3 / len(Bs)
+        del hb, h
     best = min(out, key=out.get)
-    return {"us": out, "best_fill": best}
+    return {"us": out, "best_fill": best, "batch": len(Bs)}

@@ -5,7 +5,7 @@ import pytest
 from oracle import oracle as O
 from spreg import synth
 from spreg.autotune import (Candidate, Costs, candidates, fit_costs, heuristic_bucket, mapping_of, model_row,
-                            panel_codes, panel_stats, rank)
+                            panel_codes, panel_stats, rank, tune)
 
 CASES = [(2, "identity"), (4, "identity"), (8, "identity"), (8, "400fa"), (8, "747f9")]
 
@@ -98,7 +98,7 @@ def test_tune_picks_a_measured_candidate_and_it_is_exact(cuda):
     from spreg import PackedMatrix
     from spreg.autotune import tune
     A = synth.row_skew(1024, 512, 0.9, seed=4)
-    res = tune(A, 128, "f32", top=3)
+    res = tune(A, 128, "f32", top=3, tc=False, warps=False)
     assert res.best.name() in res.measured_ns and len(res.measured_ns) == 3
     assert res.measured_ns[res.best.name()] == min(res.measured_ns.values())
     m = mapping_of(res.best.mr, res.best.mapping)
@@ -109,12 +109,54 @@ def test_tune_picks_a_measured_candidate_and_it_is_exact(cuda):
     np.testing.assert_array_equal(got.view(np.uint32), want.view(np.uint32))
 
 
-def test_rank_adds_greedy_nanokernel_set_for_mr8():
+def test_rank_adds_greedy_nanokernel_sets_for_mr8_and_tiled_mr4():
     from spreg.autotune import GENERATED
     A = synth.row_skew(256, 384, 0.9, seed=2)
     ranked, stats = rank(A != 0, 64, "f32", Costs.default())
-    gen = {c.mapping for _, c in ranked if c.mapping in GENERATED}
-    assert len(gen) == 1
-    gid = gen.pop()
-    assert all(c.mr == 8 for _, c in ranked if c.mapping == gid)
-    assert (8, gid) in stats and mapping_of(8, gid).mapping_id == gid
+    gen = {(c.mr, c.mapping) for _, c in ranked if c.mapping in GENERATED}
+    assert {mr for mr, _ in gen} == {4, 8} and len(gen) == 2
+    for mr, gid in gen:
+        assert (mr, gid) in stats and mapping_of(mr, gid).mapping_id == gid
+        assert all(c.k_tile > 0 for _, c in ranked if c.mr == 4 and c.mapping == gid)  # B-tile executor sets
+
+
+def test_candidate_names_carry_cta_tiling_and_tensor_core_threshold():
+    assert Candidate(4, "identity", 128, 128, warps=8).name() == "M4N128_identity_K128_W8"
+    assert Candidate(2, "identity", 64, tc_fill=0.0).name() == "M2N64_identity_TC0"
+    assert Candidate(2, "identity", 64).tc_fill > 1.0  # no tensor-core panels by default
+
+
+def test_tensor_core_prediction_grows_with_the_panels_it_takes():
+    from spreg.autotune import tc_predict_ns
+    A = synth.row_skew(1024, 512, 0.9, seed=3)
+    t_all, share_all = tc_predict_ns(A != 0, 256, "bf16", 0.0, 4)
+    t_none, share_none = tc_predict_ns(A != 0, 256, "bf16", 1.01, 4)
+    t_f32, _ = tc_predict_ns(A != 0, 256, "f32", 0.0, 4)
+    assert share_all == 1.0 and share_none == 0.0 and t_all > t_none and t_f32 > t_all
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dtype,n", [("f32", 512), ("bf16", 256), ("bf16", 32)])
+def test_full_tune_best_is_measured_and_within_tolerance(cuda, dtype, n):
+    """CTA tiling and tensor-core thresholds take part; the winner is the fastest measured and its
+    result holds the storage's tolerance (FP32 1e-5, BF16 1e-2 against FP64)."""
+    import torch
+    from spreg import _lib
+    from spreg.hybrid import HybridMatrix
+    A = synth.row_skew(1024, 512, 0.9, seed=6, std=0.02)
+    res = tune(A, n, dtype, top=2, batch=8)
+    assert res.measured_ns[res.best.name()] == min(res.measured_ns.values())
+    assert any("_W" in k for k in res.measured_ns)
+    assert dtype == "f32" or n < 64 or any("_TC" in k for k in res.measured_ns)
+    c = res.best
+    m = mapping_of(c.mr, c.mapping)
+    vd = _lib.F32 if dtype == "f32" else _lib.BF16
+    h = HybridMatrix.from_dense(torch.from_numpy(A).cuda(), m, c.tc_fill, k_tile=c.k_tile, value_dtype=vd)
+    B = synth.dense(512, n, seed=7)
+    Bt = torch.from_numpy(B).cuda()
+    if dtype == "bf16":
+        Bt = Bt.to(torch.bfloat16)
+    got = h.execute(Bt, nr=c.nr).cpu().numpy()
+    Bq = Bt.float().cpu().numpy()
+    Aq = A if dtype == "f32" else torch.from_numpy(A).to(torch.bfloat16).float().numpy()
+    assert O.rel_err(got, O.dense_fp64(Aq, Bq)) <= (1e-5 if dtype == "f32" else 1e-2)

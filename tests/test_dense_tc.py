@@ -273,3 +273,43 @@ def test_products_of_many_shapes_alone_batched_and_coalesced_are_repeatable(cuda
     for x, y in zip(first, again):
         assert torch.equal(x.view(torch.int16) if x.dtype == torch.bfloat16 else x.view(torch.int32),
                            y.view(torch.int16) if y.dtype == torch.bfloat16 else y.view(torch.int32))
+
+
+def test_bf16_plan_equals_batched_call(cuda):
+    """spreg_dense_rows_bf16_plan_create: the same products as one batched call (many shapes, products
+    coalesced over one weight, B read in place and transposed), run twice."""
+    import torch
+    from spreg.hybrid import DenseRowsPlan, bf16_items
+    g = torch.Generator(device="cuda").manual_seed(44)
+    rows, outs, keep = [], [], []
+    a_sh = torch.randn((300, 264), device="cuda", generator=g).to(torch.bfloat16)
+    i_sh = torch.arange(300, device="cuda", dtype=torch.int32)
+    for j, (R, K, n) in enumerate([(128, 64, 128), (7, 300, 33), (700, 1000, 200), (256, 520, 257)] * 2):
+        k8 = (K + 7) // 8 * 8
+        a = torch.zeros((R, k8), device="cuda", dtype=torch.bfloat16)
+        a[:, :K] = torch.randn((R, K), device="cuda", generator=g).to(torch.bfloat16)
+        B = torch.randn((K, n), device="cuda", generator=g).to(torch.bfloat16)
+        idx = torch.arange(R, device="cuda", dtype=torch.int32)
+        C = torch.zeros((R, n), device="cuda")
+        rows.append((a, idx, B, C, n, K, j % 2, (j // 2) % 2))
+        keep += [a, B, idx]
+        outs.append(C)
+    for n in (64, 130, 33):
+        B = torch.randn((264, n), device="cuda", generator=g).to(torch.bfloat16)
+        C = torch.zeros((300, n), device="cuda")
+        rows.append((a_sh, i_sh, B, C, n, 264, 0, 0))
+        keep.append(B)
+        outs.append(C)
+    items = bf16_items(rows)
+    _lib.check(_lib.lib().spreg_dense_rows_bf16_batched(items.ctypes.data, len(items), _lib.stream_handle(None)))
+    torch.cuda.synchronize()
+    want = [C.clone() for C in outs]
+    plan = DenseRowsPlan(items)
+    for _ in range(2):
+        for C in outs:
+            C.zero_()
+        plan.run()
+        torch.cuda.synchronize()
+        for C, W in zip(outs, want):
+            assert torch.equal(C.view(torch.int32), W.view(torch.int32))
+    plan.close()
