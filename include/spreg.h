@@ -217,6 +217,11 @@ typedef struct {
     int32_t b_staging;   /* 0 automatic, 1 stage B strips in shared memory (bulk copies), 2 read B via L1/L2 */
     int32_t meta_staging; /* 0 automatic, 1 stage each panel's execution block in shared memory, 2 stream
                              the packed arena through registers */
+    int32_t job_order;   /* order in which the (row panel, column strip) jobs are handed out: 0 = row
+                            panels outer (a panel's strips one after another, its metadata reused), 1 =
+                            column strips outer (a strip of B reused across panels).  Results do not
+                            depend on it (each element's FMA order is fixed). */
+    int32_t reserved;    /* 0 */
 } spreg_exec_args;
 
 /* One SpMM: C (+)= A . B over the first n columns -- sop_multiple_panel_executor (template:265-305). */
@@ -365,7 +370,10 @@ int spreg_csr_spmm_timed(int64_t rows, int64_t cols, int64_t n, int64_t nnz, con
 typedef struct {
     int32_t m_tile, k_tile, n_tile; /* M_c, K_c, N_c (SOPConfig m_tile/k_tile/n_tile) */
     int32_t nr;                     /* columns per warp strip, 0 = automatic */
-    int32_t outer_schedule;         /* KNM=0, NKM=1, ... accepted; the GPU grid order is fixed */
+    int32_t outer_schedule;         /* KNM=0, NKM=1, MNK=2, NMK=3, KMN=4, MKN=5, KM=6, MK=7, KN=8, NK=9, MN=10,
+                                       NM=11, K=12, N=13, M=14 (tools/paper/configs.py:9-25): K runs inside
+                                       every GPU job, so a schedule with N outside M hands out column
+                                       strips outer (job_order 1), the others row panels outer */
     int32_t value_dtype;            /* spreg_dtype of stored values */
     int32_t sparse_a, tiling_strategy, beta_10x; /* accepted and reported; no GPU effect */
 } spreg_tile_config;

@@ -548,8 +548,21 @@ int spreg_matmul_allocate_executor(spreg_matmul *mm, int32_t n) {
     return SPREG_OK;
 }
 
+// Job order of an outer schedule (tools/paper/configs.py:9-25, codes as spreg_tile_config documents):
+// the K loop runs inside every job (K tiles accumulate in registers), so what a schedule decides on
+// the GPU is whether the N loop (column strips) is outside the M loop (row panels).
+static int32_t job_order_of_schedule(int32_t sched) {
+    static const char *const names[] = {"KNM", "NKM", "MNK", "NMK", "KMN", "MKN", "KM", "MK",
+                                        "KN",  "NK",  "MN",  "NM",  "K",   "N",   "M"};
+    if (sched < 0 || sched >= (int32_t)(sizeof names / sizeof names[0])) return 0;
+    const char *n = names[sched];
+    const char *pn = std::strchr(n, 'N'), *pm = std::strchr(n, 'M');
+    return (pn && (!pm || pn < pm)) ? 1 : 0;
+}
+
 static int matmul_exec(spreg_matmul *mm, float *c, const float *b, cudaStream_t s) {
     spreg_exec_args a = {};
+    a.job_order = job_order_of_schedule(mm->cfg.outer_schedule);
     a.b = b;
     a.ldb = mm->n;
     a.c = c;

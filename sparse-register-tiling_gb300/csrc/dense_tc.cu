@@ -540,9 +540,11 @@ struct SplitBItem {
     int32_t k, n, k64, pad;
 };
 
-// One CTA per (64-column chunk, item): lane l of each warp takes columns 2l and 2l + 1 of the chunk,
-// the 8 warps interleave the rows; a column's maximum over k, then the split.
-__global__ void __launch_bounds__(256) split_cols_kernel(const SplitBItem *__restrict__ items) {
+// One CTA of 16 warps per (64-column chunk, item): lane l of each warp takes columns 2l and 2l + 1 of
+// the chunk, warp w the rows w, w + 16, ...; four rows' loads are issued before they are used.  A
+// column's maximum over k (shared-memory reduction over the warps), then the split.
+constexpr int SPLIT_WARPS = 16;
+__global__ void __launch_bounds__(32 * SPLIT_WARPS) split_cols_kernel(const SplitBItem *__restrict__ items) {
     const SplitBItem it = items[blockIdx.y];
     const int j0 = blockIdx.x * 64;
     if (j0 >= it.n) return;  // uniform per block
@@ -551,31 +553,38 @@ __global__ void __launch_bounds__(256) split_cols_kernel(const SplitBItem *__res
     const bool c0 = j < it.n, c1 = j + 1 < it.n;
     const bool vec = ((reinterpret_cast<uintptr_t>(it.b) | (uintptr_t)(it.ldb * 4)) % 8) == 0;
     auto load2 = [&](int r, float &x0, float &x1) {
+        x0 = x1 = 0.0f;
+        if (r >= it.k) return;
         const float *row = it.b + (int64_t)r * it.ldb;
         if (vec && c1) {
-            const float2 v = *reinterpret_cast<const float2 *>(row + j);
+            const float2 v = __ldg(reinterpret_cast<const float2 *>(row + j));
             x0 = v.x;
             x1 = v.y;
         } else {
-            x0 = c0 ? row[j] : 0.0f;
-            x1 = c1 ? row[j + 1] : 0.0f;
+            if (c0) x0 = __ldg(row + j);
+            if (c1) x1 = __ldg(row + j + 1);
         }
     };
+    constexpr int STEP = 4 * SPLIT_WARPS;  // rows per unrolled iteration of the CTA
     float m0 = 0.0f, m1 = 0.0f;
-    for (int r = w; r < it.k; r += 8) {
-        float x0, x1;
-        load2(r, x0, x1);
-        m0 = fmaxf(m0, fabsf(x0));
-        m1 = fmaxf(m1, fabsf(x1));
+    for (int r = w; r < it.k; r += STEP) {
+        float x[4][2];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) load2(r + u * SPLIT_WARPS, x[u][0], x[u][1]);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            m0 = fmaxf(m0, fabsf(x[u][0]));
+            m1 = fmaxf(m1, fabsf(x[u][1]));
+        }
     }
-    __shared__ float red[8][64];
+    __shared__ float red[SPLIT_WARPS][64];
     red[w][2 * lane] = m0;
     red[w][2 * lane + 1] = m1;
     __syncthreads();
     m0 = red[0][2 * lane];
     m1 = red[0][2 * lane + 1];
 #pragma unroll
-    for (int v = 1; v < 8; ++v) {
+    for (int v = 1; v < SPLIT_WARPS; ++v) {
         m0 = fmaxf(m0, red[v][2 * lane]);
         m1 = fmaxf(m1, red[v][2 * lane + 1]);
     }
@@ -587,19 +596,25 @@ __global__ void __launch_bounds__(256) split_cols_kernel(const SplitBItem *__res
         if (c1) it.inv_scale[j + 1] = pow2f(-s1);
     }
     const bool vec_out = ((reinterpret_cast<uintptr_t>(it.hi + j0) | (uintptr_t)(it.ld * 2)) % 4) == 0;
-    for (int r = w; r < it.k64; r += 8) {
-        float x0 = 0.0f, x1 = 0.0f;
-        if (r < it.k) load2(r, x0, x1);
-        __half h0, l0, h1, l1;
-        split_half(x0 * sc0, h0, l0);
-        split_half(x1 * sc1, h1, l1);
-        __half *hp = it.hi + (int64_t)r * it.ld + j, *lp = hp + it.lo_off;
-        if (vec_out && c1) {
-            *reinterpret_cast<__half2 *>(hp) = __halves2half2(h0, h1);
-            *reinterpret_cast<__half2 *>(lp) = __halves2half2(l0, l1);
-        } else {
-            if (c0) { hp[0] = h0; lp[0] = l0; }
-            if (c1) { hp[1] = h1; lp[1] = l1; }
+    for (int r = w; r < it.k64; r += STEP) {
+        float x[4][2];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) load2(r + u * SPLIT_WARPS, x[u][0], x[u][1]);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int rr = r + u * SPLIT_WARPS;
+            if (rr >= it.k64) break;
+            __half h0, l0, h1, l1;
+            split_half(x[u][0] * sc0, h0, l0);
+            split_half(x[u][1] * sc1, h1, l1);
+            __half *hp = it.hi + (int64_t)rr * it.ld + j, *lp = hp + it.lo_off;
+            if (vec_out && c1) {
+                *reinterpret_cast<__half2 *>(hp) = __halves2half2(h0, h1);
+                *reinterpret_cast<__half2 *>(lp) = __halves2half2(l0, l1);
+            } else {
+                if (c0) { hp[0] = h0; lp[0] = l0; }
+                if (c1) { hp[1] = h1; lp[1] = l1; }
+            }
         }
     }
 }
@@ -1037,7 +1052,7 @@ int tc_plan_launch(const TcPlan &pl, cudaStream_t stream) {
     const char *tabd = pl.scratch + pl.tab_base;
     if (pl.nprep > 0) {
         if (pl.split)
-            split_cols_kernel<<<dim3((unsigned)pl.max_ct, (unsigned)pl.nprep), 256, 0, stream>>>(
+            split_cols_kernel<<<dim3((unsigned)pl.max_ct, (unsigned)pl.nprep), 32 * SPLIT_WARPS, 0, stream>>>(
                 reinterpret_cast<const SplitBItem *>(tabd + pl.prep_off));
         else
             transpose_items_kernel<<<dim3((unsigned)pl.max_kt, (unsigned)pl.max_nt, (unsigned)pl.nprep), 256, 0,

@@ -301,6 +301,7 @@ int plan_call(const spreg_packed *a, const spreg_exec_args *args, CallPlan *cp, 
     SPREG_CHECK_ARG(args->epilogue == SPREG_EPILOGUE_NONE || args->epilogue == SPREG_EPILOGUE_RELU, "bad epilogue");
     SPREG_CHECK_ARG(args->meta_staging >= 0 && args->meta_staging <= 2, "meta_staging must be 0, 1 or 2");
     SPREG_CHECK_ARG(args->b_staging >= 0 && args->b_staging <= 2, "b_staging must be 0, 1 or 2");
+    SPREG_CHECK_ARG(args->job_order == 0 || args->job_order == 1, "job_order must be 0 or 1");
     int dev = -1;
     SPREG_CUDA(cudaGetDevice(&dev));
     SPREG_CHECK_ARG(dev == a->device, "packed matrix lives on device %d, current device is %d", a->device, dev);
@@ -387,6 +388,7 @@ int plan_call(const spreg_packed *a, const spreg_exec_args *args, CallPlan *cp, 
     base.ppt = (int32_t)a->geom.ppt;
     base.load_c = args->load_c ? 1 : 0;
     base.epilogue = args->epilogue;
+    base.order = args->job_order;
     cp->has_main = n_main > 0 && base.P > 0;
     cp->has_tail = args->n > n_main && base.P > 0;
     cp->main = base;
@@ -427,7 +429,8 @@ int plan_call(const spreg_packed *a, const spreg_exec_args *args, CallPlan *cp, 
         tb.T = (int32_t)a->geom.T;
         tb.ppt = (int32_t)a->geom.ppt;
         tb.load_c = args->load_c ? 1 : 0;
-        tb.epilogue = args->epilogue;
+        tb.epilogue = (int16_t)args->epilogue;
+        tb.order = args->job_order;
         tb.kt = (int32_t)kt_rows;
         tb.krows = (int32_t)a->geom.K;
         tb.col_offset = (int32_t)in.col_offset;

@@ -953,8 +953,10 @@ struct XProblem {
     int32_t P, S, T, ppt;       // row panels, strips, K tiles, panels per row tile
     int32_t load_c, epilogue;
     const int32_t *panel_rank;  // panel -> position in the work order (exec_slot)
+    int32_t order;              // job order: 0 = row panels outer (a panel's strips in a row), 1 = strips outer
+    int32_t pad_;
 };
-static_assert(sizeof(XProblem) == 120, "XProblem layout");
+static_assert(sizeof(XProblem) == 128, "XProblem layout");
 
 struct BatchParams {
     int *counter;               // work counter, zero at launch
@@ -990,6 +992,7 @@ __device__ __forceinline__ XJob next_job(const BatchParams &bp, const XJob &j, i
     const int pi = find_problem(bp, item);
     const XProblem &pr = bp.prob[pi];
     const int64_t local = item - pr.item_begin;
+    if (pr.order == 1) return XJob{local % pr.P, pi, (int32_t)(local / pr.P), 0};
     return XJob{local / pr.S, pi, (int32_t)(local % pr.S), 0};
 }
 

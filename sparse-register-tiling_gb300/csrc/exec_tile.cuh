@@ -53,7 +53,8 @@ struct TProblem {
     int32_t col_begin;          // first column of the problem's strips
     int32_t col_end;            // columns >= col_end are not computed
     int32_t P, S, T, ppt;       // row panels, strips, K tiles, panels per row tile
-    int32_t load_c, epilogue;
+    int16_t load_c, epilogue;
+    int32_t order;              // job order: 0 = panel groups outer (a group's strips in a row), 1 = strips outer
     int32_t kt, krows;          // B rows per K tile, B rows of all tiles (columns of A)
     int32_t col_offset;         // first B row of tile 0
     int32_t box_rows;           // rows of one tensor copy (K tile copied in ceil(kt / box_rows) copies)
@@ -255,8 +256,14 @@ __global__ void __launch_bounds__(32 * (kTileMaxWarps + 1), 1) exec_tile_kernel(
             }
             pi = find_tproblem(tp, job);
             const int64_t local = job - tp.prob[pi].job_begin;
-            group = (int)(local / tp.prob[pi].S);
-            strip = (int)(local % tp.prob[pi].S);
+            if (tp.prob[pi].order == 1) {
+                const int64_t groups = (tp.prob[pi].P + W - 1) / W;
+                group = (int)(local % groups);
+                strip = (int)(local / groups);
+            } else {
+                group = (int)(local / tp.prob[pi].S);
+                strip = (int)(local % tp.prob[pi].S);
+            }
             t = 0;
         };
         fetch();

@@ -159,6 +159,7 @@ extern "C" int spreg_execute_batched_noalloc(const spreg_work_item *items, int32
                         "work item %d: null B or C", i);
         SPREG_CHECK_ARG(args->epilogue == SPREG_EPILOGUE_NONE || args->epilogue == SPREG_EPILOGUE_RELU,
                         "work item %d: bad epilogue", i);
+        SPREG_CHECK_ARG(args->job_order == 0 || args->job_order == 1, "work item %d: job_order must be 0 or 1", i);
         SPREG_CHECK_ARG(args->b_staging != 1 && args->meta_staging != 2,
                         "work item %d: the no-allocation entry point runs the batched execution-layout kernel only", i);
         const int64_t xbuf = (a->max_exec_bytes + 127) / 128 * 128;
@@ -193,6 +194,7 @@ extern "C" int spreg_execute_batched_noalloc(const spreg_work_item *items, int32
         base.ppt = (int32_t)a->geom.ppt;
         base.load_c = args->load_c ? 1 : 0;
         base.epilogue = args->epilogue;
+        base.order = args->job_order;
         if (base.P == 0) continue;
         auto add = [&](int64_t c0, int64_t c1, int32_t strips, int v) {
             XProblem pr = base;

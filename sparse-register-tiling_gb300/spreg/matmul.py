@@ -19,7 +19,8 @@ from . import _lib
 from .mapping import Mapping
 from .packed import PackedMatrix
 
-# Outer schedules of tools/paper/configs.py:9-25 (accepted; the GPU grid order is fixed).
+# Outer schedules of tools/paper/configs.py:9-25.  K runs inside every GPU job, so a schedule with N
+# outside M hands out column strips outer (spreg_exec_args.job_order = 1), the others row panels outer.
 SCHEDULES = {"KNM": 0, "NKM": 1, "MNK": 2, "NMK": 3, "KMN": 4, "MKN": 5, "KM": 6, "MK": 7, "KN": 8, "NK": 9,
              "MN": 10, "NM": 11, "K": 12, "N": 13, "M": 14}
 
