@@ -76,6 +76,8 @@ def parse():
                     help="1: add the batched uneven transformer-layer measurement to the line")
     ap.add_argument("--ffn-sweep", type=int, default=1,
                     help="1: add the FFN-shaped FP32 sweep (2048x512 / 512x2048 at sparsity 0.7-0.98) to the line")
+    ap.add_argument("--extras", type=int, default=1,
+                    help="1: add the GPU CSR baseline and the config-1 (512x512) legs to the line")
     ap.add_argument("--serve-requests", type=int, default=768)
     ap.add_argument("--serve-slots", type=int, default=128)
     ap.add_argument("--serve-budget-mb", type=int, default=1024)
@@ -860,10 +862,13 @@ def hybrid_leg(args, As, Bs, m, dev, step_bytes: int, step_flops: int, clk, peak
     from spreg import F32
     from spreg.hybrid import HybridBatch, HybridMatrix, tune_tc_fill
     t0 = time.perf_counter()
-    tuned = tune_tc_fill(torch.from_numpy(As[0]).to(dev), m, args.n, fills=(1.01, 0.3, 0.2, 0.15, 0.1, 0.05, 0.0),
-                         k_tile=args.k_tile, value_dtype=F32, batch=16)
+    if args.tc_fill < 0:
+        tuned = tune_tc_fill(torch.from_numpy(As[0]).to(dev), m, args.n, fills=(1.01, 0.3, 0.2, 0.15, 0.1, 0.05, 0.0),
+                             k_tile=args.k_tile, value_dtype=F32, batch=16)
+    else:
+        tuned = {"us": {}, "best_fill": args.tc_fill, "batch": 0}
     t_tune = time.perf_counter() - t0
-    fill = tuned["best_fill"] if args.tc_fill < 0 else args.tc_fill
+    fill = tuned["best_fill"]
     hs = [HybridMatrix.from_dense(torch.from_numpy(A).to(dev), m, fill, k_tile=args.k_tile, value_dtype=F32)
           for A in As]
     Bd = [torch.from_numpy(B).to(dev) for B in Bs]
@@ -1102,8 +1107,9 @@ def main():
 
     # the secondary legs describe one GPU: rank 0 alone runs them, the other ranks are done
     lead = rank == 0
-    csr_leg = csr_baseline_leg(As[0], Bd[0], packs[0], args, spmm_us) if (lead and args.dtype == "f32") else None
-    cfg1 = config1_leg(dev) if lead else None
+    csr_leg = (csr_baseline_leg(As[0], Bd[0], packs[0], args, spmm_us)
+               if (lead and args.dtype == "f32" and args.extras) else None)
+    cfg1 = config1_leg(dev) if (lead and args.extras) else None
     serving = serving_bench(args, dev) if (lead and args.serving) else None
     precision = precision_suite(dev) if (lead and args.precision) else None
     tensor_cores = tensor_core_suite(dev) if (lead and args.tensor_cores) else None

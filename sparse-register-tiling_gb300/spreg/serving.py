@@ -312,6 +312,8 @@ class SparseMLP:
             it = np.zeros(self.num_layers, dtype=WORK_ITEM_DTYPE)
             it["a"] = [_handle_int(pm.handle) for pm in self.layers]
             it["b_dtype"] = it["c_dtype"] = self.act_code
+            if self.configs is not None:
+                it["warps_per_cta"] = [int(c.get("warps", 0)) for c in self.configs]
         it["load_c"] = np.where(up, 0, 1)
         it["epilogue"] = np.where(up, _lib.EPILOGUE_RELU, _lib.EPILOGUE_NONE)
         self._template = it
@@ -354,8 +356,10 @@ def tune_mlp(weights, dtype: str = "bf16", n: int = 96, batch: int = 32, top: in
     tuned for ``batch`` concurrent requests of ``n`` tokens and every block reuses them (all blocks
     share shapes and sparsity).  Returns (configs, tune results)."""
     from .autotune import tune
-    res = [tune(w, n, dtype, top=top, batch=batch, device=device) for w in weights[0]]
-    cfg = [{"mr": r.best.mr, "mapping": r.best.mapping, "k_tile": r.best.k_tile, "nr": r.best.nr} for r in res]
+    # register-tiled packings (tensor-core layers are SparseMLP(tc=True)); the CTA tiling is kept
+    res = [tune(w, n, dtype, top=top, batch=batch, device=device, tc=False) for w in weights[0]]
+    cfg = [{"mr": r.best.mr, "mapping": r.best.mapping, "k_tile": r.best.k_tile, "nr": r.best.nr,
+            "warps": r.best.warps} for r in res]
     return [dict(cfg[l % 2]) for l in range(2 * len(weights))], res
 
 
