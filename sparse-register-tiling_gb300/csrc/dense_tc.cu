@@ -56,17 +56,25 @@ int *device_status_word(int *st);  // exec.cu
 namespace {
 
 constexpr int TC_BM = 128, TC_BK = 64;
-constexpr uint32_t TC_TILE_A = TC_BM * TC_BK * 2;  // 16 KB
+// K block of a split product: 32 deep (64-byte rows, 64-byte swizzle), so that its four operand
+// tiles make stages of 48 KB and four of them are in flight (96 KB stages of 64-deep blocks allowed
+// two).
+constexpr int TC_BK_SPLIT = 32;
+template <bool SPLIT> constexpr int tc_bk() { return SPLIT ? TC_BK_SPLIT : TC_BK; }
 // Output tile width BN (128 or 256): the MMA's N, the TMEM accumulator's columns, B tile rows.
 // A split product stages both halves of A and of B.
-template <int BN> constexpr uint32_t tc_tile_b() { return (uint32_t)BN * TC_BK * 2; }
+template <int BN, bool SPLIT> constexpr uint32_t tc_tile_a() { return (uint32_t)TC_BM * tc_bk<SPLIT>() * 2; }
+template <int BN, bool SPLIT = false> constexpr uint32_t tc_tile_b() { return (uint32_t)BN * tc_bk<SPLIT>() * 2; }
 template <int BN, bool SPLIT> constexpr uint32_t tc_stage() {
-    return (SPLIT ? 2u : 1u) * (TC_TILE_A + tc_tile_b<BN>());
+    return (SPLIT ? 2u : 1u) * (tc_tile_a<BN, SPLIT>() + tc_tile_b<BN, SPLIT>());
 }
 // Stages of the ring: about 190 KB of operands.
-template <int BN, bool SPLIT> constexpr int tc_stages() { return !SPLIT ? 4 : BN == 256 ? 2 : 3; }
+template <int BN, bool SPLIT> constexpr int tc_stages() { return !SPLIT ? 4 : BN == 256 ? 4 : 6; }
+// The epilogue warps' staging buffers: 4 x 32 rows x 33 floats.
+constexpr uint32_t TC_EPI_BYTES = 4u * 32u * 33u * 4u;
 template <int BN, bool SPLIT> constexpr size_t tc_smem() {
-    return 1024 /* alignment slack */ + tc_stages<BN, SPLIT>() * tc_stage<BN, SPLIT>() + 256 /* barriers, TMEM slot */;
+    return 1024 /* alignment slack */ + tc_stages<BN, SPLIT>() * tc_stage<BN, SPLIT>() + 256 /* barriers, TMEM slot */ +
+           TC_EPI_BYTES;
 }
 
 constexpr int TC_MAX_PROBLEMS = 192;  // problems per launch (kernel parameters <= 32 KB)
@@ -167,6 +175,28 @@ __device__ __forceinline__ uint64_t tc_desc_mn(uint32_t saddr) {
     return d;
 }
 
+// The same two descriptors for the 64-byte swizzle (rows of 64 bytes = 32 FP16): K-major, 8-row
+// groups 512 bytes apart; N-major, 8-row K groups 512 bytes apart and 32-column N blocks (one tensor
+// copy of 32 K rows each) 2048 bytes apart.
+__device__ __forceinline__ uint64_t tc_desc64(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);  // start address, 16-byte units
+    d |= (uint64_t)1 << 16;                    // leading-dimension byte offset (unused for this layout)
+    d |= (uint64_t)(512 >> 4) << 32;           // stride-dimension byte offset: next 8-row group
+    d |= (uint64_t)1 << 46;                    // descriptor version of tcgen05
+    d |= (uint64_t)4 << 61;                    // layout: 64-byte swizzle
+    return d;
+}
+__device__ __forceinline__ uint64_t tc_desc64_mn(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);  // start address, 16-byte units
+    d |= (uint64_t)(2048 >> 4) << 16;          // leading-dimension byte offset: next 32-column N block
+    d |= (uint64_t)(512 >> 4) << 32;           // stride-dimension byte offset: next 8-row K group
+    d |= (uint64_t)1 << 46;                    // descriptor version of tcgen05
+    d |= (uint64_t)4 << 61;                    // layout: 64-byte swizzle
+    return d;
+}
+
 // Instruction descriptor of kind::f16: D FP32, A and B BF16 (bf16) or FP16, both K-major, M x N.
 __host__ __device__ constexpr uint32_t tc_idesc(int M, int N, bool bf16 = true) {
     return (1u << 4) | ((bf16 ? 1u : 0u) << 7) | ((bf16 ? 1u : 0u) << 10) | ((uint32_t)(N >> 3) << 17) |
@@ -209,108 +239,118 @@ __device__ __forceinline__ int tc_problem_of(const TcParams &p, int t) {
 }
 
 // Epilogue of one output tile by one warp: TMEM lanes 32 * quarter .. + 31 (tile rows) of the
-// accumulator at TMEM address tacc (lane 0, its first column); load_c / ReLU; store through the
-// row index (and segments).
+// accumulator at TMEM address tacc (lane 0, its first column); scales (split products), load_c /
+// ReLU; store through the row index (and segments).
+//
+// Whole 32-column chunks of one output go through the warp's 32 x 33 shared-memory buffer `eb`:
+// lane i writes row i's 32 values, then each store instruction covers 4 rows x 32 columns (8 lanes
+// x 16 bytes per row), where a lane storing its own row would scatter 32 rows per instruction.  The
+// 33-float row pitch keeps both passes free of bank conflicts.
 template <int BN, bool SPLIT>
 __device__ __forceinline__ void tc_store_tile(const TcProblem &q, int m0, int n0, int quarter, int lane, uint32_t tacc,
-                                              bool ok) {
+                                              bool ok, float *eb) {
     constexpr int TC_BN = BN;
     const int r = m0 + 32 * quarter + lane;
     const bool row_ok = ok && r < q.R;
-    const int64_t orow = row_ok ? q.row_index[r] : 0;
+    const long long orow = row_ok ? q.row_index[r] : 0;
     const float rs = (SPLIT && row_ok) ? q.row_scale[r] : 1.0f;
-    const uint32_t tmem = tacc;
-    const int warp = quarter;
+    const uint32_t tmem = tacc + ((uint32_t)(32 * quarter) << 16);
     // vector stores need 16-byte (F32) / 8-byte (BF16) aligned row starts of C
     const int esz = q.c_dtype == SPREG_F32 ? 4 : 2;
     const bool vec_ok = (reinterpret_cast<uintptr_t>(q.C) % (4 * esz)) == 0 && (q.ldc % 4) == 0;
-    if (ok) {
-        int seg = 0;  // segment of the current column (coalesced products)
-        if (q.nseg > 1 && row_ok) {
-            int lo2 = 0, hi2 = q.nseg - 1;
-            while (lo2 < hi2) {
-                const int mid = (lo2 + hi2 + 1) >> 1;
-                if (q.seg_start[mid] <= n0) lo2 = mid;
-                else hi2 = mid - 1;
-            }
-            seg = lo2;
+    if (!ok) return;
+    int seg = 0;  // segment of the current column (coalesced products)
+    if (q.nseg > 1 && row_ok) {
+        int lo2 = 0, hi2 = q.nseg - 1;
+        while (lo2 < hi2) {
+            const int mid = (lo2 + hi2 + 1) >> 1;
+            if (q.seg_start[mid] <= n0) lo2 = mid;
+            else hi2 = mid - 1;
         }
-        for (int c = 0; c < TC_BN; c += 16) {
-            float v[16];
-            tc_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c, v);  // every lane takes part
-            if (!row_ok) continue;
-            if constexpr (SPLIT) {
-                // undo the scales: (acc * 2^-s_row) * 2^-s_col, each factor exact
+        seg = lo2;
+    }
+    for (int c = 0; c < TC_BN; c += 32) {
+        float v[32];
+        tc_ld16(tmem + (uint32_t)c, *reinterpret_cast<float(*)[16]>(&v[0]));  // every lane takes part
+        tc_ld16(tmem + (uint32_t)(c + 16), *reinterpret_cast<float(*)[16]>(&v[16]));
+        if constexpr (SPLIT) {
+            // undo the scales: (acc * 2^-s_row) * 2^-s_col, each factor exact
 #pragma unroll
-                for (int j = 0; j < 16; ++j) {
-                    const int col = n0 + c + j;
-                    v[j] = (v[j] * rs) * (col < q.n ? __ldg(q.col_scale + col) : 0.0f);
-                }
-            }
-            if (q.nseg <= 1 && vec_ok && n0 + c + 16 <= q.n) {
-                // whole 16-column chunk of one output: 16-byte (F32) / 8-byte (BF16) stores
-                if (q.c_dtype == SPREG_F32) {
-                    float4 *cp = reinterpret_cast<float4 *>(reinterpret_cast<float *>(q.C) + orow * q.ldc + n0 + c);
-#pragma unroll
-                    for (int j4 = 0; j4 < 4; ++j4) {
-                        float4 o = make_float4(v[4 * j4], v[4 * j4 + 1], v[4 * j4 + 2], v[4 * j4 + 3]);
-                        if (q.load_c) {
-                            const float4 ci = cp[j4];
-                            o.x += ci.x; o.y += ci.y; o.z += ci.z; o.w += ci.w;
-                        }
-                        if (q.epilogue == SPREG_EPILOGUE_RELU) {
-                            o.x = fmaxf(o.x, 0.0f); o.y = fmaxf(o.y, 0.0f); o.z = fmaxf(o.z, 0.0f); o.w = fmaxf(o.w, 0.0f);
-                        }
-                        cp[j4] = o;
-                    }
-                } else {
-                    uint2 *cp = reinterpret_cast<uint2 *>(reinterpret_cast<__nv_bfloat16 *>(q.C) + orow * q.ldc + n0 + c);
-#pragma unroll
-                    for (int j4 = 0; j4 < 4; ++j4) {
-                        float o[4] = {v[4 * j4], v[4 * j4 + 1], v[4 * j4 + 2], v[4 * j4 + 3]};
-                        if (q.load_c) {
-                            const uint2 ci = cp[j4];
-                            const __nv_bfloat162 c01 = *reinterpret_cast<const __nv_bfloat162 *>(&ci.x);
-                            const __nv_bfloat162 c23 = *reinterpret_cast<const __nv_bfloat162 *>(&ci.y);
-                            o[0] += __low2float(c01); o[1] += __high2float(c01);
-                            o[2] += __low2float(c23); o[3] += __high2float(c23);
-                        }
-                        if (q.epilogue == SPREG_EPILOGUE_RELU)
-                            for (int t = 0; t < 4; ++t) o[t] = fmaxf(o[t], 0.0f);
-                        __nv_bfloat162 w01 = __floats2bfloat162_rn(o[0], o[1]), w23 = __floats2bfloat162_rn(o[2], o[3]);
-                        uint2 w;
-                        w.x = *reinterpret_cast<uint32_t *>(&w01);
-                        w.y = *reinterpret_cast<uint32_t *>(&w23);
-                        cp[j4] = w;
-                    }
-                }
-                continue;
-            }
-#pragma unroll
-            for (int j = 0; j < 16; ++j) {
+            for (int j = 0; j < 32; ++j) {
                 const int col = n0 + c + j;
-                if (col >= q.n) break;
-                void *cbase = q.C;
-                int64_t ldc = q.ldc;
-                int lcol = col;
-                if (q.nseg > 1) {
-                    while (col >= q.seg_start[seg + 1]) ++seg;
-                    cbase = q.seg_c[seg];
-                    ldc = q.seg_ldc[seg];
-                    lcol = col - q.seg_start[seg];
-                }
-                float o = v[j];
+                v[j] = (v[j] * rs) * (col < q.n ? __ldg(q.col_scale + col) : 0.0f);
+            }
+        }
+        if (q.nseg <= 1 && vec_ok && n0 + c + 32 <= q.n) {  // uniform over the warp
+            __syncwarp();
+#pragma unroll
+            for (int j = 0; j < 32; ++j) eb[lane * 33 + j] = v[j];
+            __syncwarp();
+            const int c4 = (lane & 7) * 4;
+#pragma unroll
+            for (int it = 0; it < 8; ++it) {
+                const int rr = 4 * it + (lane >> 3);  // tile row (TMEM lane) this lane stores
+                const bool ok_r = __shfl_sync(0xffffffffu, row_ok, rr);
+                const long long orow_r = __shfl_sync(0xffffffffu, orow, rr);
+                if (!ok_r) continue;
+                float o[4];
+#pragma unroll
+                for (int t = 0; t < 4; ++t) o[t] = eb[rr * 33 + c4 + t];
                 if (q.c_dtype == SPREG_F32) {
-                    float *cp = reinterpret_cast<float *>(cbase) + orow * ldc + lcol;
-                    if (q.load_c) o += *cp;
-                    if (q.epilogue == SPREG_EPILOGUE_RELU) o = fmaxf(o, 0.0f);
-                    *cp = o;
+                    float4 *cp = reinterpret_cast<float4 *>(reinterpret_cast<float *>(q.C) + orow_r * q.ldc + n0 + c + c4);
+                    if (q.load_c) {
+                        const float4 ci = *cp;
+                        o[0] += ci.x; o[1] += ci.y; o[2] += ci.z; o[3] += ci.w;
+                    }
+                    if (q.epilogue == SPREG_EPILOGUE_RELU)
+                        for (int t = 0; t < 4; ++t) o[t] = fmaxf(o[t], 0.0f);
+                    *cp = make_float4(o[0], o[1], o[2], o[3]);
                 } else {
-                    __nv_bfloat16 *cp = reinterpret_cast<__nv_bfloat16 *>(cbase) + orow * ldc + lcol;
-                    if (q.load_c) o += __bfloat162float(*cp);
-                    if (q.epilogue == SPREG_EPILOGUE_RELU) o = fmaxf(o, 0.0f);
-                    *cp = __float2bfloat16_rn(o);
+                    uint2 *cp = reinterpret_cast<uint2 *>(reinterpret_cast<__nv_bfloat16 *>(q.C) + orow_r * q.ldc + n0 + c +
+                                                          c4);
+                    if (q.load_c) {
+                        const uint2 ci = *cp;
+                        const __nv_bfloat162 c01 = *reinterpret_cast<const __nv_bfloat162 *>(&ci.x);
+                        const __nv_bfloat162 c23 = *reinterpret_cast<const __nv_bfloat162 *>(&ci.y);
+                        o[0] += __low2float(c01); o[1] += __high2float(c01);
+                        o[2] += __low2float(c23); o[3] += __high2float(c23);
+                    }
+                    if (q.epilogue == SPREG_EPILOGUE_RELU)
+                        for (int t = 0; t < 4; ++t) o[t] = fmaxf(o[t], 0.0f);
+                    __nv_bfloat162 w01 = __floats2bfloat162_rn(o[0], o[1]), w23 = __floats2bfloat162_rn(o[2], o[3]);
+                    uint2 w;
+                    w.x = *reinterpret_cast<uint32_t *>(&w01);
+                    w.y = *reinterpret_cast<uint32_t *>(&w23);
+                    *cp = w;
                 }
+            }
+            continue;
+        }
+        if (!row_ok) continue;
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+            const int col = n0 + c + j;
+            if (col >= q.n) break;
+            void *cbase = q.C;
+            int64_t ldc = q.ldc;
+            int lcol = col;
+            if (q.nseg > 1) {
+                while (col >= q.seg_start[seg + 1]) ++seg;
+                cbase = q.seg_c[seg];
+                ldc = q.seg_ldc[seg];
+                lcol = col - q.seg_start[seg];
+            }
+            float o = v[j];
+            if (q.c_dtype == SPREG_F32) {
+                float *cp = reinterpret_cast<float *>(cbase) + orow * ldc + lcol;
+                if (q.load_c) o += *cp;
+                if (q.epilogue == SPREG_EPILOGUE_RELU) o = fmaxf(o, 0.0f);
+                *cp = o;
+            } else {
+                __nv_bfloat16 *cp = reinterpret_cast<__nv_bfloat16 *>(cbase) + orow * ldc + lcol;
+                if (q.load_c) o += __bfloat162float(*cp);
+                if (q.epilogue == SPREG_EPILOGUE_RELU) o = fmaxf(o, 0.0f);
+                *cp = __float2bfloat16_rn(o);
             }
         }
     }
@@ -327,9 +367,11 @@ __device__ __forceinline__ void tc_store_tile(const TcProblem &q, int m0, int n0
 template <int BN, bool SPLIT>
 __global__ void __launch_bounds__(192, 1) tc_rows_kernel(const __grid_constant__ TcParams p, const int total_tiles) {
     constexpr int STAGES = tc_stages<BN, SPLIT>();
+    constexpr int BK = tc_bk<SPLIT>();
     constexpr uint32_t TC_STAGE = tc_stage<BN, SPLIT>(), TC_TMEM_COLS = 2 * BN;
-    constexpr uint32_t A_BYTES = (SPLIT ? 2u : 1u) * TC_TILE_A;  // B tiles start here
-    constexpr uint32_t B_HALF = tc_tile_b<BN>();                 // B hi -> B lo
+    constexpr uint32_t TILE_A = tc_tile_a<BN, SPLIT>();         // A hi -> A lo
+    constexpr uint32_t A_BYTES = (SPLIT ? 2u : 1u) * TILE_A;     // B tiles start here
+    constexpr uint32_t B_HALF = tc_tile_b<BN, SPLIT>();          // B hi -> B lo
     constexpr int TC_BN = BN;
     extern __shared__ unsigned char smem_raw[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -339,6 +381,7 @@ __global__ void __launch_bounds__(192, 1) tc_rows_kernel(const __grid_constant__
     const uint32_t full0 = bars, empty0 = bars + 8u * STAGES;
     const uint32_t accf0 = bars + 16u * STAGES, acce0 = accf0 + 16u;  // acc full / empty, 2 each
     const uint32_t tmem_slot = acce0 + 16u;
+    float *const epi = reinterpret_cast<float *>(smem_raw + (bars + 256u - raw));  // epilogue staging buffers
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; ++s) {
             tc_mbar_init(full0 + 8u * s, 1);
@@ -391,18 +434,22 @@ __global__ void __launch_bounds__(192, 1) tc_rows_kernel(const __grid_constant__
                     }
                     const uint32_t st = sbase + (uint32_t)s * TC_STAGE;
                     tc_expect_tx(full0 + 8u * s, TC_STAGE);
-                    const int kx = (q.kb0 + kb) * TC_BK;  // K offset of this block
+                    const int kx = (q.kb0 + kb) * BK;  // K offset of this block
                     tc_tma_2d(st, q.a_map, kx, m0, full0 + 8u * s);
-                    if constexpr (SPLIT) tc_tma_2d(st + TC_TILE_A, q.a_map, kx, q.a_lo_row + m0, full0 + 8u * s);
-                    if (q.b_mn) {
+                    if constexpr (SPLIT) {
+                        tc_tma_2d(st + TILE_A, q.a_map, kx, q.a_lo_row + m0, full0 + 8u * s);
+                        // B halves: BN / 32 copies of 32 columns x 32 K rows each, 2 KB apart
+#pragma unroll
+                        for (int jb = 0; jb < TC_BN / 32; ++jb) {
+                            tc_tma_2d(st + A_BYTES + 2048u * jb, q.b_map, n0 + 32 * jb, kx, full0 + 8u * s);
+                            tc_tma_2d(st + A_BYTES + B_HALF + 2048u * jb, q.b_map, n0 + 32 * jb, q.b_lo_row + kx,
+                                      full0 + 8u * s);
+                        }
+                    } else if (q.b_mn) {
                         // N-major B: BN / 64 copies of 64 columns x 64 K rows, 8 KB apart
 #pragma unroll
-                        for (int jb = 0; jb < TC_BN / 64; ++jb) {
+                        for (int jb = 0; jb < TC_BN / 64; ++jb)
                             tc_tma_2d(st + A_BYTES + 8192u * jb, q.b_map, n0 + 64 * jb, kx, full0 + 8u * s);
-                            if constexpr (SPLIT)
-                                tc_tma_2d(st + A_BYTES + B_HALF + 8192u * jb, q.b_map, n0 + 64 * jb, q.b_lo_row + kx,
-                                          full0 + 8u * s);
-                        }
                     } else {
                         tc_tma_2d(st + A_BYTES, q.b_map, kx, n0, full0 + 8u * s);
                     }
@@ -434,21 +481,26 @@ __global__ void __launch_bounds__(192, 1) tc_rows_kernel(const __grid_constant__
                     }
                     tc_fence_after();
                     const uint32_t st = sbase + (uint32_t)s * TC_STAGE;
-                    if (q.b_mn) {
+                    if constexpr (SPLIT) {
+                        // 64-byte swizzle; a 16-deep K step is 32 bytes into each A row and 16 rows of
+                        // 64 bytes of B; N-major B (transpose-B bit of the instruction descriptor)
+#pragma unroll
+                        for (int k = 0; k < BK / 16; ++k) {
+                            const uint64_t ah = tc_desc64(st + 32u * k), bh = tc_desc64_mn(st + A_BYTES + 1024u * k);
+                            tc_mma(dacc, ah, bh, idesc | (1u << 16), (kb | k) != 0);
+                            tc_mma(dacc, ah, tc_desc64_mn(st + A_BYTES + B_HALF + 1024u * k), idesc | (1u << 16), 1);
+                            tc_mma(dacc, tc_desc64(st + TILE_A + 32u * k), bh, idesc | (1u << 16), 1);
+                        }
+                    } else if (q.b_mn) {
                         // N-major B (transpose-B bit of the instruction descriptor); a 16-deep K step is
                         // 16 rows of 128 bytes
 #pragma unroll
-                        for (int k = 0; k < TC_BK / 16; ++k) {
-                            const uint64_t ah = tc_desc(st + 32u * k), bh = tc_desc_mn(st + A_BYTES + 2048u * k);
-                            tc_mma(dacc, ah, bh, idesc | (1u << 16), (kb | k) != 0);
-                            if constexpr (SPLIT) {
-                                tc_mma(dacc, ah, tc_desc_mn(st + A_BYTES + B_HALF + 2048u * k), idesc | (1u << 16), 1);
-                                tc_mma(dacc, tc_desc(st + TC_TILE_A + 32u * k), bh, idesc | (1u << 16), 1);
-                            }
-                        }
+                        for (int k = 0; k < BK / 16; ++k)
+                            tc_mma(dacc, tc_desc(st + 32u * k), tc_desc_mn(st + A_BYTES + 2048u * k), idesc | (1u << 16),
+                                   (kb | k) != 0);
                     } else {
 #pragma unroll
-                        for (int k = 0; k < TC_BK / 16; ++k)
+                        for (int k = 0; k < BK / 16; ++k)
                             tc_mma(dacc, tc_desc(st + 32u * k), tc_desc(st + A_BYTES + 32u * k), idesc,
                                    (kb | k) != 0);
                     }
@@ -470,7 +522,8 @@ __global__ void __launch_bounds__(192, 1) tc_rows_kernel(const __grid_constant__
             ok = ok && __all_sync(0xffffffffu, tc_wait(accf0 + 8u * a, (uint32_t)((j >> 1) & 1), p.status, 24));
             tc_fence_after();
             if (!ok) break;
-            tc_store_tile<BN, SPLIT>(q, m0, n0, quarter, lane, tmem + (uint32_t)(a * TC_BN), ok);  // adds the lane quarter
+            tc_store_tile<BN, SPLIT>(q, m0, n0, quarter, lane, tmem + (uint32_t)(a * TC_BN), ok,
+                                     epi + quarter * (32 * 33));  // adds the lane quarter
             tc_fence_before();
             __syncwarp();
             if (lane == 0) mbar_arrive_tc(acce0 + 8u * a);
@@ -683,16 +736,19 @@ PFN_cuTensorMapEncodeTiled_v12000 tc_encoder() {
 }
 
 // 16-bit matrix of `rows` x `cols` (row stride ld elements) as 64 x box_rows boxes with the 128-byte swizzle.
+// f16: FP16 with 32-element (64-byte) box rows and the 64-byte swizzle (split products); else BF16
+// with 64-element (128-byte) box rows and the 128-byte swizzle.
 int tc_map(CUtensorMap *map, const void *base, int64_t cols, int64_t rows, int64_t ld, int box_rows, bool f16) {
     auto enc = tc_encoder();
     SPREG_CHECK_ARG(enc, "cuTensorMapEncodeTiled is not available from the driver");
     const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
     const cuuint64_t strides[1] = {(cuuint64_t)(ld * 2)};
-    const cuuint32_t box[2] = {(cuuint32_t)TC_BK, (cuuint32_t)box_rows};
+    const cuuint32_t box[2] = {(cuuint32_t)(f16 ? TC_BK_SPLIT : TC_BK), (cuuint32_t)box_rows};
     const cuuint32_t es[2] = {1, 1};
     CUresult r = enc(map, f16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
                      const_cast<void *>(base), dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                     CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+                     f16 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     SPREG_CHECK_ARG(r == CUDA_SUCCESS, "cuTensorMapEncodeTiled failed (%d) for a %lld x %lld 16-bit operand", (int)r,
                     (long long)rows, (long long)cols);
     return SPREG_OK;
@@ -989,8 +1045,9 @@ int tc_plan_fill(TcPlan &pl, int *status) {
             const int64_t k0 = split ? (int64_t)ps * TC_SPLIT_CHUNK : 0;
             const int64_t kc = split ? std::min<int64_t>(TC_SPLIT_CHUNK, it.k - k0) : it.k;
             const bool last = k0 + kc >= it.k;
-            q.kb0 = (int32_t)(k0 / TC_BK);
-            q.kblocks = (int32_t)((kc + TC_BK - 1) / TC_BK);
+            const int64_t bk = split ? TC_BK_SPLIT : TC_BK;  // the kernel's K block
+            q.kb0 = (int32_t)(k0 / bk);
+            q.kblocks = (int32_t)((kc + bk - 1) / bk);
             q.c_dtype = it.c_dtype;
             q.load_c = (it.load_c || ps > 0) ? 1 : 0;
             q.epilogue = last ? it.epilogue : SPREG_EPILOGUE_NONE;
@@ -1015,7 +1072,7 @@ int tc_plan_fill(TcPlan &pl, int *status) {
                 q.row_scale = it.row_scale;
                 q.col_scale = reinterpret_cast<const float *>(scratch + g.scale_off);
                 if ((st = tc_map(&maps_h[2 * gi], it.a, it.k, 2 * it.rows, it.lda, TC_BM, true)) ||
-                    (st = tc_map(&maps_h[2 * gi + 1], scratch + g.buf_off, g.n, 2 * g.k64, g.ldn, 64, true)))
+                    (st = tc_map(&maps_h[2 * gi + 1], scratch + g.buf_off, g.n, 2 * g.k64, g.ldn, TC_BK_SPLIT, true)))
                     return st;
             } else {
                 const int64_t K8 = (it.k + 7) / 8 * 8;
