@@ -214,17 +214,19 @@ __device__ __forceinline__ void tc_commit(uint32_t bar) {
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
-__device__ __forceinline__ void tc_ld16(uint32_t taddr, float (&v)[16]) {
-    uint32_t r[16];
-    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
-                 "%14, %15}, [%16];"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-                   "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
-                   "=r"(r[15])
+// 32 consecutive accumulator columns of the warp's 32 TMEM lanes, issued without waiting;
+// tc_ld32_wait completes it.  The wait takes the same registers as operands, so no use of them can be
+// scheduled above it.
+__device__ __forceinline__ void tc_ld32_issue(uint32_t taddr, uint32_t (&r)[32]) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
                  : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+__device__ __forceinline__ void tc_ld32_wait(uint32_t (&r)[32]) {
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]), "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]), "+r"(r[15]), "+r"(r[16]), "+r"(r[17]), "+r"(r[18]), "+r"(r[19]), "+r"(r[20]), "+r"(r[21]), "+r"(r[22]), "+r"(r[23]), "+r"(r[24]), "+r"(r[25]), "+r"(r[26]), "+r"(r[27]), "+r"(r[28]), "+r"(r[29]), "+r"(r[30]), "+r"(r[31])
+                 :
+                 : "memory");
 }
 
 // Problem of output tile t of the launch (binary search over the problems' first tiles).
@@ -238,29 +240,128 @@ __device__ __forceinline__ int tc_problem_of(const TcParams &p, int t) {
     return lo;
 }
 
-// Epilogue of one output tile by one warp: TMEM lanes 32 * quarter .. + 31 (tile rows) of the
-// accumulator at TMEM address tacc (lane 0, its first column); scales (split products), load_c /
-// ReLU; store through the row index (and segments).
+// One 32-column chunk of the epilogue (columns n0 + c .. + 31, registers r from TMEM; cs = lane j's
+// column scale 2^-s of column n0 + c + j for split products): scales, load_c / ReLU, store.
 //
 // Whole 32-column chunks of one output go through the warp's 32 x 33 shared-memory buffer `eb`:
 // lane i writes row i's 32 values, then each store instruction covers 4 rows x 32 columns (8 lanes
 // x 16 bytes per row), where a lane storing its own row would scatter 32 rows per instruction.  The
 // 33-float row pitch keeps both passes free of bank conflicts.
-template <int BN, bool SPLIT>
-__device__ __forceinline__ void tc_store_tile(const TcProblem &q, int m0, int n0, int quarter, int lane, uint32_t tacc,
-                                              bool ok, float *eb) {
-    constexpr int TC_BN = BN;
+template <bool SPLIT>
+__device__ __forceinline__ void tc_store_chunk(const TcProblem &q, int n0, int c, int lane, const uint32_t (&r)[32],
+                                               float cs, float rs, bool row_ok, long long orow, bool vec_ok, int &seg,
+                                               float *eb) {
+    float v[32];
+#pragma unroll
+    for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(r[j]);
+    if constexpr (SPLIT) {
+        // undo the scales: (acc * 2^-s_row) * 2^-s_col, each factor exact (every lane takes part)
+#pragma unroll
+        for (int j = 0; j < 32; ++j) v[j] = (v[j] * rs) * __shfl_sync(0xffffffffu, cs, j);
+    }
+    if (q.nseg <= 1 && vec_ok && n0 + c + 32 <= q.n) {  // uniform over the warp
+        __syncwarp();
+#pragma unroll
+        for (int j = 0; j < 32; ++j) eb[lane * 33 + j] = v[j];
+        __syncwarp();
+        const int c4 = (lane & 7) * 4;
+#pragma unroll
+        for (int it = 0; it < 8; ++it) {
+            const int rr = 4 * it + (lane >> 3);  // tile row (TMEM lane) this lane stores
+            const bool ok_r = __shfl_sync(0xffffffffu, row_ok, rr);
+            const long long orow_r = __shfl_sync(0xffffffffu, orow, rr);
+            if (!ok_r) continue;
+            float o[4];
+#pragma unroll
+            for (int t = 0; t < 4; ++t) o[t] = eb[rr * 33 + c4 + t];
+            if (q.c_dtype == SPREG_F32) {
+                float4 *cp = reinterpret_cast<float4 *>(reinterpret_cast<float *>(q.C) + orow_r * q.ldc + n0 + c + c4);
+                if (q.load_c) {
+                    const float4 ci = *cp;
+                    o[0] += ci.x; o[1] += ci.y; o[2] += ci.z; o[3] += ci.w;
+                }
+                if (q.epilogue == SPREG_EPILOGUE_RELU)
+                    for (int t = 0; t < 4; ++t) o[t] = fmaxf(o[t], 0.0f);
+                *cp = make_float4(o[0], o[1], o[2], o[3]);
+            } else {
+                uint2 *cp = reinterpret_cast<uint2 *>(reinterpret_cast<__nv_bfloat16 *>(q.C) + orow_r * q.ldc + n0 + c + c4);
+                if (q.load_c) {
+                    const uint2 ci = *cp;
+                    const __nv_bfloat162 c01 = *reinterpret_cast<const __nv_bfloat162 *>(&ci.x);
+                    const __nv_bfloat162 c23 = *reinterpret_cast<const __nv_bfloat162 *>(&ci.y);
+                    o[0] += __low2float(c01); o[1] += __high2float(c01);
+                    o[2] += __low2float(c23); o[3] += __high2float(c23);
+                }
+                if (q.epilogue == SPREG_EPILOGUE_RELU)
+                    for (int t = 0; t < 4; ++t) o[t] = fmaxf(o[t], 0.0f);
+                __nv_bfloat162 w01 = __floats2bfloat162_rn(o[0], o[1]), w23 = __floats2bfloat162_rn(o[2], o[3]);
+                uint2 w;
+                w.x = *reinterpret_cast<uint32_t *>(&w01);
+                w.y = *reinterpret_cast<uint32_t *>(&w23);
+                *cp = w;
+            }
+        }
+        return;
+    }
+    if (!row_ok) return;
+#pragma unroll
+    for (int j = 0; j < 32; ++j) {
+        const int col = n0 + c + j;
+        if (col >= q.n) break;
+        void *cbase = q.C;
+        int64_t ldc = q.ldc;
+        int lcol = col;
+        if (q.nseg > 1) {
+            while (col >= q.seg_start[seg + 1]) ++seg;
+            cbase = q.seg_c[seg];
+            ldc = q.seg_ldc[seg];
+            lcol = col - q.seg_start[seg];
+        }
+        float o = v[j];
+        if (q.c_dtype == SPREG_F32) {
+            float *cp = reinterpret_cast<float *>(cbase) + orow * ldc + lcol;
+            if (q.load_c) o += *cp;
+            if (q.epilogue == SPREG_EPILOGUE_RELU) o = fmaxf(o, 0.0f);
+            *cp = o;
+        } else {
+            __nv_bfloat16 *cp = reinterpret_cast<__nv_bfloat16 *>(cbase) + orow * ldc + lcol;
+            if (q.load_c) o += __bfloat162float(*cp);
+            if (q.epilogue == SPREG_EPILOGUE_RELU) o = fmaxf(o, 0.0f);
+            *cp = __float2bfloat16_rn(o);
+        }
+    }
+}
+
+// Row index and (split) row scale of lane `lane`'s tile row, read before the accumulator is ready.
+struct TcRowInfo {
+    long long orow;
+    float rs;
+    bool ok;
+};
+template <bool SPLIT>
+__device__ __forceinline__ TcRowInfo tc_row_info(const TcProblem &q, int m0, int quarter, int lane) {
     const int r = m0 + 32 * quarter + lane;
-    const bool row_ok = ok && r < q.R;
-    const long long orow = row_ok ? q.row_index[r] : 0;
-    const float rs = (SPLIT && row_ok) ? q.row_scale[r] : 1.0f;
+    TcRowInfo ri;
+    ri.ok = r < q.R;
+    ri.orow = ri.ok ? q.row_index[r] : 0;
+    ri.rs = (SPLIT && ri.ok) ? q.row_scale[r] : 1.0f;
+    return ri;
+}
+
+// Epilogue of one output tile by one warp: TMEM lanes 32 * quarter .. + 31 (tile rows) of the
+// accumulator at TMEM address tacc (lane 0, its first column); store through the row index (and
+// segments).  The TMEM load of chunk c + 1 (and its column scales) is issued before chunk c is
+// processed, so the TMEM latency overlaps the stores.
+template <int BN, bool SPLIT>
+__device__ __forceinline__ void tc_store_tile(const TcProblem &q, int n0, int quarter, int lane, uint32_t tacc,
+                                              const TcRowInfo &ri, float *eb) {
+    constexpr int NCH = BN / 32;
     const uint32_t tmem = tacc + ((uint32_t)(32 * quarter) << 16);
     // vector stores need 16-byte (F32) / 8-byte (BF16) aligned row starts of C
     const int esz = q.c_dtype == SPREG_F32 ? 4 : 2;
     const bool vec_ok = (reinterpret_cast<uintptr_t>(q.C) % (4 * esz)) == 0 && (q.ldc % 4) == 0;
-    if (!ok) return;
     int seg = 0;  // segment of the current column (coalesced products)
-    if (q.nseg > 1 && row_ok) {
+    if (q.nseg > 1 && ri.ok) {
         int lo2 = 0, hi2 = q.nseg - 1;
         while (lo2 < hi2) {
             const int mid = (lo2 + hi2 + 1) >> 1;
@@ -269,90 +370,34 @@ __device__ __forceinline__ void tc_store_tile(const TcProblem &q, int m0, int n0
         }
         seg = lo2;
     }
-    for (int c = 0; c < TC_BN; c += 32) {
-        float v[32];
-        tc_ld16(tmem + (uint32_t)c, *reinterpret_cast<float(*)[16]>(&v[0]));  // every lane takes part
-        tc_ld16(tmem + (uint32_t)(c + 16), *reinterpret_cast<float(*)[16]>(&v[16]));
+    auto col_scale = [&](int c) -> float {
         if constexpr (SPLIT) {
-            // undo the scales: (acc * 2^-s_row) * 2^-s_col, each factor exact
-#pragma unroll
-            for (int j = 0; j < 32; ++j) {
-                const int col = n0 + c + j;
-                v[j] = (v[j] * rs) * (col < q.n ? __ldg(q.col_scale + col) : 0.0f);
-            }
+            const int col = n0 + c + lane;
+            return col < q.n ? __ldg(q.col_scale + col) : 0.0f;
+        } else {
+            return 1.0f;
         }
-        if (q.nseg <= 1 && vec_ok && n0 + c + 32 <= q.n) {  // uniform over the warp
-            __syncwarp();
+    };
+    uint32_t ra[32], rb[32];
+    tc_ld32_issue(tmem, ra);
+    float cs = col_scale(0);
+    tc_ld32_wait(ra);
 #pragma unroll
-            for (int j = 0; j < 32; ++j) eb[lane * 33 + j] = v[j];
-            __syncwarp();
-            const int c4 = (lane & 7) * 4;
-#pragma unroll
-            for (int it = 0; it < 8; ++it) {
-                const int rr = 4 * it + (lane >> 3);  // tile row (TMEM lane) this lane stores
-                const bool ok_r = __shfl_sync(0xffffffffu, row_ok, rr);
-                const long long orow_r = __shfl_sync(0xffffffffu, orow, rr);
-                if (!ok_r) continue;
-                float o[4];
-#pragma unroll
-                for (int t = 0; t < 4; ++t) o[t] = eb[rr * 33 + c4 + t];
-                if (q.c_dtype == SPREG_F32) {
-                    float4 *cp = reinterpret_cast<float4 *>(reinterpret_cast<float *>(q.C) + orow_r * q.ldc + n0 + c + c4);
-                    if (q.load_c) {
-                        const float4 ci = *cp;
-                        o[0] += ci.x; o[1] += ci.y; o[2] += ci.z; o[3] += ci.w;
-                    }
-                    if (q.epilogue == SPREG_EPILOGUE_RELU)
-                        for (int t = 0; t < 4; ++t) o[t] = fmaxf(o[t], 0.0f);
-                    *cp = make_float4(o[0], o[1], o[2], o[3]);
-                } else {
-                    uint2 *cp = reinterpret_cast<uint2 *>(reinterpret_cast<__nv_bfloat16 *>(q.C) + orow_r * q.ldc + n0 + c +
-                                                          c4);
-                    if (q.load_c) {
-                        const uint2 ci = *cp;
-                        const __nv_bfloat162 c01 = *reinterpret_cast<const __nv_bfloat162 *>(&ci.x);
-                        const __nv_bfloat162 c23 = *reinterpret_cast<const __nv_bfloat162 *>(&ci.y);
-                        o[0] += __low2float(c01); o[1] += __high2float(c01);
-                        o[2] += __low2float(c23); o[3] += __high2float(c23);
-                    }
-                    if (q.epilogue == SPREG_EPILOGUE_RELU)
-                        for (int t = 0; t < 4; ++t) o[t] = fmaxf(o[t], 0.0f);
-                    __nv_bfloat162 w01 = __floats2bfloat162_rn(o[0], o[1]), w23 = __floats2bfloat162_rn(o[2], o[3]);
-                    uint2 w;
-                    w.x = *reinterpret_cast<uint32_t *>(&w01);
-                    w.y = *reinterpret_cast<uint32_t *>(&w23);
-                    *cp = w;
-                }
-            }
-            continue;
+    for (int ci = 0; ci < NCH; ++ci) {
+        const int c = 32 * ci;
+        float cs_next = 1.0f;
+        if (ci + 1 < NCH) {
+            if (ci & 1) tc_ld32_issue(tmem + (uint32_t)(c + 32), ra);
+            else tc_ld32_issue(tmem + (uint32_t)(c + 32), rb);
+            cs_next = col_scale(c + 32);
         }
-        if (!row_ok) continue;
-#pragma unroll
-        for (int j = 0; j < 32; ++j) {
-            const int col = n0 + c + j;
-            if (col >= q.n) break;
-            void *cbase = q.C;
-            int64_t ldc = q.ldc;
-            int lcol = col;
-            if (q.nseg > 1) {
-                while (col >= q.seg_start[seg + 1]) ++seg;
-                cbase = q.seg_c[seg];
-                ldc = q.seg_ldc[seg];
-                lcol = col - q.seg_start[seg];
-            }
-            float o = v[j];
-            if (q.c_dtype == SPREG_F32) {
-                float *cp = reinterpret_cast<float *>(cbase) + orow * ldc + lcol;
-                if (q.load_c) o += *cp;
-                if (q.epilogue == SPREG_EPILOGUE_RELU) o = fmaxf(o, 0.0f);
-                *cp = o;
-            } else {
-                __nv_bfloat16 *cp = reinterpret_cast<__nv_bfloat16 *>(cbase) + orow * ldc + lcol;
-                if (q.load_c) o += __bfloat162float(*cp);
-                if (q.epilogue == SPREG_EPILOGUE_RELU) o = fmaxf(o, 0.0f);
-                *cp = __float2bfloat16_rn(o);
-            }
+        if (ci & 1) tc_store_chunk<SPLIT>(q, n0, c, lane, rb, cs, ri.rs, ri.ok, ri.orow, vec_ok, seg, eb);
+        else tc_store_chunk<SPLIT>(q, n0, c, lane, ra, cs, ri.rs, ri.ok, ri.orow, vec_ok, seg, eb);
+        if (ci + 1 < NCH) {
+            if (ci & 1) tc_ld32_wait(ra);
+            else tc_ld32_wait(rb);
         }
+        cs = cs_next;
     }
 }
 
@@ -518,11 +563,12 @@ __global__ void __launch_bounds__(192, 1) tc_rows_kernel(const __grid_constant__
             const TcProblem &q = p.prob[tc_problem_of(p, t)];
             int m0, n0;
             tile_of(q, t, m0, n0);
+            const TcRowInfo ri = tc_row_info<SPLIT>(q, m0, quarter, lane);  // before the accumulator is ready
             const int a = j & 1;
             ok = ok && __all_sync(0xffffffffu, tc_wait(accf0 + 8u * a, (uint32_t)((j >> 1) & 1), p.status, 24));
             tc_fence_after();
             if (!ok) break;
-            tc_store_tile<BN, SPLIT>(q, m0, n0, quarter, lane, tmem + (uint32_t)(a * TC_BN), ok,
+            tc_store_tile<BN, SPLIT>(q, n0, quarter, lane, tmem + (uint32_t)(a * TC_BN), ri,
                                      epi + quarter * (32 * 33));  // adds the lane quarter
             tc_fence_before();
             __syncwarp();
