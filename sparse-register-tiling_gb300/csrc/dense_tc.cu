@@ -251,6 +251,7 @@ template <bool SPLIT>
 __device__ __forceinline__ void tc_store_chunk(const TcProblem &q, int n0, int c, int lane, const uint32_t (&r)[32],
                                                float cs, float rs, bool row_ok, long long orow, bool vec_ok, int &seg,
                                                float *eb) {
+    if (n0 + c >= q.n) return;  // uniform: a chunk past the last column
     float v[32];
 #pragma unroll
     for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(r[j]);
@@ -259,7 +260,21 @@ __device__ __forceinline__ void tc_store_chunk(const TcProblem &q, int n0, int c
 #pragma unroll
         for (int j = 0; j < 32; ++j) v[j] = (v[j] * rs) * __shfl_sync(0xffffffffu, cs, j);
     }
-    if (q.nseg <= 1 && vec_ok && n0 + c + 32 <= q.n) {  // uniform over the warp
+    // output of this chunk: C itself, or (coalesced products) the segment it lies in, when it lies in one
+    void *cbase = q.C;
+    int64_t cld = q.ldc;
+    int ccol = n0 + c;
+    bool whole = vec_ok && n0 + c + 32 <= q.n;
+    if (q.nseg > 1) {
+        while (n0 + c >= q.seg_start[seg + 1]) ++seg;  // uniform: every lane sees the same columns
+        const int esz = q.c_dtype == SPREG_F32 ? 4 : 2;
+        cbase = q.seg_c[seg];
+        cld = q.seg_ldc[seg];
+        ccol = n0 + c - q.seg_start[seg];
+        whole = n0 + c + 32 <= q.seg_start[seg + 1] && (reinterpret_cast<uintptr_t>(cbase) % (4 * esz)) == 0 &&
+                (cld % 4) == 0 && (ccol % 4) == 0;
+    }
+    if (whole) {  // uniform over the warp
         __syncwarp();
 #pragma unroll
         for (int j = 0; j < 32; ++j) eb[lane * 33 + j] = v[j];
@@ -275,7 +290,7 @@ __device__ __forceinline__ void tc_store_chunk(const TcProblem &q, int n0, int c
 #pragma unroll
             for (int t = 0; t < 4; ++t) o[t] = eb[rr * 33 + c4 + t];
             if (q.c_dtype == SPREG_F32) {
-                float4 *cp = reinterpret_cast<float4 *>(reinterpret_cast<float *>(q.C) + orow_r * q.ldc + n0 + c + c4);
+                float4 *cp = reinterpret_cast<float4 *>(reinterpret_cast<float *>(cbase) + orow_r * cld + ccol + c4);
                 if (q.load_c) {
                     const float4 ci = *cp;
                     o[0] += ci.x; o[1] += ci.y; o[2] += ci.z; o[3] += ci.w;
@@ -284,7 +299,7 @@ __device__ __forceinline__ void tc_store_chunk(const TcProblem &q, int n0, int c
                     for (int t = 0; t < 4; ++t) o[t] = fmaxf(o[t], 0.0f);
                 *cp = make_float4(o[0], o[1], o[2], o[3]);
             } else {
-                uint2 *cp = reinterpret_cast<uint2 *>(reinterpret_cast<__nv_bfloat16 *>(q.C) + orow_r * q.ldc + n0 + c + c4);
+                uint2 *cp = reinterpret_cast<uint2 *>(reinterpret_cast<__nv_bfloat16 *>(cbase) + orow_r * cld + ccol + c4);
                 if (q.load_c) {
                     const uint2 ci = *cp;
                     const __nv_bfloat162 c01 = *reinterpret_cast<const __nv_bfloat162 *>(&ci.x);
