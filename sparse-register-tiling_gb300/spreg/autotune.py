@@ -395,7 +395,15 @@ def tune(A: np.ndarray, n: int, dtype: str = "f32", top: int = 4, costs: Optiona
             return packs[key].execute_timed(Bs[0], Cs[0], num_runs=runs, nr=c.nr, warps=c.warps)
         return _time_batched(packs[key], Bs, Cs, c.nr, warps=c.warps)
 
-    for _, c in ranked[:max(1, top)]:
+    # the model's top candidates, and the best-ranked candidate of every (M_r, nanokernel set) family,
+    # so that a family the model underrates is still timed
+    timed = [c for _, c in ranked[:max(1, top)]]
+    seen = {(c.mr, c.mapping) for c in timed}
+    for _, c in ranked:
+        if (c.mr, c.mapping) not in seen:
+            seen.add((c.mr, c.mapping))
+            timed.append(c)
+    for c in timed:
         measured[c.name()] = time_reg(c)
     best_reg = by_name[min(measured, key=measured.get)]
     if warps:

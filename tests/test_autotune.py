@@ -99,7 +99,10 @@ def test_tune_picks_a_measured_candidate_and_it_is_exact(cuda):
     from spreg.autotune import tune
     A = synth.row_skew(1024, 512, 0.9, seed=4)
     res = tune(A, 128, "f32", top=3, tc=False, warps=False)
-    assert res.best.name() in res.measured_ns and len(res.measured_ns) == 3
+    assert res.best.name() in res.measured_ns and len(res.measured_ns) >= 3
+    # every (M_r, nanokernel set) family was timed at least once
+    fams = {n.split("_")[0][:2] + "_" + n.split("_")[1] for n in res.measured_ns}
+    assert {"M2_identity", "M4_identity", "M8_identity", "M8_400fa", "M8_747f9"} <= fams
     assert res.measured_ns[res.best.name()] == min(res.measured_ns.values())
     m = mapping_of(res.best.mr, res.best.mapping)
     B = synth.dense(512, 128, seed=5)
