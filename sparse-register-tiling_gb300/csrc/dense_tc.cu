@@ -63,25 +63,18 @@ constexpr int TC_BK_SPLIT = 32;
 template <bool SPLIT> constexpr int tc_bk() { return SPLIT ? TC_BK_SPLIT : TC_BK; }
 // Output tile width BN (128 or 256): the MMA's N, the TMEM accumulator's columns, B tile rows.
 // A split product stages both halves of A and of B.
-// MH: 128-row halves of an output tile (1 or 2).  A tile of 256 rows runs two M = 128 MMAs per K
-// step that share the stage's B tile, so each B tile leaves L2 half as often (the kernel's rate is
-// set by how fast operands arrive, not by the tensor pipe).
 template <int BN, bool SPLIT> constexpr uint32_t tc_tile_a() { return (uint32_t)TC_BM * tc_bk<SPLIT>() * 2; }
 template <int BN, bool SPLIT = false> constexpr uint32_t tc_tile_b() { return (uint32_t)BN * tc_bk<SPLIT>() * 2; }
-template <int BN, bool SPLIT, int MH> constexpr uint32_t tc_stage() {
-    return (SPLIT ? 2u : 1u) * ((uint32_t)MH * tc_tile_a<BN, SPLIT>() + tc_tile_b<BN, SPLIT>());
+template <int BN, bool SPLIT> constexpr uint32_t tc_stage() {
+    return (SPLIT ? 2u : 1u) * (tc_tile_a<BN, SPLIT>() + tc_tile_b<BN, SPLIT>());
 }
-// Stages of the ring: as many as fit in 192 KB of operands.
-template <int BN, bool SPLIT, int MH> constexpr int tc_stages() { return (int)(196608u / tc_stage<BN, SPLIT, MH>()); }
-// TMEM columns of one accumulator set (MH halves x BN) and how many sets (2: the next tile's MMAs
-// overlap this tile's epilogue) fit the 512 columns.
-template <int BN, int MH> constexpr uint32_t tc_acc_cols() { return (uint32_t)(MH * BN); }
-template <int BN, int MH> constexpr int tc_acc_bufs() { return 2 * tc_acc_cols<BN, MH>() <= 512 ? 2 : 1; }
+// Stages of the ring: about 190 KB of operands.
+template <int BN, bool SPLIT> constexpr int tc_stages() { return !SPLIT ? 4 : BN == 256 ? 4 : 6; }
 // The epilogue warps' staging buffers: 4 x 32 rows x 33 floats.
 constexpr uint32_t TC_EPI_BYTES = 4u * 32u * 33u * 4u;
-template <int BN, bool SPLIT, int MH> constexpr size_t tc_smem() {
-    return 1024 /* alignment slack */ + tc_stages<BN, SPLIT, MH>() * tc_stage<BN, SPLIT, MH>() +
-           256 /* barriers, TMEM slot */ + TC_EPI_BYTES;
+template <int BN, bool SPLIT> constexpr size_t tc_smem() {
+    return 1024 /* alignment slack */ + tc_stages<BN, SPLIT>() * tc_stage<BN, SPLIT>() + 256 /* barriers, TMEM slot */ +
+           TC_EPI_BYTES;
 }
 
 constexpr int TC_MAX_PROBLEMS = 192;  // problems per launch (kernel parameters <= 32 KB)
@@ -423,30 +416,23 @@ __device__ __forceinline__ void tc_store_tile(const TcProblem &q, int n0, int qu
     }
 }
 
-// Persistent.  CTA b takes output tiles (MH x 128 rows x BN columns) b, b + gridDim.x, ...  Warp 0
-// (lane 0) loads the operand tiles of every K block of those tiles into the stage ring; warp 1 (lane
-// 0) issues the MMAs of tile j into TMEM accumulator set j % NBUF (MH x BN columns; half h at column
-// h x BN) and commits "acc full"; warps 2..5 read an accumulator set (warp w reads TMEM lane quarter
-// w % 4 of each half), store the tile and arrive on "acc empty".  With two sets the next tile's MMAs
-// overlap this tile's stores.
+// Persistent.  CTA b takes output tiles b, b + gridDim.x, ...  Warp 0 (lane 0) loads the operand
+// tiles of every K block of those tiles into the stage ring; warp 1 (lane 0) issues the MMAs of tile j
+// into TMEM accumulator j % 2 (2 x BN columns) and commits "acc full"; warps 2..5 read an
+// accumulator (warp w reads TMEM lane quarter w % 4), store the tile and arrive on "acc empty", so
+// the next tile's MMAs overlap this tile's stores.
 //
-// A stage holds, per 128-row half h, [A h] (SPLIT: [A hi h | A lo h]), then B (SPLIT: [B hi | B lo]);
-// per 16-deep K step the issuer runs, for each half, one MMA (SPLIT: hi.hi, hi.lo and lo.hi into the
-// same accumulator, FP16 operands).
-template <int BN, bool SPLIT, int MH>
+// SPLIT: a stage holds [A hi | A lo | B hi | B lo]; per 16-deep K step the issuer runs
+// hi.hi, hi.lo and lo.hi into the same accumulator (FP16 operands).
+template <int BN, bool SPLIT>
 __global__ void __launch_bounds__(192, 1) tc_rows_kernel(const __grid_constant__ TcParams p, const int total_tiles) {
-    constexpr int STAGES = tc_stages<BN, SPLIT, MH>();
+    constexpr int STAGES = tc_stages<BN, SPLIT>();
     constexpr int BK = tc_bk<SPLIT>();
-    constexpr int NBUF = tc_acc_bufs<BN, MH>();
-    constexpr uint32_t ACC_COLS = tc_acc_cols<BN, MH>(), TC_TMEM_COLS = NBUF * ACC_COLS;
-    constexpr uint32_t TC_STAGE = tc_stage<BN, SPLIT, MH>();
+    constexpr uint32_t TC_STAGE = tc_stage<BN, SPLIT>(), TC_TMEM_COLS = 2 * BN;
     constexpr uint32_t TILE_A = tc_tile_a<BN, SPLIT>();         // A hi -> A lo
-    constexpr uint32_t A_HALF = (SPLIT ? 2u : 1u) * TILE_A;      // one 128-row half's A tiles
-    constexpr uint32_t A_BYTES = (uint32_t)MH * A_HALF;          // B tiles start here
+    constexpr uint32_t A_BYTES = (SPLIT ? 2u : 1u) * TILE_A;     // B tiles start here
     constexpr uint32_t B_HALF = tc_tile_b<BN, SPLIT>();          // B hi -> B lo
-    constexpr int TC_BN = BN, TM = TC_BM * MH;                   // output tile rows
-    static_assert(MH == 1 || MH == 2, "tiles of 128 or 256 rows");
-    static_assert(TC_TMEM_COLS <= 512 && STAGES >= 2, "TMEM and shared-memory budget");
+    constexpr int TC_BN = BN;
     extern __shared__ unsigned char smem_raw[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t raw = smem_u32(smem_raw);
@@ -480,7 +466,7 @@ __global__ void __launch_bounds__(192, 1) tc_rows_kernel(const __grid_constant__
     // output tile t of problem q
     auto tile_of = [&](const TcProblem &q, int t, int &m0, int &n0) {
         const int local = t - q.tile_begin;
-        m0 = (local / q.tiles_n) * TM;
+        m0 = (local / q.tiles_n) * TC_BM;
         n0 = (local % q.tiles_n) * TC_BN;
     };
 
@@ -509,13 +495,9 @@ __global__ void __launch_bounds__(192, 1) tc_rows_kernel(const __grid_constant__
                     const uint32_t st = sbase + (uint32_t)s * TC_STAGE;
                     tc_expect_tx(full0 + 8u * s, TC_STAGE);
                     const int kx = (q.kb0 + kb) * BK;  // K offset of this block
-#pragma unroll
-                    for (int h = 0; h < MH; ++h) {
-                        tc_tma_2d(st + A_HALF * h, q.a_map, kx, m0 + TC_BM * h, full0 + 8u * s);
-                        if constexpr (SPLIT)
-                            tc_tma_2d(st + A_HALF * h + TILE_A, q.a_map, kx, q.a_lo_row + m0 + TC_BM * h, full0 + 8u * s);
-                    }
+                    tc_tma_2d(st, q.a_map, kx, m0, full0 + 8u * s);
                     if constexpr (SPLIT) {
+                        tc_tma_2d(st + TILE_A, q.a_map, kx, q.a_lo_row + m0, full0 + 8u * s);
                         // B halves: BN / 32 copies of 32 columns x 32 K rows each, 2 KB apart
 #pragma unroll
                         for (int jb = 0; jb < TC_BN / 32; ++jb) {
@@ -547,10 +529,10 @@ __global__ void __launch_bounds__(192, 1) tc_rows_kernel(const __grid_constant__
             bool ok = true;
             for (int t = (int)blockIdx.x; t < total_tiles && ok; t += (int)gridDim.x, ++j) {
                 const TcProblem &q = p.prob[tc_problem_of(p, t)];
-                const int a = j % NBUF;
-                if (j >= NBUF && !tc_wait(acce0 + 8u * a, (uint32_t)(((j / NBUF) - 1) & 1), p.status, 25)) break;
+                const int a = j & 1;
+                if (j >= 2 && !tc_wait(acce0 + 8u * a, (uint32_t)(((j >> 1) - 1) & 1), p.status, 25)) break;
                 tc_fence_after();
-                const uint32_t dacc0 = tmem + (uint32_t)a * ACC_COLS;
+                const uint32_t dacc = tmem + (uint32_t)(a * TC_BN);
                 for (int kb = 0; kb < q.kblocks; ++kb, ++g) {
                     const int s = (int)(g % STAGES);
                     if (!tc_wait(full0 + 8u * s, (uint32_t)((g / STAGES) & 1), p.status, 23)) {
@@ -564,33 +546,23 @@ __global__ void __launch_bounds__(192, 1) tc_rows_kernel(const __grid_constant__
                         // 64 bytes of B; N-major B (transpose-B bit of the instruction descriptor)
 #pragma unroll
                         for (int k = 0; k < BK / 16; ++k) {
-                            const uint64_t bh = tc_desc64_mn(st + A_BYTES + 1024u * k);
-                            const uint64_t bl = tc_desc64_mn(st + A_BYTES + B_HALF + 1024u * k);
-#pragma unroll
-                            for (int h = 0; h < MH; ++h) {
-                                const uint32_t dacc = dacc0 + (uint32_t)(h * TC_BN);
-                                const uint64_t ah = tc_desc64(st + A_HALF * h + 32u * k);
-                                tc_mma(dacc, ah, bh, idesc | (1u << 16), (kb | k) != 0);
-                                tc_mma(dacc, ah, bl, idesc | (1u << 16), 1);
-                                tc_mma(dacc, tc_desc64(st + A_HALF * h + TILE_A + 32u * k), bh, idesc | (1u << 16), 1);
-                            }
+                            const uint64_t ah = tc_desc64(st + 32u * k), bh = tc_desc64_mn(st + A_BYTES + 1024u * k);
+                            tc_mma(dacc, ah, bh, idesc | (1u << 16), (kb | k) != 0);
+                            tc_mma(dacc, ah, tc_desc64_mn(st + A_BYTES + B_HALF + 1024u * k), idesc | (1u << 16), 1);
+                            tc_mma(dacc, tc_desc64(st + TILE_A + 32u * k), bh, idesc | (1u << 16), 1);
                         }
                     } else if (q.b_mn) {
                         // N-major B (transpose-B bit of the instruction descriptor); a 16-deep K step is
                         // 16 rows of 128 bytes
 #pragma unroll
                         for (int k = 0; k < BK / 16; ++k)
-#pragma unroll
-                            for (int h = 0; h < MH; ++h)
-                                tc_mma(dacc0 + (uint32_t)(h * TC_BN), tc_desc(st + A_HALF * h + 32u * k),
-                                       tc_desc_mn(st + A_BYTES + 2048u * k), idesc | (1u << 16), (kb | k) != 0);
+                            tc_mma(dacc, tc_desc(st + 32u * k), tc_desc_mn(st + A_BYTES + 2048u * k), idesc | (1u << 16),
+                                   (kb | k) != 0);
                     } else {
 #pragma unroll
                         for (int k = 0; k < BK / 16; ++k)
-#pragma unroll
-                            for (int h = 0; h < MH; ++h)
-                                tc_mma(dacc0 + (uint32_t)(h * TC_BN), tc_desc(st + A_HALF * h + 32u * k),
-                                       tc_desc(st + A_BYTES + 32u * k), idesc, (kb | k) != 0);
+                            tc_mma(dacc, tc_desc(st + 32u * k), tc_desc(st + A_BYTES + 32u * k), idesc,
+                                   (kb | k) != 0);
                     }
                     tc_commit(empty0 + 8u * s);  // the stage is free once these MMAs have read it
                 }
@@ -606,17 +578,13 @@ __global__ void __launch_bounds__(192, 1) tc_rows_kernel(const __grid_constant__
             const TcProblem &q = p.prob[tc_problem_of(p, t)];
             int m0, n0;
             tile_of(q, t, m0, n0);
-            TcRowInfo ri[MH];  // read before the accumulator is ready
-#pragma unroll
-            for (int h = 0; h < MH; ++h) ri[h] = tc_row_info<SPLIT>(q, m0 + TC_BM * h, quarter, lane);
-            const int a = j % NBUF;
-            ok = ok && __all_sync(0xffffffffu, tc_wait(accf0 + 8u * a, (uint32_t)((j / NBUF) & 1), p.status, 24));
+            const TcRowInfo ri = tc_row_info<SPLIT>(q, m0, quarter, lane);  // before the accumulator is ready
+            const int a = j & 1;
+            ok = ok && __all_sync(0xffffffffu, tc_wait(accf0 + 8u * a, (uint32_t)((j >> 1) & 1), p.status, 24));
             tc_fence_after();
             if (!ok) break;
-#pragma unroll
-            for (int h = 0; h < MH; ++h)
-                tc_store_tile<BN, SPLIT>(q, n0, quarter, lane, tmem + (uint32_t)a * ACC_COLS + (uint32_t)(h * TC_BN), ri[h],
-                                         epi + quarter * (32 * 33));  // adds the lane quarter
+            tc_store_tile<BN, SPLIT>(q, n0, quarter, lane, tmem + (uint32_t)(a * TC_BN), ri,
+                                     epi + quarter * (32 * 33));  // adds the lane quarter
             tc_fence_before();
             __syncwarp();
             if (lane == 0) mbar_arrive_tc(acce0 + 8u * a);
@@ -873,7 +841,7 @@ struct TcGroup {
 
 struct TcLaunch {
     std::unique_ptr<TcParams> p;
-    int bn = 128, mh = 1, tiles = 0;
+    int bn = 128, tiles = 0;
 };
 
 // Everything one call (or one reusable plan) launches: the B preparation (transpose or split) and
@@ -908,18 +876,14 @@ int tc_device_setup(int *sms_out) {
     int dev = 0;
     SPREG_CUDA(cudaGetDevice(&dev));
     if (dev >= 0 && dev < 64 && !configured[dev].load()) {
-#define SPREG_TC_SMEM_ATTR(BN, SPLIT, MH)                                                                       \
-    SPREG_CUDA(cudaFuncSetAttribute(tc_rows_kernel<BN, SPLIT, MH>, cudaFuncAttributeMaxDynamicSharedMemorySize,   \
-                                    (int)tc_smem<BN, SPLIT, MH>()))
-        SPREG_TC_SMEM_ATTR(128, false, 1);
-        SPREG_TC_SMEM_ATTR(256, false, 1);
-        SPREG_TC_SMEM_ATTR(128, true, 1);
-        SPREG_TC_SMEM_ATTR(256, true, 1);
-        SPREG_TC_SMEM_ATTR(128, false, 2);
-        SPREG_TC_SMEM_ATTR(256, false, 2);
-        SPREG_TC_SMEM_ATTR(128, true, 2);
-        SPREG_TC_SMEM_ATTR(256, true, 2);
-#undef SPREG_TC_SMEM_ATTR
+        SPREG_CUDA(cudaFuncSetAttribute(tc_rows_kernel<128, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)tc_smem<128, false>()));
+        SPREG_CUDA(cudaFuncSetAttribute(tc_rows_kernel<256, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)tc_smem<256, false>()));
+        SPREG_CUDA(cudaFuncSetAttribute(tc_rows_kernel<128, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)tc_smem<128, true>()));
+        SPREG_CUDA(cudaFuncSetAttribute(tc_rows_kernel<256, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)tc_smem<256, true>()));
         configured[dev].store(true);
     }
     if (dev >= 0 && dev < 64 && !sms_of[dev].load()) {
@@ -1125,17 +1089,6 @@ int tc_plan_fill(TcPlan &pl, int *status) {
                 if (!hint && (pl.items[m].tile_n == 128 || pl.items[m].tile_n == 256)) hint = pl.items[m].tile_n;
         }
         const int bn = hint ? hint : (min_n > 128 ? 256 : 128);
-        // 256-row tiles (two halves sharing each B tile) when every problem of the launch has more than
-        // 128 rows and at most 2048 K per pass: the rate of these launches is set by operand traffic,
-        // and a B tile then leaves L2 half as often.  Longer K keeps 128-row tiles with two accumulator
-        // sets, whose epilogue overlaps the next tile's MMAs.
-        int64_t min_r = INT64_MAX, max_kc = 0;
-        for (size_t j = 0; j < cnt; ++j) {
-            const TcItem &f = pl.items[pl.groups[specs[first + j].first].first];
-            min_r = std::min<int64_t>(min_r, f.rows);
-            max_kc = std::max<int64_t>(max_kc, split ? std::min<int64_t>(f.k, TC_SPLIT_CHUNK) : f.k);
-        }
-        const int mh = (min_r > TC_BM && max_kc <= 2048) ? 2 : 1;
         int64_t tiles = 0;
         for (size_t j = 0; j < cnt; ++j) {
             const size_t gi = (size_t)specs[first + j].first;
@@ -1167,7 +1120,7 @@ int tc_plan_fill(TcPlan &pl, int *status) {
             }
             q.tiles_n = (int32_t)((g.n + bn - 1) / bn);
             q.tile_begin = (int32_t)tiles;
-            tiles += (it.rows + TC_BM * mh - 1) / (TC_BM * mh) * q.tiles_n;
+            tiles += (it.rows + TC_BM - 1) / TC_BM * q.tiles_n;
             q.b_mn = g.mn ? 1 : 0;
             if (ps > 0) {  // later pass of a split product: the maps exist
                 q.a_lo_row = (int32_t)it.rows;
@@ -1192,7 +1145,6 @@ int tc_plan_fill(TcPlan &pl, int *status) {
         }
         SPREG_CHECK_ARG(tiles <= INT32_MAX, "too many output tiles in one launch");
         L.bn = bn;
-        L.mh = mh;
         L.tiles = (int)tiles;
         pl.launches.push_back(std::move(L));
     }
@@ -1206,19 +1158,10 @@ int tc_plan_upload(const TcPlan &pl, cudaStream_t stream) {
     return SPREG_OK;
 }
 
-template <int BN, bool SPLIT, int MH>
+template <int BN, bool SPLIT>
 cudaError_t tc_launch(const TcParams &p, int tiles, int sms, cudaStream_t stream) {
-    tc_rows_kernel<BN, SPLIT, MH><<<(unsigned)std::min(tiles, sms), 192, tc_smem<BN, SPLIT, MH>(), stream>>>(p, tiles);
+    tc_rows_kernel<BN, SPLIT><<<(unsigned)std::min(tiles, sms), 192, tc_smem<BN, SPLIT>(), stream>>>(p, tiles);
     return cudaGetLastError();
-}
-
-template <bool SPLIT>
-cudaError_t tc_launch_shape(const TcLaunch &L, int sms, cudaStream_t stream) {
-    if (L.mh == 2)
-        return L.bn == 256 ? tc_launch<256, SPLIT, 2>(*L.p, L.tiles, sms, stream)
-                           : tc_launch<128, SPLIT, 2>(*L.p, L.tiles, sms, stream);
-    return L.bn == 256 ? tc_launch<256, SPLIT, 1>(*L.p, L.tiles, sms, stream)
-                       : tc_launch<128, SPLIT, 1>(*L.p, L.tiles, sms, stream);
 }
 
 // The B preparation, then every tensor-core launch.
@@ -1237,7 +1180,12 @@ int tc_plan_launch(const TcPlan &pl, cudaStream_t stream) {
     for (size_t i = 0; i < pl.launches.size() && e == cudaSuccess; ++i) {
         const TcLaunch &L = pl.launches[i];
         if (L.tiles == 0) continue;
-        e = pl.split ? tc_launch_shape<true>(L, pl.sms, stream) : tc_launch_shape<false>(L, pl.sms, stream);
+        if (pl.split)
+            e = L.bn == 256 ? tc_launch<256, true>(*L.p, L.tiles, pl.sms, stream)
+                            : tc_launch<128, true>(*L.p, L.tiles, pl.sms, stream);
+        else
+            e = L.bn == 256 ? tc_launch<256, false>(*L.p, L.tiles, pl.sms, stream)
+                            : tc_launch<128, false>(*L.p, L.tiles, pl.sms, stream);
     }
     if (e != cudaSuccess) SPREG_FAIL(SPREG_ERR_CUDA, "tensor-core launch: %s", cudaGetErrorString(e));
     return SPREG_OK;
