@@ -245,7 +245,7 @@ def fit_costs(samples: Sequence[Tuple[str, PanelStats, int, int, float]], sms: i
 
 
 # ---------------------------------------------------------------------------- tuning
-K_TILES = (0, 128, 512, 1024)
+K_TILES = (0, 128, 256, 512, 1024)
 
 
 def candidates(n: int, mrs: Iterable[int] = (2, 4, 8), k: int = 0,

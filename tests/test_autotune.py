@@ -84,7 +84,7 @@ def test_rank_orders_all_candidates():
     wide = {c.name() for c in candidates(64, (2,), k=2048)}
     assert {"M2N64_identity", "M2N64_identity_K512", "M2N64_identity_K1024"} <= wide
     assert not any("_K" in c.name() for c in candidates(64, (4,), k=128))
-    assert {c.k_tile for c in candidates(64, (4,), k=512)} == {0, 128}
+    assert {c.k_tile for c in candidates(64, (4,), k=512)} == {0, 128, 256}
     # 256-column strips: 16-bit B, M_r <= 4, K_c <= 128, n >= 128
     w = {c.name() for c in candidates(512, (4, 8), k=1024, wide=True)}
     assert "M4N256_identity_K128" in w and not any(n.startswith("M8N256") for n in w)
