@@ -361,10 +361,10 @@ def precision_suite(dev) -> list:
             c = tuned[tkey]
             pm = PackedMatrix.from_dense(At, mapping_of(c.mr, c.mapping), k_tile=c.k_tile, value_dtype=vd)
             Bt = torch.from_numpy(B).to(dev).to(tdt)
-            C = pm.execute(Bt, nr=c.nr)
+            C = pm.execute(Bt, nr=c.nr, warps=c.warps, rounds=c.rounds)
             row[f"rel_err_{name}"] = float(O.rel_err(C.cpu().numpy(), ref))
             Cf = torch.empty((M, 3136), device=dev)
-            t = pm.execute_timed(Bt, Cf, num_runs=2, nr=c.nr)
+            t = pm.execute_timed(Bt, Cf, num_runs=2, nr=c.nr, warps=c.warps, rounds=c.rounds)
             row[f"{name}_us"] = t / 1e3
             row[f"{name}_gflops"] = 2 * int(pm.info["nnz"]) * 3136 / t
             row[f"{name}_gbs"] = pm.algorithmic_bytes(3136, b_bytes=4 if vd == F32 else 2) / t
@@ -514,7 +514,7 @@ def ffn_sweep(dev, min_replicas: int = 96, steps: int = 20) -> list:
                                 for A in As[1:replicas]]
                 Bd = [B0.roll(r, 0).to(tdt) for r in range(replicas)]  # a distinct B per replica
                 Cd = [torch.empty((M, 512), device=dev) for _ in range(replicas)]
-                work = [(p, b, cc, dict(nr=c.nr, warps=c.warps)) for p, b, cc in zip(packs, Bd, Cd)]
+                work = [(p, b, cc, dict(nr=c.nr, warps=c.warps, rounds=c.rounds)) for p, b, cc in zip(packs, Bd, Cd)]
                 sec = timed(lambda: execute_batched(work))
                 bsz = 4 if vd == F32 else 2
                 nbytes = sum(p.algorithmic_bytes(512, b_bytes=bsz) for p in packs)
@@ -615,9 +615,9 @@ def layers_suite(dev, steps: int = 50) -> dict:
             if t.tc_rows:
                 tc_rows.append((t.a_rows, t.row_index, B, C, B.shape[1], t.cols, False, 0))
             if not t.all_tc:
-                work.append((t.packed, B, C, dict(nr=c.nr, warps=c.warps)))
+                work.append((t.packed, B, C, dict(nr=c.nr, warps=c.warps, rounds=c.rounds)))
         else:
-            work.append((t, B, C, dict(nr=c.nr, warps=c.warps)))
+            work.append((t, B, C, dict(nr=c.nr, warps=c.warps, rounds=c.rounds)))
     plan = DenseRowsPlan(bf16_items(tc_rows)) if tc_rows else None
 
     def batched_step():

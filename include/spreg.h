@@ -23,7 +23,7 @@
  * Device status word: kernels never trap.  A bounded wait that gives up, or an index a kernel's
  * own bounds check refuses, records a nonzero code in a per-device word instead (read and clear it
  * with spreg_device_status):
- *   2, 5-7   executor waits (batched and B-tile kernels);   20  CSR column index out of range;
+ *   2, 5-8   executor waits (batched and B-tile kernels);   20  CSR column index out of range;
  *   21-25    tensor-core kernel waits;                         30  spreg_selftest_wait_timeout.
  */
 #ifndef SPREG_H
@@ -221,7 +221,11 @@ typedef struct {
                             panels outer (a panel's strips one after another, its metadata reused), 1 =
                             column strips outer (a strip of B reused across panels).  Results do not
                             depend on it (each element's FMA order is fixed). */
-    int32_t reserved;    /* 0 */
+    int32_t panel_rounds; /* 0 or 1: one round; R > 1 (<= 64): the B-tile kernel keeps a job's strip of B
+                             for every K tile resident in shared memory while R rounds of its consumer
+                             warps' panels run against it (B read from L2 once per R x warps panels).
+                             Needs b_staging 0 or 1 and a strip (K x 32 * nr/32 columns) that fits
+                             shared memory; results do not depend on it. */
 } spreg_exec_args;
 
 /* One SpMM: C (+)= A . B over the first n columns -- sop_multiple_panel_executor (template:265-305). */

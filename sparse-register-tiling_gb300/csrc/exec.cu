@@ -285,6 +285,7 @@ struct CallPlan {
     ExecParams sp;           // parameters of the register-stream kernel
     int warps;
     int warps_req;           // warps_per_cta as asked (0: each kernel's own choice) -- the CTA tiling
+    int rounds;              // panel rounds of the B-tile kernel (1: B tiles in the ring stages)
 };
 
 int plan_call(const spreg_packed *a, const spreg_exec_args *args, CallPlan *cp, int64_t others1) {
@@ -302,6 +303,11 @@ int plan_call(const spreg_packed *a, const spreg_exec_args *args, CallPlan *cp, 
     SPREG_CHECK_ARG(args->meta_staging >= 0 && args->meta_staging <= 2, "meta_staging must be 0, 1 or 2");
     SPREG_CHECK_ARG(args->b_staging >= 0 && args->b_staging <= 2, "b_staging must be 0, 1 or 2");
     SPREG_CHECK_ARG(args->job_order == 0 || args->job_order == 1, "job_order must be 0 or 1");
+    SPREG_CHECK_ARG(args->panel_rounds >= 0 && args->panel_rounds <= kTileMaxRounds, "panel_rounds must be in [0, %d]",
+                    kTileMaxRounds);
+    const int rounds = args->panel_rounds > 1 ? args->panel_rounds : 1;
+    SPREG_CHECK_ARG(rounds == 1 || (args->b_staging != 2 && args->meta_staging != 2),
+                    "panel_rounds > 1 runs the shared-memory B-tile kernel (b_staging 0 or 1, meta_staging 0 or 1)");
     int dev = -1;
     SPREG_CUDA(cudaGetDevice(&dev));
     SPREG_CHECK_ARG(dev == a->device, "packed matrix lives on device %d, current device is %d", a->device, dev);
@@ -341,6 +347,20 @@ int plan_call(const spreg_packed *a, const spreg_exec_args *args, CallPlan *cp, 
     auto tile_rows_ok = [&](int nvv) { return staged_rows * 32 * nvv * (int64_t)bsz <= kTileMaxStageB; };
     const bool tile_base_ok = a->exec && !a->list_packed && aligned(args->b, 16) &&
                               (args->ldb * (int64_t)bsz) % 16 == 0 && 1024 + 2 * cp->xbuf <= f->smem_optin;
+    // Panel rounds keep the strip of every K tile resident: T tiles of staged_rows rows each.
+    auto strip_bytes = [&](int nvv) { return (a->geom.T * staged_rows * 32 * nvv * (int64_t)bsz + 127) / 128 * 128; };
+    auto strip_fits = [&](int nvv) { return 1024 + strip_bytes(nvv) + 2 * cp->xbuf <= f->smem_optin; };
+    cp->rounds = rounds;
+    if (rounds > 1) {
+        SPREG_CHECK_ARG(tile_base_ok, "panel rounds need a dense/CSR pack, a 16-byte aligned B with 16-byte aligned "
+                        "rows, and execution blocks that fit shared memory");
+        SPREG_CHECK_ARG(args->n <= INT32_MAX && a->geom.T < 65536, "panel rounds: n or the K tile count out of range");
+        if (args->nr == 0)
+            while (nv > 1 && !strip_fits(nv)) nv >>= 1;
+        SPREG_CHECK_ARG(strip_fits(nv) && strip_fits(1),
+                        "panel rounds: the strip of B for all K tiles (%lld bytes at %d columns) does not fit shared "
+                        "memory; use a narrower strip (nr) or panel_rounds 0", (long long)strip_bytes(nv), 32 * nv);
+    }
     if (args->b_staging == 1) {
         SPREG_CHECK_ARG(tile_base_ok, "shared-memory B tiles need a dense/CSR pack, a 16-byte aligned B with "
                         "16-byte aligned rows, and execution blocks that fit shared memory");
@@ -362,10 +382,11 @@ int plan_call(const spreg_packed *a, const spreg_exec_args *args, CallPlan *cp, 
     }
     const bool hot_set = all > 0 && 100 * hot >= 85 * all;
     const bool tile_kernel =
-        args->b_staging == 1 || (args->b_staging == 0 && tile_base_ok && args->meta_staging != 2 &&
+        args->b_staging == 1 || rounds > 1 || (args->b_staging == 0 && tile_base_ok && args->meta_staging != 2 &&
                                  !cp->stream_kernel && a->geom.T > 1 && args->n <= INT32_MAX &&
                                  staged_rows * 32 * nv * (int64_t)bsz <= 64 * 1024);
     if (tile_kernel && bsz == 2 && in.mr <= 4 && nv == 4 && (args->nr == 0 || args->nr == 256) && args->n >= 256 &&
+        (rounds == 1 || strip_fits(8)) &&
         staged_rows * 256 * (int64_t)bsz <= 64 * 1024 && aligned(args->b, 16) && args->ldb % 8 == 0 &&
         aligned(args->c, csz * 8) && args->ldc % 8 == 0 &&
         (args->nr == 256 || (hot_set && in.num_panels * (args->n / 256) + others1 / 8 >= (int64_t)f->sms * 8)))
@@ -407,9 +428,9 @@ int plan_call(const spreg_packed *a, const spreg_exec_args *args, CallPlan *cp, 
     const bool auto_tile = args->b_staging == 0 && tile_base_ok && args->meta_staging != 2 && !cp->stream_kernel &&
                            a->geom.T > 1 && args->n <= INT32_MAX &&
                            staged_rows * 32 * nv * (int64_t)bsz <= 64 * 1024;
-    if (args->b_staging == 1 || auto_tile) {
-        const bool main_ok = !cp->has_main || tile_rows_ok(nv);
-        const bool tail_ok = !cp->has_tail || tile_rows_ok(1);
+    if (args->b_staging == 1 || rounds > 1 || auto_tile) {
+        const bool main_ok = !cp->has_main || rounds > 1 || tile_rows_ok(nv);
+        const bool tail_ok = !cp->has_tail || rounds > 1 || tile_rows_ok(1);
         SPREG_CHECK_ARG(main_ok && tail_ok, "shared-memory B tiles: a K tile of %lld rows x %d columns exceeds a "
                         "stage (%lld bytes); pack with a smaller k_tile", (long long)kt_rows, 32 * nv,
                         (long long)kTileMaxStageB);
@@ -450,8 +471,8 @@ int plan_call(const spreg_packed *a, const spreg_exec_args *args, CallPlan *cp, 
         if (cp->has_tail && (st = encode_b_map(&cp->ttail.tmap, args->b, args->b_dtype, args->n, brows, args->ldb, 32,
                                                box_rows)))
             return st;
-        cp->stage_b_main = (staged_rows * 32 * nv * (int64_t)bsz + 127) / 128 * 128;
-        cp->stage_b_tail = (staged_rows * 32 * (int64_t)bsz + 127) / 128 * 128;
+        cp->stage_b_main = rounds > 1 ? strip_bytes(nv) : (staged_rows * 32 * nv * (int64_t)bsz + 127) / 128 * 128;
+        cp->stage_b_tail = rounds > 1 ? strip_bytes(1) : (staged_rows * 32 * (int64_t)bsz + 127) / 128 * 128;
     }
 
     ExecParams &p = cp->sp;
@@ -546,25 +567,43 @@ int launch_groups(std::map<std::tuple<int, int, int>, Group> &groups, cudaStream
 
 // One tile-kernel launch per group of at most kMaxBatchProblems problems of one configuration.
 struct TileGroup {
-    int mr, combo, nv;
+    int mr, combo, nv, rounds;
     int warps_req = 0;  // consumer warps (panels per job) asked by the first call that asked (0: 16)
     std::vector<TProblem> probs;
     int64_t xbuf = 0, stage_b = 0;
 };
 
-int launch_tile_groups(std::map<std::tuple<int, int, int>, TileGroup> &groups, cudaStream_t stream) {
+int launch_tile_groups(std::map<std::tuple<int, int, int, int>, TileGroup> &groups, cudaStream_t stream) {
     DevFacts *f;
     int st = dev_facts(&f);
     if (st) return st;
     for (auto &kv : groups) {
         TileGroup &g = kv.second;
-        // consumer warps: as asked, else 16; fewer if the stages do not fit
+        // consumer warps: as asked, else 15; fewer if the stages do not fit.  With panel rounds: two
+        // resident strips and four ring stages where they fit, else one strip (the producer then waits
+        // for a job's last stage before loading the next job's strip) and two stages.
+        const bool res = g.rounds > 1;
         int W = g.warps_req > 0 ? std::min(g.warps_req, kTileMaxWarps) : kTileMaxWarps;
-        auto smem_for = [&](int w) { return (int64_t)1024 + kTileStages * (g.stage_b + (int64_t)w * g.xbuf); };
-        while (W > 1 && smem_for(W) > f->smem_optin) W >>= 1;
-        SPREG_CHECK_ARG(smem_for(W) <= f->smem_optin, "shared-memory B tiles: a stage does not fit (%lld bytes)",
-                        (long long)smem_for(W));
-        const size_t smem = (size_t)smem_for(W);
+        int nbuf = 0, stages = kTileStages;
+        auto smem_of = [&](int w, int nb, int ns) {
+            return res ? (int64_t)1024 + nb * g.stage_b + (int64_t)ns * w * g.xbuf
+                       : (int64_t)1024 + kTileStages * (g.stage_b + (int64_t)w * g.xbuf);
+        };
+        auto pick = [&](int w) {
+            if (!res) return smem_of(w, 0, kTileStages) <= f->smem_optin;
+            const int cand[4][2] = {{2, kTileMaxStages}, {2, 2}, {1, kTileMaxStages}, {1, 2}};
+            for (auto &c : cand)
+                if (smem_of(w, c[0], c[1]) <= f->smem_optin) {
+                    nbuf = c[0];
+                    stages = c[1];
+                    return true;
+                }
+            return false;
+        };
+        while (W > 1 && !pick(W)) W >>= 1;
+        SPREG_CHECK_ARG(pick(W), "shared-memory B tiles: a stage does not fit (%lld bytes)",
+                        (long long)smem_of(W, res ? 1 : 0, kTileStages));
+        const size_t smem = (size_t)smem_of(W, nbuf, stages);
         const int threads = 32 * (W + 1);
         for (size_t first = 0; first < g.probs.size(); first += kTileMaxProblems) {
             const size_t cnt = std::min<size_t>(kTileMaxProblems, g.probs.size() - first);
@@ -575,7 +614,8 @@ int launch_tile_groups(std::map<std::tuple<int, int, int>, TileGroup> &groups, c
                 TProblem &pr = tp.prob[i];
                 pr = g.probs[first + i];
                 pr.job_begin = jobs;
-                jobs += (int64_t)((pr.P + W - 1) / W) * pr.S;
+                const int64_t per_job = (int64_t)W * g.rounds;
+                jobs += (int64_t)((pr.P + per_job - 1) / per_job) * pr.S;
             }
             if (jobs == 0) continue;
             SPREG_CHECK_ARG(jobs <= INT32_MAX, "too many jobs in one launch");
@@ -583,6 +623,10 @@ int launch_tile_groups(std::map<std::tuple<int, int, int>, TileGroup> &groups, c
             tp.xbuf = (int32_t)g.xbuf;
             tp.warps = W;
             tp.stage_b = (int32_t)g.stage_b;
+            tp.stages = stages;
+            tp.rounds = g.rounds;
+            tp.nbuf = nbuf;
+            tp.pad_ = 0;
             tp.status = f->status;
             tp.counter = next_counter(f);
             const int per_sm = std::max(1, std::min((int)(f->smem_per_sm / (int64_t)smem), 2048 / threads));
@@ -595,12 +639,13 @@ int launch_tile_groups(std::map<std::tuple<int, int, int>, TileGroup> &groups, c
     return SPREG_OK;
 }
 
-void add_tile_call(std::map<std::tuple<int, int, int>, TileGroup> &groups, const CallPlan &cp) {
+void add_tile_call(std::map<std::tuple<int, int, int, int>, TileGroup> &groups, const CallPlan &cp) {
     auto add = [&](const TProblem &pr, int nv, int64_t stage_b) {
-        TileGroup &g = groups[std::make_tuple(cp.mr, cp.combo, nv)];
+        TileGroup &g = groups[std::make_tuple(cp.mr, cp.combo, nv, cp.rounds)];
         g.mr = cp.mr;
         g.combo = cp.combo;
         g.nv = nv;
+        g.rounds = cp.rounds;
         if (!g.warps_req) g.warps_req = cp.warps_req;
         g.probs.push_back(pr);
         g.xbuf = std::max(g.xbuf, cp.xbuf);
@@ -626,7 +671,7 @@ void add_call(std::map<std::tuple<int, int, int>, Group> &groups, const CallPlan
 
 int run_calls(const spreg_packed *const *as, const spreg_exec_args *const *args, int32_t n, cudaStream_t stream) {
     std::map<std::tuple<int, int, int>, Group> groups;
-    std::map<std::tuple<int, int, int>, TileGroup> tgroups;
+    std::map<std::tuple<int, int, int, int>, TileGroup> tgroups;
     std::vector<CallPlan> streams;
     int64_t items1 = 0;
     for (int32_t i = 0; i < n; ++i) items1 += strip_items1(as[i], args[i]);

@@ -24,6 +24,13 @@
 // the same as the other executors (K tiles in order, entries in packed order), so the results
 // are bit-identical.
 //
+// Panel rounds (TileParams::rounds > 1, any K tiling): a job is R rounds of W panels on one strip.
+// The strip of B for every K tile stays in shared memory for the whole job (one of nbuf resident
+// buffers, loaded by the job's first stage), and the ring stages carry only the execution blocks
+// of one round's units (round r, K tile t).  A B row then comes from L2 once per W * R panels:
+// at high sparsity, where a job of W panels gathers about as many B bytes as its stage copies,
+// this divides the L2-to-SM traffic by R.  The FMA chain per element is unchanged.
+//
 // Every wait is bounded; a wait that gives up records a code in the device status word and the
 // warp stops, the producer first waiting (bounded) for the copies it issued.
 #pragma once
@@ -36,8 +43,10 @@
 
 namespace spreg {
 
-constexpr int kTileStages = 2;
-constexpr int kTileMaxWarps = 15;    // consumer warps per CTA (with the producer: 512 threads, 128 registers each)
+constexpr int kTileStages = 2;      // ring stages of a launch without panel rounds
+constexpr int kTileMaxStages = 4;   // ring stages with panel rounds (metadata only, small)
+constexpr int kTileMaxRounds = 64;  // panel rounds per job
+constexpr int kTileMaxWarps = 15;   // consumer warps per CTA (with the producer: 512 threads, 128 registers each)
 constexpr int kTileMaxProblems = 96; // problems per launch (a tensor map each; kernel parameters <= 32 KB)
 constexpr int kTileBoxRows = 256;    // rows of one tensor copy (TMA box limit)
 
@@ -69,7 +78,11 @@ struct TileParams {
     int32_t nprob;
     int32_t xbuf;               // bytes of one consumer's metadata slot
     int32_t warps;              // consumer warps W
-    int32_t stage_b;            // bytes of one stage's B tile
+    int32_t stage_b;            // bytes of one stage's B tile; with panel rounds, of one resident B strip
+    int32_t stages;             // ring stages (2 .. kTileMaxStages)
+    int32_t rounds;             // panel rounds per job (1: B tiles travel in the ring stages)
+    int32_t nbuf;               // resident B strips (1 or 2) with panel rounds, else 0
+    int32_t pad_;
     TProblem prob[kTileMaxProblems];
 };
 static_assert(sizeof(TileParams) <= 32764, "kernel parameters are limited to 32764 bytes");
@@ -230,12 +243,17 @@ __global__ void __launch_bounds__(32 * (kTileMaxWarps + 1), 1) exec_tile_kernel(
     constexpr uint32_t ROWB = 32u * NV * (uint32_t)sizeof(TB);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int W = tp.warps;
+    const int NS = tp.stages;
+    const int R = tp.rounds;
+    const bool res = tp.nbuf > 0;  // panel rounds: B strips resident outside the ring
     const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(smem);
-    const uint32_t full0 = sbase, empty0 = sbase + 8u * kTileStages, jobs0 = sbase + 256u, moffs0 = sbase + 512u;
-    const uint32_t stage_bytes = (uint32_t)tp.stage_b + (uint32_t)W * (uint32_t)tp.xbuf;
-    const uint32_t stage0 = sbase + 1024u;
+    const uint32_t full0 = sbase, empty0 = sbase + 8u * kTileMaxStages, jobs0 = sbase + 256u, moffs0 = sbase + 512u;
+    const uint32_t res0 = sbase + 1024u;                          // resident B strips (panel rounds)
+    const uint32_t meta_off = res ? 0u : (uint32_t)tp.stage_b;    // execution blocks within a ring stage
+    const uint32_t stage_bytes = meta_off + (uint32_t)W * (uint32_t)tp.xbuf;
+    const uint32_t stage0 = res0 + (res ? (uint32_t)tp.nbuf * (uint32_t)tp.stage_b : 0u);
     if (threadIdx.x == 0) {
-        for (int s = 0; s < kTileStages; ++s) {
+        for (int s = 0; s < NS; ++s) {
             mbar_init(full0 + 8u * s, 1);
             mbar_init(empty0 + 8u * s, (uint32_t)W);
         }
@@ -245,7 +263,8 @@ __global__ void __launch_bounds__(32 * (kTileMaxWarps + 1), 1) exec_tile_kernel(
 
     if (warp == W) {
         // ------------------------------------------------------------ producer
-        int pi = -1, group = 0, strip = 0, t = 0;
+        int pi = -1, group = 0, strip = 0, t = 0, r = 0, rounds_job = 1;
+        int64_t njob = 0;  // jobs fetched by this CTA: job j reads resident strip j % nbuf
         auto fetch = [&]() {
             int it = 0;
             if (lane == 0) it = atomicAdd(tp.counter, 1);
@@ -255,28 +274,34 @@ __global__ void __launch_bounds__(32 * (kTileMaxWarps + 1), 1) exec_tile_kernel(
                 return;
             }
             pi = find_tproblem(tp, job);
-            const int64_t local = job - tp.prob[pi].job_begin;
-            if (tp.prob[pi].order == 1) {
-                const int64_t groups = (tp.prob[pi].P + W - 1) / W;
+            const TProblem &pr = tp.prob[pi];
+            const int64_t local = job - pr.job_begin;
+            const int64_t gsz = (int64_t)W * R;  // panels per job
+            if (pr.order == 1) {
+                const int64_t groups = (pr.P + gsz - 1) / gsz;
                 group = (int)(local % groups);
                 strip = (int)(local / groups);
             } else {
-                group = (int)(local / tp.prob[pi].S);
-                strip = (int)(local % tp.prob[pi].S);
+                group = (int)(local / pr.S);
+                strip = (int)(local % pr.S);
             }
             t = 0;
+            r = 0;
+            const int64_t left = (int64_t)pr.P - (int64_t)group * gsz;  // panels from this job's first on
+            rounds_job = (int)((left + W - 1) / W < R ? (left + W - 1) / W : R);
+            ++njob;
         };
         fetch();
-        int64_t last_seq[kTileStages];
+        int64_t last_seq[kTileMaxStages];
 #pragma unroll
-        for (int s = 0; s < kTileStages; ++s) last_seq[s] = -1;
+        for (int s = 0; s < kTileMaxStages; ++s) last_seq[s] = -1;
+        int64_t buf_last[2] = {-1, -1};  // last stage that read each resident strip
         bool ok = true;
 #pragma unroll 1
         for (int64_t seq = 0;; ++seq) {
-            const int s = (int)(seq % kTileStages);
+            const int s = (int)(seq % NS);
             const uint32_t full = full0 + 8u * s, empty = empty0 + 8u * s;
-            if (seq >= kTileStages &&
-                !mbar_wait_bounded(empty, (uint32_t)(((seq / kTileStages) - 1) & 1), tp.status, 5)) {
+            if (seq >= NS && !mbar_wait_bounded(empty, (uint32_t)(((seq / NS) - 1) & 1), tp.status, 5)) {
                 ok = false;
                 break;
             }
@@ -288,13 +313,24 @@ __global__ void __launch_bounds__(32 * (kTileMaxWarps + 1), 1) exec_tile_kernel(
                 break;
             }
             const TProblem &pr = tp.prob[pi];
-            const int r0 = pr.col_offset + t * pr.kt;
             const int c0 = pr.col_begin + strip * (32 * NV);
             const int nbox = (pr.kt + pr.box_rows - 1) / pr.box_rows;
-            // metadata: lane w < W holds the block of unit (group * W + w, t)
+            const int b = res ? (int)((njob - 1) % tp.nbuf) : 0;
+            const bool load_b = !res || (r == 0 && t == 0);
+            if (res && load_b) {
+                // the job that read this strip before must be done with it: its last stage released
+                // (a stage NS or more back is already covered by the ring wait above)
+                const int64_t L = buf_last[b];
+                if (L >= 0 && seq - L < NS &&
+                    !mbar_wait_bounded(empty0 + 8u * (uint32_t)(L % NS), (uint32_t)((L / NS) & 1), tp.status, 8)) {
+                    ok = false;
+                    break;
+                }
+            }
+            // metadata: lane w < W holds the block of unit (panel (group * R + r) * W + w, t)
             int64_t moff = 0;
             uint32_t mbytes = 0;
-            const int64_t pos = (int64_t)group * W + lane;  // position in the work order
+            const int64_t pos = ((int64_t)group * R + r) * W + lane;  // position in the work order
             const bool act = lane < W && pos < pr.P;
             if (act) {
                 const int64_t slot = (int64_t)t * pr.P + pos;
@@ -312,26 +348,41 @@ __global__ void __launch_bounds__(32 * (kTileMaxWarps + 1), 1) exec_tile_kernel(
                 sts_u32(moffs0 + 4u * (uint32_t)(s * kTileMaxWarps + lane),
                         contig ? (uint32_t)(moff - m0) : (uint32_t)lane * (uint32_t)tp.xbuf);
             const uint32_t sb = stage0 + (uint32_t)s * stage_bytes;
+            const uint32_t tile_b = (uint32_t)(nbox * pr.box_rows) * ROWB;  // one K tile of the strip
             if (lane == 0) {
-                sts_v4(jobs0 + 16u * s, pi, group, strip, t);
-                mbar_arrive_expect_tx(full, (uint32_t)nbox * (uint32_t)pr.box_rows * ROWB + mtotal);
-                for (int b = 0; b < nbox; ++b)
-                    tma_load_2d(sb + (uint32_t)(b * pr.box_rows) * ROWB, &pr.tmap, c0, r0 + b * pr.box_rows, full);
-                if (contig && mtotal) bulk_copy_g2s(sb + (uint32_t)tp.stage_b, pr.exec + m0, mtotal, full);
+                sts_v4(jobs0 + 16u * s, pi, group * R + r, strip, t | (b << 16));
+                const uint32_t bbytes = load_b ? (res ? (uint32_t)pr.T : 1u) * tile_b : 0u;
+                mbar_arrive_expect_tx(full, bbytes + mtotal);
+                if (res && load_b) {
+                    // every K tile of the strip, into resident strip b
+                    const uint32_t dst = res0 + (uint32_t)b * (uint32_t)tp.stage_b;
+                    for (int tt = 0; tt < pr.T; ++tt)
+                        for (int bx = 0; bx < nbox; ++bx)
+                            tma_load_2d(dst + (uint32_t)tt * tile_b + (uint32_t)(bx * pr.box_rows) * ROWB, &pr.tmap, c0,
+                                        pr.col_offset + tt * pr.kt + bx * pr.box_rows, full);
+                } else if (load_b) {
+                    const int r0 = pr.col_offset + t * pr.kt;
+                    for (int bx = 0; bx < nbox; ++bx)
+                        tma_load_2d(sb + (uint32_t)(bx * pr.box_rows) * ROWB, &pr.tmap, c0, r0 + bx * pr.box_rows,
+                                    full);
+                }
+                if (contig && mtotal) bulk_copy_g2s(sb + meta_off, pr.exec + m0, mtotal, full);
             }
             if (!contig && mbytes)
-                bulk_copy_g2s(sb + (uint32_t)tp.stage_b + (uint32_t)lane * (uint32_t)tp.xbuf, pr.exec + moff, mbytes,
-                              full);
+                bulk_copy_g2s(sb + meta_off + (uint32_t)lane * (uint32_t)tp.xbuf, pr.exec + moff, mbytes, full);
             __syncwarp();
             last_seq[s] = seq;
-            if (++t == pr.T) fetch();
+            if (res) buf_last[b] = seq;
+            if (++t == pr.T) {
+                t = 0;
+                if (++r == rounds_job) fetch();
+            }
         }
         if (!ok) {
             // copies still in flight land in stages whose full barrier has not flipped yet
-#pragma unroll
-            for (int s = 0; s < kTileStages; ++s)
+            for (int s = 0; s < NS; ++s)
                 if (last_seq[s] >= 0)
-                    mbar_wait_bounded(full0 + 8u * s, (uint32_t)((last_seq[s] / kTileStages) & 1), tp.status, 7);
+                    mbar_wait_bounded(full0 + 8u * s, (uint32_t)((last_seq[s] / NS) & 1), tp.status, 7);
         }
         return;
     }
@@ -340,13 +391,13 @@ __global__ void __launch_bounds__(32 * (kTileMaxWarps + 1), 1) exec_tile_kernel(
     float acc[MR][NV];
 #pragma unroll 1
     for (int64_t seq = 0;; ++seq) {
-        const int s = (int)(seq % kTileStages);
-        if (!mbar_wait_bounded(full0 + 8u * s, (uint32_t)((seq / kTileStages) & 1), tp.status, 6)) break;
+        const int s = (int)(seq % NS);
+        if (!mbar_wait_bounded(full0 + 8u * s, (uint32_t)((seq / NS) & 1), tp.status, 6)) break;
         const int4 ji = lds_v4(jobs0 + 16u * s);
         if (ji.x < 0) break;
         const TProblem &pr = tp.prob[ji.x];
         const int64_t pos = (int64_t)ji.y * W + warp;
-        const int t = ji.w;
+        const int t = ji.w & 0xffff;
         if (pos < pr.P) {
             const int64_t gp = pr.panel_order[pos];
             const int64_t row0 = gp * MR;
@@ -354,10 +405,12 @@ __global__ void __launch_bounds__(32 * (kTileMaxWarps + 1), 1) exec_tile_kernel(
             const bool valid = col0 < pr.col_end;
             if (t == 0) t_acc_init<MR, NV, TV, TC>(pr, row0, col0, valid, acc);
             const uint32_t sb = stage0 + (uint32_t)s * stage_bytes;
-            const uint32_t buf =
-                sb + (uint32_t)tp.stage_b + lds_u32(moffs0 + 4u * (uint32_t)(s * kTileMaxWarps + warp));
+            // B tile t: in the ring stage, or in resident strip ji.w >> 16
+            const uint32_t tile_b = (uint32_t)((pr.kt + pr.box_rows - 1) / pr.box_rows * pr.box_rows) * ROWB;
+            const uint32_t bt = res ? res0 + (uint32_t)(ji.w >> 16) * (uint32_t)tp.stage_b + (uint32_t)t * tile_b : sb;
+            const uint32_t buf = sb + meta_off + lds_u32(moffs0 + 4u * (uint32_t)(s * kTileMaxWarps + warp));
             const uint32_t r0 = (uint32_t)(pr.col_offset + t * pr.kt);  // B row of tile row 0
-            const SmemB<NV, TB> bl{sb + (uint32_t)lane * (uint32_t)(NV * sizeof(TB)) - r0 * ROWB, ROWB};
+            const SmemB<NV, TB> bl{bt + (uint32_t)lane * (uint32_t)(NV * sizeof(TB)) - r0 * ROWB, ROWB};
             const uint32_t G = lds_u32(buf);
 #pragma unroll 1
             for (uint32_t g = 0; g < G; ++g) {

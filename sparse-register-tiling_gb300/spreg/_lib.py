@@ -72,7 +72,7 @@ class ExecArgs(C.Structure):
     _fields_ = [("b", C.c_void_p), ("ldb", C.c_int64), ("c", C.c_void_p), ("ldc", C.c_int64), ("n", C.c_int64),
                 ("b_dtype", C.c_int32), ("c_dtype", C.c_int32), ("load_c", C.c_int32), ("epilogue", C.c_int32),
                 ("nr", C.c_int32), ("warps_per_cta", C.c_int32), ("b_staging", C.c_int32),
-                ("meta_staging", C.c_int32), ("job_order", C.c_int32), ("reserved", C.c_int32)]
+                ("meta_staging", C.c_int32), ("job_order", C.c_int32), ("panel_rounds", C.c_int32)]
 
 
 class WorkItem(C.Structure):

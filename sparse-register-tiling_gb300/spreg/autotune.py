@@ -21,13 +21,14 @@ model in greedy form; for K-tiled M_r = 4 with the B-tile executor's penalty for
 loop of their own).
 
 Beyond the reference's M_r / N_r / mapping, a candidate carries the CTA tiling (`warps`: warps per
-CTA of the batched kernel, row panels per job of the B-tile kernel) and a tensor-core threshold
-(`tc_fill`: panels whose fill reaches it run as dense tcgen05 products, `spreg.hybrid`).
+CTA of the batched kernel, row panels per job of the B-tile kernel), panel rounds (`rounds`: the
+B-tile kernel keeps a job's strip of B resident for that many rounds of panels) and a tensor-core
+threshold (`tc_fill`: panels whose fill reaches it run as dense tcgen05 products, `spreg.hybrid`).
 
 `tune` ranks every candidate with the model, times the best few on the device with the reference's
 timing protocol (`execute_timed`: median of repeated runs) or as a batch, then times the CTA tiling
-of the best and the tensor-core thresholds (all panels; the densest tenth), and returns the
-fastest, so a poor model costs tuning time, not speed.
+and the panel rounds of the best and the tensor-core thresholds (all panels; the densest tenth),
+and returns the fastest, so a poor model costs tuning time, not speed.
 """
 from __future__ import annotations
 
@@ -57,6 +58,7 @@ class Candidate:
     k_tile: int = 0  # K_c of the packing (0: one K tile)
     warps: int = 0   # CTA tiling (spreg_exec_args.warps_per_cta; 0: the executor's choice)
     tc_fill: float = 2.0  # panels with fill >= tc_fill on the tensor cores (> 1: none)
+    rounds: int = 0  # panel rounds of the B-tile kernel (spreg_exec_args.panel_rounds; 0: none)
 
     @property
     def nv(self) -> int:
@@ -66,7 +68,8 @@ class Candidate:
         """The reference's method grammar, M{Mr}N{nr}_{mapping} (tools/paper/configs.py:54-68), with
         the K tile appended as _K{K_c} when the packing is K-tiled."""
         return (f"M{self.mr}N{self.nr}_{self.mapping}" + (f"_K{self.k_tile}" if self.k_tile else "") +
-                (f"_W{self.warps}" if self.warps else "") + (f"_TC{self.tc_fill:g}" if self.tc_fill <= 1.0 else ""))
+                (f"_W{self.warps}" if self.warps else "") + (f"_R{self.rounds}" if self.rounds > 1 else "") +
+                (f"_TC{self.tc_fill:g}" if self.tc_fill <= 1.0 else ""))
 
 
 # Mappings built in this process (greedy sets from a matrix's histogram), by mapping id.
@@ -307,11 +310,11 @@ def rank(mask: np.ndarray, n: int, dtype: str = "f32", costs: Optional[Costs] = 
     return ranked, stats
 
 
-def _time_batched(pm, Bs, Cs, nr: int, reps: int = 5, warps: int = 0) -> float:
+def _time_batched(pm, Bs, Cs, nr: int, reps: int = 5, warps: int = 0, rounds: int = 0) -> float:
     """ns per SpMM of len(Bs) SpMMs of one packed matrix in one batched call (CUDA events)."""
     import torch
     from .packed import execute_batched
-    work = [(pm, b, c, dict(nr=nr, warps=warps)) for b, c in zip(Bs, Cs)]
+    work = [(pm, b, c, dict(nr=nr, warps=warps, rounds=rounds)) for b, c in zip(Bs, Cs)]
     execute_batched(work)
     s = torch.cuda.current_stream()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -365,13 +368,14 @@ def tc_predict_ns(mask: np.ndarray, n: int, dtype: str, fill: float, mr: int) ->
 
 def tune(A: np.ndarray, n: int, dtype: str = "f32", top: int = 4, costs: Optional[Costs] = None,
          mrs: Iterable[int] = (2, 4, 8), k_tiles: Iterable[int] = K_TILES, runs: int = 1, batch: int = 1,
-         device=None, tc: bool = True, warps: bool = True) -> TuneResult:
+         device=None, tc: bool = True, warps: bool = True, rounds: bool = True) -> TuneResult:
     """Pick the fastest candidate for weight A (M x K, float32, zeros pruned) and n columns of B:
     rank by the cost model, then time the ``top`` best on the device -- one SpMM at a time with
     the reference's protocol (execute_timed) when ``batch`` is 1, else ``batch`` SpMMs of A with
     distinct B in one batched launch, as a serving loop runs them.  Then (``warps``) the CTA tiling
-    of the best register-tiled candidate, and (``tc``) the tensor-core thresholds: every panel, and
-    the densest tenth of the panels, each timed as a batch of SpMMs through `spreg.hybrid`."""
+    of the best register-tiled candidate, (``rounds``) its panel rounds, and (``tc``) the tensor-core
+    thresholds: every panel, and the densest tenth of the panels, each timed as a batch of SpMMs
+    through `spreg.hybrid`."""
     import torch
     from . import _lib
     from .packed import PackedMatrix
@@ -392,8 +396,8 @@ def tune(A: np.ndarray, n: int, dtype: str = "f32", top: int = 4, costs: Optiona
         if key not in packs:
             packs[key] = PackedMatrix.from_dense(At, mapping_of(c.mr, c.mapping), k_tile=c.k_tile, value_dtype=vd)
         if nb == 1:
-            return packs[key].execute_timed(Bs[0], Cs[0], num_runs=runs, nr=c.nr, warps=c.warps)
-        return _time_batched(packs[key], Bs, Cs, c.nr, warps=c.warps)
+            return packs[key].execute_timed(Bs[0], Cs[0], num_runs=runs, nr=c.nr, warps=c.warps, rounds=c.rounds)
+        return _time_batched(packs[key], Bs, Cs, c.nr, warps=c.warps, rounds=c.rounds)
 
     # the model's top candidates, and the best-ranked candidate of every (M_r, nanokernel set) family,
     # so that a family the model underrates is still timed
@@ -414,6 +418,21 @@ def tune(A: np.ndarray, n: int, dtype: str = "f32", top: int = 4, costs: Optiona
             by_name[c.name()] = c
             measured[c.name()] = time_reg(c)
     best_reg = by_name[min(measured, key=measured.get)]
+    if rounds:
+        # panel rounds: the B-tile kernel with the strip of B for every K tile resident, for the best
+        # packing at its strip width and the narrower ones (a strip that does not fit shared memory
+        # is refused by the executor and skipped)
+        base = best_reg
+        for nr in sorted({min(base.nr, 128), 64, 32}, reverse=True):
+            for r in (4, 16):
+                c = dataclasses.replace(base, nr=nr, warps=0, rounds=r)
+                try:
+                    t = time_reg(c)
+                except _lib.SpregError:
+                    break
+                by_name[c.name()] = c
+                measured[c.name()] = t
+        best_reg = by_name[min(measured, key=measured.get)]
     predicted = {c.name(): t for t, c in ranked}
     if tc and n >= 16:
         mask = A != 0

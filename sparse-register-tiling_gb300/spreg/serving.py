@@ -45,7 +45,7 @@ WORK_ITEM_DTYPE = np.dtype([
     ("a", np.uint64), ("b", np.uint64), ("ldb", np.int64), ("c", np.uint64), ("ldc", np.int64), ("n", np.int64),
     ("b_dtype", np.int32), ("c_dtype", np.int32), ("load_c", np.int32), ("epilogue", np.int32), ("nr", np.int32),
     ("warps_per_cta", np.int32), ("b_staging", np.int32), ("meta_staging", np.int32), ("job_order", np.int32),
-    ("reserved", np.int32)])
+    ("panel_rounds", np.int32)])
 assert WORK_ITEM_DTYPE.itemsize == C.sizeof(_lib.WorkItem)
 
 # numpy view of spreg_dense_rows_item (include/spreg.h): one tensor-core product
@@ -356,8 +356,9 @@ def tune_mlp(weights, dtype: str = "bf16", n: int = 96, batch: int = 32, top: in
     tuned for ``batch`` concurrent requests of ``n`` tokens and every block reuses them (all blocks
     share shapes and sparsity).  Returns (configs, tune results)."""
     from .autotune import tune
-    # register-tiled packings (tensor-core layers are SparseMLP(tc=True)); the CTA tiling is kept
-    res = [tune(w, n, dtype, top=top, batch=batch, device=device, tc=False) for w in weights[0]]
+    # register-tiled packings (tensor-core layers are SparseMLP(tc=True)); the CTA tiling is kept; no
+    # panel rounds (the strip width follows each request's token count)
+    res = [tune(w, n, dtype, top=top, batch=batch, device=device, tc=False, rounds=False) for w in weights[0]]
     cfg = [{"mr": r.best.mr, "mapping": r.best.mapping, "k_tile": r.best.k_tile, "nr": r.best.nr,
             "warps": r.best.warps} for r in res]
     return [dict(cfg[l % 2]) for l in range(2 * len(weights))], res
