@@ -70,12 +70,19 @@ template <int BN, bool SPLIT> constexpr uint32_t tc_stage() {
 }
 // Stages of the ring: about 190 KB of operands.
 template <int BN, bool SPLIT> constexpr int tc_stages() { return !SPLIT ? 4 : BN == 256 ? 4 : 6; }
-// The epilogue warps' staging buffers: 4 x 32 rows x 33 floats.
-constexpr uint32_t TC_EPI_BYTES = 4u * 32u * 33u * 4u;
+// Epilogue warps: two per TMEM lane quarter, each storing half of the tile's columns.
+constexpr int TC_EPI_WARPS = 8;
+constexpr int TC_THREADS = 32 * (2 + TC_EPI_WARPS);
+// The epilogue warps' staging buffers: 8 x 32 rows x 33 floats.
+constexpr uint32_t TC_EPI_BYTES = (uint32_t)TC_EPI_WARPS * 32u * 33u * 4u;
 template <int BN, bool SPLIT> constexpr size_t tc_smem() {
     return 1024 /* alignment slack */ + tc_stages<BN, SPLIT>() * tc_stage<BN, SPLIT>() + 256 /* barriers, TMEM slot */ +
            TC_EPI_BYTES;
 }
+
+static_assert(tc_smem<256, true>() <= 232448 && tc_smem<128, true>() <= 232448 && tc_smem<256, false>() <= 232448 &&
+                  tc_smem<128, false>() <= 232448,
+              "tensor-core kernel shared memory exceeds 227 KB per CTA");
 
 constexpr int TC_MAX_PROBLEMS = 192;  // problems per launch (kernel parameters <= 32 KB)
 // K per pass of a split product (a multiple of TC_BK): bounds the MMA steps of one accumulator.
@@ -240,80 +247,141 @@ __device__ __forceinline__ int tc_problem_of(const TcParams &p, int t) {
     return lo;
 }
 
-// One 32-column chunk of the epilogue (columns n0 + c .. + 31, registers r from TMEM; cs = lane j's
-// column scale 2^-s of column n0 + c + j for split products): scales, load_c / ReLU, store.
+// Epilogue constants of one output tile, read once from the problem (kernel parameter space).
+struct TcEpi {
+    void *C;
+    int64_t ldc;
+    int n, c_dtype, load_c, epilogue, nseg;
+    const int32_t *seg_start;
+    void *const *seg_c;
+    const int64_t *seg_ldc;
+    const float *col_scale;
+};
+__device__ __forceinline__ TcEpi tc_epi_of(const TcProblem &q) {
+    TcEpi e;
+    e.C = q.C;
+    e.ldc = q.ldc;
+    e.n = q.n;
+    e.c_dtype = q.c_dtype;
+    e.load_c = q.load_c;
+    e.epilogue = q.epilogue;
+    e.nseg = q.nseg;
+    e.seg_start = q.seg_start;
+    e.seg_c = q.seg_c;
+    e.seg_ldc = q.seg_ldc;
+    e.col_scale = q.col_scale;
+    return e;
+}
+
+// One 32-column chunk of the epilogue (columns n0 + c .. + 31, registers r from TMEM, lane i holding
+// tile row i): scales (split products: (acc * row_scale) * col_scale, each factor a power of two),
+// load_c / ReLU, store.
 //
 // Whole 32-column chunks of one output go through the warp's 32 x 33 shared-memory buffer `eb`:
-// lane i writes row i's 32 values, then each store instruction covers 4 rows x 32 columns (8 lanes
-// x 16 bytes per row), where a lane storing its own row would scatter 32 rows per instruction.  The
-// 33-float row pitch keeps both passes free of bank conflicts.
+// lane i writes row i's 32 raw values, then each store instruction covers 4 rows x 32 columns (8
+// lanes x 16 bytes per row), where a lane storing its own row would scatter 32 rows per
+// instruction.  The 33-float row pitch keeps both passes free of bank conflicts.  The scales are
+// applied after the transpose (a lane's 4 columns keep their 4 column scales for the whole chunk);
+// with load_c the chunk's 8 reads of C are issued before any of them is used.
 template <bool SPLIT>
-__device__ __forceinline__ void tc_store_chunk(const TcProblem &q, int n0, int c, int lane, const uint32_t (&r)[32],
-                                               float cs, float rs, bool row_ok, long long orow, bool vec_ok, int &seg,
+__device__ __forceinline__ void tc_store_chunk(const TcEpi &e, int n0, int c, int lane, const uint32_t (&r)[32],
+                                               float rs, bool row_ok, long long orow, bool vec_ok, int &seg,
                                                float *eb) {
-    if (n0 + c >= q.n) return;  // uniform: a chunk past the last column
-    float v[32];
-#pragma unroll
-    for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(r[j]);
-    if constexpr (SPLIT) {
-        // undo the scales: (acc * 2^-s_row) * 2^-s_col, each factor exact (every lane takes part)
-#pragma unroll
-        for (int j = 0; j < 32; ++j) v[j] = (v[j] * rs) * __shfl_sync(0xffffffffu, cs, j);
-    }
+    if (n0 + c >= e.n) return;  // uniform: a chunk past the last column
     // output of this chunk: C itself, or (coalesced products) the segment it lies in, when it lies in one
-    void *cbase = q.C;
-    int64_t cld = q.ldc;
+    void *cbase = e.C;
+    int64_t cld = e.ldc;
     int ccol = n0 + c;
-    bool whole = vec_ok && n0 + c + 32 <= q.n;
-    if (q.nseg > 1) {
-        while (n0 + c >= q.seg_start[seg + 1]) ++seg;  // uniform: every lane sees the same columns
-        const int esz = q.c_dtype == SPREG_F32 ? 4 : 2;
-        cbase = q.seg_c[seg];
-        cld = q.seg_ldc[seg];
-        ccol = n0 + c - q.seg_start[seg];
-        whole = n0 + c + 32 <= q.seg_start[seg + 1] && (reinterpret_cast<uintptr_t>(cbase) % (4 * esz)) == 0 &&
+    bool whole = vec_ok && n0 + c + 32 <= e.n;
+    if (e.nseg > 1) {
+        while (n0 + c >= e.seg_start[seg + 1]) ++seg;  // uniform: every lane sees the same columns
+        const int esz = e.c_dtype == SPREG_F32 ? 4 : 2;
+        cbase = e.seg_c[seg];
+        cld = e.seg_ldc[seg];
+        ccol = n0 + c - e.seg_start[seg];
+        whole = n0 + c + 32 <= e.seg_start[seg + 1] && (reinterpret_cast<uintptr_t>(cbase) % (4 * esz)) == 0 &&
                 (cld % 4) == 0 && (ccol % 4) == 0;
     }
     if (whole) {  // uniform over the warp
         __syncwarp();
 #pragma unroll
-        for (int j = 0; j < 32; ++j) eb[lane * 33 + j] = v[j];
-        __syncwarp();
+        for (int j = 0; j < 32; ++j) eb[lane * 33 + j] = __uint_as_float(r[j]);
         const int c4 = (lane & 7) * 4;
+        float cs[4] = {1.0f, 1.0f, 1.0f, 1.0f};
+        if constexpr (SPLIT) {
+            const float4 v = __ldg(reinterpret_cast<const float4 *>(e.col_scale + n0 + c + c4));
+            cs[0] = v.x; cs[1] = v.y; cs[2] = v.z; cs[3] = v.w;
+        }
+        // rows of this lane's 8 stores: 4 * it + lane / 8
+        long long orow_r[8];
+        bool ok_r[8];
+        float rs_r[8];
 #pragma unroll
         for (int it = 0; it < 8; ++it) {
-            const int rr = 4 * it + (lane >> 3);  // tile row (TMEM lane) this lane stores
-            const bool ok_r = __shfl_sync(0xffffffffu, row_ok, rr);
-            const long long orow_r = __shfl_sync(0xffffffffu, orow, rr);
-            if (!ok_r) continue;
-            float o[4];
+            const int rr = 4 * it + (lane >> 3);
+            ok_r[it] = __shfl_sync(0xffffffffu, row_ok, rr);
+            orow_r[it] = __shfl_sync(0xffffffffu, orow, rr);
+            rs_r[it] = SPLIT ? __shfl_sync(0xffffffffu, rs, rr) : 1.0f;
+        }
+        __syncwarp();
+        if (e.c_dtype == SPREG_F32) {
+            float4 *cp[8];
+            float4 ci[8];
 #pragma unroll
-            for (int t = 0; t < 4; ++t) o[t] = eb[rr * 33 + c4 + t];
-            if (q.c_dtype == SPREG_F32) {
-                float4 *cp = reinterpret_cast<float4 *>(reinterpret_cast<float *>(cbase) + orow_r * cld + ccol + c4);
-                if (q.load_c) {
-                    const float4 ci = *cp;
-                    o[0] += ci.x; o[1] += ci.y; o[2] += ci.z; o[3] += ci.w;
+            for (int it = 0; it < 8; ++it) {
+                cp[it] = reinterpret_cast<float4 *>(reinterpret_cast<float *>(cbase) + orow_r[it] * cld + ccol + c4);
+                ci[it] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                if (e.load_c && ok_r[it]) ci[it] = *cp[it];
+            }
+#pragma unroll
+            for (int it = 0; it < 8; ++it) {
+                const int rr = 4 * it + (lane >> 3);
+                float o[4];
+#pragma unroll
+                for (int t = 0; t < 4; ++t) {
+                    o[t] = eb[rr * 33 + c4 + t];
+                    if constexpr (SPLIT) o[t] = (o[t] * rs_r[it]) * cs[t];
                 }
-                if (q.epilogue == SPREG_EPILOGUE_RELU)
+                if (e.load_c) {
+                    o[0] += ci[it].x; o[1] += ci[it].y; o[2] += ci[it].z; o[3] += ci[it].w;
+                }
+                if (e.epilogue == SPREG_EPILOGUE_RELU)
+#pragma unroll
                     for (int t = 0; t < 4; ++t) o[t] = fmaxf(o[t], 0.0f);
-                *cp = make_float4(o[0], o[1], o[2], o[3]);
-            } else {
-                uint2 *cp = reinterpret_cast<uint2 *>(reinterpret_cast<__nv_bfloat16 *>(cbase) + orow_r * cld + ccol + c4);
-                if (q.load_c) {
-                    const uint2 ci = *cp;
-                    const __nv_bfloat162 c01 = *reinterpret_cast<const __nv_bfloat162 *>(&ci.x);
-                    const __nv_bfloat162 c23 = *reinterpret_cast<const __nv_bfloat162 *>(&ci.y);
+                if (ok_r[it]) *cp[it] = make_float4(o[0], o[1], o[2], o[3]);
+            }
+        } else {
+            uint2 *cp[8];
+            uint2 ci[8];
+#pragma unroll
+            for (int it = 0; it < 8; ++it) {
+                cp[it] = reinterpret_cast<uint2 *>(reinterpret_cast<__nv_bfloat16 *>(cbase) + orow_r[it] * cld + ccol + c4);
+                ci[it] = make_uint2(0u, 0u);
+                if (e.load_c && ok_r[it]) ci[it] = *cp[it];
+            }
+#pragma unroll
+            for (int it = 0; it < 8; ++it) {
+                const int rr = 4 * it + (lane >> 3);
+                float o[4];
+#pragma unroll
+                for (int t = 0; t < 4; ++t) {
+                    o[t] = eb[rr * 33 + c4 + t];
+                    if constexpr (SPLIT) o[t] = (o[t] * rs_r[it]) * cs[t];
+                }
+                if (e.load_c) {
+                    const __nv_bfloat162 c01 = *reinterpret_cast<const __nv_bfloat162 *>(&ci[it].x);
+                    const __nv_bfloat162 c23 = *reinterpret_cast<const __nv_bfloat162 *>(&ci[it].y);
                     o[0] += __low2float(c01); o[1] += __high2float(c01);
                     o[2] += __low2float(c23); o[3] += __high2float(c23);
                 }
-                if (q.epilogue == SPREG_EPILOGUE_RELU)
+                if (e.epilogue == SPREG_EPILOGUE_RELU)
+#pragma unroll
                     for (int t = 0; t < 4; ++t) o[t] = fmaxf(o[t], 0.0f);
                 __nv_bfloat162 w01 = __floats2bfloat162_rn(o[0], o[1]), w23 = __floats2bfloat162_rn(o[2], o[3]);
                 uint2 w;
                 w.x = *reinterpret_cast<uint32_t *>(&w01);
                 w.y = *reinterpret_cast<uint32_t *>(&w23);
-                *cp = w;
+                if (ok_r[it]) *cp[it] = w;
             }
         }
         return;
@@ -322,26 +390,27 @@ __device__ __forceinline__ void tc_store_chunk(const TcProblem &q, int n0, int c
 #pragma unroll
     for (int j = 0; j < 32; ++j) {
         const int col = n0 + c + j;
-        if (col >= q.n) break;
-        void *cbase = q.C;
-        int64_t ldc = q.ldc;
+        if (col >= e.n) break;
+        void *cb = e.C;
+        int64_t ldc = e.ldc;
         int lcol = col;
-        if (q.nseg > 1) {
-            while (col >= q.seg_start[seg + 1]) ++seg;
-            cbase = q.seg_c[seg];
-            ldc = q.seg_ldc[seg];
-            lcol = col - q.seg_start[seg];
+        if (e.nseg > 1) {
+            while (col >= e.seg_start[seg + 1]) ++seg;
+            cb = e.seg_c[seg];
+            ldc = e.seg_ldc[seg];
+            lcol = col - e.seg_start[seg];
         }
-        float o = v[j];
-        if (q.c_dtype == SPREG_F32) {
-            float *cp = reinterpret_cast<float *>(cbase) + orow * ldc + lcol;
-            if (q.load_c) o += *cp;
-            if (q.epilogue == SPREG_EPILOGUE_RELU) o = fmaxf(o, 0.0f);
+        float o = __uint_as_float(r[j]);
+        if constexpr (SPLIT) o = (o * rs) * __ldg(e.col_scale + col);
+        if (e.c_dtype == SPREG_F32) {
+            float *cp = reinterpret_cast<float *>(cb) + orow * ldc + lcol;
+            if (e.load_c) o += *cp;
+            if (e.epilogue == SPREG_EPILOGUE_RELU) o = fmaxf(o, 0.0f);
             *cp = o;
         } else {
-            __nv_bfloat16 *cp = reinterpret_cast<__nv_bfloat16 *>(cbase) + orow * ldc + lcol;
-            if (q.load_c) o += __bfloat162float(*cp);
-            if (q.epilogue == SPREG_EPILOGUE_RELU) o = fmaxf(o, 0.0f);
+            __nv_bfloat16 *cp = reinterpret_cast<__nv_bfloat16 *>(cb) + orow * ldc + lcol;
+            if (e.load_c) o += __bfloat162float(*cp);
+            if (e.epilogue == SPREG_EPILOGUE_RELU) o = fmaxf(o, 0.0f);
             *cp = __float2bfloat16_rn(o);
         }
     }
@@ -363,69 +432,60 @@ __device__ __forceinline__ TcRowInfo tc_row_info(const TcProblem &q, int m0, int
     return ri;
 }
 
-// Epilogue of one output tile by one warp: TMEM lanes 32 * quarter .. + 31 (tile rows) of the
-// accumulator at TMEM address tacc (lane 0, its first column); store through the row index (and
-// segments).  The TMEM load of chunk c + 1 (and its column scales) is issued before chunk c is
+// Epilogue of one output tile by one warp: TMEM lanes 32 * quarter .. + 31 (tile rows) and columns
+// [c0, c0 + NC) of the accumulator at TMEM address tacc (lane 0, its first column); store through
+// the row index (and segments).  The TMEM load of chunk c + 1 is issued before chunk c is
 // processed, so the TMEM latency overlaps the stores.
-template <int BN, bool SPLIT>
-__device__ __forceinline__ void tc_store_tile(const TcProblem &q, int n0, int quarter, int lane, uint32_t tacc,
+template <int NC, bool SPLIT>
+__device__ __forceinline__ void tc_store_tile(const TcEpi &e, int n0, int c0, int quarter, int lane, uint32_t tacc,
                                               const TcRowInfo &ri, float *eb) {
-    constexpr int NCH = BN / 32;
-    const uint32_t tmem = tacc + ((uint32_t)(32 * quarter) << 16);
+    constexpr int NCH = NC / 32;
+    const uint32_t tmem = tacc + ((uint32_t)(32 * quarter) << 16) + (uint32_t)c0;
     // vector stores need 16-byte (F32) / 8-byte (BF16) aligned row starts of C
-    const int esz = q.c_dtype == SPREG_F32 ? 4 : 2;
-    const bool vec_ok = (reinterpret_cast<uintptr_t>(q.C) % (4 * esz)) == 0 && (q.ldc % 4) == 0;
+    const int esz = e.c_dtype == SPREG_F32 ? 4 : 2;
+    const bool vec_ok = (reinterpret_cast<uintptr_t>(e.C) % (4 * esz)) == 0 && (e.ldc % 4) == 0;
     int seg = 0;  // segment of the current column (coalesced products)
-    if (q.nseg > 1 && ri.ok) {
-        int lo2 = 0, hi2 = q.nseg - 1;
+    if (e.nseg > 1 && ri.ok) {
+        int lo2 = 0, hi2 = e.nseg - 1;
         while (lo2 < hi2) {
             const int mid = (lo2 + hi2 + 1) >> 1;
-            if (q.seg_start[mid] <= n0) lo2 = mid;
+            if (e.seg_start[mid] <= n0 + c0) lo2 = mid;
             else hi2 = mid - 1;
         }
         seg = lo2;
     }
-    auto col_scale = [&](int c) -> float {
-        if constexpr (SPLIT) {
-            const int col = n0 + c + lane;
-            return col < q.n ? __ldg(q.col_scale + col) : 0.0f;
-        } else {
-            return 1.0f;
-        }
-    };
     uint32_t ra[32], rb[32];
     tc_ld32_issue(tmem, ra);
-    float cs = col_scale(0);
     tc_ld32_wait(ra);
 #pragma unroll
     for (int ci = 0; ci < NCH; ++ci) {
-        const int c = 32 * ci;
-        float cs_next = 1.0f;
+        const int c = c0 + 32 * ci;
         if (ci + 1 < NCH) {
-            if (ci & 1) tc_ld32_issue(tmem + (uint32_t)(c + 32), ra);
-            else tc_ld32_issue(tmem + (uint32_t)(c + 32), rb);
-            cs_next = col_scale(c + 32);
+            if (ci & 1) tc_ld32_issue(tmem + (uint32_t)(32 * ci + 32), ra);
+            else tc_ld32_issue(tmem + (uint32_t)(32 * ci + 32), rb);
         }
-        if (ci & 1) tc_store_chunk<SPLIT>(q, n0, c, lane, rb, cs, ri.rs, ri.ok, ri.orow, vec_ok, seg, eb);
-        else tc_store_chunk<SPLIT>(q, n0, c, lane, ra, cs, ri.rs, ri.ok, ri.orow, vec_ok, seg, eb);
+        if (ci & 1) tc_store_chunk<SPLIT>(e, n0, c, lane, rb, ri.rs, ri.ok, ri.orow, vec_ok, seg, eb);
+        else tc_store_chunk<SPLIT>(e, n0, c, lane, ra, ri.rs, ri.ok, ri.orow, vec_ok, seg, eb);
         if (ci + 1 < NCH) {
             if (ci & 1) tc_ld32_wait(ra);
             else tc_ld32_wait(rb);
         }
-        cs = cs_next;
     }
 }
 
 // Persistent.  CTA b takes output tiles b, b + gridDim.x, ...  Warp 0 (lane 0) loads the operand
 // tiles of every K block of those tiles into the stage ring; warp 1 (lane 0) issues the MMAs of tile j
-// into TMEM accumulator j % 2 (2 x BN columns) and commits "acc full"; warps 2..5 read an
-// accumulator (warp w reads TMEM lane quarter w % 4), store the tile and arrive on "acc empty", so
-// the next tile's MMAs overlap this tile's stores.
+// into TMEM accumulator j % 2 (2 x BN columns) and commits "acc full"; warps 2..9 read an
+// accumulator (warp w reads TMEM lane quarter w % 4, columns [BN / 2 * h, BN / 2 * (h + 1)) with
+// h = (w - 2) / 4), store the tile and arrive on "acc empty", so the next tile's MMAs overlap this
+// tile's stores.  Eight epilogue warps, two per SM sub-partition, hide the latency of the TMEM
+// loads, shuffles and shared-memory transposes of the stores (four took longer per tile than the
+// MMAs of a 512-deep tile).
 //
 // SPLIT: a stage holds [A hi | A lo | B hi | B lo]; per 16-deep K step the issuer runs
 // hi.hi, hi.lo and lo.hi into the same accumulator (FP16 operands).
 template <int BN, bool SPLIT>
-__global__ void __launch_bounds__(192, 1) tc_rows_kernel(const __grid_constant__ TcParams p, const int total_tiles) {
+__global__ void __launch_bounds__(TC_THREADS, 1) tc_rows_kernel(const __grid_constant__ TcParams p, const int total_tiles) {
     constexpr int STAGES = tc_stages<BN, SPLIT>();
     constexpr int BK = tc_bk<SPLIT>();
     constexpr uint32_t TC_STAGE = tc_stage<BN, SPLIT>(), TC_TMEM_COLS = 2 * BN;
@@ -449,7 +509,7 @@ __global__ void __launch_bounds__(192, 1) tc_rows_kernel(const __grid_constant__
         }
         for (int a = 0; a < 2; ++a) {
             tc_mbar_init(accf0 + 8u * a, 1);
-            tc_mbar_init(acce0 + 8u * a, 4);  // the 4 epilogue warps
+            tc_mbar_init(acce0 + 8u * a, TC_EPI_WARPS);
         }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -570,8 +630,8 @@ __global__ void __launch_bounds__(192, 1) tc_rows_kernel(const __grid_constant__
             }
         }
     } else {
-        // epilogue warps 2..5
-        const int quarter = warp & 3;
+        // epilogue warps 2..9
+        const int quarter = warp & 3, half = (warp - 2) >> 2;
         int j = 0;
         bool ok = true;
         for (int t = (int)blockIdx.x; t < total_tiles; t += (int)gridDim.x, ++j) {
@@ -583,8 +643,9 @@ __global__ void __launch_bounds__(192, 1) tc_rows_kernel(const __grid_constant__
             ok = ok && __all_sync(0xffffffffu, tc_wait(accf0 + 8u * a, (uint32_t)((j >> 1) & 1), p.status, 24));
             tc_fence_after();
             if (!ok) break;
-            tc_store_tile<BN, SPLIT>(q, n0, quarter, lane, tmem + (uint32_t)(a * TC_BN), ri,
-                                     epi + quarter * (32 * 33));  // adds the lane quarter
+            const TcEpi e = tc_epi_of(q);
+            tc_store_tile<BN / 2, SPLIT>(e, n0, half * (BN / 2), quarter, lane, tmem + (uint32_t)(a * TC_BN), ri,
+                                         epi + (warp - 2) * (32 * 33));  // adds the lane quarter
             tc_fence_before();
             __syncwarp();
             if (lane == 0) mbar_arrive_tc(acce0 + 8u * a);
@@ -1160,7 +1221,7 @@ int tc_plan_upload(const TcPlan &pl, cudaStream_t stream) {
 
 template <int BN, bool SPLIT>
 cudaError_t tc_launch(const TcParams &p, int tiles, int sms, cudaStream_t stream) {
-    tc_rows_kernel<BN, SPLIT><<<(unsigned)std::min(tiles, sms), 192, tc_smem<BN, SPLIT>(), stream>>>(p, tiles);
+    tc_rows_kernel<BN, SPLIT><<<(unsigned)std::min(tiles, sms), TC_THREADS, tc_smem<BN, SPLIT>(), stream>>>(p, tiles);
     return cudaGetLastError();
 }
 
