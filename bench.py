@@ -406,6 +406,38 @@ def csr_baseline_leg(A, B_dev, pack, args, batched_spmm_us: float) -> dict:
             "note": "replica 0; one SpMM per launch (median of 150 x 10 runs), except sop_batched_us (96 per launch)"}
 
 
+def load_balance_leg(dev) -> list:
+    """Single-SpMM latency with and without the load-balanced split (spreg_exec_args.load_balance): one
+    SpMM per call, the reference's protocol (median of 150 x 10 runs), FP32, K tiles of 128, N = 512,
+    the tile executor (b_staging 1) in both arms.  A 2048 x 512 @ 90 % with the headline's row skew
+    (sigma 0.5) and with a heavier tail (sigma 1.2).  Alone, a launch has about one job per SM and the
+    heaviest panels set its time; the split halves their K chains.  Checked bit for bit against the
+    oracle's restatement of the split order and within 1e-6 of the unsplit result."""
+    import torch
+    from oracle import oracle as O
+    from spreg import Mapping, PackedMatrix, synth
+    rows = []
+    m = Mapping.identity(4)
+    for sigma in (0.5, 1.2):
+        A = synth.row_skew(2048, 512, 0.9, seed=77, sigma=sigma, std=0.02)
+        B = synth.dense(512, 512, seed=78)
+        pm = PackedMatrix.from_dense(torch.from_numpy(A).to(dev), m, k_tile=128)
+        Bd = torch.from_numpy(B).to(dev)
+        C = torch.empty((2048, 512), device=dev)
+        H, split, heavy = pm.load_balance_plan()
+        t_plain = pm.execute_timed(Bd, C, num_runs=10, staging=1)
+        t_lb = pm.execute_timed(Bd, C, num_runs=10, staging=1, balance=1)
+        got = pm.execute(Bd, C, staging=1, balance=1).cpu().numpy()
+        want = O.load_balanced_execute(O.Tables.of(m), A, B, heavy, split, 128)
+        plain = O.Packed(O.Tables.of(m), A, k_tile=128).execute(B)
+        rows.append({"workload": f"A 2048x512 @90% row skew sigma {sigma}, N=512, FP32, K_c=128, M_r=4",
+                     "heavy_panels": H, "panels": int(pm.info["num_panels"]), "split_tile": split,
+                     "plain_us": t_plain / 1e3, "load_balanced_us": t_lb / 1e3, "speedup": t_plain / t_lb,
+                     "bit_exact_vs_stated_order": bool(np.array_equal(got.view(np.uint32), want.view(np.uint32))),
+                     "rel_err_vs_unsplit": float(O.rel_err(got, plain))})
+    return rows
+
+
 def config1_leg(dev) -> dict:
     """The minimum slice as the workload states it: A 512 x 512 at 80 % Bernoulli sparsity, N(0, 1)
     values, B 512 x 256 N(0, 1), M_r = 4, identity mapping 61fee, N_r = 64.  GPU: one SpMM per call
@@ -1135,6 +1167,7 @@ def main():
     csr_leg = (csr_baseline_leg(As[0], Bd[0], packs[0], args, spmm_us)
                if (lead and args.dtype == "f32" and args.extras) else None)
     cfg1 = config1_leg(dev) if (lead and args.extras) else None
+    lbal = load_balance_leg(dev) if (lead and args.extras) else None
     serving = serving_bench(args, dev) if (lead and args.serving) else None
     precision = precision_suite(dev) if (lead and args.precision) else None
     tensor_cores = tensor_core_suite(dev) if (lead and args.tensor_cores) else None
@@ -1177,6 +1210,7 @@ def main():
                 "cpu_baseline": cpu, "e2e": e2e, "serving": serving,
                 "precision": precision, "batched_layers": layers, "tensor_cores": tensor_cores,
                 "ffn_sparsity_sweep": sweep, "gpu_csr_baseline": csr_leg, "config1_minimum_slice": cfg1,
+                "load_balanced_single_spmm": lbal,
                 "clocks": clocks, "gpu_launches": launches,
                 "parity": parity}
         print(json.dumps(line))

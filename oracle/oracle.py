@@ -233,6 +233,40 @@ class Packed:
         return out
 
 
+def load_balanced_execute(t: Tables, A: np.ndarray, B: np.ndarray, heavy_panels, split_tile: int, k_tile: int,
+                          m_tile=0, col_offset=0, value_dtype=F32, out: np.ndarray | None = None, load_c=False,
+                          epilogue=0) -> np.ndarray:
+    """The stated order of a load-balanced SpMM (the GPU executor's spreg_exec_args.load_balance):
+    row panels in `heavy_panels` are C = lo + hi, one FP32 add, then the epilogue, where lo is the
+    reference executor's chain over K tiles [0, split_tile) (from C with load_c, else from zero) and hi
+    the chain over tiles [split_tile, T) from zero; every other panel is the reference executor's
+    chain over all K tiles (template:265-305).
+
+    Each half is executed from A with the other half's columns zeroed: units (panel, K tile) are
+    packed independently, so the kept tiles pack and run exactly as in A, and the zeroed tiles have
+    no entries (no FMAs).  FP32 or BF16 values (F16 packing scales each panel over all of K)."""
+    if value_dtype == F16:
+        raise ValueError("the load-balanced order is stated for FP32 and BF16 values")
+    A = np.ascontiguousarray(A, dtype=np.float32)
+    C0 = np.zeros((A.shape[0], B.shape[1]), dtype=np.float32) if out is None else out.astype(np.float32)
+    kw = dict(m_tile=m_tile, k_tile=k_tile, col_offset=col_offset, value_dtype=value_dtype)
+    full = Packed(t, A, **kw).execute(B, C0.copy(), load_c=load_c, epilogue=epilogue)
+    kc = split_tile * k_tile
+    a_lo, a_hi = A.copy(), A.copy()
+    a_lo[:, kc:] = 0.0
+    a_hi[:, :kc] = 0.0
+    lo = Packed(t, a_lo, **kw).execute(B, C0.copy(), load_c=load_c)
+    hi = Packed(t, a_hi, **kw).execute(B, np.zeros_like(C0))
+    mr = t.mr
+    for p in heavy_panels:
+        r0, r1 = int(p) * mr, min(int(p) * mr + mr, A.shape[0])
+        v = (lo[r0:r1] + hi[r0:r1]).astype(np.float32)
+        full[r0:r1] = np.where(v > 0, v, np.float32(0.0)).astype(np.float32) if epilogue == 1 else v
+    if out is not None:
+        out[...] = full
+    return full
+
+
 def C_int64(v):
     return C.c_int64(int(v))
 

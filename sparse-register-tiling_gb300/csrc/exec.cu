@@ -286,7 +286,33 @@ struct CallPlan {
     int warps;
     int warps_req;           // warps_per_cta as asked (0: each kernel's own choice) -- the CTA tiling
     int rounds;              // panel rounds of the B-tile kernel (1: B tiles in the ring stages)
+    // Load balance: work-order positions [0, lb_heavy) run K tiles [0, lb_split) into C and
+    // [lb_split, T) into lb_scratch (row stride lb_ld), then C = C + scratch over their rows.
+    int64_t lb_heavy = 0;
+    int32_t lb_split = 0;
+    float *lb_scratch = nullptr;
+    int64_t lb_ld = 0;
+    const spreg_packed *a = nullptr;
+    const spreg_exec_args *args = nullptr;
 };
+
+// The load-balanced split of a pack: the panels whose work estimate exceeds half the heaviest
+// one's, when they are at most three quarters of the panels (else the work is balanced already and
+// no panel is split), split at K tile T / 2.  Splitting them halves the longest job of a launch
+// that has about one job per SM (a single SpMM); in a launch of many SpMMs the work counter
+// balances the SMs already and the split only adds the combine.
+void balance_of(const spreg_packed *a, int64_t *heavy, int32_t *split) {
+    *heavy = 0;
+    *split = 0;
+    const int64_t P = a->geom.P, T = a->geom.T;
+    if (T < 2 || P < 2 || a->list_packed || (int64_t)a->work_desc.size() != P || a->work_desc[0] <= 0) return;
+    const int64_t top = a->work_desc[0];
+    int64_t H = 0;
+    while (H < P && 2 * a->work_desc[(size_t)H] > top) ++H;
+    if (H == 0 || 4 * H > 3 * P) return;
+    *heavy = H;
+    *split = (int32_t)(T / 2);
+}
 
 int plan_call(const spreg_packed *a, const spreg_exec_args *args, CallPlan *cp, int64_t others1) {
     SPREG_CHECK_ARG(a && args, "null packed matrix or args");
@@ -306,6 +332,11 @@ int plan_call(const spreg_packed *a, const spreg_exec_args *args, CallPlan *cp, 
     SPREG_CHECK_ARG(args->panel_rounds >= 0 && args->panel_rounds <= kTileMaxRounds, "panel_rounds must be in [0, %d]",
                     kTileMaxRounds);
     const int rounds = args->panel_rounds > 1 ? args->panel_rounds : 1;
+    SPREG_CHECK_ARG(args->load_balance == 0 || args->load_balance == 1, "load_balance must be 0 or 1");
+    SPREG_CHECK_ARG(args->load_balance == 0 ||
+                        (args->c_dtype == SPREG_F32 && in.value_dtype != SPREG_F16 && args->b_staging != 2 &&
+                         args->meta_staging != 2),
+                    "load_balance needs FP32 C, FP32 or BF16 values and the B-tile kernel (b_staging 0 or 1)");
     SPREG_CHECK_ARG(rounds == 1 || (args->b_staging != 2 && args->meta_staging != 2),
                     "panel_rounds > 1 runs the shared-memory B-tile kernel (b_staging 0 or 1, meta_staging 0 or 1)");
     int dev = -1;
@@ -381,8 +412,15 @@ int plan_call(const spreg_packed *a, const spreg_exec_args *args, CallPlan *cp, 
         if ((p & (p - 1)) == 0 || p == (1 << in.mr) - 1) hot += a->id_entries[i];
     }
     const bool hot_set = all > 0 && 100 * hot >= 85 * all;
+    int64_t lb_heavy = 0;
+    int32_t lb_split = 0;
+    if (args->load_balance) balance_of(a, &lb_heavy, &lb_split);
+    const bool lb = lb_heavy > 0;
+    SPREG_CHECK_ARG(!lb || (tile_base_ok && args->n <= INT32_MAX),
+                    "load_balance: the B-tile kernel cannot run this call (a 16-byte aligned B with 16-byte "
+                    "aligned rows is needed)");
     const bool tile_kernel =
-        args->b_staging == 1 || rounds > 1 || (args->b_staging == 0 && tile_base_ok && args->meta_staging != 2 &&
+        args->b_staging == 1 || rounds > 1 || lb || (args->b_staging == 0 && tile_base_ok && args->meta_staging != 2 &&
                                  !cp->stream_kernel && a->geom.T > 1 && args->n <= INT32_MAX &&
                                  staged_rows * 32 * nv * (int64_t)bsz <= 64 * 1024);
     if (tile_kernel && bsz == 2 && in.mr <= 4 && nv == 4 && (args->nr == 0 || args->nr == 256) && args->n >= 256 &&
@@ -428,7 +466,7 @@ int plan_call(const spreg_packed *a, const spreg_exec_args *args, CallPlan *cp, 
     const bool auto_tile = args->b_staging == 0 && tile_base_ok && args->meta_staging != 2 && !cp->stream_kernel &&
                            a->geom.T > 1 && args->n <= INT32_MAX &&
                            staged_rows * 32 * nv * (int64_t)bsz <= 64 * 1024;
-    if (args->b_staging == 1 || rounds > 1 || auto_tile) {
+    if (args->b_staging == 1 || rounds > 1 || lb || auto_tile) {
         const bool main_ok = !cp->has_main || rounds > 1 || tile_rows_ok(nv);
         const bool tail_ok = !cp->has_tail || rounds > 1 || tile_rows_ok(1);
         SPREG_CHECK_ARG(main_ok && tail_ok, "shared-memory B tiles: a K tile of %lld rows x %d columns exceeds a "
@@ -445,17 +483,26 @@ int plan_call(const spreg_packed *a, const spreg_exec_args *args, CallPlan *cp, 
         tb.C = args->c;
         tb.ldb = args->ldb;
         tb.ldc = args->ldc;
-        tb.M = in.rows;
+        SPREG_CHECK_ARG(in.rows <= INT32_MAX && a->geom.T < 32768, "shared-memory B tiles: too many rows or K tiles");
+        tb.M = (int32_t)in.rows;
         tb.P = (int32_t)a->geom.P;
         tb.T = (int32_t)a->geom.T;
         tb.ppt = (int32_t)a->geom.ppt;
         tb.load_c = args->load_c ? 1 : 0;
         tb.epilogue = (int16_t)args->epilogue;
-        tb.order = args->job_order;
+        tb.order = (int16_t)args->job_order;
         tb.kt = (int32_t)kt_rows;
         tb.krows = (int32_t)a->geom.K;
         tb.col_offset = (int32_t)in.col_offset;
-        tb.box_rows = box_rows;
+        tb.box_rows = (int16_t)box_rows;
+        tb.t_begin = 0;
+        tb.t_end = (int16_t)a->geom.T;
+        tb.pos_begin = 0;
+        tb.count = (int32_t)a->geom.P;
+        cp->lb_heavy = lb_heavy;
+        cp->lb_split = lb_split;
+        cp->a = a;
+        cp->args = args;
         const int64_t brows = in.col_offset + a->geom.K;
         cp->tmain = tb;
         cp->tmain.col_begin = 0;
@@ -613,9 +660,10 @@ int launch_tile_groups(std::map<std::tuple<int, int, int, int>, TileGroup> &grou
             for (size_t i = 0; i < cnt; ++i) {
                 TProblem &pr = tp.prob[i];
                 pr = g.probs[first + i];
-                pr.job_begin = jobs;
+                pr.job_begin = (int32_t)jobs;
                 const int64_t per_job = (int64_t)W * g.rounds;
-                jobs += (int64_t)((pr.P + per_job - 1) / per_job) * pr.S;
+                jobs += (int64_t)((pr.count + per_job - 1) / per_job) * pr.S;
+                if (jobs > INT32_MAX) break;
             }
             if (jobs == 0) continue;
             SPREG_CHECK_ARG(jobs <= INT32_MAX, "too many jobs in one launch");
@@ -651,8 +699,50 @@ void add_tile_call(std::map<std::tuple<int, int, int, int>, TileGroup> &groups, 
         g.xbuf = std::max(g.xbuf, cp.xbuf);
         g.stage_b = std::max(g.stage_b, stage_b);
     };
-    if (cp.has_main) add(cp.tmain, cp.nv, cp.stage_b_main);
-    if (cp.has_tail) add(cp.ttail, 1, cp.stage_b_tail);
+    auto add_split = [&](const TProblem &pr, int nv, int64_t stage_b) {
+        if (cp.lb_heavy <= 0) {
+            add(pr, nv, stage_b);
+            return;
+        }
+        // heavy panels: K tiles [0, split) into C (no epilogue), [split, T) from zero into the scratch
+        TProblem lo = pr, hi = pr, rest = pr;
+        lo.count = hi.count = (int32_t)cp.lb_heavy;
+        lo.t_end = (int16_t)cp.lb_split;
+        lo.epilogue = SPREG_EPILOGUE_NONE;
+        hi.t_begin = (int16_t)cp.lb_split;
+        hi.C = cp.lb_scratch;
+        hi.ldc = cp.lb_ld;
+        hi.load_c = 0;
+        hi.epilogue = SPREG_EPILOGUE_NONE;
+        add(lo, nv, stage_b);
+        add(hi, nv, stage_b);
+        if (cp.lb_heavy < pr.P) {
+            rest.pos_begin = (int32_t)cp.lb_heavy;
+            rest.count = pr.P - (int32_t)cp.lb_heavy;
+            add(rest, nv, stage_b);
+        }
+    };
+    if (cp.has_main) add_split(cp.tmain, cp.nv, cp.stage_b_main);
+    if (cp.has_tail) add_split(cp.ttail, 1, cp.stage_b_tail);
+}
+
+// C = C + S (then the epilogue) over the rows of the split panels: the last step of a load-balanced
+// SpMM (one FP32 add per element, C holding K tiles [0, split) and S tiles [split, T)).
+__global__ void lb_combine_kernel(float *__restrict__ C, int64_t ldc, const float *__restrict__ S, int64_t lds,
+                                  const int32_t *__restrict__ panel_order, int64_t heavy, int mr, int64_t M,
+                                  int64_t n, int epilogue) {
+    for (int64_t p = blockIdx.y; p < heavy; p += gridDim.y) {
+        const int64_t row0 = (int64_t)panel_order[p] * mr;
+        for (int r = 0; r < mr && row0 + r < M; ++r) {
+            float *c = C + (row0 + r) * ldc;
+            const float *s = S + (row0 + r) * lds;
+            for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
+                float o = c[j] + s[j];
+                if (epilogue == SPREG_EPILOGUE_RELU) o = fmaxf(o, 0.0f);
+                c[j] = o;
+            }
+        }
+    }
 }
 
 void add_call(std::map<std::tuple<int, int, int>, Group> &groups, const CallPlan &cp) {
@@ -675,19 +765,61 @@ int run_calls(const spreg_packed *const *as, const spreg_exec_args *const *args,
     std::vector<CallPlan> streams;
     int64_t items1 = 0;
     for (int32_t i = 0; i < n; ++i) items1 += strip_items1(as[i], args[i]);
+    std::vector<CallPlan> plans((size_t)n);
+    int64_t lb_bytes = 0;
     for (int32_t i = 0; i < n; ++i) {
-        CallPlan cp;
+        CallPlan &cp = plans[(size_t)i];
         int st = plan_call(as[i], args[i], &cp, items1 - strip_items1(as[i], args[i]));
         if (st != SPREG_OK) return st;
+        if (cp.lb_heavy > 0) {
+            cp.lb_ld = (args[i]->n + 7) / 8 * 8;
+            lb_bytes += (as[i]->info.rows * cp.lb_ld * 4 + 255) / 256 * 256;
+        }
+    }
+    // scratch of the split panels' upper K halves: stream-ordered (capturable in a CUDA graph)
+    char *lb_mem = nullptr;
+    if (lb_bytes > 0) {
+        cudaError_t e = cudaMallocAsync(reinterpret_cast<void **>(&lb_mem), (size_t)lb_bytes, stream);
+        if (e != cudaSuccess) SPREG_FAIL(SPREG_ERR_NOMEM, "load-balance scratch (%lld B): %s", (long long)lb_bytes,
+                                         cudaGetErrorString(e));
+        int64_t off = 0;
+        for (CallPlan &cp : plans)
+            if (cp.lb_heavy > 0) {
+                cp.lb_scratch = reinterpret_cast<float *>(lb_mem + off);
+                off += (cp.a->info.rows * cp.lb_ld * 4 + 255) / 256 * 256;
+            }
+    }
+    for (const CallPlan &cp : plans) {
         if (cp.tile) add_tile_call(tgroups, cp);
         else if (cp.stream_kernel) streams.push_back(cp);
         else add_call(groups, cp);
     }
     int st = launch_groups(groups, stream);
-    if (st != SPREG_OK) return st;
-    if ((st = launch_tile_groups(tgroups, stream))) return st;
-    for (const CallPlan &cp : streams)
-        if ((st = launch_stream(cp, stream))) return st;
+    if (st == SPREG_OK) st = launch_tile_groups(tgroups, stream);
+    for (size_t i = 0; i < streams.size() && st == SPREG_OK; ++i) st = launch_stream(streams[i], stream);
+    for (const CallPlan &cp : plans) {
+        if (st != SPREG_OK || cp.lb_heavy <= 0) continue;
+        const int64_t nn = cp.args->n;
+        const unsigned gx = (unsigned)std::max<int64_t>(1, std::min<int64_t>((nn + 255) / 256, 8));
+        const unsigned gy = (unsigned)std::min<int64_t>(cp.lb_heavy, 65535);
+        lb_combine_kernel<<<dim3(gx, gy), 256, 0, stream>>>(reinterpret_cast<float *>(cp.args->c), cp.args->ldc,
+                                                            cp.lb_scratch, cp.lb_ld, cp.a->panel_order, cp.lb_heavy,
+                                                            cp.mr, cp.a->info.rows, nn, cp.args->epilogue);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) {
+            set_error(std::string("load-balance combine launch: ") + cudaGetErrorString(e));
+            st = SPREG_ERR_CUDA;
+        }
+    }
+    if (lb_mem) cudaFreeAsync(lb_mem, stream);
+    return st;
+}
+
+int load_balance_plan_impl(const spreg_packed *a, int64_t *heavy, int32_t *split, int32_t *ids, int64_t max_ids) {
+    SPREG_CHECK_ARG(a && heavy && split, "null argument");
+    balance_of(a, heavy, split);
+    if (ids)
+        for (int64_t i = 0; i < *heavy && i < max_ids; ++i) ids[i] = a->order_host[(size_t)i];
     return SPREG_OK;
 }
 

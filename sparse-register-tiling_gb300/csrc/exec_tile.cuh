@@ -57,16 +57,22 @@ struct TProblem {
     const float *scales;        // per-row-panel F16 scales (else null)
     const void *B;
     void *C;
-    int64_t ldb, ldc, M;
-    int64_t job_begin;          // first global job
+    int64_t ldb, ldc;
+    int32_t M;                  // rows of A and C
+    int32_t job_begin;          // first global job
     int32_t col_begin;          // first column of the problem's strips
     int32_t col_end;            // columns >= col_end are not computed
     int32_t P, S, T, ppt;       // row panels, strips, K tiles, panels per row tile
     int16_t load_c, epilogue;
-    int32_t order;              // job order: 0 = panel groups outer (a group's strips in a row), 1 = strips outer
+    int16_t order;              // job order: 0 = panel groups outer (a group's strips in a row), 1 = strips outer
+    int16_t box_rows;           // rows of one tensor copy (K tile copied in ceil(kt / box_rows) copies)
     int32_t kt, krows;          // B rows per K tile, B rows of all tiles (columns of A)
     int32_t col_offset;         // first B row of tile 0
-    int32_t box_rows;           // rows of one tensor copy (K tile copied in ceil(kt / box_rows) copies)
+    // The units this problem runs: K tiles [t_begin, t_end) of the panels at work-order positions
+    // [pos_begin, pos_begin + count) (the whole pack: 0, T, 0, P).  A load-balanced SpMM splits its
+    // heaviest panels' K tiles between two problems (spreg_exec_args.load_balance).
+    int16_t t_begin, t_end;
+    int32_t pos_begin, count;
     CUtensorMap tmap;           // B as a 2-D tensor: columns [0, col_end) x rows [0, col_offset + krows)
 };
 static_assert(sizeof(TProblem) == 256 && offsetof(TProblem, tmap) == 128, "TProblem layout");
@@ -278,16 +284,16 @@ __global__ void __launch_bounds__(32 * (kTileMaxWarps + 1), 1) exec_tile_kernel(
             const int64_t local = job - pr.job_begin;
             const int64_t gsz = (int64_t)W * R;  // panels per job
             if (pr.order == 1) {
-                const int64_t groups = (pr.P + gsz - 1) / gsz;
+                const int64_t groups = (pr.count + gsz - 1) / gsz;
                 group = (int)(local % groups);
                 strip = (int)(local / groups);
             } else {
                 group = (int)(local / pr.S);
                 strip = (int)(local % pr.S);
             }
-            t = 0;
+            t = pr.t_begin;
             r = 0;
-            const int64_t left = (int64_t)pr.P - (int64_t)group * gsz;  // panels from this job's first on
+            const int64_t left = (int64_t)pr.count - (int64_t)group * gsz;  // panels from this job's first on
             rounds_job = (int)((left + W - 1) / W < R ? (left + W - 1) / W : R);
             ++njob;
         };
@@ -316,7 +322,7 @@ __global__ void __launch_bounds__(32 * (kTileMaxWarps + 1), 1) exec_tile_kernel(
             const int c0 = pr.col_begin + strip * (32 * NV);
             const int nbox = (pr.kt + pr.box_rows - 1) / pr.box_rows;
             const int b = res ? (int)((njob - 1) % tp.nbuf) : 0;
-            const bool load_b = !res || (r == 0 && t == 0);
+            const bool load_b = !res || (r == 0 && t == pr.t_begin);
             if (res && load_b) {
                 // the job that read this strip before must be done with it: its last stage released
                 // (a stage NS or more back is already covered by the ring wait above)
@@ -327,11 +333,11 @@ __global__ void __launch_bounds__(32 * (kTileMaxWarps + 1), 1) exec_tile_kernel(
                     break;
                 }
             }
-            // metadata: lane w < W holds the block of unit (panel (group * R + r) * W + w, t)
+            // metadata: lane w < W holds the block of unit (panel pos_begin + (group * R + r) * W + w, t)
             int64_t moff = 0;
             uint32_t mbytes = 0;
-            const int64_t pos = ((int64_t)group * R + r) * W + lane;  // position in the work order
-            const bool act = lane < W && pos < pr.P;
+            const int64_t pos = pr.pos_begin + ((int64_t)group * R + r) * W + lane;  // position in the work order
+            const bool act = lane < W && pos < (int64_t)pr.pos_begin + pr.count;
             if (act) {
                 const int64_t slot = (int64_t)t * pr.P + pos;
                 moff = pr.exec_offs[slot];
@@ -351,12 +357,12 @@ __global__ void __launch_bounds__(32 * (kTileMaxWarps + 1), 1) exec_tile_kernel(
             const uint32_t tile_b = (uint32_t)(nbox * pr.box_rows) * ROWB;  // one K tile of the strip
             if (lane == 0) {
                 sts_v4(jobs0 + 16u * s, pi, group * R + r, strip, t | (b << 16));
-                const uint32_t bbytes = load_b ? (res ? (uint32_t)pr.T : 1u) * tile_b : 0u;
+                const uint32_t bbytes = load_b ? (res ? (uint32_t)(pr.t_end - pr.t_begin) : 1u) * tile_b : 0u;
                 mbar_arrive_expect_tx(full, bbytes + mtotal);
                 if (res && load_b) {
-                    // every K tile of the strip, into resident strip b
+                    // every K tile of the problem's range, into resident strip b (tile tt at tt * tile_b)
                     const uint32_t dst = res0 + (uint32_t)b * (uint32_t)tp.stage_b;
-                    for (int tt = 0; tt < pr.T; ++tt)
+                    for (int tt = pr.t_begin; tt < pr.t_end; ++tt)
                         for (int bx = 0; bx < nbox; ++bx)
                             tma_load_2d(dst + (uint32_t)tt * tile_b + (uint32_t)(bx * pr.box_rows) * ROWB, &pr.tmap, c0,
                                         pr.col_offset + tt * pr.kt + bx * pr.box_rows, full);
@@ -373,8 +379,8 @@ __global__ void __launch_bounds__(32 * (kTileMaxWarps + 1), 1) exec_tile_kernel(
             __syncwarp();
             last_seq[s] = seq;
             if (res) buf_last[b] = seq;
-            if (++t == pr.T) {
-                t = 0;
+            if (++t == pr.t_end) {
+                t = pr.t_begin;
                 if (++r == rounds_job) fetch();
             }
         }
@@ -396,14 +402,14 @@ __global__ void __launch_bounds__(32 * (kTileMaxWarps + 1), 1) exec_tile_kernel(
         const int4 ji = lds_v4(jobs0 + 16u * s);
         if (ji.x < 0) break;
         const TProblem &pr = tp.prob[ji.x];
-        const int64_t pos = (int64_t)ji.y * W + warp;
+        const int64_t pos = pr.pos_begin + (int64_t)ji.y * W + warp;
         const int t = ji.w & 0xffff;
-        if (pos < pr.P) {
+        if (pos < (int64_t)pr.pos_begin + pr.count) {
             const int64_t gp = pr.panel_order[pos];
             const int64_t row0 = gp * MR;
             const int64_t col0 = pr.col_begin + (int64_t)ji.z * (32 * NV) + (int64_t)lane * NV;
             const bool valid = col0 < pr.col_end;
-            if (t == 0) t_acc_init<MR, NV, TV, TC>(pr, row0, col0, valid, acc);
+            if (t == pr.t_begin) t_acc_init<MR, NV, TV, TC>(pr, row0, col0, valid, acc);
             const uint32_t sb = stage0 + (uint32_t)s * stage_bytes;
             // B tile t: in the ring stage, or in resident strip ji.w >> 16
             const uint32_t tile_b = (uint32_t)((pr.kt + pr.box_rows - 1) / pr.box_rows * pr.box_rows) * ROWB;
@@ -417,7 +423,7 @@ __global__ void __launch_bounds__(32 * (kTileMaxWarps + 1), 1) exec_tile_kernel(
                 const uint4 rec = lds_u128(buf + 16u + 16u * g);
                 run_group_x<MR, NV, TV, true>((int)rec.x, (int)rec.y, buf + rec.z, buf + rec.w, bl, acc);
             }
-            if (t == pr.T - 1) t_store<MR, NV, TV, TC>(pr, gp, row0, col0, valid, acc);
+            if (t == pr.t_end - 1) t_store<MR, NV, TV, TC>(pr, gp, row0, col0, valid, acc);
         }
         __syncwarp();
         if (lane == 0) mbar_arrive(empty0 + 8u * s);

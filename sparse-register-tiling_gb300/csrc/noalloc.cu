@@ -160,7 +160,8 @@ extern "C" int spreg_execute_batched_noalloc(const spreg_work_item *items, int32
         SPREG_CHECK_ARG(args->epilogue == SPREG_EPILOGUE_NONE || args->epilogue == SPREG_EPILOGUE_RELU,
                         "work item %d: bad epilogue", i);
         SPREG_CHECK_ARG(args->job_order == 0 || args->job_order == 1, "work item %d: job_order must be 0 or 1", i);
-        SPREG_CHECK_ARG(args->b_staging != 1 && args->meta_staging != 2 && args->panel_rounds <= 1,
+        SPREG_CHECK_ARG(args->b_staging != 1 && args->meta_staging != 2 && args->panel_rounds <= 1 &&
+                            args->load_balance == 0,
                         "work item %d: the no-allocation entry point runs the batched execution-layout kernel only", i);
         const int64_t xbuf = (a->max_exec_bytes + 127) / 128 * 128;
         SPREG_CHECK_ARG(a->exec && 1024 + 2 * xbuf <= d->smem_optin,

@@ -953,6 +953,9 @@ int finish_pack(const spreg_mapping *m, const Geom &g, int value_dtype, int64_t 
         std::stable_sort(order.begin(), order.end(),
                          [&](int32_t x, int32_t y) { return work[(size_t)x] > work[(size_t)y]; });
         for (int64_t i = 0; i < g.P; ++i) rank[(size_t)order[(size_t)i]] = (int32_t)i;
+        p->work_desc.resize((size_t)g.P);
+        for (int64_t i = 0; i < g.P; ++i) p->work_desc[(size_t)i] = work[(size_t)order[(size_t)i]];
+        p->order_host = order;
         if (g.P > 0) {
             e = cudaMemcpyAsync(p->panel_order, order.data(), (size_t)g.P * sizeof(int32_t), cudaMemcpyHostToDevice,
                                 stream);

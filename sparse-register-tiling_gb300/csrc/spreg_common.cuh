@@ -8,6 +8,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <string>
+#include <vector>
 
 #include "../../include/spreg.h"
 
@@ -192,4 +193,6 @@ struct spreg_packed {
     int64_t exec_bytes = 0;
     int64_t max_exec_bytes = 0;
     bool list_packed = false;       // packed panel by panel (per-panel column offsets, no K tiles)
+    std::vector<int64_t> work_desc; // the panels' work estimates in panel_order (descending), host copy
+    std::vector<int32_t> order_host; // panel_order, host copy
 };

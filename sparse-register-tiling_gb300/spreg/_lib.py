@@ -72,7 +72,8 @@ class ExecArgs(C.Structure):
     _fields_ = [("b", C.c_void_p), ("ldb", C.c_int64), ("c", C.c_void_p), ("ldc", C.c_int64), ("n", C.c_int64),
                 ("b_dtype", C.c_int32), ("c_dtype", C.c_int32), ("load_c", C.c_int32), ("epilogue", C.c_int32),
                 ("nr", C.c_int32), ("warps_per_cta", C.c_int32), ("b_staging", C.c_int32),
-                ("meta_staging", C.c_int32), ("job_order", C.c_int32), ("panel_rounds", C.c_int32)]
+                ("meta_staging", C.c_int32), ("job_order", C.c_int32), ("panel_rounds", C.c_int32),
+                ("load_balance", C.c_int32), ("reserved", C.c_int32)]
 
 
 class WorkItem(C.Structure):
@@ -89,7 +90,7 @@ class DenseRowsF32Item(C.Structure):
 class TileConfig(C.Structure):
     _fields_ = [("m_tile", C.c_int32), ("k_tile", C.c_int32), ("n_tile", C.c_int32), ("nr", C.c_int32),
                 ("outer_schedule", C.c_int32), ("value_dtype", C.c_int32), ("sparse_a", C.c_int32),
-                ("tiling_strategy", C.c_int32), ("beta_10x", C.c_int32)]
+                ("tiling_strategy", C.c_int32), ("beta_10x", C.c_int32), ("load_balance", C.c_int32)]
 
 
 P = C.c_void_p
@@ -134,6 +135,7 @@ PROTOTYPES = {
     "spreg_device_status": (C.c_int, [C.POINTER(C.c_int32), C.c_int32]),
     "spreg_execute_batched_noalloc": (C.c_int, [P, C.c_int32, P]),
     "spreg_execute_timed": (C.c_int, [P, C.POINTER(ExecArgs), C.c_int64, C.POINTER(C.c_double), P]),
+    "spreg_load_balance_plan": (C.c_int, [P, C.POINTER(C.c_int64), C.POINTER(C.c_int32), P, C.c_int64]),
     "spreg_selftest_wait_timeout": (C.c_int, [C.c_uint32, C.POINTER(C.c_int32), C.POINTER(C.c_uint32), P]),
     "spreg_csr_spmm": (C.c_int, [C.c_int64, C.c_int64, C.c_int64, C.c_int64, P, P, P, P, C.c_int64, P, C.c_int64,
                                  C.c_int32, P]),

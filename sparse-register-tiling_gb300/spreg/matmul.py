@@ -37,15 +37,16 @@ class TileConfig:
     sparse_a: int = 1
     tiling_strategy: int = 0
     beta: float = 1.0
+    load_balance: int = 0  # the load-balanced kernel (KD_IntelLoadBalanced; spreg_exec_args.load_balance)
 
     def to_c(self) -> _lib.TileConfig:
         return _lib.TileConfig(self.M_c, self.K_c, self.N_c, self.nr, self.runtimeSchedule, self.value_dtype,
-                               self.sparse_a, self.tiling_strategy, int(round(self.beta * 10)))
+                               self.sparse_a, self.tiling_strategy, int(round(self.beta * 10)), int(self.load_balance))
 
     @classmethod
     def from_c(cls, t: _lib.TileConfig) -> "TileConfig":
         return cls(t.m_tile, t.k_tile, t.n_tile, t.nr, t.outer_schedule, t.value_dtype, t.sparse_a,
-                   t.tiling_strategy, t.beta_10x / 10.0)
+                   t.tiling_strategy, t.beta_10x / 10.0, t.load_balance)
 
     @classmethod
     def from_sop_config(cls, cfg: dict) -> "TileConfig":

@@ -116,11 +116,12 @@ class PackedMatrix:
 
     # ---------------------------------------------------------------- executor
     def exec_args(self, B, C_out, n=None, load_c=False, epilogue=_lib.EPILOGUE_NONE, nr=0, warps=0,
-                  staging=0, meta=0, order=0, rounds=0) -> _lib.ExecArgs:
+                  staging=0, meta=0, order=0, rounds=0, balance=0) -> _lib.ExecArgs:
         n = B.shape[1] if n is None else int(n)
         return _lib.ExecArgs(B.data_ptr(), B.stride(0), C_out.data_ptr(), C_out.stride(0), n,
                              torch_dtype_code(B.dtype), torch_dtype_code(C_out.dtype), int(bool(load_c)),
-                             int(epilogue), int(nr), int(warps), int(staging), int(meta), int(order), int(rounds))
+                             int(epilogue), int(nr), int(warps), int(staging), int(meta), int(order), int(rounds),
+                             int(balance), 0)
 
     def _check_operands(self, B, C_out):
         _require_cuda(B, "B")
@@ -134,10 +135,11 @@ class PackedMatrix:
             raise ValueError(f"C has {C_out.shape[0]} rows, A has {self.info['rows']}")
 
     def execute(self, B, C_out=None, n=None, load_c=False, epilogue=_lib.EPILOGUE_NONE, nr=0, warps=0,
-                out_dtype=None, stream=None, staging=0, meta=0, order=0, rounds=0):
+                out_dtype=None, stream=None, staging=0, meta=0, order=0, rounds=0, balance=0):
         """C (+)= A . B over the first n columns of B; returns C.  ``rounds`` > 1: panel rounds of the
         B-tile kernel (the strip of B for every K tile stays in shared memory for that many rounds of
-        panels)."""
+        panels).  ``balance`` = 1: the load-balanced split of the heaviest panels' K tiles
+        (`load_balance_plan`)."""
         import torch
         if C_out is None:
             if load_c:
@@ -145,19 +147,27 @@ class PackedMatrix:
             C_out = torch.empty((self.info["rows"], B.shape[1]), device=B.device,
                                 dtype=out_dtype if out_dtype is not None else torch.float32)
         self._check_operands(B, C_out)
-        args = self.exec_args(B, C_out, n, load_c, epilogue, nr, warps, staging, meta, order, rounds)
+        args = self.exec_args(B, C_out, n, load_c, epilogue, nr, warps, staging, meta, order, rounds, balance)
         _lib.check(_lib.lib().spreg_execute(self._h, C.byref(args), _lib.stream_handle(stream)))
         return C_out
 
     def execute_timed(self, B, C_out, num_runs: int = 1, n=None, nr=0, warps=0, stream=None, staging=0,
-                      meta=0, rounds=0) -> float:
+                      meta=0, rounds=0, balance=0) -> float:
         """Median per-run time (ns) over 150 x num_runs runs of C = A . B (template:308-349)."""
         self._check_operands(B, C_out)
-        args = self.exec_args(B, C_out, n, False, 0, nr, warps, staging, meta, rounds=rounds)
+        args = self.exec_args(B, C_out, n, False, 0, nr, warps, staging, meta, rounds=rounds, balance=balance)
         t = C.c_double()
         _lib.check(_lib.lib().spreg_execute_timed(self._h, C.byref(args), int(num_runs), C.byref(t),
                                                   _lib.stream_handle(stream)))
         return float(t.value)
+
+    def load_balance_plan(self):
+        """(heavy panels, split K tile, their row-panel indices) of the load-balanced split
+        (spreg_load_balance_plan); (0, 0, []) when the pack's work is balanced already."""
+        h, t = C.c_int64(), C.c_int32()
+        ids = np.zeros(max(1, int(self.info["num_panels"])), dtype=np.int32)
+        _lib.check(_lib.lib().spreg_load_balance_plan(self._h, C.byref(h), C.byref(t), ids.ctypes.data, ids.size))
+        return int(h.value), int(t.value), ids[: int(h.value)].copy()
 
     # ---------------------------------------------------------------- bytes / flops
     def algorithmic_bytes(self, n: int, b_bytes: int = 4, c_bytes: int = 4, load_c: bool = False) -> int:

@@ -45,7 +45,7 @@ WORK_ITEM_DTYPE = np.dtype([
     ("a", np.uint64), ("b", np.uint64), ("ldb", np.int64), ("c", np.uint64), ("ldc", np.int64), ("n", np.int64),
     ("b_dtype", np.int32), ("c_dtype", np.int32), ("load_c", np.int32), ("epilogue", np.int32), ("nr", np.int32),
     ("warps_per_cta", np.int32), ("b_staging", np.int32), ("meta_staging", np.int32), ("job_order", np.int32),
-    ("panel_rounds", np.int32)])
+    ("panel_rounds", np.int32), ("load_balance", np.int32), ("reserved", np.int32)])
 assert WORK_ITEM_DTYPE.itemsize == C.sizeof(_lib.WorkItem)
 
 # numpy view of spreg_dense_rows_item (include/spreg.h): one tensor-core product

@@ -243,3 +243,30 @@ def test_simd_csr_baseline_is_bit_identical():
     B = synth.dense(256, 128, seed=9)
     assert np.array_equal(O.csr_spmm_fast(rp, ci, v, B, threads=3).view(np.uint32),
                           O.csr_spmm(rp, ci, v, B).view(np.uint32))
+
+
+@pytest.mark.parametrize("load_c,relu", [(False, False), (True, True)])
+def test_load_balanced_order_known_answers(load_c, relu):
+    """The restated load-balanced order: a split at K tile 0 (zero + the whole chain from zero) or at
+    K tile T (the whole chain + zero) gives the executor's own bits; a split in the middle stays within
+    FP32 rounding of it, and panels that are not split keep its bits."""
+    m = Mapping.identity(4)
+    A = synth.row_skew(90, 384, 0.8, seed=11, std=1.0)
+    B = synth.dense(384, 40, seed=12)
+    C0 = synth.dense(90, 40, seed=13)
+    t = O.Tables.of(m)
+    plain = O.Packed(t, A, k_tile=64).execute(B, C0.copy() if load_c else None, load_c=load_c, epilogue=int(relu))
+    heavy = [0, 3, 7, 22]
+    if not load_c:  # from zero: 0 + chain = chain
+        at0 = O.load_balanced_execute(t, A, B, heavy, 0, 64, epilogue=int(relu))
+        assert np.array_equal(at0.view(np.uint32), plain.view(np.uint32))
+    atT = O.load_balanced_execute(t, A, B, heavy, 6, 64, out=C0.copy() if load_c else None, load_c=load_c,
+                                  epilogue=int(relu))
+    assert np.array_equal(atT.view(np.uint32), plain.view(np.uint32))
+    mid = O.load_balanced_execute(t, A, B, heavy, 3, 64, out=C0.copy() if load_c else None, load_c=load_c,
+                                  epilogue=int(relu))
+    rows = np.concatenate([np.arange(4 * p, 4 * p + 4) for p in heavy])
+    rows = rows[rows < 90]  # panel 22 is the ragged last one (rows 88, 89)
+    others = np.setdiff1d(np.arange(90), rows)
+    assert np.array_equal(mid[others].view(np.uint32), plain[others].view(np.uint32))
+    assert O.rel_err(mid[rows], plain[rows]) < 1e-6
