@@ -410,9 +410,10 @@ def load_balance_leg(dev) -> list:
     """Single-SpMM latency with and without the load-balanced split (spreg_exec_args.load_balance): one
     SpMM per call, the reference's protocol (median of 150 x 10 runs), FP32, K tiles of 128, N = 512,
     the tile executor (b_staging 1) in both arms.  A 2048 x 512 @ 90 % with the headline's row skew
-    (sigma 0.5) and with a heavier tail (sigma 1.2).  Alone, a launch has about one job per SM and the
-    heaviest panels set its time; the split halves their K chains.  Checked bit for bit against the
-    oracle's restatement of the split order and within 1e-6 of the unsplit result."""
+    (sigma 0.5) and with a heavier tail (sigma 1.2).  Alone, a launch has fewer jobs than SMs and the
+    heaviest job groups set its time; the split halves their K chains on the idle SMs.  Checked bit
+    for bit against the oracle's restatement of the split order and within 1e-6 of the unsplit
+    result."""
     import torch
     from oracle import oracle as O
     from spreg import Mapping, PackedMatrix, synth
@@ -424,7 +425,7 @@ def load_balance_leg(dev) -> list:
         pm = PackedMatrix.from_dense(torch.from_numpy(A).to(dev), m, k_tile=128)
         Bd = torch.from_numpy(B).to(dev)
         C = torch.empty((2048, 512), device=dev)
-        H, split, heavy = pm.load_balance_plan()
+        H, split, heavy = pm.load_balance_plan(Bd, C, staging=1)
         t_plain = pm.execute_timed(Bd, C, num_runs=10, staging=1)
         t_lb = pm.execute_timed(Bd, C, num_runs=10, staging=1, balance=1)
         got = pm.execute(Bd, C, staging=1, balance=1).cpu().numpy()

@@ -228,24 +228,26 @@ typedef struct {
                              shared memory; results do not depend on it. */
     int32_t load_balance; /* 0: off.  1: split the heaviest row panels' K tiles between two concurrent jobs
                              (the reference's load-balanced kernel choice, KD_IntelLoadBalanced in
-                             cpp_testbed/src/spmm/nano/runtime_yaml_config.register:84-99).  Panels whose
-                             work estimate exceeds half the heaviest one's are split at K tile T / 2
-                             when they are at most 3/4 of the panels: K tiles [0, T/2) accumulate
-                             into C (from C with load_c), tiles [T/2, T) from zero into scratch, then
-                             C = C + scratch (one FP32 add per element; the epilogue after it).  Needs
-                             a K-tiled pack (T >= 2) of FP32 or BF16 values, FP32 C and the B-tile
-                             kernel (b_staging 0 or 1).  spreg_load_balance_plan reports the split. */
+                             cpp_testbed/src/spmm/nano/runtime_yaml_config.register:84-99).  When the
+                             launch leaves SMs idle (fewer jobs of W panels x strips than SMs), the
+                             heaviest whole groups of W panels (work estimate above half the heaviest
+                             panel's) are split at K tile T / 2 until the idle SMs are used: K tiles
+                             [0, T/2) accumulate into C (from C with load_c), tiles [T/2, T) from zero
+                             into scratch, then C = C + scratch (one FP32 add per element; the epilogue
+                             after it).  Needs a K-tiled pack (T >= 2) of FP32 or BF16 values, FP32 C
+                             and the B-tile kernel (b_staging 0 or 1); other packs run unsplit.
+                             spreg_load_balance_plan reports the split. */
     int32_t reserved;     /* 0 */
 } spreg_exec_args;
 
 /* One SpMM: C (+)= A . B over the first n columns -- sop_multiple_panel_executor (template:265-305). */
 int spreg_execute(const spreg_packed *a, const spreg_exec_args *args, spreg_stream_t stream);
 
-/* The load-balanced split spreg_execute would make for this pack (spreg_exec_args.load_balance = 1):
- * *heavy_panels panels are split at K tile *split_tile (0 and 0: no split); heavy_ids (may be NULL,
- * else room for max_ids) receives their row-panel indices.  Host-only. */
-int spreg_load_balance_plan(const spreg_packed *a, int64_t *heavy_panels, int32_t *split_tile, int32_t *heavy_ids,
-                            int64_t max_ids);
+/* The load-balanced split spreg_execute(a, args) would make (as with args->load_balance = 1), the
+ * call running alone: *heavy_panels panels are split at K tile *split_tile (0 and 0: no split);
+ * heavy_ids (may be NULL, else room for max_ids) receives their row-panel indices.  No launch. */
+int spreg_load_balance_plan(const spreg_packed *a, const spreg_exec_args *args, int64_t *heavy_panels,
+                            int32_t *split_tile, int32_t *heavy_ids, int64_t max_ids);
 
 /* Many SpMMs of uneven shape in ONE launch, from a (matrix, panel, column-strip) work list. */
 typedef struct {

@@ -38,7 +38,7 @@ void packed_release(spreg_packed *);
 int execute_impl(const spreg_packed *, const spreg_exec_args *, cudaStream_t);
 int execute_timed_impl(const spreg_packed *, const spreg_exec_args *, int64_t, double *, cudaStream_t);
 int execute_batched_impl(const spreg_work_item *, int32_t, cudaStream_t);
-int load_balance_plan_impl(const spreg_packed *, int64_t *, int32_t *, int32_t *, int64_t);
+int load_balance_plan_impl(const spreg_packed *, const spreg_exec_args *, int64_t *, int32_t *, int32_t *, int64_t);
 int device_status_impl(int32_t *, int);
 int selftest_wait_impl(uint32_t, int32_t *, uint32_t *, cudaStream_t);
 int csr_spmm_impl(int64_t, int64_t, int64_t, int64_t, const int32_t *, const int32_t *, const float *, const float *,
@@ -433,10 +433,10 @@ int spreg_execute(const spreg_packed *a, const spreg_exec_args *args, spreg_stre
     return execute_impl(a, args, (cudaStream_t)stream);
 }
 
-int spreg_load_balance_plan(const spreg_packed *a, int64_t *heavy_panels, int32_t *split_tile, int32_t *heavy_ids,
-                            int64_t max_ids) {
+int spreg_load_balance_plan(const spreg_packed *a, const spreg_exec_args *args, int64_t *heavy_panels,
+                            int32_t *split_tile, int32_t *heavy_ids, int64_t max_ids) {
     clear_error();
-    return load_balance_plan_impl(a, heavy_panels, split_tile, heavy_ids, max_ids);
+    return load_balance_plan_impl(a, args, heavy_panels, split_tile, heavy_ids, max_ids);
 }
 
 int spreg_execute_batched(const spreg_work_item *items, int32_t num_items, spreg_stream_t stream) {

@@ -296,22 +296,34 @@ struct CallPlan {
     const spreg_exec_args *args = nullptr;
 };
 
-// The load-balanced split of a pack: the panels whose work estimate exceeds half the heaviest
-// one's, when they are at most three quarters of the panels (else the work is balanced already and
-// no panel is split), split at K tile T / 2.  Splitting them halves the longest job of a launch
-// that has about one job per SM (a single SpMM); in a launch of many SpMMs the work counter
-// balances the SMs already and the split only adds the combine.
-void balance_of(const spreg_packed *a, int64_t *heavy, int32_t *split) {
+// The load-balanced split of a pack run by the B-tile kernel with W panels per job and S strips:
+// the launch has ceil(P / W) x S jobs (+ other_jobs of other SpMMs).  When that leaves SMs idle, the
+// heaviest job groups (whole groups of W panels in work order, as long as their first panel's work
+// estimate exceeds half the heaviest one's) are split at K tile T / 2, each split group adding S
+// jobs, until the idle SMs are used.  That shortens the longest jobs of a launch with about one
+// job per SM (a single SpMM); a launch with a full wave of jobs or more is balanced by the work
+// counter already and is not split.
+void balance_of(const spreg_packed *a, int W, int64_t S, int64_t slots, int64_t other_jobs, int64_t *heavy,
+                int32_t *split) {
     *heavy = 0;
     *split = 0;
     const int64_t P = a->geom.P, T = a->geom.T;
-    if (T < 2 || P < 2 || a->list_packed || (int64_t)a->work_desc.size() != P || a->work_desc[0] <= 0) return;
+    if (T < 2 || P < 2 || W < 1 || S < 1 || a->list_packed || (int64_t)a->work_desc.size() != P ||
+        a->work_desc[0] <= 0)
+        return;
+    const int64_t groups = (P + W - 1) / W;
+    const int64_t free_slots = slots - groups * S - other_jobs;
     const int64_t top = a->work_desc[0];
-    int64_t H = 0;
-    while (H < P && 2 * a->work_desc[(size_t)H] > top) ++H;
-    if (H == 0 || 4 * H > 3 * P) return;
-    *heavy = H;
+    int64_t g = 0;
+    while (g < groups && (g + 1) * S <= free_slots && 2 * a->work_desc[(size_t)(g * W)] > top) ++g;
+    if (g == 0) return;
+    *heavy = std::min<int64_t>(g * W, P);
     *split = (int32_t)(T / 2);
+}
+
+// Consumer warps (panels per job) of the B-tile kernel for a call: as asked, else 15.
+int tile_warps_of(const spreg_exec_args *args) {
+    return args->warps_per_cta > 0 ? std::min(args->warps_per_cta, kTileMaxWarps) : kTileMaxWarps;
 }
 
 int plan_call(const spreg_packed *a, const spreg_exec_args *args, CallPlan *cp, int64_t others1) {
@@ -412,10 +424,9 @@ int plan_call(const spreg_packed *a, const spreg_exec_args *args, CallPlan *cp, 
         if ((p & (p - 1)) == 0 || p == (1 << in.mr) - 1) hot += a->id_entries[i];
     }
     const bool hot_set = all > 0 && 100 * hot >= 85 * all;
-    int64_t lb_heavy = 0;
-    int32_t lb_split = 0;
-    if (args->load_balance) balance_of(a, &lb_heavy, &lb_split);
-    const bool lb = lb_heavy > 0;
+    // load balance: K-tiled packs run the B-tile kernel; the split itself is decided below, once
+    // the strip width is known
+    const bool lb = args->load_balance && a->geom.T >= 2 && !a->list_packed;
     SPREG_CHECK_ARG(!lb || (tile_base_ok && args->n <= INT32_MAX),
                     "load_balance: the B-tile kernel cannot run this call (a 16-byte aligned B with 16-byte "
                     "aligned rows is needed)");
@@ -431,6 +442,14 @@ int plan_call(const spreg_packed *a, const spreg_exec_args *args, CallPlan *cp, 
         nv = 8;
     cp->nv = nv;
     const int64_t n_main = (args->n / (32 * nv)) * (32 * nv);
+    int64_t lb_heavy = 0;
+    int32_t lb_split = 0;
+    if (lb) {
+        const int64_t strips = n_main / (32 * nv) + (args->n - n_main + 31) / 32;
+        const int W = tile_warps_of(args) * rounds;  // panels per job
+        // other SpMMs of the launch: their (panel, 32-column) items over W panels and 4 columns a job
+        balance_of(a, W, strips, f->sms, others1 / ((int64_t)W * 4), &lb_heavy, &lb_split);
+    }
 
     XProblem base = {};
     base.exec = a->exec;
@@ -815,9 +834,16 @@ int run_calls(const spreg_packed *const *as, const spreg_exec_args *const *args,
     return st;
 }
 
-int load_balance_plan_impl(const spreg_packed *a, int64_t *heavy, int32_t *split, int32_t *ids, int64_t max_ids) {
-    SPREG_CHECK_ARG(a && heavy && split, "null argument");
-    balance_of(a, heavy, split);
+int load_balance_plan_impl(const spreg_packed *a, const spreg_exec_args *args, int64_t *heavy, int32_t *split,
+                           int32_t *ids, int64_t max_ids) {
+    SPREG_CHECK_ARG(a && args && heavy && split, "null argument");
+    CallPlan cp;
+    spreg_exec_args x = *args;
+    x.load_balance = 1;
+    int st = plan_call(a, &x, &cp, 0);
+    if (st != SPREG_OK) return st;
+    *heavy = cp.lb_heavy;
+    *split = cp.lb_split;
     if (ids)
         for (int64_t i = 0; i < *heavy && i < max_ids; ++i) ids[i] = a->order_host[(size_t)i];
     return SPREG_OK;

@@ -161,12 +161,16 @@ class PackedMatrix:
                                                   _lib.stream_handle(stream)))
         return float(t.value)
 
-    def load_balance_plan(self):
-        """(heavy panels, split K tile, their row-panel indices) of the load-balanced split
-        (spreg_load_balance_plan); (0, 0, []) when the pack's work is balanced already."""
+    def load_balance_plan(self, B, C_out, n=None, nr=0, warps=0, staging=0, rounds=0):
+        """(heavy panels, split K tile, their row-panel indices) of the load-balanced split that
+        execute(B, C_out, ..., balance=1) makes when it runs alone (spreg_load_balance_plan);
+        (0, 0, []) when nothing is split."""
+        self._check_operands(B, C_out)
+        args = self.exec_args(B, C_out, n, nr=nr, warps=warps, staging=staging, rounds=rounds, balance=1)
         h, t = C.c_int64(), C.c_int32()
         ids = np.zeros(max(1, int(self.info["num_panels"])), dtype=np.int32)
-        _lib.check(_lib.lib().spreg_load_balance_plan(self._h, C.byref(h), C.byref(t), ids.ctypes.data, ids.size))
+        _lib.check(_lib.lib().spreg_load_balance_plan(self._h, C.byref(args), C.byref(h), C.byref(t),
+                                                      ids.ctypes.data, ids.size))
         return int(h.value), int(t.value), ids[: int(h.value)].copy()
 
     # ---------------------------------------------------------------- bytes / flops

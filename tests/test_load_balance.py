@@ -1,9 +1,9 @@
 """Load-balanced SpMM (spreg_exec_args.load_balance, the reference's load-balanced kernel choice in
-cpp_testbed/src/spmm/nano/runtime_yaml_config.register:84-99): the heaviest row panels' K tiles
-are split between two concurrent jobs, C = (tiles [0, split) from C or zero) + (tiles [split, T)
-from zero), one FP32 add per element, then the epilogue.  Every case is compared bit for bit with
-the oracle's restatement of that order (oracle.load_balanced_execute), and within FP32 rounding
-with the unsplit executor."""
+cpp_testbed/src/spmm/nano/runtime_yaml_config.register:84-99): when a launch leaves SMs idle, the
+heaviest groups of row panels have their K tiles split between two concurrent jobs, C = (tiles
+[0, split) from C or zero) + (tiles [split, T) from zero), one FP32 add per element, then the
+epilogue.  Every case is compared bit for bit with the oracle's restatement of that order
+(oracle.load_balanced_execute), and within FP32 rounding with the unsplit executor."""
 import numpy as np
 import pytest
 import torch
@@ -28,11 +28,11 @@ def run(A, k_tile, n=256, vd=_lib.F32, load_c=False, epilogue=0, mr=4, **kw):
     m = Mapping.identity(mr)
     B = synth.dense(A.shape[1], n, seed=7)
     pm = PackedMatrix.from_dense(torch.from_numpy(A).cuda(), m, k_tile=k_tile, value_dtype=vd)
-    H, split, heavy = pm.load_balance_plan()
     Bt = torch.from_numpy(B).cuda().to(TORCH[vd])
     Bref = B if vd == _lib.F32 else Bt.cpu().view(torch.int16).numpy().view(np.uint16)
     C0 = synth.dense(A.shape[0], n, seed=8)
     Cg = torch.from_numpy(C0.copy()).cuda()
+    H, split, heavy = pm.load_balance_plan(Bt, Cg, **kw)
     pm.execute(Bt, Cg, load_c=load_c, epilogue=epilogue, balance=1, **kw)
     want = O.load_balanced_execute(O.Tables.of(m), A, Bref, heavy, split, k_tile, value_dtype=vd,
                                    out=C0.copy() if load_c else None, load_c=load_c, epilogue=epilogue)
@@ -75,10 +75,19 @@ def test_split_with_panel_rounds_and_strip_widths(cuda):
         assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), (nr, rounds)
 
 
-def test_balanced_matrix_is_not_split(cuda):
-    """Uniform nonzeros: no heavy tail, so nothing is split and the result is the executor's own chain."""
+def test_uniform_matrix_alone_is_split(cuda):
+    """Uniform nonzeros, a single SpMM with idle SMs: its groups are split too (halving each job)."""
     A = synth.bernoulli(1024, 512, 0.9, seed=1, std=1.0)
     got, want, plain, (H, split, _) = run(A, 128)
+    assert H > 0 and split == 2
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
+def test_full_launch_is_not_split(cuda):
+    """A launch with at least one job per SM is balanced by the work counter: nothing is split and
+    the result is the executor's own chain."""
+    A = skewed(8192, 512, seed=6)
+    got, want, plain, (H, split, _) = run(A, 128, n=512)
     assert (H, split) == (0, 0)
     assert np.array_equal(got.view(np.uint32), plain.view(np.uint32))
 
@@ -99,15 +108,23 @@ def test_split_in_a_batched_launch_and_a_cuda_graph(cuda):
     work = [(p, B, C, dict(balance=i % 2 ^ 1)) for i, (p, B, C) in enumerate(zip(packs, Bs, Cs))]
     execute_batched(work)
     torch.cuda.synchronize()
+    # in a launch with other SpMMs fewer SMs are idle, so a balanced SpMM splits at most the groups it
+    # splits alone: its result is the stated order for one of those group counts
     wants = []
-    for i, (A, p, B) in enumerate(zip(As, packs, Bs)):
-        H, split, heavy = p.load_balance_plan()
+    for i, (A, p, B, C) in enumerate(zip(As, packs, Bs, Cs)):
+        got = C.cpu().numpy()
         if i % 2 == 0:
-            wants.append(O.load_balanced_execute(O.Tables.of(m), A, B.cpu().numpy(), heavy, split, 128))
+            H, split, heavy = p.load_balance_plan(B, C)
+            assert H > 0
+            counts = sorted({min(15 * g, H) for g in range(0, H // 15 + 2)}, reverse=True)  # whole groups of 15
+            cands = [O.load_balanced_execute(O.Tables.of(m), A, B.cpu().numpy(), heavy[:h], split, 128)
+                     for h in counts]
+            match = [w for w in cands if np.array_equal(got.view(np.uint32), w.view(np.uint32))]
+            assert match, i
+            wants.append(match[0])
         else:
             wants.append(O.Packed(O.Tables.of(m), A, k_tile=128).execute(B.cpu().numpy()))
-    for C, want in zip(Cs, wants):
-        assert np.array_equal(C.cpu().numpy().view(np.uint32), want.view(np.uint32))
+            assert np.array_equal(got.view(np.uint32), wants[-1].view(np.uint32))
     # the same launch captured in a CUDA graph (the scratch is stream-ordered) and replayed
     s = torch.cuda.Stream()
     s.wait_stream(torch.cuda.current_stream())
@@ -137,7 +154,7 @@ def test_matmul_specialized_load_balanced(cuda):
     C = torch.zeros((800, 128))
     mm(C, torch.from_numpy(B))
     pm = PackedMatrix.from_dense(torch.from_numpy(A).cuda(), m, k_tile=128)
-    H, split, heavy = pm.load_balance_plan()
+    H, split, heavy = pm.load_balance_plan(torch.from_numpy(B).cuda(), torch.empty((800, 128), device="cuda"))
     assert H > 0
     want = O.load_balanced_execute(O.Tables.of(m), A, B, heavy, split, 128)
     assert np.array_equal(C.numpy().view(np.uint32), want.view(np.uint32))
