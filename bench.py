@@ -339,12 +339,35 @@ def precision_suite(dev) -> list:
     """1x1-conv-shaped SpMMs (B = K x 3136: batch 1, 56 x 56 spatial) at sparsity 0.8-0.95 with
     log-normal row skew: rel err against FP64 of FP32, BF16 and FP16 (per-panel scaled) storage,
     FP32 accumulation, and the kernel time of each layer in each storage through the product's best
-    path: the autotuner's packing (M_r, nanokernel set, K tile, N_r) for that storage, one SpMM per
-    launch timed with the reference's protocol (median of 150 x num_runs runs)."""
+    path:
+    * register-tiled: the autotuner's packing (M_r, nanokernel set, K tile, N_r, CTA tiling, panel
+      rounds) for that storage, one SpMM per launch timed with the reference's protocol (median of
+      150 x num_runs runs);
+    * tensor cores (every panel, `spreg.hybrid`): BF16 storage as BF16 products, FP32 storage as the
+      FP32-accurate split products; one SpMM per plan run (no host work), CUDA events over 50 runs.
+    `best_*` takes the faster path of each storage; `bf16_speedup_vs_fp32` compares the best paths,
+    `bf16_speedup_vs_fp32_register_tiled` the register-tiled ones."""
     import torch
     from oracle import oracle as O
     from spreg import BF16, F16, F32, PackedMatrix, synth
     from spreg.autotune import mapping_of, tune
+    from spreg.hybrid import HybridBatch, HybridMatrix
+
+    def tc_time(At, m, vd, Bt, M):
+        h = HybridMatrix.from_dense(At, m, 0.0, value_dtype=vd)
+        Ch = torch.empty((M, Bt.shape[1]), device=dev)
+        hb = HybridBatch([(h, Bt, Ch)])
+        for _ in range(3):
+            hb.run()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(50):
+            hb.run()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) * 1e3 / 50, Ch.cpu().numpy()
+
     rows = []
     for i, (M, K) in enumerate(((64, 256), (128, 512), (256, 1024), (512, 2048), (2048, 512))):
         sp = (0.8, 0.85, 0.9, 0.95, 0.9)[i]
@@ -369,12 +392,21 @@ def precision_suite(dev) -> list:
             row[f"{name}_gflops"] = 2 * int(pm.info["nnz"]) * 3136 / t
             row[f"{name}_gbs"] = pm.algorithmic_bytes(3136, b_bytes=4 if vd == F32 else 2) / t
             row[f"{name}_config"] = c.name()
+            if name != "fp16":
+                # every panel on the tensor cores: BF16 products, or the FP32-accurate split
+                t_tc, Ct = tc_time(At, mapping_of(c.mr, c.mapping), vd, Bt, M)
+                row[f"{name}_tc_us"] = t_tc
+                row[f"{name}_tc_gbs"] = pm.algorithmic_bytes(3136, b_bytes=4 if vd == F32 else 2) / (t_tc * 1e3)
+                row[f"rel_err_{name}_tc"] = float(O.rel_err(Ct, ref))
+                row[f"best_{name}_us"] = min(row[f"{name}_us"], t_tc)
+                row[f"best_{name}_path"] = "tensor cores" if t_tc < row[f"{name}_us"] else "register-tiled"
             if name != "fp32":
                 # the same storage with its own inputs rounded: the error the kernel adds
                 Bq = Bt.float().cpu().numpy()
                 row[f"rel_err_{name}_vs_rounded_inputs"] = float(O.rel_err(
                     C.cpu().numpy(), O.dense_fp64(_rounded(A, vd, pm), Bq)))
-        row["bf16_speedup_vs_fp32"] = row["fp32_us"] / row["bf16_us"]
+        row["bf16_speedup_vs_fp32_register_tiled"] = row["fp32_us"] / row["bf16_us"]
+        row["bf16_speedup_vs_fp32"] = row["best_fp32_us"] / row["best_bf16_us"]
         rows.append(row)
     return rows
 

@@ -105,16 +105,17 @@ def test_split_in_a_batched_launch_and_a_cuda_graph(cuda):
     packs = [PackedMatrix.from_dense(torch.from_numpy(A).cuda(), m, k_tile=128) for A in As]
     Bs = [torch.from_numpy(synth.dense(512, 256, seed=30 + i)).cuda() for i in range(3)]
     Cs = [torch.empty((A.shape[0], 256), device="cuda") for A in As]
-    work = [(p, B, C, dict(balance=i % 2 ^ 1)) for i, (p, B, C) in enumerate(zip(packs, Bs, Cs))]
+    # a fixed strip width: alone and in the launch the SpMM has the same strips
+    work = [(p, B, C, dict(balance=i % 2 ^ 1, nr=128)) for i, (p, B, C) in enumerate(zip(packs, Bs, Cs))]
     execute_batched(work)
     torch.cuda.synchronize()
     # in a launch with other SpMMs fewer SMs are idle, so a balanced SpMM splits at most the groups it
-    # splits alone: its result is the stated order for one of those group counts
+    # splits alone (same strips): its result is the stated order for one of those group counts
     wants = []
     for i, (A, p, B, C) in enumerate(zip(As, packs, Bs, Cs)):
         got = C.cpu().numpy()
         if i % 2 == 0:
-            H, split, heavy = p.load_balance_plan(B, C)
+            H, split, heavy = p.load_balance_plan(B, C, nr=128)
             assert H > 0
             counts = sorted({min(15 * g, H) for g in range(0, H // 15 + 2)}, reverse=True)  # whole groups of 15
             cands = [O.load_balanced_execute(O.Tables.of(m), A, B.cpu().numpy(), heavy[:h], split, 128)
