@@ -71,6 +71,9 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end leg")
     ap.add_argument("--serving", type=int, default=1, help="1: add the serving-loop measurement to the line")
     ap.add_argument("--precision", type=int, default=1, help="1: add the storage-precision sweep to the line")
+    ap.add_argument("--precision-only", default="",
+                    help="run only this layer of the precision sweep, SHAPE:STORAGE (e.g. 2048x512:bf16); each "
+                         "path's first launch is an NVTX range precision_<shape>_<storage>[_tc] for ncu --nvtx")
     ap.add_argument("--tensor-cores", type=int, default=1, help="1: add the tensor-core (tcgen05) leg to the line")
     ap.add_argument("--layers", type=int, default=1,
                     help="1: add the batched uneven transformer-layer measurement to the line")
@@ -335,7 +338,7 @@ def serving_bench(args, dev) -> dict:
             "capacity_note": "capacity = all requests queued at t=0; latency = arrival to output in host memory"}
 
 
-def precision_suite(dev) -> list:
+def precision_suite(dev, only: str = "") -> list:
     """1x1-conv-shaped SpMMs (B = K x 3136: batch 1, 56 x 56 spatial) at sparsity 0.8-0.95 with
     log-normal row skew: rel err against FP64 of FP32, BF16 and FP16 (per-panel scaled) storage,
     FP32 accumulation, and the kernel time of each layer in each storage through the product's best
@@ -353,10 +356,15 @@ def precision_suite(dev) -> list:
     from spreg.autotune import mapping_of, tune
     from spreg.hybrid import HybridBatch, HybridMatrix
 
-    def tc_time(At, m, vd, Bt, M):
+    def tc_time(At, m, vd, Bt, M, tag):
         h = HybridMatrix.from_dense(At, m, 0.0, value_dtype=vd)
         Ch = torch.empty((M, Bt.shape[1]), device=dev)
         hb = HybridBatch([(h, Bt, Ch)])
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_push(tag + "_tc")
+        hb.run()
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
         for _ in range(3):
             hb.run()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -369,8 +377,11 @@ def precision_suite(dev) -> list:
         return e0.elapsed_time(e1) * 1e3 / 50, Ch.cpu().numpy()
 
     rows = []
+    only_shape, _, only_store = only.partition(":")
     for i, (M, K) in enumerate(((64, 256), (128, 512), (256, 1024), (512, 2048), (2048, 512))):
         sp = (0.8, 0.85, 0.9, 0.95, 0.9)[i]
+        if only_shape and only_shape != f"{M}x{K}":
+            continue
         A = synth.row_skew(M, K, sp, seed=300 + i, sigma=0.5, std=0.02)
         B = synth.dense(K, 3136, seed=400 + i)
         ref = O.dense_fp64(A, B)
@@ -378,13 +389,20 @@ def precision_suite(dev) -> list:
         row = {"shape": [M, K], "sparsity": sp, "n": 3136}
         tuned = {}
         for name, vd, tdt in (("fp32", F32, torch.float32), ("bf16", BF16, torch.bfloat16), ("fp16", F16, torch.float16)):
+            if only_store and only_store != name:
+                continue
+            tag = f"precision_{M}x{K}_{name}"
             tkey = "f32" if vd == F32 else "bf16"  # FP16 runs the 16-bit executor paths that BF16 tunes
             if tkey not in tuned:
                 tuned[tkey] = tune(A, 3136, tkey, top=4, device=dev, tc=False).best
             c = tuned[tkey]
             pm = PackedMatrix.from_dense(At, mapping_of(c.mr, c.mapping), k_tile=c.k_tile, value_dtype=vd)
             Bt = torch.from_numpy(B).to(dev).to(tdt)
+            torch.cuda.synchronize()
+            torch.cuda.nvtx.range_push(tag)
             C = pm.execute(Bt, nr=c.nr, warps=c.warps, rounds=c.rounds)
+            torch.cuda.synchronize()
+            torch.cuda.nvtx.range_pop()
             row[f"rel_err_{name}"] = float(O.rel_err(C.cpu().numpy(), ref))
             Cf = torch.empty((M, 3136), device=dev)
             t = pm.execute_timed(Bt, Cf, num_runs=2, nr=c.nr, warps=c.warps, rounds=c.rounds)
@@ -394,7 +412,7 @@ def precision_suite(dev) -> list:
             row[f"{name}_config"] = c.name()
             if name != "fp16":
                 # every panel on the tensor cores: BF16 products, or the FP32-accurate split
-                t_tc, Ct = tc_time(At, mapping_of(c.mr, c.mapping), vd, Bt, M)
+                t_tc, Ct = tc_time(At, mapping_of(c.mr, c.mapping), vd, Bt, M, tag)
                 row[f"{name}_tc_us"] = t_tc
                 row[f"{name}_tc_gbs"] = pm.algorithmic_bytes(3136, b_bytes=4 if vd == F32 else 2) / (t_tc * 1e3)
                 row[f"rel_err_{name}_tc"] = float(O.rel_err(Ct, ref))
@@ -405,8 +423,9 @@ def precision_suite(dev) -> list:
                 Bq = Bt.float().cpu().numpy()
                 row[f"rel_err_{name}_vs_rounded_inputs"] = float(O.rel_err(
                     C.cpu().numpy(), O.dense_fp64(_rounded(A, vd, pm), Bq)))
-        row["bf16_speedup_vs_fp32_register_tiled"] = row["fp32_us"] / row["bf16_us"]
-        row["bf16_speedup_vs_fp32"] = row["best_fp32_us"] / row["best_bf16_us"]
+        if "fp32_us" in row and "bf16_us" in row:
+            row["bf16_speedup_vs_fp32_register_tiled"] = row["fp32_us"] / row["bf16_us"]
+            row["bf16_speedup_vs_fp32"] = row["best_fp32_us"] / row["best_bf16_us"]
         rows.append(row)
     return rows
 
@@ -1202,7 +1221,7 @@ def main():
     cfg1 = config1_leg(dev) if (lead and args.extras) else None
     lbal = load_balance_leg(dev) if (lead and args.extras) else None
     serving = serving_bench(args, dev) if (lead and args.serving) else None
-    precision = precision_suite(dev) if (lead and args.precision) else None
+    precision = precision_suite(dev, args.precision_only) if (lead and args.precision) else None
     tensor_cores = tensor_core_suite(dev) if (lead and args.tensor_cores) else None
     layers = layers_suite(dev) if (lead and args.layers) else None
     sweep = ffn_sweep(dev) if (lead and args.ffn_sweep) else None
