@@ -410,6 +410,7 @@ def precision_suite(dev, only: str = "") -> list:
             row[f"{name}_gflops"] = 2 * int(pm.info["nnz"]) * 3136 / t
             row[f"{name}_gbs"] = pm.algorithmic_bytes(3136, b_bytes=4 if vd == F32 else 2) / t
             row[f"{name}_config"] = c.name()
+            row[f"{name}_plan"] = pm.explain(Bt, Cf, nr=c.nr, warps=c.warps, rounds=c.rounds)
             if name != "fp16":
                 # every panel on the tensor cores: BF16 products, or the FP32-accurate split
                 t_tc, Ct = tc_time(At, mapping_of(c.mr, c.mapping), vd, Bt, M, tag)

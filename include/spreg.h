@@ -243,6 +243,11 @@ typedef struct {
 /* One SpMM: C (+)= A . B over the first n columns -- sop_multiple_panel_executor (template:265-305). */
 int spreg_execute(const spreg_packed *a, const spreg_exec_args *args, spreg_stream_t stream);
 
+/* The plan spreg_execute(a, args) would make, as one line of text into buf (len bytes): the kernel,
+ * M_r, strip width, main / tail columns, K tiles, warps, panel rounds and load-balanced split.
+ * Checks the arguments as spreg_execute does; no launch. */
+int spreg_execute_explain(const spreg_packed *a, const spreg_exec_args *args, char *buf, int64_t len);
+
 /* The load-balanced split spreg_execute(a, args) would make (as with args->load_balance = 1), the
  * call running alone: *heavy_panels panels are split at K tile *split_tile (0 and 0: no split);
  * heavy_ids (may be NULL, else room for max_ids) receives their row-panel indices.  No launch. */

@@ -39,6 +39,7 @@ int execute_impl(const spreg_packed *, const spreg_exec_args *, cudaStream_t);
 int execute_timed_impl(const spreg_packed *, const spreg_exec_args *, int64_t, double *, cudaStream_t);
 int execute_batched_impl(const spreg_work_item *, int32_t, cudaStream_t);
 int load_balance_plan_impl(const spreg_packed *, const spreg_exec_args *, int64_t *, int32_t *, int32_t *, int64_t);
+int explain_impl(const spreg_packed *, const spreg_exec_args *, char *, int64_t);
 int device_status_impl(int32_t *, int);
 int selftest_wait_impl(uint32_t, int32_t *, uint32_t *, cudaStream_t);
 int csr_spmm_impl(int64_t, int64_t, int64_t, int64_t, const int32_t *, const int32_t *, const float *, const float *,
@@ -431,6 +432,11 @@ void spreg_tile_destroy(spreg_tile *t) {
 int spreg_execute(const spreg_packed *a, const spreg_exec_args *args, spreg_stream_t stream) {
     clear_error();
     return execute_impl(a, args, (cudaStream_t)stream);
+}
+
+int spreg_execute_explain(const spreg_packed *a, const spreg_exec_args *args, char *buf, int64_t len) {
+    clear_error();
+    return explain_impl(a, args, buf, len);
 }
 
 int spreg_load_balance_plan(const spreg_packed *a, const spreg_exec_args *args, int64_t *heavy_panels,

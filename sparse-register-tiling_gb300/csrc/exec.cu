@@ -834,6 +834,22 @@ int run_calls(const spreg_packed *const *as, const spreg_exec_args *const *args,
     return st;
 }
 
+int explain_impl(const spreg_packed *a, const spreg_exec_args *args, char *buf, int64_t len) {
+    SPREG_CHECK_ARG(a && args && buf && len > 0, "null argument");
+    CallPlan cp;
+    int st = plan_call(a, args, &cp, 0);
+    if (st != SPREG_OK) return st;
+    const char *kernel = cp.tile ? "exec_tile_kernel" : cp.stream_kernel ? "exec_kernel" : "exec_batch_kernel";
+    const int64_t n_main = cp.has_main ? (cp.tile ? (int64_t)cp.tmain.col_end : (int64_t)cp.main.col_end) : 0;
+    snprintf(buf, (size_t)len,
+             "kernel=%s mr=%d nv=%d strip_columns=%d main_columns=%lld tail_columns=%lld k_tiles=%lld k_tile=%lld "
+             "warps=%d rounds=%d load_balance_heavy=%lld load_balance_split=%d",
+             kernel, cp.mr, cp.nv, 32 * cp.nv, (long long)n_main, (long long)(cp.has_tail ? args->n - n_main : 0),
+             (long long)a->geom.T, (long long)a->geom.kt, cp.tile ? tile_warps_of(args) : cp.warps, cp.rounds,
+             (long long)cp.lb_heavy, cp.lb_split);
+    return SPREG_OK;
+}
+
 int load_balance_plan_impl(const spreg_packed *a, const spreg_exec_args *args, int64_t *heavy, int32_t *split,
                            int32_t *ids, int64_t max_ids) {
     SPREG_CHECK_ARG(a && args && heavy && split, "null argument");

@@ -135,6 +135,7 @@ PROTOTYPES = {
     "spreg_device_status": (C.c_int, [C.POINTER(C.c_int32), C.c_int32]),
     "spreg_execute_batched_noalloc": (C.c_int, [P, C.c_int32, P]),
     "spreg_execute_timed": (C.c_int, [P, C.POINTER(ExecArgs), C.c_int64, C.POINTER(C.c_double), P]),
+    "spreg_execute_explain": (C.c_int, [P, C.POINTER(ExecArgs), C.c_char_p, C.c_int64]),
     "spreg_load_balance_plan": (C.c_int, [P, C.POINTER(ExecArgs), C.POINTER(C.c_int64), C.POINTER(C.c_int32), P,
                                           C.c_int64]),
     "spreg_selftest_wait_timeout": (C.c_int, [C.c_uint32, C.POINTER(C.c_int32), C.POINTER(C.c_uint32), P]),

@@ -161,6 +161,19 @@ class PackedMatrix:
                                                   _lib.stream_handle(stream)))
         return float(t.value)
 
+    def explain(self, B, C_out, n=None, load_c=False, epilogue=_lib.EPILOGUE_NONE, nr=0, warps=0, staging=0, meta=0,
+                order=0, rounds=0, balance=0) -> dict:
+        """The plan execute() would make with these arguments (spreg_execute_explain), as a dict."""
+        self._check_operands(B, C_out)
+        args = self.exec_args(B, C_out, n, load_c, epilogue, nr, warps, staging, meta, order, rounds, balance)
+        buf = C.create_string_buffer(512)
+        _lib.check(_lib.lib().spreg_execute_explain(self._h, C.byref(args), buf, len(buf)))
+        out = {}
+        for kv in buf.value.decode().split():
+            k, _, v = kv.partition("=")
+            out[k] = int(v) if v.lstrip("-").isdigit() else v
+        return out
+
     def load_balance_plan(self, B, C_out, n=None, nr=0, warps=0, staging=0, rounds=0):
         """(heavy panels, split K tile, their row-panel indices) of the load-balanced split that
         execute(B, C_out, ..., balance=1) makes when it runs alone (spreg_load_balance_plan);
