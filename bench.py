@@ -74,6 +74,9 @@ def parse():
     ap.add_argument("--precision-only", default="",
                     help="run only this layer of the precision sweep, SHAPE:STORAGE (e.g. 2048x512:bf16); each "
                          "path's first launch is an NVTX range precision_<shape>_<storage>[_tc] for ncu --nvtx")
+    ap.add_argument("--precision-configs", default="",
+                    help="fixed packings of the precision sweep instead of tuning, f32=NAME,bf16=NAME (autotuner "
+                         "candidate names, e.g. f32=M4N128_75a1b_K128): a profiled run makes the plain run's plan")
     ap.add_argument("--tensor-cores", type=int, default=1, help="1: add the tensor-core (tcgen05) leg to the line")
     ap.add_argument("--layers", type=int, default=1,
                     help="1: add the batched uneven transformer-layer measurement to the line")
@@ -338,7 +341,7 @@ def serving_bench(args, dev) -> dict:
             "capacity_note": "capacity = all requests queued at t=0; latency = arrival to output in host memory"}
 
 
-def precision_suite(dev, only: str = "") -> list:
+def precision_suite(dev, only: str = "", configs: str = "") -> list:
     """1x1-conv-shaped SpMMs (B = K x 3136: batch 1, 56 x 56 spatial) at sparsity 0.8-0.95 with
     log-normal row skew: rel err against FP64 of FP32, BF16 and FP16 (per-panel scaled) storage,
     FP32 accumulation, and the kernel time of each layer in each storage through the product's best
@@ -353,8 +356,9 @@ def precision_suite(dev, only: str = "") -> list:
     import torch
     from oracle import oracle as O
     from spreg import BF16, F16, F32, PackedMatrix, synth
-    from spreg.autotune import mapping_of, tune
+    from spreg.autotune import candidate_from_name, mapping_of, tune
     from spreg.hybrid import HybridBatch, HybridMatrix
+    fixed = dict(kv.split("=", 1) for kv in configs.split(",") if kv)
 
     def tc_time(At, m, vd, Bt, M, tag):
         h = HybridMatrix.from_dense(At, m, 0.0, value_dtype=vd)
@@ -394,7 +398,8 @@ def precision_suite(dev, only: str = "") -> list:
             tag = f"precision_{M}x{K}_{name}"
             tkey = "f32" if vd == F32 else "bf16"  # FP16 runs the 16-bit executor paths that BF16 tunes
             if tkey not in tuned:
-                tuned[tkey] = tune(A, 3136, tkey, top=4, device=dev, tc=False).best
+                tuned[tkey] = (candidate_from_name(fixed[tkey], A) if tkey in fixed else
+                               tune(A, 3136, tkey, top=4, device=dev, tc=False).best)
             c = tuned[tkey]
             pm = PackedMatrix.from_dense(At, mapping_of(c.mr, c.mapping), k_tile=c.k_tile, value_dtype=vd)
             Bt = torch.from_numpy(B).to(dev).to(tdt)
@@ -1222,7 +1227,8 @@ def main():
     cfg1 = config1_leg(dev) if (lead and args.extras) else None
     lbal = load_balance_leg(dev) if (lead and args.extras) else None
     serving = serving_bench(args, dev) if (lead and args.serving) else None
-    precision = precision_suite(dev, args.precision_only) if (lead and args.precision) else None
+    precision = (precision_suite(dev, args.precision_only, args.precision_configs)
+                 if (lead and args.precision) else None)
     tensor_cores = tensor_core_suite(dev) if (lead and args.tensor_cores) else None
     layers = layers_suite(dev) if (lead and args.layers) else None
     sweep = ffn_sweep(dev) if (lead and args.ffn_sweep) else None

@@ -95,6 +95,32 @@ def greedy_mapping(mask: np.ndarray, mr: int, budget: int = 19, k_c: int = 128, 
     return m
 
 
+def candidate_from_name(name: str, A: Optional[np.ndarray] = None) -> Candidate:
+    """The candidate a `Candidate.name()` string describes (M{mr}N{nr}_{mapping}[_K..][_W..][_R..]
+    [_TC..]).  A mapping id built from a matrix's histogram is rebuilt from `A` (the greedy sets `rank`
+    adds for M_r = 8 and for K-tiled M_r = 4), so that `mapping_of` finds it."""
+    import re
+    m = re.fullmatch(r"M(\d+)N(\d+)_([0-9a-z]+)((?:_[KWR]\d+|_TC[0-9.eE+-]+)*)", name)
+    if not m:
+        raise ValueError(f"not a candidate name: {name}")
+    mr, nr, mapping, rest = int(m.group(1)), int(m.group(2)), m.group(3), m.group(4)
+    kw = {}
+    for tag, val in re.findall(r"_(K|W|R|TC)([0-9.eE+-]+)", rest):
+        if tag == "K":
+            kw["k_tile"] = int(val)
+        elif tag == "W":
+            kw["warps"] = int(val)
+        elif tag == "R":
+            kw["rounds"] = int(val)
+        else:
+            kw["tc_fill"] = float(val)
+    if mapping != "identity" and mapping not in GENERATED and A is not None:
+        mask = A != 0
+        for gm in (greedy_mapping(mask, 8), greedy_mapping(mask, 4, budget=15, tile=True)):
+            GENERATED.setdefault(gm.mapping_id, gm)
+    return Candidate(mr, mapping, nr, **kw)
+
+
 # ---------------------------------------------------------------------------- statistics
 def panel_codes(mask: np.ndarray, mr: int) -> np.ndarray:
     """Pattern code of every (row panel, column): bit r set if row r of the panel is nonzero.

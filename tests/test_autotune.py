@@ -163,3 +163,17 @@ def test_full_tune_best_is_measured_and_within_tolerance(cuda, dtype, n):
     Bq = Bt.float().cpu().numpy()
     Aq = A if dtype == "f32" else torch.from_numpy(A).to(torch.bfloat16).float().numpy()
     assert O.rel_err(got, O.dense_fp64(Aq, Bq)) <= (1e-5 if dtype == "f32" else 1e-2)
+
+
+def test_candidate_names_round_trip():
+    """candidate_from_name inverts Candidate.name(), greedy mapping ids included (rebuilt from A)."""
+    from spreg.autotune import GENERATED, candidate_from_name, greedy_mapping, mapping_of
+    A = synth.row_skew(512, 256, 0.9, seed=5, std=1.0)
+    gid = greedy_mapping(A != 0, 4, budget=15, tile=True).mapping_id
+    GENERATED.pop(gid, None)
+    for name in ("M4N128_identity_K128", f"M4N256_{gid}_K128", "M8N64_400fa_W4_R16", "M2N32_identity_K256_TC0.1"):
+        c = candidate_from_name(name, A)
+        assert c.name() == name
+        mapping_of(c.mr, c.mapping)  # registered, or a named mapping file
+    with pytest.raises(ValueError):
+        candidate_from_name("N128M4")
