@@ -445,7 +445,8 @@ int plan_call(const spreg_packed *a, const spreg_exec_args *args, CallPlan *cp, 
     int64_t lb_heavy = 0;
     int32_t lb_split = 0;
     if (lb) {
-        const int64_t strips = n_main / (32 * nv) + (args->n - n_main + 31) / 32;
+        const int64_t strips = args->n % nv == 0 ? (args->n + 32 * nv - 1) / (32 * nv)
+                                                 : n_main / (32 * nv) + (args->n - n_main + 31) / 32;
         const int W = tile_warps_of(args) * rounds;  // panels per job
         // other SpMMs of the launch: their (panel, 32-column) items over W panels and 4 columns a job
         balance_of(a, W, strips, f->sms, others1 / ((int64_t)W * 4), &lb_heavy, &lb_split);
@@ -523,11 +524,21 @@ int plan_call(const spreg_packed *a, const spreg_exec_args *args, CallPlan *cp, 
         cp->a = a;
         cp->args = args;
         const int64_t brows = in.col_offset + a->geom.K;
+        // Columns past the last whole strip: when n is a multiple of NV they run as one more strip of
+        // the main problem, masked per lane (B tiles past column n are zero-filled by the tensor copy;
+        // lanes whose columns start at or past n store nothing), inside the same launch.  Else (the
+        // lanes' NV-column stores would cross n) as 32-column strips of their own launch.
+        const bool merge_tail = cp->has_tail && args->n % nv == 0;
+        const int64_t n_tile_main = merge_tail ? args->n : n_main;
+        if (merge_tail) {
+            cp->has_main = true;
+            cp->has_tail = false;
+        }
         cp->tmain = tb;
         cp->tmain.col_begin = 0;
-        cp->tmain.col_end = (int32_t)n_main;
-        cp->tmain.S = cp->main.S;
-        if (cp->has_main && (st = encode_b_map(&cp->tmain.tmap, args->b, args->b_dtype, n_main, brows, args->ldb,
+        cp->tmain.col_end = (int32_t)n_tile_main;
+        cp->tmain.S = (int32_t)((n_tile_main + 32 * nv - 1) / (32 * nv));
+        if (cp->has_main && (st = encode_b_map(&cp->tmain.tmap, args->b, args->b_dtype, n_tile_main, brows, args->ldb,
                                                32 * nv, box_rows)))
             return st;
         cp->ttail = tb;

@@ -22,7 +22,8 @@ def test_strip_width_and_tail_follow_nr(cuda):
     C = torch.empty((2048, 3136), device="cuda")
     e = pm.explain(B, C, nr=128)
     assert e["kernel"] == "exec_tile_kernel" and e["k_tiles"] == 4 and e["k_tile"] == 128
-    assert (e["nv"], e["main_columns"], e["tail_columns"]) == (4, 3072, 64), e
+    # the 64 columns past the last whole 128-column strip are one more (masked) strip of the same launch
+    assert (e["nv"], e["main_columns"], e["tail_columns"]) == (4, 3136, 0), e
     e = pm.explain(B, C, nr=64)
     assert (e["nv"], e["main_columns"], e["tail_columns"]) == (2, 3136, 0), e
 
@@ -50,3 +51,17 @@ def test_explain_refuses_what_execute_refuses(cuda):
     C = torch.empty((256, 64), device="cuda")
     with pytest.raises(_lib.SpregError, match="nr must be"):
         pm.explain(B, C, nr=48)
+
+
+def test_tail_needs_whole_lane_columns(cuda):
+    """n not a multiple of the lane's columns: the tail keeps 32-column strips of their own."""
+    pm = packed(512, 256, 64)
+    B = torch.randn((256, 200), device="cuda")  # 200 = 1 x 128 + 72; 200 % 4 == 0: merged
+    C = torch.empty((512, 200), device="cuda")
+    assert (pm.explain(B, C, nr=128)["main_columns"], pm.explain(B, C, nr=128)["tail_columns"]) == (200, 0)
+    Bo = torch.randn((256, 203), device="cuda")[:, :202]  # 202: 2 leftover columns in a lane, rows 16-byte aligned
+    Bp = torch.zeros((256, 204), device="cuda")
+    Bp[:, :202] = Bo
+    Cp = torch.empty((512, 204), device="cuda")
+    e = pm.explain(Bp, Cp, n=202, nr=128, staging=1)
+    assert (e["main_columns"], e["tail_columns"]) == (128, 74), e
