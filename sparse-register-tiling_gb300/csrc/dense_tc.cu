@@ -17,7 +17,7 @@
 //
 // One launch runs up to TC_MAX_PROBLEMS products ("problems"; their tensor maps sit in a device
 // table).  Its output tiles (128 rows x BN columns; BN 256 when every product of the launch has
-// more than 128 columns, else 128) are shared out over persistent CTAs of 6 warps, at most one per
+// more than 128 columns, else 128) are shared out over persistent CTAs of 10 warps, at most one per
 // SM, each finding a tile's problem by a binary search over the problems' first tiles:
 //   * warp 0 (one lane) loads 64-deep K blocks of A_rows (128 x 64, K-major) and of B into a ring of
 //     stages with 2-D tensor copies (TMA, 128-byte swizzle; "full" mbarriers with expected bytes).
@@ -27,10 +27,10 @@
 //   * warp 1 (one lane) issues tcgen05.mma.kind::f16 (M 128, N BN, K 16; four per K block, twelve for
 //     a split product) into one of two TMEM accumulators, tcgen05.commit releasing the stage
 //     ("empty") and, per tile, the accumulator ("acc full");
-//   * warps 2-5 each read one 32-lane quarter of the accumulator with tcgen05.ld (the tile's rows),
-//     apply the scales, load_c and ReLU, store through the row index (and the segment table of
-//     coalesced products) and release the accumulator ("acc empty"), so the next tile's MMAs overlap
-//     these stores.
+//   * warps 2-9 each read one 32-lane quarter of the accumulator (the tile's rows) and half of its
+//     columns with tcgen05.ld, apply the scales, load_c and ReLU, store through the row index (and
+//     the segment table of coalesced products) and release the accumulator ("acc empty"), so the
+//     next tile's MMAs overlap these stores.
 // Columns past n are zero-filled by the tensor copies and never stored; K past the end of A reads
 // as zero; rows past R are never stored.  Every wait is bounded: a wait that gives up records a
 // code in the device status word; TMEM is released on every path.
@@ -56,10 +56,11 @@ int *device_status_word(int *st);  // exec.cu
 namespace {
 
 constexpr int TC_BM = 128, TC_BK = 64;
-// K block of a split product: 32 deep (64-byte rows, 64-byte swizzle), so that its four operand
-// tiles make stages of 48 KB and four of them are in flight (96 KB stages of 64-deep blocks allowed
-// two).
-constexpr int TC_BK_SPLIT = 32;
+// K block of a split product: 64 deep (128-byte rows, 128-byte swizzle) as for BF16, its four operand
+// tiles (A hi, A lo, B hi, B lo) making stages of 96 KB (two in flight) for 256-wide tiles and 64 KB
+// (three) for 128-wide ones.  Measured against 32-deep blocks with the 64-byte swizzle and four
+// stages of 48 KB: 11-25 % faster (half the tensor copies per byte, 128-byte rows).
+constexpr int TC_BK_SPLIT = 64;
 template <bool SPLIT> constexpr int tc_bk() { return SPLIT ? TC_BK_SPLIT : TC_BK; }
 // Output tile width BN (128 or 256): the MMA's N, the TMEM accumulator's columns, B tile rows.
 // A split product stages both halves of A and of B.
@@ -69,7 +70,7 @@ template <int BN, bool SPLIT> constexpr uint32_t tc_stage() {
     return (SPLIT ? 2u : 1u) * (tc_tile_a<BN, SPLIT>() + tc_tile_b<BN, SPLIT>());
 }
 // Stages of the ring: about 190 KB of operands.
-template <int BN, bool SPLIT> constexpr int tc_stages() { return !SPLIT ? 4 : BN == 256 ? 4 : 6; }
+template <int BN, bool SPLIT> constexpr int tc_stages() { return !SPLIT ? 4 : BN == 256 ? 2 : 3; }
 // Epilogue warps: two per TMEM lane quarter, each storing half of the tile's columns.
 constexpr int TC_EPI_WARPS = 8;
 constexpr int TC_THREADS = 32 * (2 + TC_EPI_WARPS);
@@ -179,28 +180,6 @@ __device__ __forceinline__ uint64_t tc_desc_mn(uint32_t saddr) {
     d |= (uint64_t)(1024 >> 4) << 32;          // stride-dimension byte offset: next 8-row K group
     d |= (uint64_t)1 << 46;                    // descriptor version of tcgen05
     d |= (uint64_t)2 << 61;                    // layout: 128-byte swizzle
-    return d;
-}
-
-// The same two descriptors for the 64-byte swizzle (rows of 64 bytes = 32 FP16): K-major, 8-row
-// groups 512 bytes apart; N-major, 8-row K groups 512 bytes apart and 32-column N blocks (one tensor
-// copy of 32 K rows each) 2048 bytes apart.
-__device__ __forceinline__ uint64_t tc_desc64(uint32_t saddr) {
-    uint64_t d = 0;
-    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);  // start address, 16-byte units
-    d |= (uint64_t)1 << 16;                    // leading-dimension byte offset (unused for this layout)
-    d |= (uint64_t)(512 >> 4) << 32;           // stride-dimension byte offset: next 8-row group
-    d |= (uint64_t)1 << 46;                    // descriptor version of tcgen05
-    d |= (uint64_t)4 << 61;                    // layout: 64-byte swizzle
-    return d;
-}
-__device__ __forceinline__ uint64_t tc_desc64_mn(uint32_t saddr) {
-    uint64_t d = 0;
-    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);  // start address, 16-byte units
-    d |= (uint64_t)(2048 >> 4) << 16;          // leading-dimension byte offset: next 32-column N block
-    d |= (uint64_t)(512 >> 4) << 32;           // stride-dimension byte offset: next 8-row K group
-    d |= (uint64_t)1 << 46;                    // descriptor version of tcgen05
-    d |= (uint64_t)4 << 61;                    // layout: 64-byte swizzle
     return d;
 }
 
@@ -558,11 +537,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_rows_kernel(const __grid_con
                     tc_tma_2d(st, q.a_map, kx, m0, full0 + 8u * s);
                     if constexpr (SPLIT) {
                         tc_tma_2d(st + TILE_A, q.a_map, kx, q.a_lo_row + m0, full0 + 8u * s);
-                        // B halves: BN / 32 copies of 32 columns x 32 K rows each, 2 KB apart
+                        // B halves, N-major: BN / 64 copies of 64 columns x 64 K rows each, 8 KB apart
 #pragma unroll
-                        for (int jb = 0; jb < TC_BN / 32; ++jb) {
-                            tc_tma_2d(st + A_BYTES + 2048u * jb, q.b_map, n0 + 32 * jb, kx, full0 + 8u * s);
-                            tc_tma_2d(st + A_BYTES + B_HALF + 2048u * jb, q.b_map, n0 + 32 * jb, q.b_lo_row + kx,
+                        for (int jb = 0; jb < TC_BN / 64; ++jb) {
+                            tc_tma_2d(st + A_BYTES + 8192u * jb, q.b_map, n0 + 64 * jb, kx, full0 + 8u * s);
+                            tc_tma_2d(st + A_BYTES + B_HALF + 8192u * jb, q.b_map, n0 + 64 * jb, q.b_lo_row + kx,
                                       full0 + 8u * s);
                         }
                     } else if (q.b_mn) {
@@ -602,14 +581,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_rows_kernel(const __grid_con
                     tc_fence_after();
                     const uint32_t st = sbase + (uint32_t)s * TC_STAGE;
                     if constexpr (SPLIT) {
-                        // 64-byte swizzle; a 16-deep K step is 32 bytes into each A row and 16 rows of
-                        // 64 bytes of B; N-major B (transpose-B bit of the instruction descriptor)
+                        // 128-byte swizzle; a 16-deep K step is 32 bytes into each A row and 16 rows of
+                        // 128 bytes of B; N-major B (transpose-B bit of the instruction descriptor)
 #pragma unroll
                         for (int k = 0; k < BK / 16; ++k) {
-                            const uint64_t ah = tc_desc64(st + 32u * k), bh = tc_desc64_mn(st + A_BYTES + 1024u * k);
+                            const uint64_t ah = tc_desc(st + 32u * k), bh = tc_desc_mn(st + A_BYTES + 2048u * k);
                             tc_mma(dacc, ah, bh, idesc | (1u << 16), (kb | k) != 0);
-                            tc_mma(dacc, ah, tc_desc64_mn(st + A_BYTES + B_HALF + 1024u * k), idesc | (1u << 16), 1);
-                            tc_mma(dacc, tc_desc64(st + TILE_A + 32u * k), bh, idesc | (1u << 16), 1);
+                            tc_mma(dacc, ah, tc_desc_mn(st + A_BYTES + B_HALF + 2048u * k), idesc | (1u << 16), 1);
+                            tc_mma(dacc, tc_desc(st + TILE_A + 32u * k), bh, idesc | (1u << 16), 1);
                         }
                     } else if (q.b_mn) {
                         // N-major B (transpose-B bit of the instruction descriptor); a 16-deep K step is
@@ -857,9 +836,8 @@ PFN_cuTensorMapEncodeTiled_v12000 tc_encoder() {
     return fn;
 }
 
-// 16-bit matrix of `rows` x `cols` (row stride ld elements) as 64 x box_rows boxes with the 128-byte swizzle.
-// f16: FP16 with 32-element (64-byte) box rows and the 64-byte swizzle (split products); else BF16
-// with 64-element (128-byte) box rows and the 128-byte swizzle.
+// 16-bit matrix of `rows` x `cols` (row stride ld elements) as 64 x box_rows boxes (128-byte rows) with the
+// 128-byte swizzle; FP16 (split products) or BF16.
 int tc_map(CUtensorMap *map, const void *base, int64_t cols, int64_t rows, int64_t ld, int box_rows, bool f16) {
     auto enc = tc_encoder();
     SPREG_CHECK_ARG(enc, "cuTensorMapEncodeTiled is not available from the driver");
@@ -869,7 +847,7 @@ int tc_map(CUtensorMap *map, const void *base, int64_t cols, int64_t rows, int64
     const cuuint32_t es[2] = {1, 1};
     CUresult r = enc(map, f16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
                      const_cast<void *>(base), dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                     f16 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     SPREG_CHECK_ARG(r == CUDA_SUCCESS, "cuTensorMapEncodeTiled failed (%d) for a %lld x %lld 16-bit operand", (int)r,
                     (long long)rows, (long long)cols);
