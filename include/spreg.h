@@ -231,7 +231,8 @@ typedef struct {
                              cpp_testbed/src/spmm/nano/runtime_yaml_config.register:84-99).  When the
                              launch leaves SMs idle (fewer jobs of W panels x strips than SMs), the
                              heaviest whole groups of W panels (work estimate above half the heaviest
-                             panel's) are split at K tile T / 2 until the idle SMs are used: K tiles
+                             panel's) are split at K tile T / 2 until the idle SMs are used, unless the
+                             first unsplit group is within a fifth of the heaviest panel: K tiles
                              [0, T/2) accumulate into C (from C with load_c), tiles [T/2, T) from zero
                              into scratch, then C = C + scratch (one FP32 add per element; the epilogue
                              after it).  Needs a K-tiled pack (T >= 2) of FP32 or BF16 values, FP32 C

@@ -300,9 +300,10 @@ struct CallPlan {
 // the launch has ceil(P / W) x S jobs (+ other_jobs of other SpMMs).  When that leaves SMs idle, the
 // heaviest job groups (whole groups of W panels in work order, as long as their first panel's work
 // estimate exceeds half the heaviest one's) are split at K tile T / 2, each split group adding S
-// jobs, until the idle SMs are used.  That shortens the longest jobs of a launch with about one
-// job per SM (a single SpMM); a launch with a full wave of jobs or more is balanced by the work
-// counter already and is not split.
+// jobs, until the idle SMs are used, unless the first unsplit group is within a fifth of the
+// heaviest.  That shortens the longest jobs of a launch with about one job per SM (a single SpMM);
+// a launch with a full wave of jobs or more is balanced by the work counter already and is not
+// split.
 void balance_of(const spreg_packed *a, int W, int64_t S, int64_t slots, int64_t other_jobs, int64_t *heavy,
                 int32_t *split) {
     *heavy = 0;
@@ -317,6 +318,9 @@ void balance_of(const spreg_packed *a, int W, int64_t S, int64_t slots, int64_t 
     int64_t g = 0;
     while (g < groups && (g + 1) * S <= free_slots && 2 * a->work_desc[(size_t)(g * W)] > top) ++g;
     if (g == 0) return;
+    // the longest job after the split is the first unsplit group's (or half the heaviest one's): skip a
+    // split that would shorten it by less than a fifth (the combine and the scratch cost more)
+    if (g < groups && 5 * a->work_desc[(size_t)(g * W)] > 4 * top) return;
     *heavy = std::min<int64_t>(g * W, P);
     *split = (int32_t)(T / 2);
 }
