@@ -298,16 +298,26 @@ __global__ void __launch_bounds__(32 * (kTileMaxWarps + 1), 1) exec_tile_kernel(
             ++njob;
         };
         fetch();
-        int64_t last_seq[kTileMaxStages];
+        // ring position: fill `seq` goes to stage s in fill round rnd (seq = rnd * NS + s), kept
+        // incrementally (no division per stage)
+        uint32_t last_rnd[kTileMaxStages];  // fill round of each stage's last fill
+        bool filled[kTileMaxStages];
 #pragma unroll
-        for (int s = 0; s < kTileMaxStages; ++s) last_seq[s] = -1;
-        int64_t buf_last[2] = {-1, -1};  // last stage that read each resident strip
+        for (int i = 0; i < kTileMaxStages; ++i) {
+            last_rnd[i] = 0;
+            filled[i] = false;
+        }
+        // the last stage that read each resident strip: its fill number, stage and round
+        int64_t buf_last[2] = {-1, -1};
+        int buf_stage[2] = {0, 0};
+        uint32_t buf_rnd[2] = {0, 0};
         bool ok = true;
+        int s = 0;
+        uint32_t rnd = 0;
 #pragma unroll 1
         for (int64_t seq = 0;; ++seq) {
-            const int s = (int)(seq % NS);
             const uint32_t full = full0 + 8u * s, empty = empty0 + 8u * s;
-            if (seq >= NS && !mbar_wait_bounded(empty, (uint32_t)(((seq / NS) - 1) & 1), tp.status, 5)) {
+            if (rnd > 0 && !mbar_wait_bounded(empty, (rnd - 1) & 1u, tp.status, 5)) {
                 ok = false;
                 break;
             }
@@ -321,14 +331,14 @@ __global__ void __launch_bounds__(32 * (kTileMaxWarps + 1), 1) exec_tile_kernel(
             const TProblem &pr = tp.prob[pi];
             const int c0 = pr.col_begin + strip * (32 * NV);
             const int nbox = (pr.kt + pr.box_rows - 1) / pr.box_rows;
-            const int b = res ? (int)((njob - 1) % tp.nbuf) : 0;
+            const int b = res ? (int)((njob - 1) & (int64_t)(tp.nbuf - 1)) : 0;  // nbuf is 1 or 2
             const bool load_b = !res || (r == 0 && t == pr.t_begin);
             if (res && load_b) {
                 // the job that read this strip before must be done with it: its last stage released
                 // (a stage NS or more back is already covered by the ring wait above)
                 const int64_t L = buf_last[b];
                 if (L >= 0 && seq - L < NS &&
-                    !mbar_wait_bounded(empty0 + 8u * (uint32_t)(L % NS), (uint32_t)((L / NS) & 1), tp.status, 8)) {
+                    !mbar_wait_bounded(empty0 + 8u * (uint32_t)buf_stage[b], buf_rnd[b] & 1u, tp.status, 8)) {
                     ok = false;
                     break;
                 }
@@ -377,28 +387,37 @@ __global__ void __launch_bounds__(32 * (kTileMaxWarps + 1), 1) exec_tile_kernel(
             if (!contig && mbytes)
                 bulk_copy_g2s(sb + meta_off + (uint32_t)lane * (uint32_t)tp.xbuf, pr.exec + moff, mbytes, full);
             __syncwarp();
-            last_seq[s] = seq;
-            if (res) buf_last[b] = seq;
+            filled[s] = true;
+            last_rnd[s] = rnd;
+            if (res) {
+                buf_last[b] = seq;
+                buf_stage[b] = s;
+                buf_rnd[b] = rnd;
+            }
             if (++t == pr.t_end) {
                 t = pr.t_begin;
                 if (++r == rounds_job) fetch();
             }
+            if (++s == NS) {
+                s = 0;
+                ++rnd;
+            }
         }
         if (!ok) {
             // copies still in flight land in stages whose full barrier has not flipped yet
-            for (int s = 0; s < NS; ++s)
-                if (last_seq[s] >= 0)
-                    mbar_wait_bounded(full0 + 8u * s, (uint32_t)((last_seq[s] / NS) & 1), tp.status, 7);
+            for (int i = 0; i < NS; ++i)
+                if (filled[i]) mbar_wait_bounded(full0 + 8u * i, last_rnd[i] & 1u, tp.status, 7);
         }
         return;
     }
 
     // ---------------------------------------------------------------- consumers
     float acc[MR][NV];
+    int s = 0;          // stage of this fill
+    uint32_t rnd = 0;   // its fill round (the full barrier's phase parity)
 #pragma unroll 1
-    for (int64_t seq = 0;; ++seq) {
-        const int s = (int)(seq % NS);
-        if (!mbar_wait_bounded(full0 + 8u * s, (uint32_t)((seq / NS) & 1), tp.status, 6)) break;
+    for (;;) {
+        if (!mbar_wait_bounded(full0 + 8u * s, rnd & 1u, tp.status, 6)) break;
         const int4 ji = lds_v4(jobs0 + 16u * s);
         if (ji.x < 0) break;
         const TProblem &pr = tp.prob[ji.x];
@@ -412,8 +431,11 @@ __global__ void __launch_bounds__(32 * (kTileMaxWarps + 1), 1) exec_tile_kernel(
             if (t == pr.t_begin) t_acc_init<MR, NV, TV, TC>(pr, row0, col0, valid, acc);
             const uint32_t sb = stage0 + (uint32_t)s * stage_bytes;
             // B tile t: in the ring stage, or in resident strip ji.w >> 16
-            const uint32_t tile_b = (uint32_t)((pr.kt + pr.box_rows - 1) / pr.box_rows * pr.box_rows) * ROWB;
-            const uint32_t bt = res ? res0 + (uint32_t)(ji.w >> 16) * (uint32_t)tp.stage_b + (uint32_t)t * tile_b : sb;
+            uint32_t bt = sb;
+            if (res) {
+                const uint32_t tile_b = (uint32_t)((pr.kt + pr.box_rows - 1) / pr.box_rows * pr.box_rows) * ROWB;
+                bt = res0 + (uint32_t)(ji.w >> 16) * (uint32_t)tp.stage_b + (uint32_t)t * tile_b;
+            }
             const uint32_t buf = sb + meta_off + lds_u32(moffs0 + 4u * (uint32_t)(s * kTileMaxWarps + warp));
             const uint32_t r0 = (uint32_t)(pr.col_offset + t * pr.kt);  // B row of tile row 0
             const SmemB<NV, TB> bl{bt + (uint32_t)lane * (uint32_t)(NV * sizeof(TB)) - r0 * ROWB, ROWB};
@@ -427,6 +449,10 @@ __global__ void __launch_bounds__(32 * (kTileMaxWarps + 1), 1) exec_tile_kernel(
         }
         __syncwarp();
         if (lane == 0) mbar_arrive(empty0 + 8u * s);
+        if (++s == NS) {
+            s = 0;
+            ++rnd;
+        }
     }
 }
 

@@ -76,11 +76,16 @@ def test_split_with_panel_rounds_and_strip_widths(cuda):
 
 
 def test_uniform_matrix_alone_is_split(cuda):
-    """Uniform nonzeros, a single SpMM with idle SMs: its groups are split too (halving each job)."""
+    """Uniform nonzeros, a single SpMM whose groups all fit the idle SMs twice over (128-column strips):
+    every group is split (halving each job); with 32-column strips only one group would fit, which
+    would not shorten the longest job, so nothing is split."""
     A = synth.bernoulli(1024, 512, 0.9, seed=1, std=1.0)
-    got, want, plain, (H, split, _) = run(A, 128)
-    assert H > 0 and split == 2
+    got, want, plain, (H, split, _) = run(A, 128, nr=128)
+    assert H == 256 and split == 2
     assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+    got, _, plain, (H, split, _) = run(A, 128, nr=32)
+    assert (H, split) == (0, 0)
+    assert np.array_equal(got.view(np.uint32), plain.view(np.uint32))
 
 
 def test_full_launch_is_not_split(cuda):
