@@ -23,7 +23,7 @@
  * Device status word: kernels never trap.  A bounded wait that gives up, or an index a kernel's
  * own bounds check refuses, records a nonzero code in a per-device word instead (read and clear it
  * with spreg_device_status):
- *   2, 5-8   executor waits (batched and B-tile kernels);   20  CSR column index out of range;
+ *   2, 5-9   executor waits (batched and B-tile kernels);   20  CSR column index out of range;
  *   21-25    tensor-core kernel waits;                         30  spreg_selftest_wait_timeout.
  */
 #ifndef SPREG_H
@@ -233,9 +233,10 @@ typedef struct {
                              heaviest whole groups of W panels (work estimate above half the heaviest
                              panel's) are split at K tile T / 2 until the idle SMs are used, unless the
                              first unsplit group is within a fifth of the heaviest panel: K tiles
-                             [0, T/2) accumulate into C (from C with load_c), tiles [T/2, T) from zero
-                             into scratch, then C = C + scratch (one FP32 add per element; the epilogue
-                             after it).  Needs a K-tiled pack (T >= 2) of FP32 or BF16 values, FP32 C
+                             [0, T/2) accumulate into C (from C with load_c) in one job, tiles [T/2, T)
+                             from zero in another, which adds into C once the first has stored that
+                             (panel, strip): C = C + hi, one FP32 add per element, the epilogue after
+                             it, all in one launch.  Needs a K-tiled pack (T >= 2) of FP32 or BF16 values, FP32 C
                              and the B-tile kernel (b_staging 0 or 1); other packs run unsplit.
                              spreg_load_balance_plan reports the split. */
     int32_t reserved;     /* 0 */

@@ -108,8 +108,10 @@ struct DevFacts {
     int smem_per_sm = 0;
     int *status = nullptr;     // status word of bounded waits
     int *counters = nullptr;   // work counters handed out round robin, one per launch
+    int *flags = nullptr;      // load-balance flags, handed out round robin in blocks
 };
 constexpr int kCounters = 4096;
+constexpr int kLbFlags = 1 << 16;  // flags of the load-balanced splits in flight
 
 namespace {
 DevFacts g_facts[64];
@@ -130,10 +132,11 @@ int dev_facts(DevFacts **out) {
         SPREG_CUDA(cudaDeviceGetAttribute(&f.smem_per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
         if (f.smem_optin > kMaxSmem) f.smem_optin = kMaxSmem;
         int *buf = nullptr;
-        SPREG_CUDA(cudaMalloc(&buf, sizeof(int) * (1 + kCounters)));
-        SPREG_CUDA(cudaMemset(buf, 0, sizeof(int) * (1 + kCounters)));
+        SPREG_CUDA(cudaMalloc(&buf, sizeof(int) * (1 + kCounters + kLbFlags)));
+        SPREG_CUDA(cudaMemset(buf, 0, sizeof(int) * (1 + kCounters + kLbFlags)));
         f.status = buf;
         f.counters = buf + 1;
+        f.flags = buf + 1 + kCounters;
     }
     *out = &f;
     return SPREG_OK;
@@ -149,6 +152,15 @@ int *device_status_word(int *st) {
 int *next_counter(DevFacts *f) {
     static std::atomic<unsigned> next{0};
     return f->counters + (next.fetch_add(1) % kCounters);
+}
+
+// A block of n contiguous load-balance flags (n <= kLbFlags / 4), round robin as the counters: its
+// offset in f->flags.
+int32_t next_flags(int64_t n) {
+    static std::atomic<unsigned long long> next{0};
+    unsigned long long off = next.fetch_add((unsigned long long)n) % kLbFlags;
+    if (off + (unsigned long long)n > (unsigned long long)kLbFlags) off = 0;
+    return (int32_t)off;
 }
 
 // Self-test of the bounded waits: one CTA waits on an mbarrier that nothing arrives on, with a
@@ -286,12 +298,12 @@ struct CallPlan {
     int warps;
     int warps_req;           // warps_per_cta as asked (0: each kernel's own choice) -- the CTA tiling
     int rounds;              // panel rounds of the B-tile kernel (1: B tiles in the ring stages)
-    // Load balance: work-order positions [0, lb_heavy) run K tiles [0, lb_split) into C and
-    // [lb_split, T) into lb_scratch (row stride lb_ld), then C = C + scratch over their rows.
+    // Load balance: work-order positions [0, lb_heavy) run K tiles [0, lb_split) into C (the low
+    // half), and [lb_split, T) from zero (the high half), which adds into C once the low half of its
+    // (panel, strip) is stored; flags of the main and tail problems at these offsets of f->flags.
     int64_t lb_heavy = 0;
     int32_t lb_split = 0;
-    float *lb_scratch = nullptr;
-    int64_t lb_ld = 0;
+    int32_t lb_flags_main = 0, lb_flags_tail = 0;
     const spreg_packed *a = nullptr;
     const spreg_exec_args *args = nullptr;
 };
@@ -321,6 +333,7 @@ void balance_of(const spreg_packed *a, int W, int64_t S, int64_t slots, int64_t 
     // the longest job after the split is the first unsplit group's (or half the heaviest one's): skip a
     // split that would shorten it by less than a fifth (the combine and the scratch cost more)
     if (g < groups && 5 * a->work_desc[(size_t)(g * W)] > 4 * top) return;
+    if (std::min<int64_t>(g * W, P) * S > kLbFlags / 4) return;  // one flag per split (panel, strip)
     *heavy = std::min<int64_t>(g * W, P);
     *split = (int32_t)(T / 2);
 }
@@ -511,12 +524,13 @@ int plan_call(const spreg_packed *a, const spreg_exec_args *args, CallPlan *cp, 
         tb.M = (int32_t)in.rows;
         tb.P = (int32_t)a->geom.P;
         tb.T = (int32_t)a->geom.T;
-        tb.ppt = (int32_t)a->geom.ppt;
+        tb.combine = 0;
+        tb.pad16 = 0;
+        tb.flag_off = 0;
         tb.load_c = args->load_c ? 1 : 0;
         tb.epilogue = (int16_t)args->epilogue;
         tb.order = (int16_t)args->job_order;
         tb.kt = (int32_t)kt_rows;
-        tb.krows = (int32_t)a->geom.K;
         tb.col_offset = (int32_t)in.col_offset;
         tb.box_rows = (int16_t)box_rows;
         tb.t_begin = 0;
@@ -709,6 +723,7 @@ int launch_tile_groups(std::map<std::tuple<int, int, int, int>, TileGroup> &grou
             tp.rounds = g.rounds;
             tp.nbuf = nbuf;
             tp.pad_ = 0;
+            tp.flags = f->flags;
             tp.status = f->status;
             tp.counter = next_counter(f);
             const int per_sm = std::max(1, std::min((int)(f->smem_per_sm / (int64_t)smem), 2048 / threads));
@@ -733,21 +748,25 @@ void add_tile_call(std::map<std::tuple<int, int, int, int>, TileGroup> &groups, 
         g.xbuf = std::max(g.xbuf, cp.xbuf);
         g.stage_b = std::max(g.stage_b, stage_b);
     };
-    auto add_split = [&](const TProblem &pr, int nv, int64_t stage_b) {
+    auto add_split = [&](const TProblem &pr, int nv, int64_t stage_b, int32_t flag_off) {
         if (cp.lb_heavy <= 0) {
             add(pr, nv, stage_b);
             return;
         }
-        // heavy panels: K tiles [0, split) into C (no epilogue), [split, T) from zero into the scratch
+        // heavy panels: K tiles [0, split) into C (no epilogue; flags each (panel, strip) when stored),
+        // then [split, T) from zero, added into C after the low half (the epilogue after the add).
+        // The low halves' jobs come first in the launch, so a high half waits only on jobs that are
+        // already running or done.
         TProblem lo = pr, hi = pr, rest = pr;
         lo.count = hi.count = (int32_t)cp.lb_heavy;
         lo.t_end = (int16_t)cp.lb_split;
         lo.epilogue = SPREG_EPILOGUE_NONE;
+        lo.combine = 1;
+        lo.flag_off = flag_off;
         hi.t_begin = (int16_t)cp.lb_split;
-        hi.C = cp.lb_scratch;
-        hi.ldc = cp.lb_ld;
         hi.load_c = 0;
-        hi.epilogue = SPREG_EPILOGUE_NONE;
+        hi.combine = 2;
+        hi.flag_off = flag_off;
         add(lo, nv, stage_b);
         add(hi, nv, stage_b);
         if (cp.lb_heavy < pr.P) {
@@ -756,27 +775,8 @@ void add_tile_call(std::map<std::tuple<int, int, int, int>, TileGroup> &groups, 
             add(rest, nv, stage_b);
         }
     };
-    if (cp.has_main) add_split(cp.tmain, cp.nv, cp.stage_b_main);
-    if (cp.has_tail) add_split(cp.ttail, 1, cp.stage_b_tail);
-}
-
-// C = C + S (then the epilogue) over the rows of the split panels: the last step of a load-balanced
-// SpMM (one FP32 add per element, C holding K tiles [0, split) and S tiles [split, T)).
-__global__ void lb_combine_kernel(float *__restrict__ C, int64_t ldc, const float *__restrict__ S, int64_t lds,
-                                  const int32_t *__restrict__ panel_order, int64_t heavy, int mr, int64_t M,
-                                  int64_t n, int epilogue) {
-    for (int64_t p = blockIdx.y; p < heavy; p += gridDim.y) {
-        const int64_t row0 = (int64_t)panel_order[p] * mr;
-        for (int r = 0; r < mr && row0 + r < M; ++r) {
-            float *c = C + (row0 + r) * ldc;
-            const float *s = S + (row0 + r) * lds;
-            for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
-                float o = c[j] + s[j];
-                if (epilogue == SPREG_EPILOGUE_RELU) o = fmaxf(o, 0.0f);
-                c[j] = o;
-            }
-        }
-    }
+    if (cp.has_main) add_split(cp.tmain, cp.nv, cp.stage_b_main, cp.lb_flags_main);
+    if (cp.has_tail) add_split(cp.ttail, 1, cp.stage_b_tail, cp.lb_flags_tail);
 }
 
 void add_call(std::map<std::tuple<int, int, int>, Group> &groups, const CallPlan &cp) {
@@ -800,52 +800,30 @@ int run_calls(const spreg_packed *const *as, const spreg_exec_args *const *args,
     int64_t items1 = 0;
     for (int32_t i = 0; i < n; ++i) items1 += strip_items1(as[i], args[i]);
     std::vector<CallPlan> plans((size_t)n);
-    int64_t lb_bytes = 0;
+    DevFacts *f;
+    int st = dev_facts(&f);
+    if (st) return st;
     for (int32_t i = 0; i < n; ++i) {
         CallPlan &cp = plans[(size_t)i];
-        int st = plan_call(as[i], args[i], &cp, items1 - strip_items1(as[i], args[i]));
+        st = plan_call(as[i], args[i], &cp, items1 - strip_items1(as[i], args[i]));
         if (st != SPREG_OK) return st;
         if (cp.lb_heavy > 0) {
-            cp.lb_ld = (args[i]->n + 7) / 8 * 8;
-            lb_bytes += (as[i]->info.rows * cp.lb_ld * 4 + 255) / 256 * 256;
+            // one zeroed flag per split (panel, strip) of the main and the tail problem
+            const int64_t nm = cp.has_main ? cp.lb_heavy * cp.tmain.S : 0;
+            const int64_t nt = cp.has_tail ? cp.lb_heavy * cp.ttail.S : 0;
+            cp.lb_flags_main = next_flags(nm + nt);
+            cp.lb_flags_tail = cp.lb_flags_main + (int32_t)nm;
+            SPREG_CUDA(cudaMemsetAsync(f->flags + cp.lb_flags_main, 0, (size_t)(nm + nt) * sizeof(int), stream));
         }
-    }
-    // scratch of the split panels' upper K halves: stream-ordered (capturable in a CUDA graph)
-    char *lb_mem = nullptr;
-    if (lb_bytes > 0) {
-        cudaError_t e = cudaMallocAsync(reinterpret_cast<void **>(&lb_mem), (size_t)lb_bytes, stream);
-        if (e != cudaSuccess) SPREG_FAIL(SPREG_ERR_NOMEM, "load-balance scratch (%lld B): %s", (long long)lb_bytes,
-                                         cudaGetErrorString(e));
-        int64_t off = 0;
-        for (CallPlan &cp : plans)
-            if (cp.lb_heavy > 0) {
-                cp.lb_scratch = reinterpret_cast<float *>(lb_mem + off);
-                off += (cp.a->info.rows * cp.lb_ld * 4 + 255) / 256 * 256;
-            }
     }
     for (const CallPlan &cp : plans) {
         if (cp.tile) add_tile_call(tgroups, cp);
         else if (cp.stream_kernel) streams.push_back(cp);
         else add_call(groups, cp);
     }
-    int st = launch_groups(groups, stream);
+    st = launch_groups(groups, stream);
     if (st == SPREG_OK) st = launch_tile_groups(tgroups, stream);
     for (size_t i = 0; i < streams.size() && st == SPREG_OK; ++i) st = launch_stream(streams[i], stream);
-    for (const CallPlan &cp : plans) {
-        if (st != SPREG_OK || cp.lb_heavy <= 0) continue;
-        const int64_t nn = cp.args->n;
-        const unsigned gx = (unsigned)std::max<int64_t>(1, std::min<int64_t>((nn + 255) / 256, 8));
-        const unsigned gy = (unsigned)std::min<int64_t>(cp.lb_heavy, 65535);
-        lb_combine_kernel<<<dim3(gx, gy), 256, 0, stream>>>(reinterpret_cast<float *>(cp.args->c), cp.args->ldc,
-                                                            cp.lb_scratch, cp.lb_ld, cp.a->panel_order, cp.lb_heavy,
-                                                            cp.mr, cp.a->info.rows, nn, cp.args->epilogue);
-        cudaError_t e = cudaGetLastError();
-        if (e != cudaSuccess) {
-            set_error(std::string("load-balance combine launch: ") + cudaGetErrorString(e));
-            st = SPREG_ERR_CUDA;
-        }
-    }
-    if (lb_mem) cudaFreeAsync(lb_mem, stream);
     return st;
 }
 

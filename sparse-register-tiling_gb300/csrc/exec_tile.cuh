@@ -62,11 +62,15 @@ struct TProblem {
     int32_t job_begin;          // first global job
     int32_t col_begin;          // first column of the problem's strips
     int32_t col_end;            // columns >= col_end are not computed
-    int32_t P, S, T, ppt;       // row panels, strips, K tiles, panels per row tile
+    int32_t P, S, T;            // row panels (work-order positions), strips, K tiles
+    int16_t combine;            // load-balanced halves: 0 none, 1 low half (flags its stores), 2 high half
+                                // (waits for the low half, then C = C + acc)
+    int16_t pad16;
     int16_t load_c, epilogue;
     int16_t order;              // job order: 0 = panel groups outer (a group's strips in a row), 1 = strips outer
     int16_t box_rows;           // rows of one tensor copy (K tile copied in ceil(kt / box_rows) copies)
-    int32_t kt, krows;          // B rows per K tile, B rows of all tiles (columns of A)
+    int32_t kt;                 // B rows per K tile
+    int32_t flag_off;           // combine: flags of (position - pos_begin, strip) at flags[flag_off + pos * S + strip]
     int32_t col_offset;         // first B row of tile 0
     // The units this problem runs: K tiles [t_begin, t_end) of the panels at work-order positions
     // [pos_begin, pos_begin + count) (the whole pack: 0, T, 0, P).  A load-balanced SpMM splits its
@@ -89,6 +93,7 @@ struct TileParams {
     int32_t rounds;             // panel rounds per job (1: B tiles travel in the ring stages)
     int32_t nbuf;               // resident B strips (1 or 2) with panel rounds, else 0
     int32_t pad_;
+    int *flags;                 // load-balance flags (zero at launch), indexed by TProblem::flag_off
     TProblem prob[kTileMaxProblems];
 };
 static_assert(sizeof(TileParams) <= 32764, "kernel parameters are limited to 32764 bytes");
@@ -238,6 +243,46 @@ __device__ __forceinline__ void t_store(const TProblem &pr, int64_t gp, int64_t 
         }
         VecIO<NV, TC>::store(cp, o);
     }
+}
+
+// High half of a load-balanced (panel, strip): C = C + acc (one FP32 add per element, the low half's
+// stored result first), then the epilogue.  The low half's stores are visible: every lane acquired
+// the flag its warp released after them.
+template <int MR, int NV, class TV, class TC>
+__device__ __forceinline__ void t_store_add(const TProblem &pr, int64_t row0, int64_t col0, bool valid,
+                                            const float (&acc)[MR][NV]) {
+    if (!valid) return;
+    TC *C = reinterpret_cast<TC *>(pr.C);
+#pragma unroll
+    for (int r = 0; r < MR; ++r) {
+        if (row0 + r >= pr.M) continue;
+        TC *cp = C + (row0 + r) * pr.ldc + col0;
+        float o[NV];
+        VecIO<NV, TC>::load_plain(cp, o);
+#pragma unroll
+        for (int j = 0; j < NV; ++j) o[j] = o[j] + acc[r][j];
+        if (pr.epilogue == SPREG_EPILOGUE_RELU) {
+#pragma unroll
+            for (int j = 0; j < NV; ++j) o[j] = fmaxf(o[j], 0.0f);
+        }
+        VecIO<NV, TC>::store(cp, o);
+    }
+}
+
+// Bounded wait for a load-balance flag (acquire, GPU scope).  Gives up after about a second,
+// recording `code` in the device status word.
+__device__ __forceinline__ bool lb_flag_wait(const int *f, int *status, int code) {
+    for (uint32_t it = 0; it < (1u << 23); ++it) {
+        int v;
+        asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(f) : "memory");
+        if (v) return true;
+        if (it >= 32) __nanosleep(128);
+    }
+    atomicCAS(status, 0, code);
+    return false;
+}
+__device__ __forceinline__ void lb_flag_release(int *f) {
+    asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(f), "r"(1) : "memory");
 }
 
 // Shared memory: [0, 64) full / empty barriers, [256, 256 + 16 * stages) job of each stage,
@@ -445,7 +490,23 @@ __global__ void __launch_bounds__(32 * (kTileMaxWarps + 1), 1) exec_tile_kernel(
                 const uint4 rec = lds_u128(buf + 16u + 16u * g);
                 run_group_x<MR, NV, TV, true>((int)rec.x, (int)rec.y, buf + rec.z, buf + rec.w, bl, acc);
             }
-            if (t == pr.t_end - 1) t_store<MR, NV, TV, TC>(pr, gp, row0, col0, valid, acc);
+            if (t == pr.t_end - 1) {
+                if (pr.combine == 0) {
+                    t_store<MR, NV, TV, TC>(pr, gp, row0, col0, valid, acc);
+                } else {
+                    int *fl = tp.flags + pr.flag_off + (pos - pr.pos_begin) * pr.S + ji.z;
+                    if (pr.combine == 1) {
+                        // low half: store, then release this (panel, strip)'s flag
+                        t_store<MR, NV, TV, TC>(pr, gp, row0, col0, valid, acc);
+                        __threadfence();
+                        __syncwarp();
+                        if (lane == 0) lb_flag_release(fl);
+                    } else if (lb_flag_wait(fl, tp.status, 9)) {
+                        // high half: after the low half's stores, C = C + acc
+                        t_store_add<MR, NV, TV, TC>(pr, row0, col0, valid, acc);
+                    }
+                }
+            }
         }
         __syncwarp();
         if (lane == 0) mbar_arrive(empty0 + 8u * s);
