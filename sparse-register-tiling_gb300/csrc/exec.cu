@@ -77,24 +77,24 @@ cudaError_t launch_mr_batch(int mr, const BatchParams &p, int nv, int combo, uns
 }
 
 template <int MR>
-cudaError_t launch_combo_tile(const TileParams &p, int nv, int combo, unsigned grid, int threads, size_t smem,
+cudaError_t launch_combo_tile(const TileParams &p, int nv, bool gen, int combo, unsigned grid, int threads, size_t smem,
                               cudaStream_t s) {
     switch (combo) {
-    case COMBO_F32: return launch_exec_tile<MR, COMBO_F32>(p, nv, grid, threads, smem, s);
-    case COMBO_BF16_F32OUT: return launch_exec_tile<MR, COMBO_BF16_F32OUT>(p, nv, grid, threads, smem, s);
-    case COMBO_BF16_BF16OUT: return launch_exec_tile<MR, COMBO_BF16_BF16OUT>(p, nv, grid, threads, smem, s);
-    case COMBO_F16_F32OUT: return launch_exec_tile<MR, COMBO_F16_F32OUT>(p, nv, grid, threads, smem, s);
+    case COMBO_F32: return launch_exec_tile<MR, COMBO_F32>(p, nv, gen, grid, threads, smem, s);
+    case COMBO_BF16_F32OUT: return launch_exec_tile<MR, COMBO_BF16_F32OUT>(p, nv, gen, grid, threads, smem, s);
+    case COMBO_BF16_BF16OUT: return launch_exec_tile<MR, COMBO_BF16_BF16OUT>(p, nv, gen, grid, threads, smem, s);
+    case COMBO_F16_F32OUT: return launch_exec_tile<MR, COMBO_F16_F32OUT>(p, nv, gen, grid, threads, smem, s);
     default: return cudaErrorInvalidValue;
     }
 }
 
-cudaError_t launch_mr_tile(int mr, const TileParams &p, int nv, int combo, unsigned grid, int threads, size_t smem,
-                           cudaStream_t s) {
+cudaError_t launch_mr_tile(int mr, const TileParams &p, int nv, bool gen, int combo, unsigned grid, int threads,
+                           size_t smem, cudaStream_t s) {
     switch (mr) {
-    case 2: return launch_combo_tile<2>(p, nv, combo, grid, threads, smem, s);
-    case 4: return launch_combo_tile<4>(p, nv, combo, grid, threads, smem, s);
-    case 6: return launch_combo_tile<6>(p, nv, combo, grid, threads, smem, s);
-    case 8: return launch_combo_tile<8>(p, nv, combo, grid, threads, smem, s);
+    case 2: return launch_combo_tile<2>(p, nv, gen, combo, grid, threads, smem, s);
+    case 4: return launch_combo_tile<4>(p, nv, gen, combo, grid, threads, smem, s);
+    case 6: return launch_combo_tile<6>(p, nv, gen, combo, grid, threads, smem, s);
+    case 8: return launch_combo_tile<8>(p, nv, gen, combo, grid, threads, smem, s);
     default: return cudaErrorInvalidValue;
     }
 }
@@ -663,12 +663,13 @@ int launch_groups(std::map<std::tuple<int, int, int>, Group> &groups, cudaStream
 // One tile-kernel launch per group of at most kMaxBatchProblems problems of one configuration.
 struct TileGroup {
     int mr, combo, nv, rounds;
+    bool gen = false;  // the kernel's general form: panel rounds, K-tile / position ranges, split halves
     int warps_req = 0;  // consumer warps (panels per job) asked by the first call that asked (0: 16)
     std::vector<TProblem> probs;
     int64_t xbuf = 0, stage_b = 0;
 };
 
-int launch_tile_groups(std::map<std::tuple<int, int, int, int>, TileGroup> &groups, cudaStream_t stream) {
+int launch_tile_groups(std::map<std::tuple<int, int, int, int, bool>, TileGroup> &groups, cudaStream_t stream) {
     DevFacts *f;
     int st = dev_facts(&f);
     if (st) return st;
@@ -729,20 +730,22 @@ int launch_tile_groups(std::map<std::tuple<int, int, int, int>, TileGroup> &grou
             const int per_sm = std::max(1, std::min((int)(f->smem_per_sm / (int64_t)smem), 2048 / threads));
             const int64_t ctas = std::min<int64_t>((int64_t)f->sms * per_sm, jobs);
             SPREG_CUDA(cudaMemsetAsync(tp.counter, 0, sizeof(int), stream));
-            cudaError_t e = launch_mr_tile(g.mr, tp, g.nv, g.combo, (unsigned)ctas, threads, smem, stream);
+            cudaError_t e = launch_mr_tile(g.mr, tp, g.nv, g.gen, g.combo, (unsigned)ctas, threads, smem, stream);
             if (e != cudaSuccess) SPREG_FAIL(SPREG_ERR_CUDA, "tile executor launch: %s", cudaGetErrorString(e));
         }
     }
     return SPREG_OK;
 }
 
-void add_tile_call(std::map<std::tuple<int, int, int, int>, TileGroup> &groups, const CallPlan &cp) {
+void add_tile_call(std::map<std::tuple<int, int, int, int, bool>, TileGroup> &groups, const CallPlan &cp) {
     auto add = [&](const TProblem &pr, int nv, int64_t stage_b) {
-        TileGroup &g = groups[std::make_tuple(cp.mr, cp.combo, nv, cp.rounds)];
+        const bool gen = cp.rounds > 1 || cp.lb_heavy > 0;
+        TileGroup &g = groups[std::make_tuple(cp.mr, cp.combo, nv, cp.rounds, gen)];
         g.mr = cp.mr;
         g.combo = cp.combo;
         g.nv = nv;
         g.rounds = cp.rounds;
+        g.gen = gen;
         if (!g.warps_req) g.warps_req = cp.warps_req;
         g.probs.push_back(pr);
         g.xbuf = std::max(g.xbuf, cp.xbuf);
@@ -795,7 +798,7 @@ void add_call(std::map<std::tuple<int, int, int>, Group> &groups, const CallPlan
 
 int run_calls(const spreg_packed *const *as, const spreg_exec_args *const *args, int32_t n, cudaStream_t stream) {
     std::map<std::tuple<int, int, int>, Group> groups;
-    std::map<std::tuple<int, int, int, int>, TileGroup> tgroups;
+    std::map<std::tuple<int, int, int, int, bool>, TileGroup> tgroups;
     std::vector<CallPlan> streams;
     int64_t items1 = 0;
     for (int32_t i = 0; i < n; ++i) items1 += strip_items1(as[i], args[i]);

@@ -38,6 +38,7 @@
 #include <cuda.h>
 
 #include <cstddef>
+#include <type_traits>
 
 #include "exec_kernel.cuh"
 
@@ -288,15 +289,23 @@ __device__ __forceinline__ void lb_flag_release(int *f) {
 // Shared memory: [0, 64) full / empty barriers, [256, 256 + 16 * stages) job of each stage,
 // [512, 512 + 4 * 16 * stages) each consumer's block offset in each stage's metadata area, from
 // 1024 the stages: B tile (stage_b bytes) then the metadata area (W * xbuf bytes).
-template <int MR, int NV, class TV, class TB, class TC>
+// GEN: the general form (panel rounds, per-problem K-tile and work-order ranges, load-balanced
+// halves); without it the launch runs whole problems through a ring of kTileStages stages with those
+// checks compiled out (the plain executor's hot path).
+template <int MR, int NV, class TV, class TB, class TC, bool GEN>
 __global__ void __launch_bounds__(32 * (kTileMaxWarps + 1), 1) exec_tile_kernel(const __grid_constant__ TileParams tp) {
     extern __shared__ __align__(128) unsigned char smem[];
     constexpr uint32_t ROWB = 32u * NV * (uint32_t)sizeof(TB);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int W = tp.warps;
-    const int NS = tp.stages;
-    const int R = tp.rounds;
-    const bool res = tp.nbuf > 0;  // panel rounds: B strips resident outside the ring
+    const int NS = GEN ? tp.stages : kTileStages;
+    const int R = GEN ? tp.rounds : 1;
+    const bool res = GEN && tp.nbuf > 0;  // panel rounds: B strips resident outside the ring
+    // a problem's K tiles [t_begin, t_end) and work-order positions [pos_begin, pos_begin + count)
+    auto t_lo = [](const TProblem &pr) -> int { return GEN ? (int)pr.t_begin : 0; };
+    auto t_hi = [](const TProblem &pr) -> int { return GEN ? (int)pr.t_end : pr.T; };
+    auto p_lo = [](const TProblem &pr) -> int64_t { return GEN ? (int64_t)pr.pos_begin : 0; };
+    auto p_n = [](const TProblem &pr) -> int64_t { return GEN ? (int64_t)pr.count : (int64_t)pr.P; };
     const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(smem);
     const uint32_t full0 = sbase, empty0 = sbase + 8u * kTileMaxStages, jobs0 = sbase + 256u, moffs0 = sbase + 512u;
     const uint32_t res0 = sbase + 1024u;                          // resident B strips (panel rounds)
@@ -329,16 +338,16 @@ __global__ void __launch_bounds__(32 * (kTileMaxWarps + 1), 1) exec_tile_kernel(
             const int64_t local = job - pr.job_begin;
             const int64_t gsz = (int64_t)W * R;  // panels per job
             if (pr.order == 1) {
-                const int64_t groups = (pr.count + gsz - 1) / gsz;
+                const int64_t groups = (p_n(pr) + gsz - 1) / gsz;
                 group = (int)(local % groups);
                 strip = (int)(local / groups);
             } else {
                 group = (int)(local / pr.S);
                 strip = (int)(local % pr.S);
             }
-            t = pr.t_begin;
+            t = t_lo(pr);
             r = 0;
-            const int64_t left = (int64_t)pr.count - (int64_t)group * gsz;  // panels from this job's first on
+            const int64_t left = p_n(pr) - (int64_t)group * gsz;  // panels from this job's first on
             rounds_job = (int)((left + W - 1) / W < R ? (left + W - 1) / W : R);
             ++njob;
         };
@@ -377,7 +386,7 @@ __global__ void __launch_bounds__(32 * (kTileMaxWarps + 1), 1) exec_tile_kernel(
             const int c0 = pr.col_begin + strip * (32 * NV);
             const int nbox = (pr.kt + pr.box_rows - 1) / pr.box_rows;
             const int b = res ? (int)((njob - 1) & (int64_t)(tp.nbuf - 1)) : 0;  // nbuf is 1 or 2
-            const bool load_b = !res || (r == 0 && t == pr.t_begin);
+            const bool load_b = !res || (r == 0 && t == t_lo(pr));
             if (res && load_b) {
                 // the job that read this strip before must be done with it: its last stage released
                 // (a stage NS or more back is already covered by the ring wait above)
@@ -391,8 +400,8 @@ __global__ void __launch_bounds__(32 * (kTileMaxWarps + 1), 1) exec_tile_kernel(
             // metadata: lane w < W holds the block of unit (panel pos_begin + (group * R + r) * W + w, t)
             int64_t moff = 0;
             uint32_t mbytes = 0;
-            const int64_t pos = pr.pos_begin + ((int64_t)group * R + r) * W + lane;  // position in the work order
-            const bool act = lane < W && pos < (int64_t)pr.pos_begin + pr.count;
+            const int64_t pos = p_lo(pr) + ((int64_t)group * R + r) * W + lane;  // position in the work order
+            const bool act = lane < W && pos < p_lo(pr) + p_n(pr);
             if (act) {
                 const int64_t slot = (int64_t)t * pr.P + pos;
                 moff = pr.exec_offs[slot];
@@ -412,12 +421,12 @@ __global__ void __launch_bounds__(32 * (kTileMaxWarps + 1), 1) exec_tile_kernel(
             const uint32_t tile_b = (uint32_t)(nbox * pr.box_rows) * ROWB;  // one K tile of the strip
             if (lane == 0) {
                 sts_v4(jobs0 + 16u * s, pi, group * R + r, strip, t | (b << 16));
-                const uint32_t bbytes = load_b ? (res ? (uint32_t)(pr.t_end - pr.t_begin) : 1u) * tile_b : 0u;
+                const uint32_t bbytes = load_b ? (res ? (uint32_t)(t_hi(pr) - t_lo(pr)) : 1u) * tile_b : 0u;
                 mbar_arrive_expect_tx(full, bbytes + mtotal);
                 if (res && load_b) {
                     // every K tile of the problem's range, into resident strip b (tile tt at tt * tile_b)
                     const uint32_t dst = res0 + (uint32_t)b * (uint32_t)tp.stage_b;
-                    for (int tt = pr.t_begin; tt < pr.t_end; ++tt)
+                    for (int tt = t_lo(pr); tt < t_hi(pr); ++tt)
                         for (int bx = 0; bx < nbox; ++bx)
                             tma_load_2d(dst + (uint32_t)tt * tile_b + (uint32_t)(bx * pr.box_rows) * ROWB, &pr.tmap, c0,
                                         pr.col_offset + tt * pr.kt + bx * pr.box_rows, full);
@@ -439,8 +448,8 @@ __global__ void __launch_bounds__(32 * (kTileMaxWarps + 1), 1) exec_tile_kernel(
                 buf_stage[b] = s;
                 buf_rnd[b] = rnd;
             }
-            if (++t == pr.t_end) {
-                t = pr.t_begin;
+            if (++t == t_hi(pr)) {
+                t = t_lo(pr);
                 if (++r == rounds_job) fetch();
             }
             if (++s == NS) {
@@ -466,14 +475,14 @@ __global__ void __launch_bounds__(32 * (kTileMaxWarps + 1), 1) exec_tile_kernel(
         const int4 ji = lds_v4(jobs0 + 16u * s);
         if (ji.x < 0) break;
         const TProblem &pr = tp.prob[ji.x];
-        const int64_t pos = pr.pos_begin + (int64_t)ji.y * W + warp;
+        const int64_t pos = p_lo(pr) + (int64_t)ji.y * W + warp;
         const int t = ji.w & 0xffff;
-        if (pos < (int64_t)pr.pos_begin + pr.count) {
+        if (pos < p_lo(pr) + p_n(pr)) {
             const int64_t gp = pr.panel_order[pos];
             const int64_t row0 = gp * MR;
             const int64_t col0 = pr.col_begin + (int64_t)ji.z * (32 * NV) + (int64_t)lane * NV;
             const bool valid = col0 < pr.col_end;
-            if (t == pr.t_begin) t_acc_init<MR, NV, TV, TC>(pr, row0, col0, valid, acc);
+            if (t == t_lo(pr)) t_acc_init<MR, NV, TV, TC>(pr, row0, col0, valid, acc);
             const uint32_t sb = stage0 + (uint32_t)s * stage_bytes;
             // B tile t: in the ring stage, or in resident strip ji.w >> 16
             uint32_t bt = sb;
@@ -490,8 +499,8 @@ __global__ void __launch_bounds__(32 * (kTileMaxWarps + 1), 1) exec_tile_kernel(
                 const uint4 rec = lds_u128(buf + 16u + 16u * g);
                 run_group_x<MR, NV, TV, true>((int)rec.x, (int)rec.y, buf + rec.z, buf + rec.w, bl, acc);
             }
-            if (t == pr.t_end - 1) {
-                if (pr.combine == 0) {
+            if (t == t_hi(pr) - 1) {
+                if (!GEN || pr.combine == 0) {
                     t_store<MR, NV, TV, TC>(pr, gp, row0, col0, valid, acc);
                 } else {
                     int *fl = tp.flags + pr.flag_off + (pos - pr.pos_begin) * pr.S + ji.z;
@@ -519,44 +528,49 @@ __global__ void __launch_bounds__(32 * (kTileMaxWarps + 1), 1) exec_tile_kernel(
 
 // 256-column strips (NV = 8) are built for 16-bit B and M_r <= 4 only.
 using TileKernelPtr = void (*)(TileParams);
-template <int MR, class V, class B, class C> inline TileKernelPtr tile_nv8_kernel() {
-    if constexpr (sizeof(B) == 2 && MR <= 4) return exec_tile_kernel<MR, 8, V, B, C>;
+template <int MR, class V, class B, class C, bool GEN> inline TileKernelPtr tile_nv8_kernel() {
+    if constexpr (sizeof(B) == 2 && MR <= 4) return exec_tile_kernel<MR, 8, V, B, C, GEN>;
     else return nullptr;
 }
 
 template <int MR, int COMBO>
-cudaError_t launch_exec_tile(const TileParams &p, int nv, unsigned grid, int threads, size_t smem, cudaStream_t s);
+cudaError_t launch_exec_tile(const TileParams &p, int nv, bool gen, unsigned grid, int threads, size_t smem,
+                             cudaStream_t s);
 
 #define SPREG_INSTANTIATE_TILE(MR, COMBO)                                                             \
     template <>                                                                                       \
-    cudaError_t launch_exec_tile<MR, COMBO>(const TileParams &p, int nv, unsigned grid, int threads, size_t smem, \
-                                            cudaStream_t s) {                                         \
+    cudaError_t launch_exec_tile<MR, COMBO>(const TileParams &p, int nv, bool gen, unsigned grid, int threads, \
+                                            size_t smem, cudaStream_t s) {                            \
         using V = ComboTypes<COMBO>::V;                                                               \
         using B = ComboTypes<COMBO>::B;                                                               \
         using C = ComboTypes<COMBO>::C;                                                               \
-        static std::atomic<bool> configured[64][9];                                                           \
+        static std::atomic<bool> configured[64][9][2];                                                \
         int dev = 0;                                                                                  \
         cudaGetDevice(&dev);                                                                          \
         auto run = [&](auto kern) -> cudaError_t {                                                    \
             if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;                                  \
-            if (!configured[dev][nv].load()) {                                                               \
+            if (!configured[dev][nv][gen].load()) {                                                   \
                 cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem); \
                 if (e != cudaSuccess) return e;                                                       \
-                configured[dev][nv].store(true);                                                           \
+                configured[dev][nv][gen].store(true);                                                 \
             }                                                                                         \
             kern<<<grid, threads, smem, s>>>(p);                                                      \
             return cudaGetLastError();                                                                \
         };                                                                                            \
-        switch (nv) {                                                                                 \
-        case 1: return run(exec_tile_kernel<MR, 1, V, B, C>);                                         \
-        case 2: return run(exec_tile_kernel<MR, 2, V, B, C>);                                         \
-        case 4: return run(exec_tile_kernel<MR, 4, V, B, C>);                                         \
-        case 8: {                                                                                     \
-            auto k8 = tile_nv8_kernel<MR, V, B, C>();                                                 \
-            return k8 ? run(k8) : cudaErrorInvalidValue;                                              \
-        }                                                                                             \
-        default: return cudaErrorInvalidValue;                                                        \
-        }                                                                                             \
+        auto pick = [&](auto gtag) -> cudaError_t {                                                   \
+            constexpr bool G = decltype(gtag)::value;                                                 \
+            switch (nv) {                                                                             \
+            case 1: return run(exec_tile_kernel<MR, 1, V, B, C, G>);                                  \
+            case 2: return run(exec_tile_kernel<MR, 2, V, B, C, G>);                                  \
+            case 4: return run(exec_tile_kernel<MR, 4, V, B, C, G>);                                  \
+            case 8: {                                                                                 \
+                auto k8 = tile_nv8_kernel<MR, V, B, C, G>();                                          \
+                return k8 ? run(k8) : cudaErrorInvalidValue;                                          \
+            }                                                                                         \
+            default: return cudaErrorInvalidValue;                                                    \
+            }                                                                                         \
+        };                                                                                            \
+        return gen ? pick(std::true_type{}) : pick(std::false_type{});                                \
     }
 
 }  // namespace spreg
