@@ -122,3 +122,17 @@ def test_noalloc_rejects_more_launches_than_its_scratch(cuda):
     st = _lib.lib().spreg_execute_batched_noalloc(arr, n, _lib.stream_handle(None))
     assert st == _lib.SPREG_ERR_INVALID_ARG
     assert "at most 64" in _lib.last_error()
+
+
+@pytest.mark.parametrize("kw", [dict(rounds=2, nr=32), dict(balance=1), dict(staging=1)])
+def test_noalloc_refuses_the_b_tile_kernel_options(cuda, kw):
+    """The no-allocation entry point runs the batched kernel alone: panel rounds, the load-balanced
+    split and forced B tiles are refused with an error, nothing launched."""
+    m = Mapping.identity(4)
+    pm = PackedMatrix.from_dense(torch.from_numpy(synth.row_skew(256, 256, 0.9, seed=3)).cuda(), m, k_tile=64)
+    B = torch.ones((256, 64), device="cuda")
+    C = torch.zeros((256, 64), device="cuda")
+    st = _lib.lib().spreg_execute_batched_noalloc(_work([(pm, B, C, kw)]), 1, _lib.stream_handle(None))
+    assert st == _lib.SPREG_ERR_INVALID_ARG
+    assert "batched execution-layout kernel only" in _lib.last_error()
+    assert float(C.abs().sum()) == 0.0
