@@ -573,7 +573,8 @@ def ffn_sweep(dev, min_replicas: int = 96, steps: int = 20) -> list:
 
     Each point runs enough distinct replicas that their algorithmic bytes reach 4 x L2 (at least
     `min_replicas`) in one batched launch of the autotuner's register-tiled packing for that point
-    and storage (M_r, nanokernel set, N_r, K tile, CTA tiling; tuned on replica 0 as a batch of 8),
+    and storage (M_r, nanokernel set, N_r, K tile, CTA tiling, panel rounds; tuned on replica 0 as a
+    batch of 32, the six best-ranked candidates and the best of every family timed),
     replayed from a CUDA graph.  It reports algorithmic GB/s (2-byte values and B for the 16-bit
     forms) and GFLOP/s (2 nnz N), and checks replica 0 bit for bit against the oracle and against
     FP64.  Beside it, the FP32-accurate tensor-core hybrid with every panel on the tensor cores
@@ -616,7 +617,7 @@ def ffn_sweep(dev, min_replicas: int = 96, steps: int = 20) -> list:
             for name, vd, tdt in forms:
                 tkey = "f32" if vd == F32 else "bf16"
                 if tkey not in tuned:
-                    tuned[tkey] = tune(A0, 512, tkey, top=4, batch=8, device=dev, tc=False).best
+                    tuned[tkey] = tune(A0, 512, tkey, top=6, batch=32, device=dev, tc=False).best
                 c = tuned[tkey]
                 m = mapping_of(c.mr, c.mapping)
                 p0 = PackedMatrix.from_dense(torch.from_numpy(A0).to(dev), m, k_tile=c.k_tile, value_dtype=vd)
