@@ -337,24 +337,36 @@ def rank(mask: np.ndarray, n: int, dtype: str = "f32", costs: Optional[Costs] = 
 
 
 def _time_batched(pm, Bs, Cs, nr: int, reps: int = 5, warps: int = 0, rounds: int = 0) -> float:
-    """ns per SpMM of len(Bs) SpMMs of one packed matrix in one batched call (CUDA events)."""
+    """ns per SpMM of len(Bs) SpMMs of one packed matrix in one batched call, replayed from a CUDA graph
+    (CUDA events): device time, as a serving loop or a batched layer step replays it.  Timing the calls
+    themselves would add the host's planning per SpMM (tensor maps, problem tables), which at a few
+    microseconds per SpMM is as large as the device time and favours the kernels that plan less."""
     import torch
     from .packed import execute_batched
     work = [(pm, b, c, dict(nr=nr, warps=warps, rounds=rounds)) for b, c in zip(Bs, Cs)]
-    execute_batched(work)
-    s = torch.cuda.current_stream()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(s)
-    for _ in range(reps):
+    cur = torch.cuda.current_stream()
+    side = torch.cuda.Stream()
+    side.wait_stream(cur)
+    with torch.cuda.stream(side):
+        execute_batched(work)  # checks the arguments, configures the kernels before the capture
+    cur.wait_stream(side)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
         execute_batched(work)
-    e1.record(s)
+    g.replay()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(cur)
+    for _ in range(reps):
+        g.replay()
+    e1.record(cur)
     e1.synchronize()
     return e0.elapsed_time(e1) * 1e6 / (reps * len(Bs))
 
 
 def _time_tc(At, mapping: Mapping, n: int, dtype: str, fill: float, k_tile: int, nb: int, reps: int = 5) -> float:
     """ns per SpMM of the hybrid at threshold `fill`: nb SpMMs of A with distinct B as one HybridBatch
-    (one batched register-tiled launch, one tensor-core plan), CUDA events."""
+    (one batched register-tiled launch, one tensor-core plan), replayed from a CUDA graph, CUDA events."""
     import torch
     from . import _lib
     from .hybrid import HybridBatch, HybridMatrix
@@ -364,13 +376,22 @@ def _time_tc(At, mapping: Mapping, n: int, dtype: str, fill: float, k_tile: int,
     Bs = [torch.randn((At.shape[1], n), device=At.device).to(tdt) for _ in range(nb)]
     Cs = [torch.empty((At.shape[0], n), device=At.device) for _ in range(nb)]
     hb = HybridBatch([(h, b, c) for b, c in zip(Bs, Cs)])
-    hb.run()
-    s = torch.cuda.current_stream()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(s)
-    for _ in range(reps):
+    cur = torch.cuda.current_stream()
+    side = torch.cuda.Stream()
+    side.wait_stream(cur)
+    with torch.cuda.stream(side):
         hb.run()
-    e1.record(s)
+    cur.wait_stream(side)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()  # device time, as `_time_batched`
+    with torch.cuda.graph(g):
+        hb.run()
+    g.replay()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(cur)
+    for _ in range(reps):
+        g.replay()
+    e1.record(cur)
     e1.synchronize()
     return e0.elapsed_time(e1) * 1e6 / (reps * nb)
 

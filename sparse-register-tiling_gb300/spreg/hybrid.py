@@ -304,16 +304,26 @@ def tune_tc_fill(A, mapping: Mapping, n: int, fills=(1.01, 0.5, 0.3, 0.2, 0.1, 0
     for f in fills:
         h = HybridMatrix.from_dense(A, mapping, f, k_tile=k_tile, value_dtype=value_dtype)
         hb = HybridBatch([(h, b, c) for b, c in zip(Bs, Cs)])
-        for _ in range(3):  # warm-up: lazy set-up and clock ramp stay out of the timed calls
+        cur = torch.cuda.current_stream()
+        side = torch.cuda.Stream()
+        side.wait_stream(cur)
+        with torch.cuda.stream(side):
+            hb.run()  # lazy set-up outside the capture
+        cur.wait_stream(side)
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()  # device time: the batched launch's host planning stays out
+        with torch.cuda.graph(g):
             hb.run()
+        for _ in range(3):  # warm-up: clock ramp stays out of the timed replays
+            g.replay()
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
         for _ in range(reps):
-            hb.run()
+            g.replay()
         e1.record()
         torch.cuda.synchronize()
         out[float(f)] = e0.elapsed_time(e1) / reps * 1e3 / len(Bs)
-        del hb, h
+        del g, hb, h
     best = min(out, key=out.get)
     return {"us": out, "best_fill": best, "batch": len(Bs)}
