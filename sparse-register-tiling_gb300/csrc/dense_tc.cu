@@ -1118,10 +1118,12 @@ int tc_plan_fill(TcPlan &pl, int *status) {
         p.status = status;
         p.nprob = (int32_t)cnt;
         // Output tile width: as an item asks, else 128 when a problem is 128 columns or narrower, else
-        // the width with fewer waves of tiles over the SMs, a 128-wide tile counted as 0.55 of a
-        // 256-wide one (measured: the same split products ran 110.5 us in 128-wide tiles against
-        // 106.3 us in half as many 256-wide ones).  A single wide product then takes 128-wide tiles
-        // when its 256-wide tiles leave most of a last wave idle; a launch of many takes 256.
+        // 256 -- unless the launch has at most two waves of 256-wide tiles and 128-wide ones take
+        // fewer waves, a 128-wide tile counted as 0.6 of a 256-wide one (at K = 512 the same split
+        // products ran 110.5 us in 128-wide tiles against 106.3 us in half as many 256-wide ones; at
+        // long K the narrow tiles cost relatively more: a 4096^3 BF16 product ran 149 us in 1024
+        // 128-wide tiles against 98 us in 512 256-wide ones).  A single wide product then takes
+        // 128-wide tiles when its 256-wide tiles leave most of a last wave idle.
         int64_t min_n = INT64_MAX, tiles128 = 0, tiles256 = 0;
         int hint = 0;
         for (size_t j = 0; j < cnt; ++j) {
@@ -1134,7 +1136,8 @@ int tc_plan_fill(TcPlan &pl, int *status) {
                 if (!hint && (pl.items[m].tile_n == 128 || pl.items[m].tile_n == 256)) hint = pl.items[m].tile_n;
         }
         const int64_t sms = pl.sms > 0 ? pl.sms : 148;
-        const bool narrow = 0.55 * (double)((tiles128 + sms - 1) / sms) < (double)((tiles256 + sms - 1) / sms);
+        const bool narrow = tiles256 <= 2 * sms &&
+                            0.6 * (double)((tiles128 + sms - 1) / sms) < (double)((tiles256 + sms - 1) / sms);
         const int bn = hint ? hint : (min_n <= 128 || narrow ? 128 : 256);
         int64_t tiles = 0;
         for (size_t j = 0; j < cnt; ++j) {
