@@ -111,7 +111,11 @@ struct DevFacts {
     int *flags = nullptr;      // load-balance flags, handed out round robin in blocks
 };
 constexpr int kCounters = 4096;
-constexpr int kLbFlags = 1 << 16;  // flags of the load-balanced splits in flight
+// Flags of the load-balanced splits, handed out round robin in blocks: a block is reused only
+// after the pool has gone round (at least kLbFlags / kLbMaxBlock launches later), as the work
+// counters are after kCounters launches.
+constexpr int kLbFlags = 1 << 20;
+constexpr int kLbMaxBlock = 1 << 14;  // flags of one launch's splits at most
 
 namespace {
 DevFacts g_facts[64];
@@ -154,7 +158,7 @@ int *next_counter(DevFacts *f) {
     return f->counters + (next.fetch_add(1) % kCounters);
 }
 
-// A block of n contiguous load-balance flags (n <= kLbFlags / 4), round robin as the counters: its
+// A block of n contiguous load-balance flags (n <= kLbMaxBlock), round robin as the counters: its
 // offset in f->flags.
 int32_t next_flags(int64_t n) {
     static std::atomic<unsigned long long> next{0};
@@ -333,7 +337,7 @@ void balance_of(const spreg_packed *a, int W, int64_t S, int64_t slots, int64_t 
     // the longest job after the split is the first unsplit group's (or half the heaviest one's): skip a
     // split that would shorten it by less than a fifth (the combine and the scratch cost more)
     if (g < groups && 5 * a->work_desc[(size_t)(g * W)] > 4 * top) return;
-    if (std::min<int64_t>(g * W, P) * S > kLbFlags / 4) return;  // one flag per split (panel, strip)
+    if (std::min<int64_t>(g * W, P) * S > kLbMaxBlock) return;  // one flag per split (panel, strip)
     *heavy = std::min<int64_t>(g * W, P);
     *split = (int32_t)(T / 2);
 }
