@@ -238,7 +238,10 @@ typedef struct {
                              (panel, strip): C = C + hi, one FP32 add per element, the epilogue after
                              it, all in one launch.  Needs a K-tiled pack (T >= 2) of FP32 or BF16 values, FP32 C
                              and the B-tile kernel (b_staging 0 or 1); other packs run unsplit.
-                             spreg_load_balance_plan reports the split. */
+                             The two halves meet through flags from a per-device pool that a call
+                             reuses only after at least 64 others (as the executors' work counters
+                             after 4096 launches), so fewer load-balanced calls than that may be in
+                             flight on the GPU at once.  spreg_load_balance_plan reports the split. */
     int32_t reserved;     /* 0 */
 } spreg_exec_args;
 
