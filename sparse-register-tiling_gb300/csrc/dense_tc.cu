@@ -695,9 +695,12 @@ struct SplitBItem {
 };
 
 // One CTA of 16 warps per (64-column chunk, item): lane l of each warp takes columns 2l and 2l + 1 of
-// the chunk, warp w the rows w, w + 16, ...; four rows' loads are issued before they are used.  A
-// column's maximum over k (shared-memory reduction over the warps), then the split.
+// the chunk, warp w the rows w, w + 16, ...  A column's maximum over k (shared-memory reduction over
+// the warps), then the split.  RPT > 0 (k64 <= 16 RPT): each thread's RPT rows are loaded once, all
+// in flight together, and stay in registers from the maximum to the split (one read of B); RPT = 0:
+// two passes over B, eight rows' loads in flight per thread.
 constexpr int SPLIT_WARPS = 16;
+template <int RPT>
 __global__ void __launch_bounds__(32 * SPLIT_WARPS) split_cols_kernel(const SplitBItem *__restrict__ items) {
     const SplitBItem it = items[blockIdx.y];
     const int j0 = blockIdx.x * 64;
@@ -719,16 +722,28 @@ __global__ void __launch_bounds__(32 * SPLIT_WARPS) split_cols_kernel(const Spli
             if (c1) x1 = __ldg(row + j + 1);
         }
     };
-    constexpr int STEP = 4 * SPLIT_WARPS;  // rows per unrolled iteration of the CTA
+    constexpr int U = 8;                   // rows per unrolled iteration of a thread (RPT = 0)
+    constexpr int STEP = U * SPLIT_WARPS;  // rows per unrolled iteration of the CTA
+    float xs[RPT > 0 ? RPT : 1][2];
     float m0 = 0.0f, m1 = 0.0f;
-    for (int r = w; r < it.k; r += STEP) {
-        float x[4][2];
+    if constexpr (RPT > 0) {
 #pragma unroll
-        for (int u = 0; u < 4; ++u) load2(r + u * SPLIT_WARPS, x[u][0], x[u][1]);
+        for (int u = 0; u < RPT; ++u) load2(w + u * SPLIT_WARPS, xs[u][0], xs[u][1]);
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            m0 = fmaxf(m0, fabsf(x[u][0]));
-            m1 = fmaxf(m1, fabsf(x[u][1]));
+        for (int u = 0; u < RPT; ++u) {
+            m0 = fmaxf(m0, fabsf(xs[u][0]));
+            m1 = fmaxf(m1, fabsf(xs[u][1]));
+        }
+    } else {
+        for (int r = w; r < it.k; r += STEP) {
+            float x[U][2];
+#pragma unroll
+            for (int u = 0; u < U; ++u) load2(r + u * SPLIT_WARPS, x[u][0], x[u][1]);
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                m0 = fmaxf(m0, fabsf(x[u][0]));
+                m1 = fmaxf(m1, fabsf(x[u][1]));
+            }
         }
     }
     __shared__ float red[SPLIT_WARPS][64];
@@ -750,24 +765,35 @@ __global__ void __launch_bounds__(32 * SPLIT_WARPS) split_cols_kernel(const Spli
         if (c1) it.inv_scale[j + 1] = pow2f(-s1);
     }
     const bool vec_out = ((reinterpret_cast<uintptr_t>(it.hi + j0) | (uintptr_t)(it.ld * 2)) % 4) == 0;
-    for (int r = w; r < it.k64; r += STEP) {
-        float x[4][2];
+    auto put = [&](int rr, float x0, float x1) {
+        __half h0, l0, h1, l1;
+        split_half(x0 * sc0, h0, l0);
+        split_half(x1 * sc1, h1, l1);
+        __half *hp = it.hi + (int64_t)rr * it.ld + j, *lp = hp + it.lo_off;
+        if (vec_out && c1) {
+            *reinterpret_cast<__half2 *>(hp) = __halves2half2(h0, h1);
+            *reinterpret_cast<__half2 *>(lp) = __halves2half2(l0, l1);
+        } else {
+            if (c0) { hp[0] = h0; lp[0] = l0; }
+            if (c1) { hp[1] = h1; lp[1] = l1; }
+        }
+    };
+    if constexpr (RPT > 0) {
 #pragma unroll
-        for (int u = 0; u < 4; ++u) load2(r + u * SPLIT_WARPS, x[u][0], x[u][1]);
+        for (int u = 0; u < RPT; ++u) {
+            const int rr = w + u * SPLIT_WARPS;
+            if (rr < it.k64) put(rr, xs[u][0], xs[u][1]);
+        }
+    } else {
+        for (int r = w; r < it.k64; r += STEP) {
+            float x[U][2];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            const int rr = r + u * SPLIT_WARPS;
-            if (rr >= it.k64) break;
-            __half h0, l0, h1, l1;
-            split_half(x[u][0] * sc0, h0, l0);
-            split_half(x[u][1] * sc1, h1, l1);
-            __half *hp = it.hi + (int64_t)rr * it.ld + j, *lp = hp + it.lo_off;
-            if (vec_out && c1) {
-                *reinterpret_cast<__half2 *>(hp) = __halves2half2(h0, h1);
-                *reinterpret_cast<__half2 *>(lp) = __halves2half2(l0, l1);
-            } else {
-                if (c0) { hp[0] = h0; lp[0] = l0; }
-                if (c1) { hp[1] = h1; lp[1] = l1; }
+            for (int u = 0; u < U; ++u) load2(r + u * SPLIT_WARPS, x[u][0], x[u][1]);
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int rr = r + u * SPLIT_WARPS;
+                if (rr >= it.k64) break;
+                put(rr, x[u][0], x[u][1]);
             }
         }
     }
@@ -896,6 +922,7 @@ struct TcPlan {
     int32_t nprep = 0;
     int64_t max_kt = 1, max_nt = 1;       // transpose grid
     int64_t max_ct = 1;                   // split grid: 64-column chunks
+    int64_t max_k64 = 0;                  // split: the longest K (rounded up to 64) of the prepared B
     int64_t maps_off = 0;                 // 2 tensor maps per group
     std::vector<TcLaunch> launches;
     char *scratch = nullptr;
@@ -1018,6 +1045,7 @@ int tc_plan_build(TcPlan &pl) {
             const TcItem &it = pl.items[m];
             if (split) {
                 pl.max_ct = std::max<int64_t>(pl.max_ct, (it.n + 63) / 64);
+                pl.max_k64 = std::max<int64_t>(pl.max_k64, g.k64);
             } else {
                 pl.max_kt = std::max<int64_t>(pl.max_kt, ((it.k + 7) / 8 * 8 + 63) / 64);
                 pl.max_nt = std::max<int64_t>(pl.max_nt, (it.n + 63) / 64);
@@ -1220,8 +1248,14 @@ int tc_plan_launch(const TcPlan &pl, cudaStream_t stream) {
     const char *tabd = pl.scratch + pl.tab_base;
     if (pl.nprep > 0) {
         if (pl.split)
-            split_cols_kernel<<<dim3((unsigned)pl.max_ct, (unsigned)pl.nprep), 32 * SPLIT_WARPS, 0, stream>>>(
-                reinterpret_cast<const SplitBItem *>(tabd + pl.prep_off));
+        {
+            // rows of a column block held in registers when K is short (one read of B)
+            const dim3 grid((unsigned)pl.max_ct, (unsigned)pl.nprep);
+            const SplitBItem *items = reinterpret_cast<const SplitBItem *>(tabd + pl.prep_off);
+            if (pl.max_k64 <= 16 * SPLIT_WARPS) split_cols_kernel<16><<<grid, 32 * SPLIT_WARPS, 0, stream>>>(items);
+            else if (pl.max_k64 <= 32 * SPLIT_WARPS) split_cols_kernel<32><<<grid, 32 * SPLIT_WARPS, 0, stream>>>(items);
+            else split_cols_kernel<0><<<grid, 32 * SPLIT_WARPS, 0, stream>>>(items);
+        }
         else
             transpose_items_kernel<<<dim3((unsigned)pl.max_kt, (unsigned)pl.max_nt, (unsigned)pl.nprep), 256, 0,
                                      stream>>>(reinterpret_cast<const TransposeItem *>(tabd + pl.prep_off));
