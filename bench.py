@@ -496,6 +496,69 @@ def load_balance_leg(dev) -> list:
     return rows
 
 
+def sparse_end_leg(dev, nb: int = 32, reps: int = 10) -> dict:
+    """The memory-bound end of the FFN workload: 2048 x 512 @ 98 % row skew (sigma 0.5, values N(0, 0.02)),
+    N = 512, FP32, nb SpMMs of one A with distinct B per batched launch, replayed from a CUDA graph,
+    through three paths: the gather kernel (untiled M_r = 8 pack, 747f9 set, 128-column strips, 4 warps
+    per CTA), panel rounds (64-column strips, 16 rounds of 15 panels on a resident whole-K strip), and
+    the FP32-accurate tensor-core hybrid (every panel).  Each path's first launch is an NVTX range
+    sparse_end_<path> (for ncu --nvtx).  Register-tiled paths are checked bit for bit against the
+    oracle, the hybrid against its tolerance."""
+    import torch
+    from oracle import oracle as O
+    from spreg import F32, Mapping, PackedMatrix, execute_batched, synth
+    from spreg.hybrid import HybridBatch, HybridMatrix
+    A = synth.row_skew(2048, 512, 0.98, seed=7098, sigma=0.5, std=0.02)
+    Bs = [torch.from_numpy(synth.dense(512, 512, seed=7600 + i)).to(dev) for i in range(nb)]
+    Cs = [torch.empty((2048, 512), device=dev) for _ in range(nb)]
+    m8 = Mapping.load("747f9")
+    peak, _ = measured_peaks()
+
+    def graph_time(run, tag):
+        cur = torch.cuda.current_stream()
+        side = torch.cuda.Stream()
+        side.wait_stream(cur)
+        with torch.cuda.stream(side):
+            run()
+        cur.wait_stream(side)
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_push(tag)
+        run()
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            run()
+        for _ in range(3):
+            g.replay()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(reps):
+            g.replay()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) * 1e3 / reps / nb
+
+    out = {"workload": "A 2048x512 @98% row skew, N=512, FP32, %d SpMMs of one A per launch, CUDA graph" % nb}
+    pm = PackedMatrix.from_dense(torch.from_numpy(A).to(dev), m8)
+    nbytes = pm.algorithmic_bytes(512)
+    want = O.Packed(O.Tables.of(m8), A).execute(Bs[0].cpu().numpy())
+    for name, kw in (("gather", dict(nr=128, warps=4)), ("rounds", dict(nr=64, rounds=16))):
+        work = [(pm, b, c, kw) for b, c in zip(Bs, Cs)]
+        us = graph_time(lambda: execute_batched(work), f"sparse_end_{name}")
+        got = Cs[0].cpu().numpy()
+        out[name] = {"us_per_spmm": us, "gbs": nbytes / us / 1e3, "frac_of_measured_hbm": nbytes / us / 1e3 / peak,
+                     "plan": pm.explain(Bs[0], Cs[0], **kw),
+                     "bit_exact_vs_oracle": bool(np.array_equal(got.view(np.uint32), want.view(np.uint32)))}
+    h = HybridMatrix.from_dense(torch.from_numpy(A).to(dev), m8, 0.0, value_dtype=F32)
+    hb = HybridBatch([(h, b, c) for b, c in zip(Bs, Cs)])
+    us = graph_time(hb.run, "sparse_end_tensor_cores")
+    out["tensor_cores"] = {"us_per_spmm": us, "gbs": nbytes / us / 1e3, "frac_of_measured_hbm": nbytes / us / 1e3 / peak,
+                           "rel_err_vs_oracle": float(O.rel_err(Cs[0].cpu().numpy(), want))}
+    return out
+
+
 def config1_leg(dev) -> dict:
     """The minimum slice as the workload states it: A 512 x 512 at 80 % Bernoulli sparsity, N(0, 1)
     values, B 512 x 256 N(0, 1), M_r = 4, identity mapping 61fee, N_r = 64.  GPU: one SpMM per call
@@ -1243,6 +1306,7 @@ def main():
                if (lead and args.dtype == "f32" and args.extras) else None)
     cfg1 = config1_leg(dev) if (lead and args.extras) else None
     lbal = load_balance_leg(dev) if (lead and args.extras) else None
+    sparse_end = sparse_end_leg(dev) if (lead and args.extras) else None
     serving = serving_bench(args, dev) if (lead and args.serving) else None
     precision = (precision_suite(dev, args.precision_only, args.precision_configs)
                  if (lead and args.precision) else None)
@@ -1286,7 +1350,7 @@ def main():
                 "cpu_baseline": cpu, "e2e": e2e, "serving": serving,
                 "precision": precision, "batched_layers": layers, "tensor_cores": tensor_cores,
                 "ffn_sparsity_sweep": sweep, "gpu_csr_baseline": csr_leg, "config1_minimum_slice": cfg1,
-                "load_balanced_single_spmm": lbal,
+                "load_balanced_single_spmm": lbal, "sparse_end_kernels": sparse_end,
                 "clocks": clocks, "gpu_launches": launches,
                 "parity": parity}
         print(json.dumps(line))
