@@ -540,7 +540,7 @@ def sparse_end_leg(dev, nb: int = 32, reps: int = 10) -> dict:
         torch.cuda.synchronize()
         return e0.elapsed_time(e1) * 1e3 / reps / nb
 
-    out = {"workload": "A 2048x512 @98% row skew, N=512, FP32, %d SpMMs of one A per launch, CUDA graph" % nb}
+    out = {"workload": f"A 2048x512 @98% row skew, N=512, FP32, {nb} SpMMs of one A per launch, CUDA graph"}
     pm = PackedMatrix.from_dense(torch.from_numpy(A).to(dev), m8)
     nbytes = pm.algorithmic_bytes(512)
     want = O.Packed(O.Tables.of(m8), A).execute(Bs[0].cpu().numpy())
