@@ -384,8 +384,11 @@ int plan_call(const spreg_packed *a, const spreg_exec_args *args, CallPlan *cp, 
     case 32: nv = 1; break;
     case 64: nv = 2; break;
     case 128: nv = 4; break;
-    case 256: nv = 4; break;  // 256-column strips where the B-tile kernel takes 16-bit B (below), else 128
-    default: SPREG_FAIL(SPREG_ERR_INVALID_ARG, "nr must be 0, 32, 64, 128 or 256 (got %d)", args->nr);
+    // 256 and 512: wide strips where a kernel has them (below: the B-tile kernel with 16-bit B, the
+    // gather kernel with FP32), else 128
+    case 256: nv = 4; break;
+    case 512: nv = 4; break;
+    default: SPREG_FAIL(SPREG_ERR_INVALID_ARG, "nr must be 0, 32, 64, 128, 256 or 512 (got %d)", args->nr);
     }
     const size_t bsz = dtype_bytes(args->b_dtype), csz = dtype_bytes(args->c_dtype);
     while (nv > 1 && !(aligned(args->b, bsz * nv) && args->ldb % nv == 0 && aligned(args->c, csz * nv) &&
@@ -455,12 +458,20 @@ int plan_call(const spreg_packed *a, const spreg_exec_args *args, CallPlan *cp, 
         args->b_staging == 1 || rounds > 1 || lb || (args->b_staging == 0 && tile_base_ok && args->meta_staging != 2 &&
                                  !cp->stream_kernel && a->geom.T > 1 && args->n <= INT32_MAX &&
                                  staged_rows * 32 * nv * (int64_t)bsz <= 64 * 1024);
-    if (tile_kernel && bsz == 2 && in.mr <= 4 && nv == 4 && (args->nr == 0 || args->nr == 256) && args->n >= 256 &&
+    if (tile_kernel && bsz == 2 && in.mr <= 4 && nv == 4 && (args->nr == 0 || args->nr >= 256) && args->n >= 256 &&
         (rounds == 1 || strip_fits(8)) &&
         staged_rows * 256 * (int64_t)bsz <= 64 * 1024 && aligned(args->b, 16) && args->ldb % 8 == 0 &&
         aligned(args->c, csz * 8) && args->ldc % 8 == 0 &&
-        (args->nr == 256 || (hot_set && in.num_panels * (args->n / 256) + others1 / 8 >= (int64_t)f->sms * 8)))
+        (args->nr >= 256 || (hot_set && in.num_panels * (args->n / 256) + others1 / 8 >= (int64_t)f->sms * 8)))
         nv = 8;
+    // Wide FP32 strips in the gather kernel (nr = 256: NV = 8; nr = 512 and M_r <= 4: NV = 16), lanes
+    // interleaved by 16-byte quarters: at high sparsity an entry's index, value and address work is
+    // shared by 8 or 16 columns a lane.  Whole strips only; columns past the last one run as the
+    // 32-column tail launch.
+    const bool gather_wide = (args->nr == 256 || args->nr == 512) && !tile_kernel && !cp->stream_kernel &&
+                             combo == COMBO_F32 && nv == 4 && args->n >= 256 && aligned(args->b, 16) &&
+                             args->ldb % 4 == 0 && aligned(args->c, 16) && args->ldc % 4 == 0;
+    if (gather_wide) nv = args->nr == 512 && in.mr <= 4 && args->n >= 512 ? 16 : 8;
     cp->nv = nv;
     const int64_t n_main = (args->n / (32 * nv)) * (32 * nv);
     int64_t lb_heavy = 0;
@@ -504,8 +515,8 @@ int plan_call(const spreg_packed *a, const spreg_exec_args *args, CallPlan *cp, 
     // b_staging = 0 picks the tile kernel for K-tiled packs whose stage leaves room for all 16
     // consumer warps (64 KB of B per stage): measured faster than the gather kernel there (FP32,
     // 2048 x 512 @ 90 %, K_c = 128: 13.2 vs 13.8 us per SpMM).  It never fails in that mode.
-    const bool auto_tile = args->b_staging == 0 && tile_base_ok && args->meta_staging != 2 && !cp->stream_kernel &&
-                           a->geom.T > 1 && args->n <= INT32_MAX &&
+    const bool auto_tile = args->b_staging == 0 && !gather_wide && tile_base_ok && args->meta_staging != 2 &&
+                           !cp->stream_kernel && a->geom.T > 1 && args->n <= INT32_MAX &&
                            staged_rows * 32 * nv * (int64_t)bsz <= 64 * 1024;
     if (args->b_staging == 1 || rounds > 1 || lb || auto_tile) {
         const bool main_ok = !cp->has_main || rounds > 1 || tile_rows_ok(nv);

@@ -182,6 +182,43 @@ template <int NV, class TB> struct GlobalB {
     }
 };
 
+// FP32 strips of 256 and 512 columns (NV = 8, 16) in the gather kernel.  Lane l holds columns
+// 4l .. 4l + 3 of each 128-column quarter of the strip (element j is column 128 (j / 4) + 4l + j % 4),
+// so every 16-byte load or store of the warp covers 512 contiguous bytes: whole 128-byte lines, one
+// L1 wavefront each, where NV contiguous columns a lane would spread each instruction over 32 NV
+// bytes.  At high sparsity an entry's index, value and address work is then shared by 8 or 16
+// columns a lane instead of 4.
+template <int NV> struct WideIO {
+    static_assert(NV % 4 == 0, "wide strips hold whole float4 quarters");
+    __device__ static void load(const float *__restrict__ p, float (&b)[NV]) {
+#pragma unroll
+        for (int i = 0; i < NV / 4; ++i) {
+            const float4 t = __ldg(reinterpret_cast<const float4 *>(p + 128 * i));
+            b[4 * i] = t.x; b[4 * i + 1] = t.y; b[4 * i + 2] = t.z; b[4 * i + 3] = t.w;
+        }
+    }
+    __device__ static void load_plain(const float *p, float (&b)[NV]) {
+#pragma unroll
+        for (int i = 0; i < NV / 4; ++i) {
+            const float4 t = *reinterpret_cast<const float4 *>(p + 128 * i);
+            b[4 * i] = t.x; b[4 * i + 1] = t.y; b[4 * i + 2] = t.z; b[4 * i + 3] = t.w;
+        }
+    }
+    __device__ static void store(float *p, const float (&o)[NV]) {
+#pragma unroll
+        for (int i = 0; i < NV / 4; ++i)
+            *reinterpret_cast<float4 *>(p + 128 * i) = make_float4(o[4 * i], o[4 * i + 1], o[4 * i + 2], o[4 * i + 3]);
+    }
+};
+
+template <int NV> struct GlobalBWide {
+    const float *p;  // B + this lane's first column
+    int64_t ld;
+    bool valid;      // wide strips are whole: every lane is valid
+    __device__ __forceinline__ void load(int k, float (&b)[NV]) const { WideIO<NV>::load(p + (int64_t)k * ld, b); }
+    __device__ __forceinline__ void load(int k, BSeg<NV, float> &b) const { load(k, b.f); }
+};
+
 // ------------------------------------------------------------------ metadata streams
 // A unit's column indices, values and nkern_counts are each read front to back.  A Stream keeps a
 // 64-element window of one of them in two registers per lane (element i of the window is lane
@@ -776,7 +813,7 @@ __device__ __forceinline__ void run_group_pat(const int n, uint32_t cs, uint32_t
                                               float (&acc)[MR][NV]) {
     constexpr uint32_t VSTEP = 4u * (uint32_t)sizeof(TV) * (uint32_t)cpopc(PAT);
     const int full = n >> 2;
-    if constexpr (NV >= 8) {
+    if constexpr (NV >= 8 && sizeof(TV) == 2) {
         run_group_wide<PAT, MR, NV, TV>(PAT, n, cs, vs, bl, acc);
         return;
     } else if constexpr (NV >= 4) {
@@ -852,7 +889,7 @@ __device__ __forceinline__ void run_group_x(const int pat, const int n, uint32_t
             }
         }
     }
-    if constexpr (NV >= 8) {
+    if constexpr (NV >= 8 && sizeof(TV) == 2) {
         run_group_wide<0, MR, NV, TV>(pat, n, cs, vs, bl, acc);
         return;
     }
@@ -1009,7 +1046,7 @@ __device__ __forceinline__ void issue_job(const BatchParams &bp, const XJob &j, 
 }
 
 // C tile init / store for one (problem, panel, strip).
-template <int MR, int NV, class TV, class TC>
+template <int MR, int NV, class TV, class TC, class IO = VecIO<NV, TC>>
 __device__ __forceinline__ void x_acc_init(const XProblem &pr, int64_t row0, int64_t col0, bool valid,
                                            float (&acc)[MR][NV]) {
     constexpr bool SCALED = std::is_same<TV, __half>::value;
@@ -1021,10 +1058,10 @@ __device__ __forceinline__ void x_acc_init(const XProblem &pr, int64_t row0, int
         const TC *C = reinterpret_cast<const TC *>(pr.C);
 #pragma unroll
         for (int r = 0; r < MR; ++r)
-            if (row0 + r < pr.M) VecIO<NV, TC>::load_plain(C + (row0 + r) * pr.ldc + col0, acc[r]);
+            if (row0 + r < pr.M) IO::load_plain(C + (row0 + r) * pr.ldc + col0, acc[r]);
     }
 }
-template <int MR, int NV, class TV, class TC>
+template <int MR, int NV, class TV, class TC, class IO = VecIO<NV, TC>>
 __device__ __forceinline__ void x_store(const XProblem &pr, int64_t gp, int64_t row0, int64_t col0, bool valid,
                                         const float (&acc)[MR][NV]) {
     if (!valid) return;
@@ -1041,7 +1078,7 @@ __device__ __forceinline__ void x_store(const XProblem &pr, int64_t gp, int64_t 
         if (SCALED) {
             if (pr.load_c) {
                 float cin[NV];
-                VecIO<NV, TC>::load_plain(cp, cin);
+                IO::load_plain(cp, cin);
 #pragma unroll
                 for (int j = 0; j < NV; ++j) o[j] = fmaf(o[j], s, cin[j]);
             } else {
@@ -1053,12 +1090,18 @@ __device__ __forceinline__ void x_store(const XProblem &pr, int64_t gp, int64_t 
 #pragma unroll
             for (int j = 0; j < NV; ++j) o[j] = fmaxf(o[j], 0.0f);
         }
-        VecIO<NV, TC>::store(cp, o);
+        IO::store(cp, o);
     }
 }
 
 template <int MR, int NV, class TV, class TB, class TC>
 __global__ void __launch_bounds__(256, 1) exec_batch_kernel(const __grid_constant__ BatchParams bp) {
+    // NV = 8 and 16: FP32 strips of 256 and 512 columns in the interleaved lane layout (WideIO)
+    constexpr bool WIDE = NV >= 8;
+    static_assert(!WIDE || (sizeof(TV) == 4 && sizeof(TB) == 4 && sizeof(TC) == 4),
+                  "wide gather strips are FP32 values, B and C");
+    using IO = std::conditional_t<WIDE, WideIO<NV>, VecIO<NV, TC>>;
+    using BL = std::conditional_t<WIDE, GlobalBWide<NV>, GlobalB<NV, TB>>;
     extern __shared__ __align__(128) unsigned char smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(smem);
@@ -1090,10 +1133,10 @@ __global__ void __launch_bounds__(256, 1) exec_batch_kernel(const __grid_constan
         if (b) ph1 ^= 1u; else ph0 ^= 1u;
         const XProblem &pr = bp.prob[j.pi];
         const int64_t row0 = j.gp * MR;
-        const int64_t col0 = pr.col_begin + (int64_t)j.strip * (32 * NV) + (int64_t)lane * NV;
+        const int64_t col0 = pr.col_begin + (int64_t)j.strip * (32 * NV) + (int64_t)lane * (WIDE ? 4 : NV);
         const bool valid = col0 < pr.col_end;
-        if (j.t == 0) x_acc_init<MR, NV, TV, TC>(pr, row0, col0, valid, acc);
-        const GlobalB<NV, TB> bl{reinterpret_cast<const TB *>(pr.B) + col0, pr.ldb, valid};
+        if (j.t == 0) x_acc_init<MR, NV, TV, TC, IO>(pr, row0, col0, valid, acc);
+        const BL bl{reinterpret_cast<const TB *>(pr.B) + col0, pr.ldb, valid};
         const uint32_t G = lds_u32(buf);
 #pragma unroll 1
         for (uint32_t g = 0; g < G; ++g) {
@@ -1106,7 +1149,7 @@ __global__ void __launch_bounds__(256, 1) exec_batch_kernel(const __grid_constan
         issue_job(bp, jn, buf, bar, lane);
         last = jn;
         if (b) j1 = jn; else j0 = jn;
-        if (j.t == pr.T - 1) x_store<MR, NV, TV, TC>(pr, j.gp, row0, col0, valid, acc);
+        if (j.t == pr.T - 1) x_store<MR, NV, TV, TC, IO>(pr, j.gp, row0, col0, valid, acc);
     }
 }
 
@@ -1122,6 +1165,15 @@ template <> struct ComboTypes<COMBO_F16_F32OUT> { using V = __half; using B = __
 
 // Largest dynamic shared memory a staged-strip CTA may use (opt-in limit of sm_100-class parts).
 constexpr int kMaxSmem = 227 * 1024;
+
+// FP32 strips of 256 (NV = 8) and 512 columns (NV = 16, M_r <= 4) in the gather kernel.
+using BatchKernelPtr = void (*)(BatchParams);
+template <int MR, int NV, class V, class B, class C> inline BatchKernelPtr wide_batch_kernel() {
+    if constexpr (sizeof(V) == 4 && sizeof(B) == 4 && sizeof(C) == 4 && (NV == 8 || MR <= 4))
+        return exec_batch_kernel<MR, NV, V, B, C>;
+    else
+        return nullptr;
+}
 
 template <int MR, int COMBO>
 cudaError_t launch_exec(const ExecParams &p, int nv, dim3 grid, int threads, cudaStream_t s);
@@ -1148,7 +1200,7 @@ cudaError_t launch_exec_batch(const BatchParams &p, int nv, unsigned grid, int t
         using V = ComboTypes<COMBO>::V;                                                               \
         using B = ComboTypes<COMBO>::B;                                                               \
         using C = ComboTypes<COMBO>::C;                                                               \
-        static std::atomic<bool> configured[64][5];                                                           \
+        static std::atomic<bool> configured[64][17];                                                          \
         int dev = 0;                                                                                  \
         cudaGetDevice(&dev);                                                                          \
         auto run = [&](auto kern) -> cudaError_t {                                                    \
@@ -1165,6 +1217,14 @@ cudaError_t launch_exec_batch(const BatchParams &p, int nv, unsigned grid, int t
         case 1: return run(exec_batch_kernel<MR, 1, V, B, C>);                                        \
         case 2: return run(exec_batch_kernel<MR, 2, V, B, C>);                                        \
         case 4: return run(exec_batch_kernel<MR, 4, V, B, C>);                                        \
+        case 8: {                                                                                     \
+            auto k8 = wide_batch_kernel<MR, 8, V, B, C>();                                            \
+            return k8 ? run(k8) : cudaErrorInvalidValue;                                              \
+        }                                                                                             \
+        case 16: {                                                                                    \
+            auto k16 = wide_batch_kernel<MR, 16, V, B, C>();                                          \
+            return k16 ? run(k16) : cudaErrorInvalidValue;                                            \
+        }                                                                                             \
         default: return cudaErrorInvalidValue;                                                        \
         }                                                                                             \
     }

@@ -54,7 +54,8 @@ MAPPINGS_FOR_MR = {2: ("identity",), 4: ("identity",), 8: ("identity", "400fa", 
 class Candidate:
     mr: int
     mapping: str     # "identity" or a mapping id
-    nr: int          # strip width: 32, 64, 128 or (16-bit B, K_c <= 128) 256 columns
+    nr: int          # strip width: 32, 64, 128, or wide: 256 (16-bit B with K_c <= 128, or FP32 untiled
+                     # packs on the gather kernel) and 512 (FP32 untiled, M_r <= 4) columns
     k_tile: int = 0  # K_c of the packing (0: one K tile)
     warps: int = 0   # CTA tiling (spreg_exec_args.warps_per_cta; 0: the executor's choice)
     tc_fill: float = 2.0  # panels with fill >= tc_fill on the tensor cores (> 1: none)
@@ -465,6 +466,19 @@ def tune(A: np.ndarray, n: int, dtype: str = "f32", top: int = 4, costs: Optiona
             by_name[c.name()] = c
             measured[c.name()] = time_reg(c)
     best_reg = by_name[min(measured, key=measured.get)]
+    if dtype == "f32" and n >= 256:
+        # wide FP32 strips of the gather kernel (untiled packs): 256 columns, 512 at M_r <= 4, each
+        # with the best-ranked nanokernel set of its M_r
+        first = {}
+        for _, c in ranked:
+            if c.k_tile == 0 and c.mr not in first:
+                first[c.mr] = c
+        for mr, c0 in sorted(first.items()):
+            for nr in ((256, 512) if mr <= 4 and n >= 512 else (256,)):
+                c = dataclasses.replace(c0, nr=nr, warps=4)
+                by_name[c.name()] = c
+                measured[c.name()] = time_reg(c)
+        best_reg = by_name[min(measured, key=measured.get)]
     if rounds:
         # panel rounds: the B-tile kernel with the strip of B for every K tile resident, for the best
         # packing at its strip width and the narrower ones (a strip that does not fit shared memory

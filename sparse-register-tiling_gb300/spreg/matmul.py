@@ -72,7 +72,7 @@ def nr_from_executor_id(executor_id: str) -> int:
     if not m:
         return 0
     nr = int(m.group(1)) // 32 * int(m.group(2))
-    return nr if nr in (32, 64, 128, 256) else 0
+    return nr if nr in (32, 64, 128, 256, 512) else 0
 
 
 class MatMulSpecialized:

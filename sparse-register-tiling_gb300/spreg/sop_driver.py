@@ -49,7 +49,7 @@ def panel_pattern_codes(panel_t: np.ndarray) -> np.ndarray:
 
 def _nr_of(acc: Acc) -> int:
     nr = acc.nr_floats
-    return nr if nr in (32, 64, 128, 256) else 0
+    return nr if nr in (32, 64, 128, 256, 512) else 0
 
 
 class SOPTile:
