@@ -26,9 +26,10 @@ B-tile kernel keeps a job's strip of B resident for that many rounds of panels) 
 threshold (`tc_fill`: panels whose fill reaches it run as dense tcgen05 products, `spreg.hybrid`).
 
 `tune` ranks every candidate with the model, times the best few on the device with the reference's
-timing protocol (`execute_timed`: median of repeated runs) or as a batch, then times the CTA tiling
-and the panel rounds of the best and the tensor-core thresholds (all panels; the densest tenth),
-and returns the fastest, so a poor model costs tuning time, not speed.
+timing protocol (`execute_timed`: median of repeated runs) or as a batch, then times the CTA tiling,
+(FP32) the gather kernel's wide strips, the panel rounds of the best and the tensor-core thresholds
+(all panels; the densest tenth), and returns the fastest, so a poor model costs tuning time, not
+speed.
 """
 from __future__ import annotations
 
@@ -421,7 +422,8 @@ def tune(A: np.ndarray, n: int, dtype: str = "f32", top: int = 4, costs: Optiona
     rank by the cost model, then time the ``top`` best on the device -- one SpMM at a time with
     the reference's protocol (execute_timed) when ``batch`` is 1, else ``batch`` SpMMs of A with
     distinct B in one batched launch, as a serving loop runs them.  Then (``warps``) the CTA tiling
-    of the best register-tiled candidate, (``rounds``) its panel rounds, and (``tc``) the tensor-core
+    of the best register-tiled candidate, (FP32, n >= 256) 256- and 512-column strips of untiled
+    packs on the gather kernel, (``rounds``) panel rounds, and (``tc``) the tensor-core
     thresholds: every panel, and the densest tenth of the panels, each timed as a batch of SpMMs
     through `spreg.hybrid`."""
     import torch
