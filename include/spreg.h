@@ -212,9 +212,10 @@ typedef struct {
     int32_t epilogue;    /* SPREG_EPILOGUE_* applied to the stored result */
     int32_t nr;          /* columns per warp strip: 32, 64, 128, 256 or 512; 0 = automatic.  256 and
                             512 are wide strips where a kernel has them, else 128: the B-tile kernel
-                            with 16-bit B (256), the gather kernel with FP32 values, B and C, 16-byte
+                            with 16-bit B (256); the gather kernel with FP32 values, B and C, 16-byte
                             aligned B and C with row strides in whole 16-byte units (256; 512 at
-                            M_r <= 4), its lanes holding interleaved 16-byte quarters of the strip */
+                            M_r <= 4), its lanes holding interleaved 16-byte quarters of the strip,
+                            and with 16-bit B at M_r <= 4 (256) */
     int32_t warps_per_cta; /* CTA tiling, 1..8; 0 = automatic: warps per CTA of the batched and
                               register-stream kernels (8 and 4 by default), consumer warps (row panels
                               per job) of the B-tile kernel (15 by default) */

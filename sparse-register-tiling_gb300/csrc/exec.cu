@@ -472,6 +472,12 @@ int plan_call(const spreg_packed *a, const spreg_exec_args *args, CallPlan *cp, 
                              combo == COMBO_F32 && nv == 4 && args->n >= 256 && aligned(args->b, 16) &&
                              args->ldb % 4 == 0 && aligned(args->c, 16) && args->ldc % 4 == 0;
     if (gather_wide) nv = args->nr == 512 && in.mr <= 4 && args->n >= 512 ? 16 : 8;
+    // 16-bit B in the gather kernel: 256-column strips (NV = 8, one 16-byte load of 8 columns a
+    // lane and entry, the mixed-precision FMA of the B-tile kernel's wide strips) at M_r <= 4
+    const bool gather_wide16 = (args->nr == 256 || args->nr == 512) && !tile_kernel && !cp->stream_kernel &&
+                               bsz == 2 && in.mr <= 4 && nv == 4 && args->n >= 256 && aligned(args->b, 16) &&
+                               args->ldb % 8 == 0 && aligned(args->c, csz * 8) && args->ldc % 8 == 0;
+    if (gather_wide16) nv = 8;
     cp->nv = nv;
     const int64_t n_main = (args->n / (32 * nv)) * (32 * nv);
     int64_t lb_heavy = 0;
@@ -515,7 +521,8 @@ int plan_call(const spreg_packed *a, const spreg_exec_args *args, CallPlan *cp, 
     // b_staging = 0 picks the tile kernel for K-tiled packs whose stage leaves room for all 16
     // consumer warps (64 KB of B per stage): measured faster than the gather kernel there (FP32,
     // 2048 x 512 @ 90 %, K_c = 128: 13.2 vs 13.8 us per SpMM).  It never fails in that mode.
-    const bool auto_tile = args->b_staging == 0 && !gather_wide && tile_base_ok && args->meta_staging != 2 &&
+    const bool auto_tile = args->b_staging == 0 && !gather_wide && !gather_wide16 && tile_base_ok &&
+                           args->meta_staging != 2 &&
                            !cp->stream_kernel && a->geom.T > 1 && args->n <= INT32_MAX &&
                            staged_rows * 32 * nv * (int64_t)bsz <= 64 * 1024;
     if (args->b_staging == 1 || rounds > 1 || lb || auto_tile) {

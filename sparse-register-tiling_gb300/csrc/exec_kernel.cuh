@@ -162,6 +162,13 @@ template <int NV, class TB> struct GlobalB {
             VecIO<NV, TB>::load(p + (int64_t)k * ld, b);
         }
     }
+    // 16-bit B, NV = 8 (256-column strips): the lane's 8 columns as 4 packed words (for the
+    // mixed-precision FMA of run_group_wide)
+    __device__ __forceinline__ void load_raw(int k, uint32_t (&w)[NV / 2]) const {
+        static_assert(sizeof(TB) == 2 && NV == 8, "packed B rows are 16-bit, 8 columns per lane");
+        const uint4 v = __ldg(reinterpret_cast<const uint4 *>(p + (int64_t)k * ld));
+        w[0] = v.x; w[1] = v.y; w[2] = v.z; w[3] = v.w;
+    }
     __device__ __forceinline__ void load(int k, BSeg<NV, TB> &b) const {
         if constexpr (sizeof(TB) == 4) {
             load(k, b.f);
@@ -1096,10 +1103,11 @@ __device__ __forceinline__ void x_store(const XProblem &pr, int64_t gp, int64_t 
 
 template <int MR, int NV, class TV, class TB, class TC>
 __global__ void __launch_bounds__(256, 1) exec_batch_kernel(const __grid_constant__ BatchParams bp) {
-    // NV = 8 and 16: FP32 strips of 256 and 512 columns in the interleaved lane layout (WideIO)
-    constexpr bool WIDE = NV >= 8;
-    static_assert(!WIDE || (sizeof(TV) == 4 && sizeof(TB) == 4 && sizeof(TC) == 4),
-                  "wide gather strips are FP32 values, B and C");
+    // NV = 8 and 16 with FP32: strips of 256 and 512 columns in the interleaved lane layout
+    // (WideIO).  NV = 8 with 16-bit B: 256 columns, 8 contiguous a lane (one 16-byte load).
+    constexpr bool WIDE = NV >= 8 && sizeof(TB) == 4;
+    static_assert(!WIDE || (sizeof(TV) == 4 && sizeof(TC) == 4), "wide FP32 gather strips are FP32 values, B and C");
+    static_assert(NV <= 4 || WIDE || (NV == 8 && MR <= 4), "16-bit gather strips: NV = 8 at M_r <= 4");
     using IO = std::conditional_t<WIDE, WideIO<NV>, VecIO<NV, TC>>;
     using BL = std::conditional_t<WIDE, GlobalBWide<NV>, GlobalB<NV, TB>>;
     extern __shared__ __align__(128) unsigned char smem[];
@@ -1166,10 +1174,13 @@ template <> struct ComboTypes<COMBO_F16_F32OUT> { using V = __half; using B = __
 // Largest dynamic shared memory a staged-strip CTA may use (opt-in limit of sm_100-class parts).
 constexpr int kMaxSmem = 227 * 1024;
 
-// FP32 strips of 256 (NV = 8) and 512 columns (NV = 16, M_r <= 4) in the gather kernel.
+// Wide strips of the gather kernel: FP32 256 (NV = 8) and 512 columns (NV = 16, M_r <= 4); 16-bit
+// B 256 columns (NV = 8, M_r <= 4).
 using BatchKernelPtr = void (*)(BatchParams);
 template <int MR, int NV, class V, class B, class C> inline BatchKernelPtr wide_batch_kernel() {
     if constexpr (sizeof(V) == 4 && sizeof(B) == 4 && sizeof(C) == 4 && (NV == 8 || MR <= 4))
+        return exec_batch_kernel<MR, NV, V, B, C>;
+    else if constexpr (sizeof(B) == 2 && NV == 8 && MR <= 4)
         return exec_batch_kernel<MR, NV, V, B, C>;
     else
         return nullptr;

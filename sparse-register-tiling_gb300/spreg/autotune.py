@@ -27,7 +27,7 @@ threshold (`tc_fill`: panels whose fill reaches it run as dense tcgen05 products
 
 `tune` ranks every candidate with the model, times the best few on the device with the reference's
 timing protocol (`execute_timed`: median of repeated runs) or as a batch, then times the CTA tiling,
-(FP32) the gather kernel's wide strips, the panel rounds of the best and the tensor-core thresholds
+the gather kernel's wide strips, the panel rounds of the best and the tensor-core thresholds
 (all panels; the densest tenth), and returns the fastest, so a poor model costs tuning time, not
 speed.
 """
@@ -55,8 +55,8 @@ MAPPINGS_FOR_MR = {2: ("identity",), 4: ("identity",), 8: ("identity", "400fa", 
 class Candidate:
     mr: int
     mapping: str     # "identity" or a mapping id
-    nr: int          # strip width: 32, 64, 128, or wide: 256 (16-bit B with K_c <= 128, or FP32 untiled
-                     # packs on the gather kernel) and 512 (FP32 untiled, M_r <= 4) columns
+    nr: int          # strip width: 32, 64, 128, or wide: 256 (16-bit B at M_r <= 4, FP32 untiled packs)
+                     # and 512 (FP32 untiled packs, M_r <= 4) columns
     k_tile: int = 0  # K_c of the packing (0: one K tile)
     warps: int = 0   # CTA tiling (spreg_exec_args.warps_per_cta; 0: the executor's choice)
     tc_fill: float = 2.0  # panels with fill >= tc_fill on the tensor cores (> 1: none)
@@ -422,8 +422,8 @@ def tune(A: np.ndarray, n: int, dtype: str = "f32", top: int = 4, costs: Optiona
     rank by the cost model, then time the ``top`` best on the device -- one SpMM at a time with
     the reference's protocol (execute_timed) when ``batch`` is 1, else ``batch`` SpMMs of A with
     distinct B in one batched launch, as a serving loop runs them.  Then (``warps``) the CTA tiling
-    of the best register-tiled candidate, (FP32, n >= 256) 256- and 512-column strips of untiled
-    packs on the gather kernel, (``rounds``) panel rounds, and (``tc``) the tensor-core
+    of the best register-tiled candidate, (n >= 256) the gather kernel's wide strips of untiled
+    packs (FP32 256 and 512 columns, 16-bit B 256), (``rounds``) panel rounds, and (``tc``) the tensor-core
     thresholds: every panel, and the densest tenth of the panels, each timed as a batch of SpMMs
     through `spreg.hybrid`."""
     import torch
@@ -468,15 +468,15 @@ def tune(A: np.ndarray, n: int, dtype: str = "f32", top: int = 4, costs: Optiona
             by_name[c.name()] = c
             measured[c.name()] = time_reg(c)
     best_reg = by_name[min(measured, key=measured.get)]
-    if dtype == "f32" and n >= 256:
-        # wide FP32 strips of the gather kernel (untiled packs): 256 columns, 512 at M_r <= 4, each
-        # with the best-ranked nanokernel set of its M_r
+    if n >= 256:
+        # wide strips of the gather kernel (untiled packs), each with the best-ranked nanokernel set
+        # of its M_r: FP32 256 columns, and 512 at M_r <= 4; 16-bit B 256 columns at M_r <= 4
         first = {}
         for _, c in ranked:
-            if c.k_tile == 0 and c.mr not in first:
+            if c.k_tile == 0 and c.mr not in first and (dtype == "f32" or c.mr <= 4):
                 first[c.mr] = c
         for mr, c0 in sorted(first.items()):
-            for nr in ((256, 512) if mr <= 4 and n >= 512 else (256,)):
+            for nr in ((256, 512) if dtype == "f32" and mr <= 4 and n >= 512 else (256,)):
                 c = dataclasses.replace(c0, nr=nr, warps=4)
                 by_name[c.name()] = c
                 measured[c.name()] = time_reg(c)

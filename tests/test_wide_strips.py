@@ -109,18 +109,49 @@ def test_wide_strips_batched_with_other_widths_and_a_graph(cuda):
     assert device_status() == 0
 
 
-def test_wide_request_on_16bit_storage_keeps_its_kernels(cuda):
-    """nr = 512 on BF16 storage: the gather kernel has no wide 16-bit strips, so the executor keeps
-    128 columns there (the B-tile kernel's 256-column strips need a K-tiled pack)."""
+TORCH16 = {_lib.BF16: torch.bfloat16, _lib.F16: torch.float16}
+
+
+@pytest.mark.parametrize("vd", [_lib.BF16, _lib.F16])
+@pytest.mark.parametrize("mr,n", [(2, 512), (4, 512), (4, 600), (4, 264)])
+def test_16bit_256_column_gather_strips(cuda, vd, mr, n):
+    """16-bit B on the gather kernel (untiled packs): nr = 256 or 512 runs 256-column strips, 8
+    contiguous columns a lane with the mixed-precision FMA; bit-exact with the oracle."""
+    m = Mapping.identity(mr)
+    A = synth.row_skew(777, 512, 0.97, seed=mr + n, sigma=0.5, std=1.0)
+    Bf = synth.dense(512, n, seed=5)
+    B = torch.from_numpy(Bf).cuda().to(TORCH16[vd])
+    pm = PackedMatrix.from_dense(torch.from_numpy(A).cuda(), m, value_dtype=vd)
+    want = O.Packed(O.Tables.of(m), A, value_dtype=vd).execute(B.cpu().view(torch.int16).numpy().view(np.uint16))
+    for nr in (256, 512):
+        C = torch.empty((777, n), device="cuda")
+        plan = pm.explain(B, C, nr=nr)
+        assert (plan["kernel"], plan["strip_columns"]) == ("exec_batch_kernel", 256), plan
+        pm.execute(B, C, nr=nr)
+        assert np.array_equal(bits(C), want.view(np.uint32)), nr
+    assert device_status() == 0
+
+
+def test_16bit_gather_strips_load_c_bf16_out_and_mr8(cuda):
     m = Mapping.identity(4)
-    A = synth.row_skew(512, 256, 0.9, seed=2, std=1.0)
-    B = torch.from_numpy(synth.dense(256, 512, seed=3)).cuda().bfloat16()
+    A = synth.row_skew(500, 384, 0.95, seed=9, std=1.0)
+    B = torch.from_numpy(synth.dense(384, 512, seed=2)).cuda().bfloat16()
+    Bref = B.cpu().view(torch.int16).numpy().view(np.uint16)
     pm = PackedMatrix.from_dense(torch.from_numpy(A).cuda(), m, value_dtype=_lib.BF16)
-    C = torch.empty((512, 512), device="cuda")
-    assert pm.explain(B, C, nr=512)["strip_columns"] == 128
-    pm.execute(B, C, nr=512)
-    want = O.Packed(O.Tables.of(m), A, value_dtype=_lib.BF16).execute(B.cpu().view(torch.int16).numpy().view(np.uint16))
+    ref = O.Packed(O.Tables.of(m), A, value_dtype=_lib.BF16)
+    C0 = synth.dense(500, 512, seed=3)
+    C = torch.from_numpy(C0.copy()).cuda()
+    pm.execute(B, C, load_c=True, epilogue=_lib.EPILOGUE_RELU, nr=256)
+    want = ref.execute(Bref, C0.copy(), load_c=True, epilogue=_lib.EPILOGUE_RELU)
     assert np.array_equal(bits(C), want.view(np.uint32))
+    # BF16 output: the FP32 result rounded once
+    Cb = torch.empty((500, 512), device="cuda", dtype=torch.bfloat16)
+    pm.execute(B, Cb, nr=256)
+    assert torch.equal(Cb.cpu(), torch.from_numpy(ref.execute(Bref)).bfloat16())
+    # M_r = 8 keeps 128-column strips for 16-bit B
+    m8 = Mapping.load("747f9")
+    p8 = PackedMatrix.from_dense(torch.from_numpy(A).cuda(), m8, value_dtype=_lib.BF16)
+    assert p8.explain(B, torch.empty((500, 512), device="cuda"), nr=256)["strip_columns"] == 128
 
 
 def test_nr_values_outside_the_set_are_refused(cuda):
