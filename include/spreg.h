@@ -215,7 +215,8 @@ typedef struct {
                             with 16-bit B (256); the gather kernel with FP32 values, B and C, 16-byte
                             aligned B and C with row strides in whole 16-byte units (256; 512 at
                             M_r <= 4), its lanes holding interleaved 16-byte quarters of the strip,
-                            and with 16-bit B at M_r <= 4 (256) */
+                            and with 16-bit B at M_r <= 4 (256; 512: 8 columns a lane in each
+                            256-column half) */
     int32_t warps_per_cta; /* CTA tiling, 1..8; 0 = automatic: warps per CTA of the batched and
                               register-stream kernels (8 and 4 by default), consumer warps (row panels
                               per job) of the B-tile kernel (15 by default) */

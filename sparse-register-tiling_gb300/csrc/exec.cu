@@ -472,12 +472,13 @@ int plan_call(const spreg_packed *a, const spreg_exec_args *args, CallPlan *cp, 
                              combo == COMBO_F32 && nv == 4 && args->n >= 256 && aligned(args->b, 16) &&
                              args->ldb % 4 == 0 && aligned(args->c, 16) && args->ldc % 4 == 0;
     if (gather_wide) nv = args->nr == 512 && in.mr <= 4 && args->n >= 512 ? 16 : 8;
-    // 16-bit B in the gather kernel: 256-column strips (NV = 8, one 16-byte load of 8 columns a
-    // lane and entry, the mixed-precision FMA of the B-tile kernel's wide strips) at M_r <= 4
+    // 16-bit B in the gather kernel at M_r <= 4: 256-column strips (NV = 8, one 16-byte load of 8
+    // columns a lane and entry, the mixed-precision FMA of the B-tile kernel's wide strips), and
+    // for nr = 512 512-column strips (NV = 16: 8 columns a lane in each 256-column half)
     const bool gather_wide16 = (args->nr == 256 || args->nr == 512) && !tile_kernel && !cp->stream_kernel &&
                                bsz == 2 && in.mr <= 4 && nv == 4 && args->n >= 256 && aligned(args->b, 16) &&
                                args->ldb % 8 == 0 && aligned(args->c, csz * 8) && args->ldc % 8 == 0;
-    if (gather_wide16) nv = 8;
+    if (gather_wide16) nv = args->nr == 512 && args->n >= 512 ? 16 : 8;
     cp->nv = nv;
     const int64_t n_main = (args->n / (32 * nv)) * (32 * nv);
     int64_t lb_heavy = 0;

@@ -143,6 +143,33 @@ template <int NV, class H> struct VecIO16 {
 template <int NV> struct VecIO<NV, __nv_bfloat16> : VecIO16<NV, __nv_bfloat16> {};
 template <int NV> struct VecIO<NV, __half> : VecIO16<NV, __half> {};
 
+// C of a 512-column strip with 16-bit B (NV = 16): lane l holds columns 8l .. 8l + 7 of each
+// 256-column half (element j is column 256 (j / 8) + 8l + j % 8), as its B row segments.
+template <int NV, class TC> struct HalvesIO {
+    static_assert(NV == 16, "two 256-column halves of 8 columns a lane");
+    __device__ static void load(const TC *__restrict__ p, float (&b)[NV]) {
+        float h[2][8];
+        VecIO<8, TC>::load(p, h[0]);
+        VecIO<8, TC>::load(p + 256, h[1]);
+#pragma unroll
+        for (int j = 0; j < NV; ++j) b[j] = h[j >> 3][j & 7];
+    }
+    __device__ static void load_plain(const TC *p, float (&b)[NV]) {
+        float h[2][8];
+        VecIO<8, TC>::load_plain(p, h[0]);
+        VecIO<8, TC>::load_plain(p + 256, h[1]);
+#pragma unroll
+        for (int j = 0; j < NV; ++j) b[j] = h[j >> 3][j & 7];
+    }
+    __device__ static void store(TC *p, const float (&o)[NV]) {
+        float h[2][8];
+#pragma unroll
+        for (int j = 0; j < NV; ++j) h[j >> 3][j & 7] = o[j];
+        VecIO<8, TC>::store(p, h[0]);
+        VecIO<8, TC>::store(p + 256, h[1]);
+    }
+};
+
 // ------------------------------------------------------------------ B row sources
 // One lane's NV columns of a B row in registers: FP32 as floats; 16-bit B as the packed raw values
 // (pairs per 32-bit word), which the mixed-precision FMA (fma_vb) widens itself.
@@ -162,12 +189,15 @@ template <int NV, class TB> struct GlobalB {
             VecIO<NV, TB>::load(p + (int64_t)k * ld, b);
         }
     }
-    // 16-bit B, NV = 8 (256-column strips): the lane's 8 columns as 4 packed words (for the
-    // mixed-precision FMA of run_group_wide)
+    // 16-bit B, NV = 8 and 16 (256- and 512-column strips): the lane's 8 columns of each
+    // 256-column part as 4 packed words (for the mixed-precision FMA of run_group_wide)
     __device__ __forceinline__ void load_raw(int k, uint32_t (&w)[NV / 2]) const {
-        static_assert(sizeof(TB) == 2 && NV == 8, "packed B rows are 16-bit, 8 columns per lane");
-        const uint4 v = __ldg(reinterpret_cast<const uint4 *>(p + (int64_t)k * ld));
-        w[0] = v.x; w[1] = v.y; w[2] = v.z; w[3] = v.w;
+        static_assert(sizeof(TB) == 2 && (NV == 8 || NV == 16), "packed B rows are 16-bit, 8 columns a lane and part");
+#pragma unroll
+        for (int i = 0; i < NV / 8; ++i) {
+            const uint4 v = __ldg(reinterpret_cast<const uint4 *>(p + (int64_t)k * ld + 256 * i));
+            w[4 * i] = v.x; w[4 * i + 1] = v.y; w[4 * i + 2] = v.z; w[4 * i + 3] = v.w;
+        }
     }
     __device__ __forceinline__ void load(int k, BSeg<NV, TB> &b) const {
         if constexpr (sizeof(TB) == 4) {
@@ -1104,11 +1134,13 @@ __device__ __forceinline__ void x_store(const XProblem &pr, int64_t gp, int64_t 
 template <int MR, int NV, class TV, class TB, class TC>
 __global__ void __launch_bounds__(256, 1) exec_batch_kernel(const __grid_constant__ BatchParams bp) {
     // NV = 8 and 16 with FP32: strips of 256 and 512 columns in the interleaved lane layout
-    // (WideIO).  NV = 8 with 16-bit B: 256 columns, 8 contiguous a lane (one 16-byte load).
+    // (WideIO).  16-bit B: NV = 8, 256 columns, 8 contiguous a lane (one 16-byte load); NV = 16,
+    // 512 columns, 8 a lane in each 256-column half (HalvesIO).
     constexpr bool WIDE = NV >= 8 && sizeof(TB) == 4;
     static_assert(!WIDE || (sizeof(TV) == 4 && sizeof(TC) == 4), "wide FP32 gather strips are FP32 values, B and C");
-    static_assert(NV <= 4 || WIDE || (NV == 8 && MR <= 4), "16-bit gather strips: NV = 8 at M_r <= 4");
-    using IO = std::conditional_t<WIDE, WideIO<NV>, VecIO<NV, TC>>;
+    static_assert(NV <= 4 || WIDE || ((NV == 8 || NV == 16) && MR <= 4), "16-bit gather strips: NV 8 / 16 at M_r <= 4");
+    constexpr int LANE_COLS = WIDE ? 4 : (NV == 16 ? 8 : NV);
+    using IO = std::conditional_t<WIDE, WideIO<NV>, std::conditional_t<(NV == 16), HalvesIO<NV, TC>, VecIO<NV, TC>>>;
     using BL = std::conditional_t<WIDE, GlobalBWide<NV>, GlobalB<NV, TB>>;
     extern __shared__ __align__(128) unsigned char smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -1141,7 +1173,7 @@ __global__ void __launch_bounds__(256, 1) exec_batch_kernel(const __grid_constan
         if (b) ph1 ^= 1u; else ph0 ^= 1u;
         const XProblem &pr = bp.prob[j.pi];
         const int64_t row0 = j.gp * MR;
-        const int64_t col0 = pr.col_begin + (int64_t)j.strip * (32 * NV) + (int64_t)lane * (WIDE ? 4 : NV);
+        const int64_t col0 = pr.col_begin + (int64_t)j.strip * (32 * NV) + (int64_t)lane * LANE_COLS;
         const bool valid = col0 < pr.col_end;
         if (j.t == 0) x_acc_init<MR, NV, TV, TC, IO>(pr, row0, col0, valid, acc);
         const BL bl{reinterpret_cast<const TB *>(pr.B) + col0, pr.ldb, valid};
@@ -1175,12 +1207,12 @@ template <> struct ComboTypes<COMBO_F16_F32OUT> { using V = __half; using B = __
 constexpr int kMaxSmem = 227 * 1024;
 
 // Wide strips of the gather kernel: FP32 256 (NV = 8) and 512 columns (NV = 16, M_r <= 4); 16-bit
-// B 256 columns (NV = 8, M_r <= 4).
+// B 256 and 512 columns (NV = 8, 16; M_r <= 4).
 using BatchKernelPtr = void (*)(BatchParams);
 template <int MR, int NV, class V, class B, class C> inline BatchKernelPtr wide_batch_kernel() {
     if constexpr (sizeof(V) == 4 && sizeof(B) == 4 && sizeof(C) == 4 && (NV == 8 || MR <= 4))
         return exec_batch_kernel<MR, NV, V, B, C>;
-    else if constexpr (sizeof(B) == 2 && NV == 8 && MR <= 4)
+    else if constexpr (sizeof(B) == 2 && (NV == 8 || NV == 16) && MR <= 4)
         return exec_batch_kernel<MR, NV, V, B, C>;
     else
         return nullptr;

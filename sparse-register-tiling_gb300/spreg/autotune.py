@@ -56,7 +56,7 @@ class Candidate:
     mr: int
     mapping: str     # "identity" or a mapping id
     nr: int          # strip width: 32, 64, 128, or wide: 256 (16-bit B at M_r <= 4, FP32 untiled packs)
-                     # and 512 (FP32 untiled packs, M_r <= 4) columns
+                     # and 512 (untiled packs, M_r <= 4) columns
     k_tile: int = 0  # K_c of the packing (0: one K tile)
     warps: int = 0   # CTA tiling (spreg_exec_args.warps_per_cta; 0: the executor's choice)
     tc_fill: float = 2.0  # panels with fill >= tc_fill on the tensor cores (> 1: none)
@@ -423,7 +423,7 @@ def tune(A: np.ndarray, n: int, dtype: str = "f32", top: int = 4, costs: Optiona
     the reference's protocol (execute_timed) when ``batch`` is 1, else ``batch`` SpMMs of A with
     distinct B in one batched launch, as a serving loop runs them.  Then (``warps``) the CTA tiling
     of the best register-tiled candidate, (n >= 256) the gather kernel's wide strips of untiled
-    packs (FP32 256 and 512 columns, 16-bit B 256), (``rounds``) panel rounds, and (``tc``) the tensor-core
+    packs (256 and 512 columns), (``rounds``) panel rounds, and (``tc``) the tensor-core
     thresholds: every panel, and the densest tenth of the panels, each timed as a batch of SpMMs
     through `spreg.hybrid`."""
     import torch
@@ -470,13 +470,13 @@ def tune(A: np.ndarray, n: int, dtype: str = "f32", top: int = 4, costs: Optiona
     best_reg = by_name[min(measured, key=measured.get)]
     if n >= 256:
         # wide strips of the gather kernel (untiled packs), each with the best-ranked nanokernel set
-        # of its M_r: FP32 256 columns, and 512 at M_r <= 4; 16-bit B 256 columns at M_r <= 4
+        # of its M_r: 256 columns (16-bit B: M_r <= 4), and 512 at M_r <= 4
         first = {}
         for _, c in ranked:
             if c.k_tile == 0 and c.mr not in first and (dtype == "f32" or c.mr <= 4):
                 first[c.mr] = c
         for mr, c0 in sorted(first.items()):
-            for nr in ((256, 512) if dtype == "f32" and mr <= 4 and n >= 512 else (256,)):
+            for nr in ((256, 512) if mr <= 4 and n >= 512 else (256,)):
                 c = dataclasses.replace(c0, nr=nr, warps=4)
                 by_name[c.name()] = c
                 measured[c.name()] = time_reg(c)

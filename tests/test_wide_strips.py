@@ -114,9 +114,10 @@ TORCH16 = {_lib.BF16: torch.bfloat16, _lib.F16: torch.float16}
 
 @pytest.mark.parametrize("vd", [_lib.BF16, _lib.F16])
 @pytest.mark.parametrize("mr,n", [(2, 512), (4, 512), (4, 600), (4, 264)])
-def test_16bit_256_column_gather_strips(cuda, vd, mr, n):
-    """16-bit B on the gather kernel (untiled packs): nr = 256 or 512 runs 256-column strips, 8
-    contiguous columns a lane with the mixed-precision FMA; bit-exact with the oracle."""
+def test_16bit_gather_strips(cuda, vd, mr, n):
+    """16-bit B on the gather kernel (untiled packs): nr = 256 runs 256-column strips (8 contiguous
+    columns a lane), nr = 512 512-column strips (8 a lane in each 256-column half) when n reaches
+    512, both with the mixed-precision FMA; bit-exact with the oracle."""
     m = Mapping.identity(mr)
     A = synth.row_skew(777, 512, 0.97, seed=mr + n, sigma=0.5, std=1.0)
     Bf = synth.dense(512, n, seed=5)
@@ -126,7 +127,8 @@ def test_16bit_256_column_gather_strips(cuda, vd, mr, n):
     for nr in (256, 512):
         C = torch.empty((777, n), device="cuda")
         plan = pm.explain(B, C, nr=nr)
-        assert (plan["kernel"], plan["strip_columns"]) == ("exec_batch_kernel", 256), plan
+        width = 512 if (nr == 512 and n >= 512) else 256
+        assert (plan["kernel"], plan["strip_columns"]) == ("exec_batch_kernel", width), plan
         pm.execute(B, C, nr=nr)
         assert np.array_equal(bits(C), want.view(np.uint32)), nr
     assert device_status() == 0
@@ -140,14 +142,15 @@ def test_16bit_gather_strips_load_c_bf16_out_and_mr8(cuda):
     pm = PackedMatrix.from_dense(torch.from_numpy(A).cuda(), m, value_dtype=_lib.BF16)
     ref = O.Packed(O.Tables.of(m), A, value_dtype=_lib.BF16)
     C0 = synth.dense(500, 512, seed=3)
-    C = torch.from_numpy(C0.copy()).cuda()
-    pm.execute(B, C, load_c=True, epilogue=_lib.EPILOGUE_RELU, nr=256)
     want = ref.execute(Bref, C0.copy(), load_c=True, epilogue=_lib.EPILOGUE_RELU)
-    assert np.array_equal(bits(C), want.view(np.uint32))
-    # BF16 output: the FP32 result rounded once
-    Cb = torch.empty((500, 512), device="cuda", dtype=torch.bfloat16)
-    pm.execute(B, Cb, nr=256)
-    assert torch.equal(Cb.cpu(), torch.from_numpy(ref.execute(Bref)).bfloat16())
+    for nr in (256, 512):
+        C = torch.from_numpy(C0.copy()).cuda()
+        pm.execute(B, C, load_c=True, epilogue=_lib.EPILOGUE_RELU, nr=nr)
+        assert np.array_equal(bits(C), want.view(np.uint32)), nr
+        # BF16 output: the FP32 result rounded once
+        Cb = torch.empty((500, 512), device="cuda", dtype=torch.bfloat16)
+        pm.execute(B, Cb, nr=nr)
+        assert torch.equal(Cb.cpu(), torch.from_numpy(ref.execute(Bref)).bfloat16()), nr
     # M_r = 8 keeps 128-column strips for 16-bit B
     m8 = Mapping.load("747f9")
     p8 = PackedMatrix.from_dense(torch.from_numpy(A).cuda(), m8, value_dtype=_lib.BF16)
