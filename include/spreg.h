@@ -286,7 +286,9 @@ int spreg_execute_batched(const spreg_work_item *items_host, int32_t num_items, 
  * like the regular executors' word, and keeps its value until then.  It runs only the batched
  * execution-layout kernel (no meta_staging = 2, no oversized blocks): where spreg_execute_batched's
  * automatic B staging picks the shared-memory B-tile kernel (K-tiled packs), this entry point gives
- * the same results from the batched kernel, more slowly.  It has no counterpart in the reference. */
+ * the same results from the batched kernel, more slowly.  Strip widths (nr, the wide strips of
+ * 256 and 512 columns included) are chosen as spreg_execute chooses them for the batched kernel.
+ * It has no counterpart in the reference. */
 #define SPREG_NOALLOC_MAX_LAUNCHES 64
 int spreg_execute_batched_noalloc(const spreg_work_item *items_host, int32_t num_items, spreg_stream_t stream);
 

@@ -173,12 +173,24 @@ extern "C" int spreg_execute_batched_noalloc(const spreg_work_item *items, int32
         case 32: nv = 1; break;
         case 64: nv = 2; break;
         case 128: nv = 4; break;
-        default: SPREG_FAIL(SPREG_ERR_INVALID_ARG, "work item %d: nr must be 0, 32, 64 or 128", i);
+        case 256: nv = 4; break;  // wide strips below where the gather kernel has them, else 128
+        case 512: nv = 4; break;
+        default: SPREG_FAIL(SPREG_ERR_INVALID_ARG, "work item %d: nr must be 0, 32, 64, 128, 256 or 512", i);
         }
         const size_t bsz = dtype_bytes(args->b_dtype), csz = dtype_bytes(args->c_dtype);
         while (nv > 1 && !(is_aligned(args->b, bsz * nv) && args->ldb % nv == 0 && is_aligned(args->c, csz * nv) &&
                            args->ldc % nv == 0))
             nv >>= 1;
+        // the gather kernel's wide strips, as spreg_execute chooses them: FP32 256 columns (512 at
+        // M_r <= 4), 16-bit B 256 and 512 columns at M_r <= 4
+        if ((args->nr == 256 || args->nr == 512) && nv == 4 && args->n >= 256 && is_aligned(args->b, 16) &&
+            is_aligned(args->c, 16)) {
+            const bool wide32 = combo == COMBO_F32 && args->ldb % 4 == 0 && args->ldc % 4 == 0;
+            const bool wide16 = bsz == 2 && in.mr <= 4 && args->ldb % 8 == 0 && is_aligned(args->c, csz * 8) &&
+                                args->ldc % 8 == 0;
+            const bool w512 = args->nr == 512 && in.mr <= 4 && args->n >= 512;
+            if (wide32 || wide16) nv = w512 ? 16 : 8;
+        }
         const int64_t n_main = (args->n / (32 * nv)) * (32 * nv);
         XProblem base = {};
         base.exec = a->exec;

@@ -41,6 +41,11 @@ CASES = [
     (96, 128, 20, "61fee", _lib.F32, 0, {}, 0, 0, False),                # N < 32
     (128, 256, 128, "61fee", _lib.F16, 0, {"nr": 64}, 0, 0, False),       # FP16 values with panel scales
     (144, 200, 72, "61fee", _lib.BF16, 0, {"epilogue": 1}, 0, 0, True),   # BF16 out
+    (256, 512, 512, "61fee", _lib.F32, 0, {"nr": 512}, 0, 0, False),      # wide FP32 strips (512 columns)
+    (300, 256, 600, "400fa", _lib.F32, 0, {"nr": 256}, 0, 4, False),      # 256-column FP32, M_r 8, tail
+    (260, 512, 512, "61fee", _lib.BF16, 0, {"nr": 512}, 0, 0, False),     # 512-column 16-bit strips
+    (128, 256, 512, "61fee", _lib.F16, 0, {"nr": 256}, 0, 0, False),      # 256-column, FP16 panel scales
+    (144, 200, 512, "61fee", _lib.BF16, 0, {"nr": 512, "epilogue": 1}, 0, 0, True),  # wide, BF16 out
 ]
 
 
