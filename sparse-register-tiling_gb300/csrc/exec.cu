@@ -670,6 +670,7 @@ int launch_groups(std::map<std::tuple<int, int, int>, Group> &groups, cudaStream
             bp.counter = next_counter(f);
             // warps per CTA: as asked, else 8; fewer if the buffers do not fit
             int nw = g.warps_req > 0 ? g.warps_req : 8;
+            if (g.nv >= 8 && g.combo == COMBO_F32) nw = std::min(nw, kWideMaxWarps);  // the kernel's bound
             while (nw > 1 && 1024 + 2 * g.xbuf * nw > f->smem_optin) nw >>= 1;
             const size_t smem = (size_t)(1024 + 2 * g.xbuf * nw);
             const int threads = 32 * nw;

@@ -1131,8 +1131,20 @@ __device__ __forceinline__ void x_store(const XProblem &pr, int64_t gp, int64_t 
     }
 }
 
+// Wide FP32 strips run CTAs of at most 4 warps (kWideMaxWarps).  Their 64-register B step and up
+// to 64 accumulators leave 8 warps an SM; where 168 registers a thread suffice without more than a
+// few spilled bytes (256 columns, and 512 at M_r <= 2) they are held to that: 3 CTAs, 12 warps.
+constexpr int kWideMaxWarps = 4;
+template <int MR, int NV, class TB> constexpr int batch_max_threads() {
+    return NV >= 8 && sizeof(TB) == 4 ? 32 * kWideMaxWarps : 256;
+}
+template <int MR, int NV, class TB> constexpr int batch_min_blocks() {
+    return NV >= 8 && sizeof(TB) == 4 && (NV == 8 || MR <= 2) ? 3 : 1;
+}
+
 template <int MR, int NV, class TV, class TB, class TC>
-__global__ void __launch_bounds__(256, 1) exec_batch_kernel(const __grid_constant__ BatchParams bp) {
+__global__ void __launch_bounds__(batch_max_threads<MR, NV, TB>(), batch_min_blocks<MR, NV, TB>())
+    exec_batch_kernel(const __grid_constant__ BatchParams bp) {
     // NV = 8 and 16 with FP32: strips of 256 and 512 columns in the interleaved lane layout
     // (WideIO).  16-bit B: NV = 8, 256 columns, 8 contiguous a lane (one 16-byte load); NV = 16,
     // 512 columns, 8 a lane in each 256-column half (HalvesIO).

@@ -255,7 +255,7 @@ extern "C" int spreg_execute_batched_noalloc(const spreg_work_item *items, int32
             bp.xbuf = (int32_t)g.xbuf;
             bp.status = scratch;
             bp.counter = scratch + slot;
-            int nw = 8;
+            int nw = g.nv >= 8 && g.combo == COMBO_F32 ? kWideMaxWarps : 8;  // wide FP32: the kernel's bound
             while (nw > 1 && 1024 + 2 * g.xbuf * nw > d->smem_optin) nw >>= 1;
             const size_t smem = (size_t)(1024 + 2 * g.xbuf * nw);
             const int threads = 32 * nw;
