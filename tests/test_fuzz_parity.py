@@ -81,3 +81,33 @@ def test_fuzz_alone_and_batched_bit_exact(cuda, block):
     for (pm, tb, Cb, kw), (i, c, want) in zip(work, wants):
         assert np.array_equal(Cb.cpu().numpy().view(np.uint32), want.view(np.uint32)), ("batched", i, c)
     assert device_status() == 0
+
+
+def draw_wide(g):
+    """A case for the wide strips (nr = 256 / 512): high sparsity, widths around the strip
+    boundaries, B row strides that keep or lose 16-byte alignment, untiled and K-tiled packs
+    (the latter through the gather kernel with staging 2, or the executor's own choice)."""
+    c = draw_case(g)
+    c.update(M=int(g.integers(1, 700)), sp=float(g.choice([0.9, 0.95, 0.98, 0.99])),
+             nr=int(g.choice([256, 512])), n=int(g.choice([256, 264, 300, 512, 520, 600, 1024])),
+             k_tile=int(g.choice([0, 0, 128])), staging=int(g.choice([0, 2])), ld_pad=int(g.choice([0, 4, 8, 3])))
+    return c
+
+
+@pytest.mark.parametrize("block", range(2))
+def test_fuzz_wide_strips_bit_exact(cuda, block):
+    g = np.random.default_rng(2000 + block)
+    cases = [draw_wide(g) for _ in range(40)]
+    built = [build(c, 9000 + 100 * block + i) for i, c in enumerate(cases)]
+    work, wants = [], []
+    for i, (c, (pm, tb, C0, want)) in enumerate(zip(cases, built)):
+        C = torch.from_numpy(C0).cuda() if c["load_c"] else torch.zeros((c["M"], c["n"]), device="cuda")
+        pm.execute(tb, C, **kwargs_of(c))
+        assert np.array_equal(C.cpu().numpy().view(np.uint32), want.view(np.uint32)), (i, c)
+        Cb = torch.from_numpy(C0).cuda() if c["load_c"] else torch.zeros((c["M"], c["n"]), device="cuda")
+        work.append((pm, tb, Cb, kwargs_of(c)))
+        wants.append((i, c, want))
+    execute_batched(work)
+    for (pm, tb, Cb, kw), (i, c, want) in zip(work, wants):
+        assert np.array_equal(Cb.cpu().numpy().view(np.uint32), want.view(np.uint32)), ("batched", i, c)
+    assert device_status() == 0
