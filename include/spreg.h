@@ -237,8 +237,10 @@ typedef struct {
                              cpp_testbed/src/spmm/nano/runtime_yaml_config.register:84-99).  When the
                              launch leaves SMs idle (fewer jobs of W panels x strips than SMs), the
                              heaviest whole groups of W panels (work estimate above half the heaviest
-                             panel's) are split at K tile T / 2 until the idle SMs are used, unless the
-                             first unsplit group is within a fifth of the heaviest panel: K tiles
+                             panel's) are split at K tile T / 2 until the idle SMs are used, unless
+                             some groups stay unsplit and the first of them is within a fifth of the
+                             heaviest panel, or the heaviest panel's work is below twice the median
+                             panel's: K tiles
                              [0, T/2) accumulate into C (from C with load_c) in one job, tiles [T/2, T)
                              from zero in another, which adds into C once the first has stored that
                              (panel, strip): C = C + hi, one FP32 add per element, the epilogue after
