@@ -165,6 +165,33 @@ def test_full_tune_best_is_measured_and_within_tolerance(cuda, dtype, n):
     assert O.rel_err(got, O.dense_fp64(Aq, Bq)) <= (1e-5 if dtype == "f32" else 1e-2)
 
 
+@pytest.mark.gpu
+@pytest.mark.parametrize("dtype", ["f32", "bf16"])
+def test_tune_times_the_wide_gather_strips_at_the_sparse_end(cuda, dtype):
+    """At 98 % sparsity and n = 512 the tuner times the gather kernel's 256- and 512-column strips of
+    untiled packs beside its other candidates; its pick executes bit-exact with the oracle."""
+    import torch
+    from spreg import PackedMatrix, _lib
+    A = synth.row_skew(2048, 512, 0.98, seed=11, sigma=0.5, std=0.02)
+    res = tune(A, 512, dtype, top=2, batch=8, tc=False, rounds=False)
+    wide = [k for k in res.measured_ns if k.split("_")[0].endswith(("N256", "N512")) and "_K" not in k]
+    assert any("N512" in k for k in wide) and any("N256" in k for k in wide), sorted(res.measured_ns)
+    assert res.measured_ns[res.best.name()] == min(res.measured_ns.values())
+    c = res.best
+    m = mapping_of(c.mr, c.mapping)
+    vd = _lib.F32 if dtype == "f32" else _lib.BF16
+    pm = PackedMatrix.from_dense(torch.from_numpy(A).cuda(), m, k_tile=c.k_tile, value_dtype=vd)
+    B = synth.dense(512, 512, seed=12)
+    Bt = torch.from_numpy(B).cuda()
+    Bref = B
+    if dtype == "bf16":
+        Bt = Bt.bfloat16()
+        Bref = Bt.cpu().view(torch.int16).numpy().view(np.uint16)
+    got = pm.execute(Bt, nr=c.nr, warps=c.warps).cpu().numpy()
+    want = O.Packed(O.Tables.of(m), A, k_tile=c.k_tile, value_dtype=vd).execute(Bref)
+    np.testing.assert_array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
 def test_candidate_names_round_trip():
     """candidate_from_name inverts Candidate.name(), greedy mapping ids included (rebuilt from A)."""
     from spreg.autotune import GENERATED, candidate_from_name, greedy_mapping, mapping_of
