@@ -499,11 +499,13 @@ def load_balance_leg(dev) -> list:
 def sparse_end_leg(dev, nb: int = 32, reps: int = 10) -> dict:
     """The memory-bound end of the FFN workload: 2048 x 512 @ 98 % row skew (sigma 0.5, values N(0, 0.02)),
     N = 512, FP32, nb SpMMs of one A with distinct B per batched launch, replayed from a CUDA graph,
-    through three paths: the gather kernel (untiled M_r = 8 pack, 747f9 set, 128-column strips, 4 warps
-    per CTA), panel rounds (64-column strips, 16 rounds of 15 panels on a resident whole-K strip), and
-    the FP32-accurate tensor-core hybrid (every panel).  Each path's first launch is an NVTX range
+    through these paths: the gather kernel (untiled M_r = 8 pack, 747f9 set, 128-column strips, 4 warps
+    per CTA), its wide strips (256 and 512 columns at M_r 2, 4 and 8), panel rounds (64-column strips,
+    16 rounds of 15 panels on a resident whole-K strip), and the FP32-accurate tensor-core hybrid
+    (every panel).  Each path's first launch is an NVTX range
     sparse_end_<path> (for ncu --nvtx).  Register-tiled paths are checked bit for bit against the
-    oracle, the hybrid against its tolerance."""
+    oracle, the hybrid against its tolerance.  Every path's GB/s divides the same algorithmic bytes,
+    those of the M_r = 8 (747f9) pack, so the rates compare directly."""
     import torch
     from oracle import oracle as O
     from spreg import F32, Mapping, PackedMatrix, execute_batched, synth
