@@ -1265,6 +1265,12 @@ cudaError_t launch_exec_batch(const BatchParams &p, int nv, unsigned grid, int t
                 if (e != cudaSuccess) return e;                                                       \
                 configured[dev][nv].store(true);                                                           \
             }                                                                                         \
+            /* at most the CTAs that can be resident at once (registers included): later ones would */ \
+            /* only start once the work list is empty, and then exit */                               \
+            int occ = 0, nsm = 0;                                                                     \
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, threads, smem) == cudaSuccess && occ > 0 && \
+                cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && nsm > 0) \
+                grid = std::min<unsigned>(grid, (unsigned)occ * (unsigned)nsm);                       \
             kern<<<grid, threads, smem, s>>>(p);                                                      \
             return cudaGetLastError();                                                                \
         };                                                                                            \
