@@ -554,6 +554,11 @@ cudaError_t launch_exec_tile(const TileParams &p, int nv, bool gen, unsigned gri
                 if (e != cudaSuccess) return e;                                                       \
                 configured[dev][nv][gen].store(true);                                                 \
             }                                                                                         \
+            /* at most the CTAs that can be resident at once (registers included) */                  \
+            int occ = 0, nsm = 0;                                                                     \
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, threads, smem) == cudaSuccess && occ > 0 && \
+                cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && nsm > 0) \
+                grid = std::min<unsigned>(grid, (unsigned)occ * (unsigned)nsm);                       \
             kern<<<grid, threads, smem, s>>>(p);                                                      \
             return cudaGetLastError();                                                                \
         };                                                                                            \
