@@ -569,6 +569,21 @@ def sparse_end_leg(dev, nb: int = 32, reps: int = 10) -> dict:
         out[name] = {"us_per_spmm": us, "gbs": nbytes / us / 1e3, "frac_of_measured_hbm": nbytes / us / 1e3 / peak,
                      "plan": pm.explain(Bs[0], Cs[0], **kw),
                      "bit_exact_vs_oracle": bool(np.array_equal(got.view(np.uint32), want.view(np.uint32)))}
+    # 16-bit storage: BF16 values and B, FP32 C, 512-column gather strips (M_r 2); its GB/s divides
+    # the BF16 pack's own algorithmic bytes (2-byte values and B)
+    from spreg import BF16
+    m2 = Mapping.identity(2)
+    pb = PackedMatrix.from_dense(At, m2, value_dtype=BF16)
+    Bh = [b.to(torch.bfloat16) for b in Bs]
+    wb = O.Packed(O.Tables.of(m2), A, value_dtype=BF16).execute(Bh[0].cpu().view(torch.int16).numpy().view(np.uint16))
+    kwb = dict(nr=512, warps=4)
+    workb = [(pb, b, c, kwb) for b, c in zip(Bh, Cs)]
+    us = graph_time(lambda: execute_batched(workb), "sparse_end_wide_bf16_m2_512")
+    nb16 = pb.algorithmic_bytes(512, b_bytes=2)
+    out["wide_bf16_m2_512"] = {"us_per_spmm": us, "gbs": nb16 / us / 1e3, "frac_of_measured_hbm": nb16 / us / 1e3 / peak,
+                               "plan": pb.explain(Bh[0], Cs[0], **kwb),
+                               "bit_exact_vs_oracle": bool(np.array_equal(Cs[0].cpu().numpy().view(np.uint32),
+                                                                          wb.view(np.uint32)))}
     pm, want = packs["747f9"]
     h = HybridMatrix.from_dense(torch.from_numpy(A).to(dev), m8, 0.0, value_dtype=F32)
     hb = HybridBatch([(h, b, c) for b, c in zip(Bs, Cs)])
