@@ -42,7 +42,7 @@ L2_BYTES = 129 * 2 ** 20
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["spreg", "reference"], default="spreg")
     ap.add_argument("--replicas", type=int, default=96)
@@ -128,7 +128,7 @@ def algorithmic_bytes_oracle(pk, n: int) -> int:
 
 
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled every 50 ms; `summary` keeps the samples that
+    """nvidia-smi clocks / throttle reasons sampled every 10 ms; `summary` keeps the samples that
     arrived between `mark_start` and `mark_end` (the timed region)."""
 
     QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -152,7 +152,7 @@ class ClockSampler:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
-                                          "--format=csv,noheader,nounits", "-lms", "50"],
+                                          "--format=csv,noheader,nounits", "-lms", "10"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
